@@ -1,0 +1,364 @@
+#!/usr/bin/env python
+"""Throughput of the D3Q19 AA stream-collide step on GB300, in GLUPS.
+
+Workload: the 3-D Taylor-Green vortex at Re = 1600 on a periodic 256^3 lattice
+(u0 = 0.05, L = 256 / 2pi, nu = u0 L / 1600), initialised by the library's
+initField, run in
+  fp16s_srt  FP16 (shifted) storage, SRT        -> the headline `value`
+  fp32_trt   FP32 storage, TRT Lambda = 3/16    -> reported under `variants`.
+One bench step = one logging interval of that workload: 100 lattice time steps
+(one kernel launch each) followed by the kinetic-energy and dissipation
+reductions read back to the host.
+
+value : cells x time steps / device time of the step kernels (CUDA events on
+        the library's launching stream), GLUPS, whole job over all ranks.
+e2e   : the same metric over the whole job through the C ABI with host
+        buffers: initial state uploaded from pinned host memory, K bench steps
+        with their observable read-backs, final state downloaded.
+Inputs are larger than L2 (the 256^3 state is 637 MB / 1.27 GB), so no L2
+flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference arithmetic (the
+oracle, OpenMP over all host cores) on the same workload, one bench step = one
+even+odd pair of lattice steps over the full 256^3 lattice.
+Multi-GPU (torchrun): replicas only — each rank runs its own lattice.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_EDGE = 256
+U0 = 0.05
+RE = 1600.0
+STEPS_PER_BENCH_STEP = 100
+ALG_BYTES = {"fp32": 152, "fp16s": 76}  # 19 reads + 19 writes per cell per step
+
+
+def tgv_params(n=N_EDGE, u0=U0, re=RE):
+    L = n / (2 * np.pi)
+    nu = u0 * L / re
+    tau = 3 * nu + 0.5
+    return L, nu, tau
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per cell per launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "lbm_step_tgv256_ncu.md")
+    out = {}
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_cell"):
+                # traffic_bytes_per_cell <variant> <bytes>
+                _, var, val = line.split()
+                out[var] = float(val)
+    except OSError:
+        pass
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % device)
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist  # plumbing only: barrier and max-reduce
+
+        dist.init_process_group("gloo")
+    return ws, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allreduce(dist, value, op):
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=op)
+    return float(t.item())
+
+
+def run_variant(sg, gpu, precision, lam, steps, warmup, dist, clocks=None):
+    n = N_EDGE
+    L, nu, tau = tgv_params()
+    wp, wm = sg.trtOmegas(tau, lam)
+    sim = sg.Simulation(gpu, precision=precision, nx=n, ny=n, nz=n, omega=wp, omegaMinus=wm)
+    cells = sim.cells
+    # ---- device-timed: kernels only, state resident in HBM
+    sim.initField(2, U0)
+    sim.run(warmup * STEPS_PER_BENCH_STEP)
+    sim.kineticEnergySum()
+    barrier(dist)
+    t0 = sim.gpuSeconds
+    w0 = time.perf_counter()
+    ctx = clocks if clocks is not None else _Null()
+    with ctx:
+        for _ in range(steps):
+            sim.run(STEPS_PER_BENCH_STEP)
+            sim.kineticEnergySum()
+            sim.dissipationSum()
+    wall = time.perf_counter() - w0
+    dev = sim.gpuSeconds - t0
+    barrier(dist)
+    launches = steps * STEPS_PER_BENCH_STEP
+    finite = sim.checkFinite()
+    # ---- end to end through the C ABI with host buffers
+    dtype = np.float16 if precision == "fp16s" else np.float32
+    host = sg.PinnedBuffer((19, cells), dtype)
+    sim.initField(2, U0)
+    sim.downloadState(host.array)  # initial state lives on the host
+    sim.stepsDone = 0
+    barrier(dist)
+    e0 = time.perf_counter()
+    sim.uploadState(host.array)
+    logs = []
+    for _ in range(steps):
+        sim.run(STEPS_PER_BENCH_STEP)
+        logs.append((sim.kineticEnergySum(), sim.dissipationSum()))
+    sim.downloadState(host.array)
+    e2e_wall = time.perf_counter() - e0
+    barrier(dist)
+    state_bytes = host.nbytes
+    host.close()
+    sim.close()
+    return dict(cells=cells, launches=launches, dev=dev, wall=wall, e2e_wall=e2e_wall,
+                state_bytes=state_bytes, finite=finite, ke_last=logs[-1][0] if logs else None)
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+def cpu_baseline(precision="fp16s", lam=None, pairs=1, threads=None):
+    """Oracle (CPU restatement, OpenMP) on the full 256^3 lattice, `pairs` AA pairs."""
+    from oracle import pyoracle as po
+
+    threads = threads or os.cpu_count() or 1
+    n = N_EDGE
+    L, nu, tau = tgv_params()
+    wp, wm = po.trt_omegas(tau, lam)
+    kind = po.KIND_F16 if precision == "fp16s" else po.KIND_F32
+    sim = po.OracleSim(n, n, n, omega=wp, omegaMinus=wm, kind=kind, threads=threads)
+    sim.initField(2, U0)
+    sim.run(2)  # warm-up pair
+    t0 = time.perf_counter()
+    sim.run(2 * pairs)
+    dt = time.perf_counter() - t0
+    return dict(value=sim.N * 2 * pairs / dt / 1e9, unit="GLUPS", cores=threads, kind="port",
+                seconds=dt,
+                sample="%d even+odd step pair(s) of the 256^3 TGV lattice (%s %s)"
+                       % (pairs, precision, "SRT" if lam is None else "TRT"))
+
+
+def main_reference(args, ws, rank, dist):
+    if rank != 0:
+        return 0
+    from oracle import build_oracle
+
+    build_oracle.build_oracle()
+    threads = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(pairs=1, threads=threads)
+    t_total = 0.0
+    for _ in range(args.steps):
+        r = cpu_baseline(pairs=1, threads=threads)
+        vals.append(r["value"])
+        t_total += r["seconds"]
+    cells = N_EDGE ** 3
+    value = cells * 2 * args.steps / t_total / 1e9
+    line = {
+        "metric": "D3Q19 TGV Re=1600 256^3 step throughput (GLUPS)",
+        "impl": "reference", "value": value, "unit": "GLUPS", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (analytic Taylor-Green initial field)",
+        "config": {"workload": "TGV Re=1600 periodic 256^3, FP16-storage SRT; step = one even+odd "
+                               "pair of lattice steps on the host cores"},
+        "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": threads, "kind": "port",
+                         "sample": "one even+odd step pair of the full 256^3 lattice per step"},
+        "e2e": {"value": value, "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        return main_reference(args, ws, rank, dist)
+
+    import __graft_entry__
+
+    lib_path = os.path.join(ROOT, "strouhal_gb300", "_lib", "libstrouhal_gb300.so")
+    if not os.path.exists(lib_path):
+        __graft_entry__.build()
+    import strouhal_gb300 as sg
+
+    gpu = sg.GPU(local)
+    clocks = ClockSampler(local)
+    head = run_variant(sg, gpu, "fp16s", None, args.steps, args.warmup, dist, clocks)
+    trt = run_variant(sg, gpu, "fp32", 3.0 / 16.0, args.steps, args.warmup, dist)
+    peak, peak_kind = measured_peak()
+    traffic = profile_traffic()
+
+    def summarise(r, precision):
+        dev = allreduce(dist, r["dev"], _max_op())
+        e2e_wall = allreduce(dist, r["e2e_wall"], _max_op())
+        total = r["cells"] * r["launches"] * ws
+        glups = total / dev / 1e9
+        per_launch = dev / r["launches"]
+        ach = ALG_BYTES[precision] * r["cells"] / per_launch / 1e9
+        return glups, total / e2e_wall / 1e9, per_launch, ach
+
+    g16, e16, pl16, ach16 = summarise(head, "fp16s")
+    g32, e32, pl32, ach32 = summarise(trt, "fp32")
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(pairs=1)
+            cpu.pop("seconds", None)
+        except Exception as exc:  # noqa: BLE001 — report, do not fail the bench
+            cpu = {"value": None, "unit": "GLUPS", "error": str(exc)[:200]}
+    if rank != 0:
+        return 0
+    t16 = traffic.get("fp16s_srt")
+    t32 = traffic.get("fp32_trt")
+    line = {
+        "metric": "D3Q19 TGV Re=1600 256^3 step throughput (GLUPS)",
+        "value": g16, "unit": "GLUPS", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * head["dev"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (analytic Taylor-Green initial field)",
+        "config": {"workload": "TGV Re=1600 periodic 256^3, FP16-storage SRT, u0=0.05",
+                   "lattice": [N_EDGE] * 3, "lattice_steps_per_step": STEPS_PER_BENCH_STEP,
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (state 637 MB fp16 / 1.27 GB fp32)"},
+        "roofline": {"bound": "hbm", "achieved": ach16, "peak": peak, "unit": "GB/s",
+                     "frac": ach16 / peak, "peak_source": peak_kind,
+                     "traffic": None if t16 is None else t16 * head["cells"],
+                     "kernel": "k_step_even/k_step_odd (fp16, periodic, lean)",
+                     "alg_bytes_per_cell": ALG_BYTES["fp16s"]},
+        "e2e": {"value": e16, "unit": "GLUPS",
+                "h2d_bytes_per_step": head["state_bytes"] / args.steps,
+                "d2h_bytes_per_step": (head["state_bytes"] + 16 * args.steps) / args.steps},
+        "gpu_launches": head["launches"] + 2 * 2 * args.steps,
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+        "variants": {
+            "fp32_trt": {"value": g32, "unit": "GLUPS", "e2e": e32,
+                         "roofline": {"achieved": ach32, "peak": peak, "frac": ach32 / peak,
+                                      "traffic": None if t32 is None else t32 * trt["cells"],
+                                      "alg_bytes_per_cell": ALG_BYTES["fp32"]},
+                         "ms_per_launch": 1e3 * pl32},
+            "fp16s_srt": {"ms_per_launch": 1e3 * pl16, "finite": head["finite"]},
+        },
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def _max_op():
+    try:
+        import torch.distributed as dist
+
+        return dist.ReduceOp.MAX
+    except Exception:  # noqa: BLE001
+        return None
+
+
+if __name__ == "__main__":
+    sys.exit(main())

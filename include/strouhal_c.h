@@ -1,0 +1,161 @@
+/*
+ * strouhal_c.h — C ABI of the GB300-native D3Q19 lattice-Boltzmann step.
+ *
+ * Drop-in boundary for the solver API of the reference's StrouhalCore
+ * (Sources/StrouhalCore/Sim.swift). Every entry point names the Swift member
+ * it replaces. Conventions:
+ *   - every call returns an int status (STRO_OK = 0); on failure the text of
+ *     the error is available from stro_last_error() (thread-local);
+ *   - the library owns all device memory; caller arrays are copied in/out;
+ *   - calls on one handle are synchronous and a handle must not be used from
+ *     two threads at once (Simulation is not thread-safe either);
+ *   - preconditions the reference enforces with a trap (odd step count on a
+ *     probe) return STRO_ERR_STATE instead;
+ *   - cell index n = (z * ny + y) * nx + x; DDF state is 19 planes of N values
+ *     ("shifted" f_i - w_i), plane i at offset i * N, FP32 or IEEE binary16.
+ */
+#ifndef STROUHAL_C_H
+#define STROUHAL_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define STRO_ABI_VERSION 1
+
+/* Status codes. */
+enum {
+    STRO_OK = 0,
+    STRO_ERR_INVALID = 1,   /* bad argument or size */
+    STRO_ERR_NO_DEVICE = 2, /* no CUDA device (Sim.swift:67-71 StrouhalError.noDevice) */
+    STRO_ERR_CUDA = 3,      /* CUDA runtime error (Sim.swift:328-330 command buffer failure) */
+    STRO_ERR_OOM = 4,       /* device allocation failed (Sim.swift:221) */
+    STRO_ERR_STATE = 5,     /* precondition: e.g. probe after an odd step count (Sim.swift:335,360) */
+    STRO_ERR_TIMEOUT = 6    /* a bounded device-side wait gave up */
+};
+
+/* Precision, Sim.swift:5-8: FP32 arithmetic over FP32 or FP16 ("fp16s") DDF storage. */
+enum { STRO_FP32 = 0, STRO_FP16S = 1 };
+
+/* Cell, Sim.swift:46-52 (flag values as Kernels.metal:65-69). */
+enum { STRO_FLUID = 0, STRO_SOLID = 1, STRO_LID = 2, STRO_INFLOW = 3, STRO_OUTFLOW = 4 };
+
+typedef struct stro_ctx stro_ctx;
+typedef struct stro_sim stro_sim;
+
+/* Arguments of Simulation.init (Sim.swift:195-200). omega_minus == omega is SRT. */
+typedef struct stro_sim_desc {
+    int32_t precision;     /* STRO_FP32 or STRO_FP16S */
+    int32_t nx, ny, nz;
+    float omega;           /* omega+ = 1/tau */
+    float omega_minus;     /* omega- (set equal to omega for SRT) */
+    float lid[3];          /* lid wall velocity target */
+    float uin;             /* inflow peak (parabolic) or uniform target */
+    int32_t ramp_steps;    /* cosine ramp length; 0 = none (Sim.swift:258-266) */
+    float force[3];        /* uniform Guo body force density */
+    float c_smago;         /* Smagorinsky Cs^2 (not Cs); 0 = LES off */
+    int32_t wants_forces;  /* enable probe_force (Sim.swift:199,219) */
+} stro_sim_desc;
+
+/* Last error text of the calling thread ("" if none). */
+const char* stro_last_error(void);
+int stro_abi_version(void);
+
+/* ---- context: GPU (Sim.swift:60-78) ------------------------------------ */
+int stro_ctx_create(int device, stro_ctx** out);
+int stro_ctx_destroy(stro_ctx* ctx);
+/* Device name and SM count of the context's GPU. */
+int stro_ctx_info(stro_ctx* ctx, char* name, size_t name_len, int* sm_count);
+
+/* ---- simulation: Simulation (Sim.swift:153-459) ---------------------------- */
+/* Simulation.init (Sim.swift:195-256). flags: N cell codes (STRO_*) in cell
+ * order, replacing the Swift flags(x,y,z) closure; NULL = all fluid. The
+ * state starts at rest (all shifted DDFs zero, Sim.swift:225). */
+int stro_sim_create(stro_ctx* ctx, const stro_sim_desc* desc, const uint8_t* flags,
+                    stro_sim** out);
+int stro_sim_destroy(stro_sim* sim);
+
+/* Mutable properties, Sim.swift:164-172. */
+int stro_sim_set_omega(stro_sim* sim, float omega, float omega_minus);
+int stro_sim_set_lid(stro_sim* sim, const float lid[3]);
+int stro_sim_set_uin(stro_sim* sim, float uin);
+int stro_sim_set_ramp_steps(stro_sim* sim, int32_t ramp_steps);
+int stro_sim_set_force(stro_sim* sim, const float force[3]);
+int stro_sim_set_c_smago(stro_sim* sim, float c_smago);
+int stro_sim_set_inflow_uniform(stro_sim* sim, int inflow_uniform);
+/* sponge = (x0, width, tau); enabled = 0 removes it (Sim.swift:172,277-279). */
+int stro_sim_set_sponge(stro_sim* sim, int enabled, float x0, float width, float tau);
+
+/* Simulation.setSolidFractions (Sim.swift:413-421): N floats, Noble-Torczynski eps. */
+int stro_sim_set_solid_fractions(stro_sim* sim, const float* eps);
+/* Extension with no reference counterpart: per-cell Guo force field added to
+ * the uniform force, 3 planes of N floats (fx plane, fy plane, fz plane).
+ * NULL removes it. */
+int stro_sim_set_force_field(stro_sim* sim, const float* fxyz);
+
+/* Simulation.initField (Sim.swift:424-439, Kernels.metal:393-453):
+ * mode 0 rest, 1 2-D Taylor-Green, 2 3-D Taylor-Green; tau = 1/omega. */
+int stro_sim_init_field(stro_sim* sim, uint32_t mode, float amplitude);
+
+/* Raw state access, replacing direct writes/reads of Simulation.fBuf
+ * (Sim.swift:159; used by Cases.swift:92-98). bytes must be 19*N*elem_size. */
+int stro_sim_upload_state(stro_sim* sim, const void* host, size_t bytes);
+int stro_sim_download_state(stro_sim* sim, void* host, size_t bytes);
+int stro_sim_state_bytes(stro_sim* sim, size_t* bytes);
+
+/* Simulation.run(steps:) (Sim.swift:288-331): advances the lattice, returns
+ * when the GPU has finished. */
+int stro_sim_run(stro_sim* sim, int64_t steps);
+/* stepsDone (Sim.swift:176) and gpuSeconds (Sim.swift:178). */
+int stro_sim_steps_done(stro_sim* sim, int64_t* steps);
+int stro_sim_set_steps_done(stro_sim* sim, int64_t steps);
+int stro_sim_gpu_seconds(stro_sim* sim, double* seconds);
+
+/* Simulation.probeMoments (Sim.swift:334-353): N x (ux, uy, uz, rho) float,
+ * velocity with the Guo half-force shift. Even step count only. */
+int stro_sim_moments(stro_sim* sim, float* out4);
+/* Simulation.probeForce(xRange:yRange:) (Sim.swift:359-372): runs 2 steps with
+ * momentum exchange on the odd one and sums the per-cell force over
+ * x in [x0,x1], y in [y0,y1] (inclusive), all z, in FP64 on the GPU in a fixed
+ * order. Needs wants_forces and an even step count. */
+int stro_sim_probe_force(stro_sim* sim, int32_t x0, int32_t x1, int32_t y0, int32_t y1,
+                         double out[3]);
+/* Sum over cells of |u|^2 (|u|^2 in FP32 as the host loop of
+ * Cases.swift:1240-1243 forms it, summed in FP64 on the GPU). Even steps only. */
+int stro_sim_kinetic_energy(stro_sim* sim, double* sum_u2);
+/* Extension: sum over fluid cells of the local viscous dissipation rate
+ * 2 nu S:S, with S = -(3 omega / (2 rho)) Pi_neq (lattice units, FP64 sum).
+ * Even steps only. */
+int stro_sim_dissipation(stro_sim* sim, double* sum_eps);
+/* Simulation.stateDigest (Sim.swift:441-444): SHA-256 of the raw state bytes,
+ * 64 lowercase hex chars + NUL. */
+int stro_sim_digest(stro_sim* sim, char hex[65]);
+/* Simulation.massSum (Sim.swift:447-458): sum of all 19*N slots in FP64. */
+int stro_sim_mass(stro_sim* sim, double* total);
+/* 1 if every DDF is finite, else 0 (failure detection, Cases.swift:1250-1252). */
+int stro_sim_check_finite(stro_sim* sim, int* all_finite);
+
+/* ---- host utilities ---------------------------------------------------------- */
+/* SHA-256 (FIPS 180-4) of a host buffer as 64 hex chars + NUL: the digest
+ * stro_sim_digest computes over the downloaded state, for caller-held copies. */
+int stro_sha256_hex(const void* data, size_t len, char hex[65]);
+/* Page-locked host memory for fast state transfers (cudaMallocHost). */
+int stro_host_alloc(size_t bytes, void** out);
+int stro_host_free(void* ptr);
+
+/* ---- host geometry helpers (CaseSetups.swift) -------------------------------- */
+/* diskSolidFractions (CaseSetups.swift:6-25): 16x16 subcell sampling, out = nx*ny floats. */
+int stro_disk_solid_fractions(int32_t nx, int32_t ny, double cx, double cy, double r, float* out);
+/* sphereSolidFractions (CaseSetups.swift:68-90) with sub^3 subcells per cell
+ * (the reference uses sub = 8), out = nx*ny*nz floats. */
+int stro_sphere_solid_fractions(int32_t nx, int32_t ny, int32_t nz, double cx, double cy,
+                                double cz, double r, int32_t sub, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STROUHAL_C_H */

@@ -1,0 +1,564 @@
+// CPU oracle for the D3Q19 AA stream-collide step — TEST INFRASTRUCTURE ONLY.
+//
+// A scalar restatement of the reference's Metal kernel arithmetic
+// (Sources/StrouhalCore/Kernels.metal) and of the host-side set-up in
+// Sources/StrouhalCore/Sim.swift, templated on the arithmetic type Real and the
+// DDF storage type Store:
+//   <float, float>     value-identical to the reference kernel at FPXX=float
+//   <float, _Float16>  value-identical to the reference kernel at FPXX=half
+//   <double, double>   the FP64 oracle (same algorithm, double throughout)
+// "Value-identical" means equal as IEEE numbers (+0 == -0): terms whose lattice
+// coefficient is 0 are skipped, which can only change the sign of a zero.
+// The <float,*> instances are pinned against the reference's own kernel source
+// compiled as C++ (oracle/ref_metal_driver.cpp) by tests/test_oracle_pin.py.
+//
+// Only tests/, the smoke check and bench.py's CPU-baseline leg load this
+// library. Build: g++ -O2 -std=c++17 -ffp-contract=off -fopenmp (see Makefile).
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+#include <cstring>
+
+namespace {
+
+// D3Q19 velocity set and pairing, Kernels.metal:38-47 (order is load-bearing:
+// opp(i) = i odd ? i+1 : i-1).
+const int CX[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+const int CY[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1};
+const int CZ[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
+const int OPP[19] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
+
+enum : uint8_t { FLUID = 0, SOLID = 1, LID = 2, INFLOW = 3, OUTFLOW = 4 };
+
+// Per-step uniforms, byte layout of Kernels.metal:49-63 / Sim.swift:10-24.
+struct Params {
+    uint32_t nx, ny, nz, parity;
+    float omega, omegaMinus, uin, cSmago;
+    float fx, fy, fz;
+    uint32_t writeForce;
+    float ulidX, ulidY, ulidZ;
+    uint32_t inflowUniform;
+    float spongeX0, spongeInvW, spongeTau;
+    uint32_t useEps;
+};
+static_assert(sizeof(Params) == 80, "Params layout");
+
+template <class R> inline R weight(int i) {
+    return i == 0 ? R(1) / R(3) : (i < 7 ? R(1) / R(18) : R(1) / R(36));
+}
+template <class R> inline R smagConst();  // 18*sqrt(2), Kernels.metal:156-157
+template <> inline float smagConst<float>() { return 25.455844f; }
+template <> inline double smagConst<double>() { return 18.0 * std::sqrt(2.0); }
+
+// sum_k c_k * v_k over the three components, in x,y,z order, skipping zero
+// coefficients (value-identical to the reference's (float)Cx*vx + ... form).
+template <class R> inline R cdot(int i, R vx, R vy, R vz) {
+    R s = R(0);
+    bool any = false;
+    const int c[3] = {CX[i], CY[i], CZ[i]};
+    const R v[3] = {vx, vy, vz};
+    for (int k = 0; k < 3; ++k) {
+        if (c[k] == 0) continue;
+        const R t = c[k] > 0 ? v[k] : -v[k];
+        s = any ? s + t : t;
+        any = true;
+    }
+    return s;
+}
+
+inline int wrap(int v, int n) {  // Kernels.metal:73-77
+    v += (v < 0) ? n : 0;
+    v -= (v >= n) ? n : 0;
+    return v;
+}
+
+template <class R> struct V3 { R x, y, z; };
+
+// Wall velocity of a moving-wall cell, Kernels.metal:79-87.
+template <class R> inline V3<R> wall_velocity(uint8_t wf, int wy, const Params& p) {
+    if (wf == LID) return {R(p.ulidX), R(p.ulidY), R(p.ulidZ)};
+    if (p.inflowUniform != 0u) return {R(p.uin), R(0), R(0)};
+    const R H = R(p.ny) - R(2);
+    const R yd = R(wy) - R(0.5);
+    const R prof = R(4) * R(p.uin) * yd * (H - yd) / (H * H);
+    return {std::fmax(prof, R(0)), R(0), R(0)};
+}
+
+// TRT + Guo + sponge + Smagorinsky + Noble-Torczynski collision on shifted
+// DDFs, Kernels.metal:105-228. F is the cell's body force (the reference's
+// uniform force plus the optional per-cell field extension).
+template <class R>
+void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt[3]) {
+    R wp = R(p.omega), wm = R(p.omegaMinus);
+    if (R(x) > R(p.spongeX0)) {  // sponge, Kernels.metal:112-123
+        const R frac = std::fmin((R(x) - R(p.spongeX0)) * R(p.spongeInvW), R(1));
+        const R tau0 = R(1) / wp;
+        const R tauS = tau0 + frac * (R(p.spongeTau) - tau0);
+        if (p.omegaMinus == p.omega) {
+            wp = R(1) / tauS;
+            wm = wp;
+        } else {
+            const R lambda = (R(1) / wp - R(0.5)) * (R(1) / wm - R(0.5));
+            wp = R(1) / tauS;
+            wm = R(1) / (R(0.5) + lambda / (tauS - R(0.5)));
+        }
+    }
+    // moments, Kernels.metal:124-138
+    R rhom1 = fh[0];
+    for (int i = 1; i < 19; ++i) rhom1 += fh[i];
+    const R rho = R(1) + rhom1;
+    rhoOut = rho;
+    const R inv = R(1) / rho;
+    R pc[3] = {R(0), R(0), R(0)};
+    bool started[3] = {false, false, false};
+    for (int i = 1; i < 19; ++i) {
+        const int c[3] = {CX[i], CY[i], CZ[i]};
+        for (int k = 0; k < 3; ++k) {
+            if (c[k] == 0) continue;
+            const R t = c[k] > 0 ? fh[i] : -fh[i];
+            pc[k] = started[k] ? pc[k] + t : t;
+            started[k] = true;
+        }
+    }
+    const R ux = (pc[0] + R(0.5) * F[0]) * inv;
+    const R uy = (pc[1] + R(0.5) * F[1]) * inv;
+    const R uz = (pc[2] + R(0.5) * F[2]) * inv;
+    const R u2 = ux * ux + uy * uy + uz * uz;
+
+    if (R(p.cSmago) > R(0)) {  // Smagorinsky, Kernels.metal:140-167
+        R pxx = 0, pyy = 0, pzz = 0, pxy = 0, pxz = 0, pyz = 0;
+        bool sxx = false, syy = false, szz = false, sxy = false, sxz = false, syz = false;
+        auto acc = [](R& a, bool& s, int coef, R d) {
+            if (coef == 0) return;
+            const R t = coef > 0 ? d : -d;
+            a = s ? a + t : t;
+            s = true;
+        };
+        for (int i = 1; i < 19; ++i) {
+            const R cu = R(3) * cdot<R>(i, ux, uy, uz);
+            const R feq = weight<R>(i) * (rhom1 + rho * (cu + R(0.5) * cu * cu - R(1.5) * u2));
+            const R d = fh[i] - feq;
+            acc(pxx, sxx, CX[i] * CX[i], d);
+            acc(pyy, syy, CY[i] * CY[i], d);
+            acc(pzz, szz, CZ[i] * CZ[i], d);
+            acc(pxy, sxy, CX[i] * CY[i], d);
+            acc(pxz, sxz, CX[i] * CZ[i], d);
+            acc(pyz, syz, CY[i] * CZ[i], d);
+        }
+        const R Q = std::sqrt(pxx * pxx + pyy * pyy + pzz * pzz +
+                              R(2) * (pxy * pxy + pxz * pxz + pyz * pyz));
+        const R tau0 = R(1) / wp;
+        const R tauEff =
+            R(0.5) * (tau0 + std::sqrt(tau0 * tau0 + smagConst<R>() * R(p.cSmago) * Q * inv));
+        if (p.omegaMinus == p.omega) {
+            wp = R(1) / tauEff;
+            wm = wp;
+        } else {
+            const R lambda = (R(1) / wp - R(0.5)) * (R(1) / wm - R(0.5));
+            wp = R(1) / tauEff;
+            wm = R(1) / (R(0.5) + lambda / (tauEff - R(0.5)));
+        }
+    }
+
+    const R uF = ux * F[0] + uy * F[1] + uz * F[2];
+    const R ap = R(1) - R(0.5) * wp;
+    const R am = R(1) - R(0.5) * wm;
+    const R w0 = weight<R>(0);
+    const R feq0 = w0 * (rhom1 - R(1.5) * rho * u2);
+    const R s0 = w0 * ap * (R(-3) * uF);
+
+    if (eps == R(0)) {  // Kernels.metal:177-199 (bit-compatible golden path)
+        fh[0] = std::fma(wp, feq0 - fh[0], fh[0]) + s0;
+        for (int i = 1; i < 19; i += 2) {
+            const R w = weight<R>(i);
+            const R cu = R(3) * cdot<R>(i, ux, uy, uz);
+            const R cF = cdot<R>(i, F[0], F[1], F[2]);
+            const R feqp = w * (rhom1 + rho * (R(0.5) * cu * cu - R(1.5) * u2));
+            const R feqm = w * rho * cu;
+            const R fp = R(0.5) * (fh[i] + fh[i + 1]);
+            const R fm = R(0.5) * (fh[i] - fh[i + 1]);
+            const R dp = wp * (feqp - fp);
+            const R dm = wm * (feqm - fm);
+            const R sm = w * am * (R(3) * cF);
+            const R sp = w * ap * (R(3) * cu * cF - R(3) * uF);
+            fh[i] += dp + dm + sp + sm;
+            fh[i + 1] += dp - dm + sp - sm;
+        }
+        return;
+    }
+    // Noble-Torczynski partially saturated cell, Kernels.metal:201-227
+    const R tw = R(1) / wp - R(0.5);
+    const R B = eps * tw / ((R(1) - eps) + tw);
+    const R oneMinusB = R(1) - B;
+    fh[0] += oneMinusB * (wp * (feq0 - fh[0]) + s0);
+    for (int i = 1; i < 19; i += 2) {
+        const R w = weight<R>(i);
+        const R cu = R(3) * cdot<R>(i, ux, uy, uz);
+        const R cF = cdot<R>(i, F[0], F[1], F[2]);
+        const R feqp = w * (rhom1 + rho * (R(0.5) * cu * cu - R(1.5) * u2));
+        const R feqm = w * rho * cu;
+        const R fp = R(0.5) * (fh[i] + fh[i + 1]);
+        const R fm = R(0.5) * (fh[i] - fh[i + 1]);
+        const R dp = wp * (feqp - fp);
+        const R dm = wm * (feqm - fm);
+        const R sm = w * am * (R(3) * cF);
+        const R sp = w * ap * (R(3) * cu * cF - R(3) * uF);
+        const R bounce = B * (fh[i + 1] - fh[i]);
+        fh[i] += oneMinusB * (dp + dm + sp + sm) + bounce;
+        fh[i + 1] += oneMinusB * (dp - dm + sp - sm) - bounce;
+        const int c[3] = {CX[i], CY[i], CZ[i]};
+        for (int k = 0; k < 3; ++k)
+            if (c[k] != 0) nt[k] -= R(2 * c[k]) * bounce;
+    }
+}
+
+template <class R, class S> struct Field {
+    S* f;
+    size_t N;
+    R ld(int i, size_t n) const { return R(f[size_t(i) * N + n]); }
+    void st(int i, size_t n, R v) const { f[size_t(i) * N + n] = S(v); }
+};
+
+template <class R> inline void cell_force(const Params& p, const float* ffield, size_t N,
+                                          size_t n, R F[3]) {
+    F[0] = R(p.fx);
+    F[1] = R(p.fy);
+    F[2] = R(p.fz);
+    if (ffield) {  // per-cell Guo force field extension: F = uniform + field[n]
+        F[0] = R(p.fx + ffield[n]);
+        F[1] = R(p.fy + ffield[N + n]);
+        F[2] = R(p.fz + ffield[2 * N + n]);
+    }
+}
+
+// One thread of the `step` kernel, Kernels.metal:230-355. FOut is float for
+// the FP32-arithmetic instances and double for the FP64 oracle.
+template <class R, class S, class FOut>
+void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMaskBuf,
+               const uint32_t* lMaskBuf, const Params& p, FOut* force, const float* epsBuf,
+               const float* ffield, size_t n) {
+    const size_t N = A.N;
+    if (flags && flags[n] != FLUID) return;
+    const R eps = (p.useEps != 0u && epsBuf) ? R(epsBuf[n]) : R(0);
+    const int nx = int(p.nx), ny = int(p.ny), nz = int(p.nz);
+    const int x = int(n % p.nx);
+    const int t = int(n / p.nx);
+    const int y = t % ny;
+    const int z = t / ny;
+    R F[3];
+    cell_force<R>(p, ffield, N, n, F);
+    R fh[19];
+    R rho = R(1);
+    R nt[3] = {R(0), R(0), R(0)};
+
+    if (p.parity == 0u) {  // even: in-cell pass
+        for (int i = 0; i < 19; ++i) fh[i] = A.ld(i, n);
+        collide<R>(fh, p, x, eps, F, rho, nt);
+        A.st(0, n, fh[0]);
+        for (int i = 1; i < 19; ++i) A.st(OPP[i], n, fh[i]);
+        if (p.writeForce != 0u && eps > R(0) && force) {
+            force[4 * n + 0] = FOut(nt[0]);
+            force[4 * n + 1] = FOut(nt[1]);
+            force[4 * n + 2] = FOut(nt[2]);
+            force[4 * n + 3] = FOut(0);
+        }
+        return;
+    }
+    // odd: streaming pass with walls
+    const uint32_t sMask = sMaskBuf ? sMaskBuf[n] : 0u;
+    const uint32_t lMask = lMaskBuf ? lMaskBuf[n] : 0u;
+    R a[3] = {R(0), R(0), R(0)};
+    auto acc_sub = [&](int i, R v) {  // a -= c_i * v
+        const int c[3] = {CX[i], CY[i], CZ[i]};
+        for (int k = 0; k < 3; ++k)
+            if (c[k] != 0) a[k] = c[k] > 0 ? a[k] - v : a[k] + v;
+    };
+    auto acc_add = [&](int i, R v) {  // a += c_i * v
+        const int c[3] = {CX[i], CY[i], CZ[i]};
+        for (int k = 0; k < 3; ++k)
+            if (c[k] != 0) a[k] = c[k] > 0 ? a[k] + v : a[k] - v;
+    };
+    uint32_t deferred = 0;
+    fh[0] = A.ld(0, n);
+    for (int i = 1; i < 19; ++i) {
+        const int srcBit = OPP[i] - 1;
+        if ((sMask >> srcBit) & 1u) {
+            fh[i] = A.ld(i, n);
+            if ((lMask >> srcBit) & 1u) deferred |= (1u << i);
+            if (p.writeForce != 0u) acc_sub(i, fh[i]);
+        } else {
+            const int sx = wrap(x - CX[i], nx), sy = wrap(y - CY[i], ny), sz = wrap(z - CZ[i], nz);
+            const size_t s = (size_t(sz) * ny + sy) * nx + sx;
+            fh[i] = A.ld(OPP[i], s);
+        }
+    }
+    if (deferred != 0u) {
+        for (int i = 1; i < 19; ++i) {
+            if (!((deferred >> i) & 1u)) continue;
+            const int sy = wrap(y - CY[i], ny);
+            const size_t s = (size_t(wrap(z - CZ[i], nz)) * ny + sy) * nx + wrap(x - CX[i], nx);
+            const uint8_t wf = flags[s];
+            if (wf == OUTFLOW) {
+                fh[i] = -fh[i];
+            } else {
+                const V3<R> uw = wall_velocity<R>(wf, sy, p);
+                const R cu = cdot<R>(i, uw.x, uw.y, uw.z);
+                const R corr = R(6) * weight<R>(i) * cu;
+                fh[i] += corr;
+                if (p.writeForce != 0u) acc_sub(i, corr);
+            }
+        }
+    }
+    collide<R>(fh, p, x, eps, F, rho, nt);
+    a[0] += nt[0];
+    a[1] += nt[1];
+    a[2] += nt[2];
+    A.st(0, n, fh[0]);
+    for (int i = 1; i < 19; ++i) {
+        const int dstBit = i - 1;
+        if ((sMask >> dstBit) & 1u) {
+            R corr = R(0);
+            R sign = R(1);
+            bool has_corr = false;
+            if ((lMask >> dstBit) & 1u) {
+                const int dy = wrap(y + CY[i], ny);
+                const size_t d =
+                    (size_t(wrap(z + CZ[i], nz)) * ny + dy) * nx + wrap(x + CX[i], nx);
+                const uint8_t wf = flags[d];
+                if (wf == OUTFLOW) {
+                    sign = R(-1);
+                } else {
+                    const V3<R> uw = wall_velocity<R>(wf, dy, p);
+                    corr = R(6) * weight<R>(i) * cdot<R>(i, uw.x, uw.y, uw.z);
+                    has_corr = true;
+                }
+            }
+            const R sv = sign * fh[i];
+            A.st(OPP[i], n, has_corr ? sv - corr : sv);
+            if (p.writeForce != 0u) acc_add(i, sv + R(2) * weight<R>(i));
+        } else {
+            const int dx = wrap(x + CX[i], nx), dy = wrap(y + CY[i], ny), dz = wrap(z + CZ[i], nz);
+            const size_t d = (size_t(dz) * ny + dy) * nx + dx;
+            A.st(i, d, fh[i]);
+        }
+    }
+    if (p.writeForce != 0u && (sMask != 0u || eps > R(0)) && force) {
+        force[4 * n + 0] = FOut(a[0]);
+        force[4 * n + 1] = FOut(a[1]);
+        force[4 * n + 2] = FOut(a[2]);
+        force[4 * n + 3] = FOut(0);
+    }
+}
+
+template <class R, class S, class FOut>
+void step_all(void* f, const uint8_t* flags, const uint32_t* sm, const uint32_t* lm,
+              const Params& p, FOut* force, const float* eps, const float* ffield, int threads) {
+    const size_t N = size_t(p.nx) * p.ny * p.nz;
+    Field<R, S> A{static_cast<S*>(f), N};
+    // The AA pattern gives every slot one reader and one writer, and they are the
+    // same thread, so cells may be processed in any order or in parallel.
+#pragma omp parallel for schedule(static) num_threads(threads > 0 ? threads : 1) if (threads > 1)
+    for (long long n = 0; n < (long long)N; ++n)
+        step_cell<R, S, FOut>(A, flags, sm, lm, p, force, eps, ffield, size_t(n));
+}
+
+// momentsEven, Kernels.metal:359-380 (division by rho, not by a reciprocal).
+template <class R, class S>
+void moments_all(const void* fv, const uint8_t* flags, const Params& p, const float* ffield,
+                 R* out) {
+    const size_t N = size_t(p.nx) * p.ny * p.nz;
+    const S* f = static_cast<const S*>(fv);
+    for (size_t n = 0; n < N; ++n) {
+        if (flags && flags[n] != FLUID) {
+            out[4 * n] = out[4 * n + 1] = out[4 * n + 2] = out[4 * n + 3] = R(0);
+            continue;
+        }
+        R v[19];
+        for (int i = 0; i < 19; ++i) v[i] = R(f[size_t(i) * N + n]);
+        R rhom1 = v[0];
+        for (int i = 1; i < 19; ++i) rhom1 += v[i];
+        R pc[3] = {0, 0, 0};
+        bool st[3] = {false, false, false};
+        for (int i = 1; i < 19; ++i) {
+            const int c[3] = {CX[i], CY[i], CZ[i]};
+            for (int k = 0; k < 3; ++k) {
+                if (c[k] == 0) continue;
+                const R t = c[k] > 0 ? v[i] : -v[i];
+                pc[k] = st[k] ? pc[k] + t : t;
+                st[k] = true;
+            }
+        }
+        R F[3];
+        cell_force<R>(p, ffield, N, n, F);
+        const R rho = R(1) + rhom1;
+        out[4 * n + 0] = (pc[0] + R(0.5) * F[0]) / rho;
+        out[4 * n + 1] = (pc[1] + R(0.5) * F[1]) / rho;
+        out[4 * n + 2] = (pc[2] + R(0.5) * F[2]) / rho;
+        out[4 * n + 3] = rho;
+    }
+}
+
+// initField, Kernels.metal:393-453. Trigonometric values are evaluated in
+// double and rounded to R, so FP32 results are the correctly rounded sin/cos.
+template <class R> inline R tsin(R a) { return R(std::sin(double(a))); }
+template <class R> inline R tcos(R a) { return R(std::cos(double(a))); }
+
+template <class R, class S>
+void init_all(void* fv, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t mode, float amplitude,
+              float tau) {
+    const size_t N = size_t(nx) * ny * nz;
+    S* f = static_cast<S*>(fv);
+    const R A = R(amplitude);
+    const R pi = sizeof(R) == 4 ? R(3.14159265358979323846f) : R(3.14159265358979323846);
+    for (size_t n = 0; n < N; ++n) {
+        R ux = 0, uy = 0, uz = 0, sxx = 0, sxz = 0, syz = 0, rhom1 = 0;
+        const uint32_t x = uint32_t(n % nx), t = uint32_t(n / nx), y = t % ny, z = t / ny;
+        if (mode == 1u) {
+            const R kx = R(2) * pi / R(nx), ky = R(2) * pi / R(ny);
+            const R xa = R(x) + R(0.5), ya = R(y) + R(0.5);
+            ux = A * tsin(kx * xa) * tcos(ky * ya);
+            uy = -A * tcos(kx * xa) * tsin(ky * ya);
+            sxx = A * kx * tcos(kx * xa) * tcos(ky * ya);
+            rhom1 = R(0.75) * A * A * (tcos(R(2) * kx * xa) + tcos(R(2) * ky * ya));
+        }
+        if (mode == 2u) {
+            const R kx = R(2) * pi / R(nx), ky = R(2) * pi / R(ny), kz = R(2) * pi / R(nz);
+            const R xa = kx * (R(x) + R(0.5)), ya = ky * (R(y) + R(0.5)), za = kz * (R(z) + R(0.5));
+            ux = A * tsin(xa) * tcos(ya) * tcos(za);
+            uy = -A * tcos(xa) * tsin(ya) * tcos(za);
+            sxx = A * kx * tcos(xa) * tcos(ya) * tcos(za);
+            sxz = R(-0.5) * A * kz * tsin(xa) * tcos(ya) * tsin(za);
+            syz = R(0.5) * A * kz * tcos(xa) * tsin(ya) * tsin(za);
+            rhom1 = R(0.1875) * A * A * (tcos(R(2) * xa) + tcos(R(2) * ya)) * (tcos(R(2) * za) + R(2));
+        }
+        const R rho = R(1) + rhom1;
+        const R u2 = ux * ux + uy * uy + uz * uz;
+        for (int i = 0; i < 19; ++i) {
+            const R cu = R(3) * (R(CX[i]) * ux + R(CY[i]) * uy + R(CZ[i]) * uz);
+            const R feq = weight<R>(i) * (rhom1 + rho * (cu + R(0.5) * cu * cu - R(1.5) * u2));
+            const R cc = R(CX[i] * CX[i] - CY[i] * CY[i]);
+            const R scc = sxx * cc + R(2) * sxz * R(CX[i] * CZ[i]) + R(2) * syz * R(CY[i] * CZ[i]);
+            const R fneq = R(-3) * weight<R>(i) * R(tau) * scc;
+            f[size_t(i) * N + n] = S(feq + fneq);
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+// kind: 0 = <float,float>, 1 = <float,_Float16>, 2 = <double,double>.
+
+// Neighbour masks, Sim.swift:227-255: bit i-1 of solid_mask is set when the
+// neighbour at n + c_i is not fluid; lid_mask marks the moving-wall subset.
+int orc_masks(const uint8_t* flags, int nx, int ny, int nz, uint32_t* solid_mask,
+              uint32_t* lid_mask) {
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                const size_t idx = (size_t(z) * ny + y) * nx + x;
+                uint32_t s = 0, l = 0;
+                if (flags[idx] == FLUID) {
+                    for (int i = 1; i < 19; ++i) {
+                        const int xn = (x + CX[i] + nx) % nx, yn = (y + CY[i] + ny) % ny,
+                                  zn = (z + CZ[i] + nz) % nz;
+                        const uint8_t c = flags[(size_t(zn) * ny + yn) * nx + xn];
+                        if (c == FLUID) continue;
+                        s |= 1u << (i - 1);
+                        if (c == LID || c == INFLOW || c == OUTFLOW) l |= 1u << (i - 1);
+                    }
+                }
+                solid_mask[idx] = s;
+                lid_mask[idx] = l;
+            }
+    return 0;
+}
+
+// Per-step uniforms with the C1 cosine ramp, Sim.swift:258-281. sponge_width
+// <= 0 disables the sponge (x0 = 1e9, 1/w = 0, tau = 1).
+int orc_params(void* out, uint32_t nx, uint32_t ny, uint32_t nz, long long step, float omega,
+               float omega_minus, float uin_target, long long ramp_steps, float cSmago,
+               const float force[3], int write_force, const float lid[3], int inflow_uniform,
+               float sponge_x0, float sponge_width, float sponge_tau, int use_eps) {
+    Params p{};
+    float r = 1.0f;
+    if (ramp_steps > 0) {
+        const double x = std::fmin(1.0, double(step) / double(ramp_steps));
+        r = 1.0f * float(0.5 * (1.0 - std::cos(3.141592653589793 * x)));
+    }
+    p.nx = nx; p.ny = ny; p.nz = nz;
+    p.parity = uint32_t(step & 1);
+    p.omega = omega; p.omegaMinus = omega_minus;
+    p.uin = uin_target * r;
+    p.cSmago = cSmago;
+    p.fx = force[0]; p.fy = force[1]; p.fz = force[2];
+    p.writeForce = write_force ? 1u : 0u;
+    p.ulidX = lid[0] * r; p.ulidY = lid[1] * r; p.ulidZ = lid[2] * r;
+    p.inflowUniform = inflow_uniform ? 1u : 0u;
+    if (sponge_width > 0.0f) {
+        p.spongeX0 = sponge_x0; p.spongeInvW = 1.0f / sponge_width; p.spongeTau = sponge_tau;
+    } else {
+        p.spongeX0 = 1e9f; p.spongeInvW = 0.0f; p.spongeTau = 1.0f;
+    }
+    p.useEps = use_eps ? 1u : 0u;
+    std::memcpy(out, &p, sizeof p);
+    return 0;
+}
+
+// One full step over all cells. force: N*4 float (kinds 0/1) or double (kind 2),
+// or null. ffield: optional per-cell force field, 3 planes of N floats.
+int orc_step(int kind, void* f, const uint8_t* flags, const uint32_t* solid_mask,
+             const uint32_t* lid_mask, const void* params, void* force, const float* eps,
+             const float* ffield, int threads) {
+    Params p;
+    std::memcpy(&p, params, sizeof p);
+    switch (kind) {
+        case 0: step_all<float, float, float>(f, flags, solid_mask, lid_mask, p,
+                                              static_cast<float*>(force), eps, ffield, threads);
+                return 0;
+        case 1: step_all<float, _Float16, float>(f, flags, solid_mask, lid_mask, p,
+                                                 static_cast<float*>(force), eps, ffield, threads);
+                return 0;
+        case 2: step_all<double, double, double>(f, flags, solid_mask, lid_mask, p,
+                                                 static_cast<double*>(force), eps, ffield, threads);
+                return 0;
+    }
+    return 1;
+}
+
+// (ux, uy, uz, rho) per cell; out is N*4 float (kinds 0/1) or double (kind 2).
+int orc_moments(int kind, const void* f, const uint8_t* flags, const void* params,
+                const float* ffield, void* out) {
+    Params p;
+    std::memcpy(&p, params, sizeof p);
+    switch (kind) {
+        case 0: moments_all<float, float>(f, flags, p, ffield, static_cast<float*>(out)); return 0;
+        case 1: moments_all<float, _Float16>(f, flags, p, ffield, static_cast<float*>(out)); return 0;
+        case 2: moments_all<double, double>(f, flags, p, ffield, static_cast<double*>(out)); return 0;
+    }
+    return 1;
+}
+
+int orc_init_field(int kind, void* f, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t mode,
+                   float amplitude, float tau) {
+    switch (kind) {
+        case 0: init_all<float, float>(f, nx, ny, nz, mode, amplitude, tau); return 0;
+        case 1: init_all<float, _Float16>(f, nx, ny, nz, mode, amplitude, tau); return 0;
+        case 2: init_all<double, double>(f, nx, ny, nz, mode, amplitude, tau); return 0;
+    }
+    return 1;
+}
+
+// Sum of all 19*N shifted DDFs in index order, in double (Sim.swift:447-458).
+double orc_mass(int kind, const void* f, size_t count) {
+    double total = 0.0;
+    for (size_t k = 0; k < count; ++k) {
+        if (kind == 0) total += double(static_cast<const float*>(f)[k]);
+        else if (kind == 1) total += double(static_cast<const _Float16*>(f)[k]);
+        else total += static_cast<const double*>(f)[k];
+    }
+    return total;
+}
+
+}  // extern "C"

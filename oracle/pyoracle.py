@@ -1,0 +1,250 @@
+"""ctypes front end of the CPU oracle — TEST INFRASTRUCTURE ONLY.
+
+`OracleSim` drives the scalar restatement in lbm_oracle.cpp with the same
+set-up and run semantics as the reference's `Simulation`
+(Sources/StrouhalCore/Sim.swift:195-458): per-cell flags, neighbour masks,
+per-step uniforms with the cosine ramp, AA parity, the two-step force probe,
+moments, mass sum and SHA-256 state digest. With backend="ref" the same driver
+runs the reference's own kernel source compiled as C++ (oracle/_ref), which is
+how the restatement is pinned.
+
+Imported only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+leg; the product never loads anything from oracle/.
+"""
+import ctypes
+import hashlib
+import os
+import struct
+
+import numpy as np
+
+from . import build_oracle as _build
+
+KIND_F32, KIND_F16, KIND_F64 = 0, 1, 2
+_DTYPES = {KIND_F32: np.float32, KIND_F16: np.float16, KIND_F64: np.float64}
+
+CX = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0])
+CY = np.array([0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1])
+CZ = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1])
+OPP = np.array([0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17])
+
+FLUID, SOLID, LID, INFLOW, OUTFLOW = 0, 1, 2, 3, 4
+
+_lib = None
+_ref = None
+_P = ctypes.c_void_p
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.oracle_lib_path()
+        if not os.path.exists(path):
+            _build.build_oracle()
+        L = ctypes.CDLL(path)
+        L.orc_masks.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P]
+        L.orc_params.argtypes = ([_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                  ctypes.c_longlong, ctypes.c_float, ctypes.c_float,
+                                  ctypes.c_float, ctypes.c_longlong, ctypes.c_float, _P,
+                                  ctypes.c_int, _P, ctypes.c_int, ctypes.c_float,
+                                  ctypes.c_float, ctypes.c_float, ctypes.c_int])
+        L.orc_step.argtypes = [ctypes.c_int, _P, _P, _P, _P, _P, _P, _P, _P, ctypes.c_int]
+        L.orc_moments.argtypes = [ctypes.c_int, _P, _P, _P, _P, _P]
+        L.orc_init_field.argtypes = [ctypes.c_int, _P, ctypes.c_uint32, ctypes.c_uint32,
+                                     ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
+                                     ctypes.c_float]
+        L.orc_mass.argtypes = [ctypes.c_int, _P, ctypes.c_size_t]
+        L.orc_mass.restype = ctypes.c_double
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's kernel source compiled as C++, or None when unavailable."""
+    global _ref
+    if _ref is None:
+        path = _build.ref_lib_path()
+        if not os.path.exists(path):
+            if _build.build_ref() is None:
+                return None
+        L = ctypes.CDLL(path)
+        L.ref_step.argtypes = [ctypes.c_int, _P, _P, _P, _P, _P, _P, _P]
+        L.ref_moments.argtypes = [ctypes.c_int, _P, _P, _P, _P]
+        L.ref_init_field.argtypes = [ctypes.c_int, _P, _P]
+        _ref = L
+    return _ref
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def trt_omegas(tau, lam=None):
+    """tau -> (omega+, omega-), Sim.swift:188-193 (lam None = SRT)."""
+    wp = 1.0 / tau
+    if lam is None:
+        return float(np.float32(wp)), float(np.float32(wp))
+    tm = 0.5 + lam / (tau - 0.5)
+    return float(np.float32(wp)), float(np.float32(1.0 / tm))
+
+
+def masks(flags, nx, ny, nz):
+    flags = np.ascontiguousarray(flags, dtype=np.uint8)
+    sm = np.zeros(nx * ny * nz, np.uint32)
+    lm = np.zeros(nx * ny * nz, np.uint32)
+    lib().orc_masks(_ptr(flags), nx, ny, nz, _ptr(sm), _ptr(lm))
+    return sm, lm
+
+
+def flags_from(fn, nx, ny, nz):
+    """Evaluate a flags(x, y, z) -> Cell callable in the reference's x-fastest order."""
+    fl = np.zeros(nx * ny * nz, np.uint8)
+    for z in range(nz):
+        for y in range(ny):
+            for x in range(nx):
+                fl[(z * ny + y) * nx + x] = int(fn(x, y, z))
+    return fl
+
+
+class OracleSim:
+    """CPU mirror of `Simulation` over the oracle (or the compiled reference)."""
+
+    def __init__(self, nx, ny, nz, omega, omegaMinus=None, lid=(0.0, 0.0, 0.0), uin=0.0,
+                 rampSteps=0, force=(0.0, 0.0, 0.0), cSmago=0.0, wantsForces=False,
+                 flags=None, kind=KIND_F32, backend="oracle", threads=1):
+        self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
+        self.N = self.nx * self.ny * self.nz
+        self.kind = kind
+        self.backend = backend
+        self.threads = threads
+        if backend == "ref" and kind == KIND_F64:
+            raise ValueError("the reference source has no FP64 build")
+        self.omega = float(np.float32(omega))
+        self.omegaMinus = float(np.float32(omega if omegaMinus is None else omegaMinus))
+        self.lidVel = tuple(float(np.float32(v)) for v in lid)
+        self.uinTarget = float(np.float32(uin))
+        self.rampSteps = int(rampSteps)
+        self.force = tuple(float(np.float32(v)) for v in force)
+        self.cSmago = float(np.float32(cSmago))
+        self.inflowUniform = False
+        self.sponge = None
+        self.stepsDone = 0
+        self.f = np.zeros((19, self.N), _DTYPES[kind])
+        if flags is None:
+            self.flags = np.zeros(self.N, np.uint8)
+        elif callable(flags):
+            self.flags = flags_from(flags, self.nx, self.ny, self.nz)
+        else:
+            self.flags = np.ascontiguousarray(flags, dtype=np.uint8).reshape(-1).copy()
+        self.solidMask, self.lidMask = masks(self.flags, self.nx, self.ny, self.nz)
+        fdt = np.float64 if kind == KIND_F64 else np.float32
+        self.forceBuf = np.zeros((self.N, 4), fdt) if wantsForces else None
+        self.eps = None
+        self.forceField = None
+        self._force_steps = set()
+
+    # -- set-up -------------------------------------------------------------
+    def setSolidFractions(self, eps):
+        eps = np.ascontiguousarray(eps, dtype=np.float32).reshape(-1)
+        assert eps.size == self.N
+        self.eps = eps.copy()
+
+    def setForceField(self, field):
+        """Per-cell Guo force field, shape (3, N) float32; None clears it."""
+        if field is None:
+            self.forceField = None
+            return
+        field = np.ascontiguousarray(field, dtype=np.float32).reshape(3, self.N)
+        if self.backend == "ref":
+            raise ValueError("the reference has no per-cell force field")
+        self.forceField = field.copy()
+
+    def initField(self, mode, amplitude):
+        tau = float(np.float32(1.0) / np.float32(self.omega))
+        if self.backend == "ref":
+            ip = struct.pack("4I4f", self.nx, self.ny, self.nz, mode, amplitude, tau, 0.0, 0.0)
+            ref_lib().ref_init_field(int(self.kind == KIND_F16), _ptr(self.f), ip)
+        else:
+            lib().orc_init_field(self.kind, _ptr(self.f), self.nx, self.ny, self.nz, mode,
+                                 amplitude, tau)
+
+    # -- stepping -----------------------------------------------------------
+    def params(self, step, writeForce=False):
+        buf = ctypes.create_string_buffer(80)
+        f3 = (ctypes.c_float * 3)(*self.force)
+        l3 = (ctypes.c_float * 3)(*self.lidVel)
+        if self.sponge is None:
+            sx0, sw, stau = 1e9, 0.0, 1.0
+        else:
+            sx0, sw, stau = self.sponge
+        lib().orc_params(buf, self.nx, self.ny, self.nz, step, self.omega, self.omegaMinus,
+                         self.uinTarget, self.rampSteps, self.cSmago, f3, int(writeForce), l3,
+                         int(self.inflowUniform), sx0, sw, stau, int(self.eps is not None))
+        return buf.raw
+
+    def run(self, steps):
+        dummy_eps = np.zeros(4, np.float32)
+        for _ in range(int(steps)):
+            t = self.stepsDone
+            p = self.params(t, writeForce=(t in self._force_steps))
+            eps = self.eps if self.eps is not None else dummy_eps
+            if self.backend == "ref":
+                force = self.forceBuf if self.forceBuf is not None else np.zeros((1, 4), np.float32)
+                ref_lib().ref_step(int(self.kind == KIND_F16), _ptr(self.f), _ptr(self.flags),
+                                   _ptr(self.solidMask), _ptr(self.lidMask), p, _ptr(force),
+                                   _ptr(eps))
+            else:
+                lib().orc_step(self.kind, _ptr(self.f), _ptr(self.flags), _ptr(self.solidMask),
+                               _ptr(self.lidMask), p, _ptr(self.forceBuf), _ptr(eps),
+                               _ptr(self.forceField), self.threads)
+            self.stepsDone += 1
+
+    # -- probes ---------------------------------------------------------------
+    def probeMoments(self):
+        if self.stepsDone % 2 != 0:
+            raise RuntimeError("moments probe requires even step count")
+        p = self.params(self.stepsDone)
+        if self.kind == KIND_F64:
+            out = np.zeros((self.N, 4), np.float64)
+        else:
+            out = np.zeros((self.N, 4), np.float32)
+        if self.backend == "ref":
+            ref_lib().ref_moments(int(self.kind == KIND_F16), _ptr(self.f), _ptr(self.flags), p,
+                                  _ptr(out))
+        else:
+            lib().orc_moments(self.kind, _ptr(self.f), _ptr(self.flags), p,
+                              _ptr(self.forceField), _ptr(out))
+        return out
+
+    def probeForce(self, xRange, yRange):
+        """Two steps with the odd-pass momentum exchange; box sum in double (Sim.swift:359-372)."""
+        if self.stepsDone % 2 != 0:
+            raise RuntimeError("force probe requires even step count")
+        if self.forceBuf is None:
+            raise RuntimeError("force probe requires wantsForces")
+        self.forceBuf[:] = 0
+        self._force_steps = {self.stepsDone + 1}
+        self.run(2)
+        self._force_steps = set()
+        fb = self.forceBuf.reshape(self.nz, self.ny, self.nx, 4)
+        tot = np.zeros(3)
+        for z in range(self.nz):
+            for y in range(yRange[0], yRange[1] + 1):
+                for x in range(xRange[0], xRange[1] + 1):
+                    tot += fb[z, y, x, :3].astype(np.float64)
+        return tot
+
+    def kineticEnergySum(self):
+        """sum over cells of |u|^2, |u|^2 formed in the storage arithmetic, summed in double."""
+        m = self.probeMoments()
+        if self.kind == KIND_F64:
+            return float(np.sum(m[:, 0] * m[:, 0] + m[:, 1] * m[:, 1] + m[:, 2] * m[:, 2]))
+        u2 = (m[:, 0] * m[:, 0] + m[:, 1] * m[:, 1]) + m[:, 2] * m[:, 2]
+        return float(np.sum(u2.astype(np.float64)))
+
+    def massSum(self):
+        return float(lib().orc_mass(self.kind, _ptr(self.f), self.f.size))
+
+    @property
+    def stateDigest(self):
+        return hashlib.sha256(self.f.tobytes()).hexdigest()

@@ -1,0 +1,455 @@
+"""strouhal_gb300 — GB300-native D3Q19 lattice-Boltzmann step behind a C ABI.
+
+Python mirror (ctypes) of the reference's StrouhalCore solver API
+(Sources/StrouhalCore/Sim.swift): `GPU`, `Simulation`, `Precision`, `Cell`,
+`StrouhalError` and `trtOmegas`, plus the solid-fraction generators of
+CaseSetups.swift. Every call goes through libstrouhal_gb300.so
+(include/strouhal_c.h); there is no CPU fallback — importing the wrapper
+without the built library, or running without a CUDA device, raises.
+"""
+import ctypes
+import enum
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libstrouhal_gb300.so")
+
+_lib = None
+_P = ctypes.c_void_p
+
+
+class StrouhalError(RuntimeError):
+    """Mirror of StrouhalError (Sim.swift:127-136); `code` is the C status."""
+
+    def __init__(self, code, message):
+        super().__init__(message)
+        self.code = code
+
+
+class Precision(str, enum.Enum):
+    """Sim.swift:5-8. fp32 storage or Lehmann-shifted fp16 storage (FP32 math)."""
+    fp32 = "fp32"
+    fp16s = "fp16s"
+
+    @property
+    def ddfBytes(self):
+        return 4 if self is Precision.fp32 else 2
+
+
+class Cell(enum.IntEnum):
+    """Sim.swift:46-52."""
+    fluid = 0
+    solid = 1
+    lid = 2
+    inflow = 3
+    outflow = 4
+
+
+class _Desc(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int32), ("nx", ctypes.c_int32), ("ny", ctypes.c_int32),
+                ("nz", ctypes.c_int32), ("omega", ctypes.c_float), ("omega_minus", ctypes.c_float),
+                ("lid", ctypes.c_float * 3), ("uin", ctypes.c_float),
+                ("ramp_steps", ctypes.c_int32), ("force", ctypes.c_float * 3),
+                ("c_smago", ctypes.c_float), ("wants_forces", ctypes.c_int32)]
+
+
+def lib():
+    """Load the C-ABI library (built by __graft_entry__.build() / build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise StrouhalError(-1, "libstrouhal_gb300.so is not built (%s); run "
+                                "python -c 'import __graft_entry__ as g; g.build()'" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    c_int, c_float, c_double, c_i64 = ctypes.c_int, ctypes.c_float, ctypes.c_double, ctypes.c_int64
+    sig = {
+        "stro_last_error": ([], ctypes.c_char_p),
+        "stro_abi_version": ([], c_int),
+        "stro_ctx_create": ([c_int, ctypes.POINTER(_P)], c_int),
+        "stro_ctx_destroy": ([_P], c_int),
+        "stro_ctx_info": ([_P, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(c_int)], c_int),
+        "stro_sim_create": ([_P, ctypes.POINTER(_Desc), _P, ctypes.POINTER(_P)], c_int),
+        "stro_sim_destroy": ([_P], c_int),
+        "stro_sim_set_omega": ([_P, c_float, c_float], c_int),
+        "stro_sim_set_lid": ([_P, _P], c_int),
+        "stro_sim_set_uin": ([_P, c_float], c_int),
+        "stro_sim_set_ramp_steps": ([_P, ctypes.c_int32], c_int),
+        "stro_sim_set_force": ([_P, _P], c_int),
+        "stro_sim_set_c_smago": ([_P, c_float], c_int),
+        "stro_sim_set_inflow_uniform": ([_P, c_int], c_int),
+        "stro_sim_set_sponge": ([_P, c_int, c_float, c_float, c_float], c_int),
+        "stro_sim_set_solid_fractions": ([_P, _P], c_int),
+        "stro_sim_set_force_field": ([_P, _P], c_int),
+        "stro_sim_init_field": ([_P, ctypes.c_uint32, c_float], c_int),
+        "stro_sim_upload_state": ([_P, _P, ctypes.c_size_t], c_int),
+        "stro_sim_download_state": ([_P, _P, ctypes.c_size_t], c_int),
+        "stro_sim_state_bytes": ([_P, ctypes.POINTER(ctypes.c_size_t)], c_int),
+        "stro_sim_run": ([_P, c_i64], c_int),
+        "stro_sim_steps_done": ([_P, ctypes.POINTER(c_i64)], c_int),
+        "stro_sim_set_steps_done": ([_P, c_i64], c_int),
+        "stro_sim_gpu_seconds": ([_P, ctypes.POINTER(c_double)], c_int),
+        "stro_sim_moments": ([_P, _P], c_int),
+        "stro_sim_probe_force": ([_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                  ctypes.c_int32, _P], c_int),
+        "stro_sim_kinetic_energy": ([_P, ctypes.POINTER(c_double)], c_int),
+        "stro_sim_dissipation": ([_P, ctypes.POINTER(c_double)], c_int),
+        "stro_sim_digest": ([_P, ctypes.c_char_p], c_int),
+        "stro_sim_mass": ([_P, ctypes.POINTER(c_double)], c_int),
+        "stro_sim_check_finite": ([_P, ctypes.POINTER(c_int)], c_int),
+        "stro_sha256_hex": ([_P, ctypes.c_size_t, ctypes.c_char_p], c_int),
+        "stro_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(_P)], c_int),
+        "stro_host_free": ([_P], c_int),
+        "stro_disk_solid_fractions": ([ctypes.c_int32, ctypes.c_int32, c_double, c_double,
+                                       c_double, _P], c_int),
+        "stro_sphere_solid_fractions": ([ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                         c_double, c_double, c_double, c_double, ctypes.c_int32,
+                                         _P], c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        msg = lib().stro_last_error().decode("utf-8", "replace")
+        raise StrouhalError(rc, msg)
+
+
+def _f3(v):
+    return (ctypes.c_float * 3)(*[float(x) for x in v])
+
+
+def trtOmegas(tau, lam=None):
+    """tau -> (omega+, omega-) via the TRT magic parameter Lambda (Sim.swift:188-193)."""
+    wp = 1.0 / tau
+    if lam is None:
+        w = float(np.float32(wp))
+        return w, w
+    tm = 0.5 + lam / (tau - 0.5)
+    return float(np.float32(wp)), float(np.float32(1.0 / tm))
+
+
+class GPU:
+    """One CUDA device and one stream (Sim.swift:60-78)."""
+
+    def __init__(self, device=0):
+        self._h = _P()
+        _check(lib().stro_ctx_create(int(device), ctypes.byref(self._h)))
+        name = ctypes.create_string_buffer(256)
+        sms = ctypes.c_int()
+        _check(lib().stro_ctx_info(self._h, name, 256, ctypes.byref(sms)))
+        self.name = name.value.decode()
+        self.smCount = sms.value
+
+    def close(self):
+        if self._h:
+            lib().stro_ctx_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _flags_array(flags, nx, ny, nz):
+    N = nx * ny * nz
+    if flags is None:
+        return None
+    if callable(flags):
+        arr = np.zeros((nz, ny, nx), np.uint8)
+        for z in range(nz):
+            for y in range(ny):
+                for x in range(nx):
+                    arr[z, y, x] = int(flags(x, y, z))
+        return arr.reshape(-1)
+    arr = np.ascontiguousarray(flags, dtype=np.uint8).reshape(-1)
+    if arr.size != N:
+        raise ValueError("flags must hold nx*ny*nz cell codes")
+    return arr
+
+
+class Simulation:
+    """Mirror of Simulation (Sim.swift:153-459) over the C ABI.
+
+    `flags` is an array of N cell codes in x-fastest order, or a callable
+    flags(x, y, z) -> Cell like the Swift initializer's closure.
+    """
+
+    def __init__(self, gpu, precision=Precision.fp32, nx=1, ny=1, nz=1, omega=1.0,
+                 omegaMinus=None, lid=(0.0, 0.0, 0.0), uin=0.0, rampSteps=0,
+                 force=(0.0, 0.0, 0.0), cSmago=0.0, wantsForces=False, flags=None):
+        self.gpu = gpu
+        self.precision = Precision(precision)
+        self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
+        d = _Desc()
+        d.precision = 0 if self.precision is Precision.fp32 else 1
+        d.nx, d.ny, d.nz = self.nx, self.ny, self.nz
+        d.omega = omega
+        d.omega_minus = omega if omegaMinus is None else omegaMinus
+        d.lid = _f3(lid)
+        d.uin = uin
+        d.ramp_steps = int(rampSteps)
+        d.force = _f3(force)
+        d.c_smago = cSmago
+        d.wants_forces = 1 if wantsForces else 0
+        fl = _flags_array(flags, self.nx, self.ny, self.nz)
+        self._flags = fl
+        self._h = _P()
+        _check(lib().stro_sim_create(gpu._h, ctypes.byref(d),
+                                     None if fl is None else fl.ctypes.data, ctypes.byref(self._h)))
+        self._omega = float(np.float32(d.omega))
+        self._omegaMinus = float(np.float32(d.omega_minus))
+        self._lid = tuple(float(np.float32(v)) for v in lid)
+        self._uin = float(np.float32(uin))
+        self._ramp = int(rampSteps)
+        self._force = tuple(float(np.float32(v)) for v in force)
+        self._cSmago = float(np.float32(cSmago))
+        self._inflowUniform = False
+        self._sponge = None
+
+    # -- lifetime ----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().stro_sim_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def cells(self):
+        return self.nx * self.ny * self.nz
+
+    # -- mutable properties (Sim.swift:164-172) ----------------------------
+    @property
+    def omega(self):
+        return self._omega
+
+    @omega.setter
+    def omega(self, v):
+        self._omega = float(np.float32(v))
+        _check(lib().stro_sim_set_omega(self._h, self._omega, self._omegaMinus))
+
+    @property
+    def omegaMinus(self):
+        return self._omegaMinus
+
+    @omegaMinus.setter
+    def omegaMinus(self, v):
+        self._omegaMinus = float(np.float32(v))
+        _check(lib().stro_sim_set_omega(self._h, self._omega, self._omegaMinus))
+
+    @property
+    def lidVel(self):
+        return self._lid
+
+    @lidVel.setter
+    def lidVel(self, v):
+        self._lid = tuple(float(np.float32(x)) for x in v)
+        _check(lib().stro_sim_set_lid(self._h, _f3(self._lid)))
+
+    @property
+    def uinTarget(self):
+        return self._uin
+
+    @uinTarget.setter
+    def uinTarget(self, v):
+        self._uin = float(np.float32(v))
+        _check(lib().stro_sim_set_uin(self._h, self._uin))
+
+    @property
+    def rampSteps(self):
+        return self._ramp
+
+    @rampSteps.setter
+    def rampSteps(self, v):
+        self._ramp = int(v)
+        _check(lib().stro_sim_set_ramp_steps(self._h, self._ramp))
+
+    @property
+    def force(self):
+        return self._force
+
+    @force.setter
+    def force(self, v):
+        self._force = tuple(float(np.float32(x)) for x in v)
+        _check(lib().stro_sim_set_force(self._h, _f3(self._force)))
+
+    @property
+    def cSmago(self):
+        return self._cSmago
+
+    @cSmago.setter
+    def cSmago(self, v):
+        self._cSmago = float(np.float32(v))
+        _check(lib().stro_sim_set_c_smago(self._h, self._cSmago))
+
+    @property
+    def inflowUniform(self):
+        return self._inflowUniform
+
+    @inflowUniform.setter
+    def inflowUniform(self, v):
+        self._inflowUniform = bool(v)
+        _check(lib().stro_sim_set_inflow_uniform(self._h, int(self._inflowUniform)))
+
+    @property
+    def sponge(self):
+        return self._sponge
+
+    @sponge.setter
+    def sponge(self, v):
+        """(x0, width, tau) or None."""
+        if v is None:
+            _check(lib().stro_sim_set_sponge(self._h, 0, 0.0, 0.0, 0.0))
+        else:
+            _check(lib().stro_sim_set_sponge(self._h, 1, float(v[0]), float(v[1]), float(v[2])))
+        self._sponge = v
+
+    # -- set-up ---------------------------------------------------------------
+    def setSolidFractions(self, eps):
+        eps = np.ascontiguousarray(eps, dtype=np.float32).reshape(-1)
+        if eps.size != self.cells:
+            raise ValueError("eps must hold one value per cell")
+        _check(lib().stro_sim_set_solid_fractions(self._h, eps.ctypes.data))
+
+    def setForceField(self, field):
+        """Per-cell Guo force field, shape (3, N) float32 (extension); None removes it."""
+        if field is None:
+            _check(lib().stro_sim_set_force_field(self._h, None))
+            return
+        field = np.ascontiguousarray(field, dtype=np.float32).reshape(3, self.cells)
+        _check(lib().stro_sim_set_force_field(self._h, field.ctypes.data))
+
+    def initField(self, mode, amplitude):
+        _check(lib().stro_sim_init_field(self._h, int(mode), float(amplitude)))
+
+    def _dtype(self):
+        return np.float32 if self.precision is Precision.fp32 else np.float16
+
+    def uploadState(self, f):
+        f = np.ascontiguousarray(f, dtype=self._dtype())
+        if f.size != 19 * self.cells:
+            raise ValueError("state must hold 19*N values")
+        _check(lib().stro_sim_upload_state(self._h, f.ctypes.data, f.nbytes))
+
+    def downloadState(self, out=None):
+        if out is None:
+            out = np.empty((19, self.cells), self._dtype())
+        _check(lib().stro_sim_download_state(self._h, out.ctypes.data, out.nbytes))
+        return out
+
+    # -- stepping ---------------------------------------------------------------
+    def run(self, steps):
+        _check(lib().stro_sim_run(self._h, int(steps)))
+
+    @property
+    def stepsDone(self):
+        v = ctypes.c_int64()
+        _check(lib().stro_sim_steps_done(self._h, ctypes.byref(v)))
+        return v.value
+
+    @stepsDone.setter
+    def stepsDone(self, v):
+        _check(lib().stro_sim_set_steps_done(self._h, int(v)))
+
+    @property
+    def gpuSeconds(self):
+        v = ctypes.c_double()
+        _check(lib().stro_sim_gpu_seconds(self._h, ctypes.byref(v)))
+        return v.value
+
+    # -- probes -----------------------------------------------------------------
+    def probeMoments(self):
+        out = np.empty((self.cells, 4), np.float32)
+        _check(lib().stro_sim_moments(self._h, out.ctypes.data))
+        return out
+
+    def probeForce(self, xRange, yRange):
+        out = np.zeros(3, np.float64)
+        _check(lib().stro_sim_probe_force(self._h, int(xRange[0]), int(xRange[1]),
+                                          int(yRange[0]), int(yRange[1]), out.ctypes.data))
+        return out
+
+    def kineticEnergySum(self):
+        v = ctypes.c_double()
+        _check(lib().stro_sim_kinetic_energy(self._h, ctypes.byref(v)))
+        return v.value
+
+    def dissipationSum(self):
+        v = ctypes.c_double()
+        _check(lib().stro_sim_dissipation(self._h, ctypes.byref(v)))
+        return v.value
+
+    @property
+    def stateDigest(self):
+        buf = ctypes.create_string_buffer(65)
+        _check(lib().stro_sim_digest(self._h, buf))
+        return buf.value.decode()
+
+    def massSum(self):
+        v = ctypes.c_double()
+        _check(lib().stro_sim_mass(self._h, ctypes.byref(v)))
+        return v.value
+
+    def checkFinite(self):
+        v = ctypes.c_int()
+        _check(lib().stro_sim_check_finite(self._h, ctypes.byref(v)))
+        return bool(v.value)
+
+
+def sha256Hex(data):
+    """SHA-256 of a bytes-like object or array, computed by the library."""
+    buf = np.ascontiguousarray(np.frombuffer(memoryview(data).cast("B"), np.uint8))
+    out = ctypes.create_string_buffer(65)
+    _check(lib().stro_sha256_hex(buf.ctypes.data, buf.nbytes, out))
+    return out.value.decode()
+
+
+class PinnedBuffer:
+    """Page-locked host array (cudaMallocHost) viewed as a numpy array."""
+
+    def __init__(self, shape, dtype):
+        self.nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self._p = _P()
+        _check(lib().stro_host_alloc(self.nbytes, ctypes.byref(self._p)))
+        raw = (ctypes.c_uint8 * self.nbytes).from_address(self._p.value)
+        self.array = np.frombuffer(raw, np.uint8).view(dtype).reshape(shape)
+
+    def close(self):
+        if self._p:
+            self.array = None
+            lib().stro_host_free(self._p)
+            self._p = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def diskSolidFractions(nx, ny, cx, cy, r):
+    """CaseSetups.swift:6-25 (16x16 subcells), computed in the C++ runtime."""
+    out = np.zeros(nx * ny, np.float32)
+    _check(lib().stro_disk_solid_fractions(nx, ny, cx, cy, r, out.ctypes.data))
+    return out
+
+
+def sphereSolidFractions(nx, ny, nz, cx, cy, cz, r, sub=8):
+    """CaseSetups.swift:68-90 (sub^3 subcells), computed in the C++ runtime."""
+    out = np.zeros(nx * ny * nz, np.float32)
+    _check(lib().stro_sphere_solid_fractions(nx, ny, nz, cx, cy, cz, r, sub, out.ctypes.data))
+    return out

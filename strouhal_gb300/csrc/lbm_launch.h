@@ -1,0 +1,46 @@
+// Host-side launch interface of the device kernels (internal to the library).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "lbm_device.cuh"
+
+namespace stro {
+
+// One AA pass over the lattice. block.x * block.y must be a multiple of 32
+// and at most 256; the grid is (ceil(nx/bx), ceil(ny/by), nz).
+cudaError_t launch_step(const StepArgs& a, int half_storage, int parity, int geo, bool feat,
+                        bool probe, dim3 block, cudaStream_t st);
+dim3 step_grid(const StepArgs& a, dim3 block);
+
+// Fields and reductions (lbm_probe.cu). `plane` is the DDF plane stride in
+// elements, N the cell count. Reductions write per-block FP64 partials to
+// `partials` and then fold them in a fixed order into `out`.
+struct FieldView {
+    void* f;
+    uint64_t plane;
+    uint32_t nx, ny, nz, N;
+    const uint8_t* cell;    // nullptr: all fluid
+    const float* ffield;    // nullptr: no force field
+    float fx, fy, fz;       // uniform force
+};
+
+// Number of blocks the fixed-order reductions use for N cells (depends on N only).
+int reduction_blocks(uint64_t count);
+
+cudaError_t launch_init_field(const FieldView& v, int half_storage, uint32_t mode,
+                              float amplitude, float tau, cudaStream_t st);
+cudaError_t launch_moments(const FieldView& v, int half_storage, float4* out, cudaStream_t st);
+// out[0] = sum |u|^2, out[1] = sum 2 nu S:S (lattice units)
+cudaError_t launch_observables(const FieldView& v, int half_storage, float omega,
+                               double* partials, double* out, cudaStream_t st);
+cudaError_t launch_mass(const FieldView& v, int half_storage, double* partials, double* out,
+                        cudaStream_t st);
+// out[0] = number of non-finite DDFs (as a double)
+cudaError_t launch_nonfinite(const FieldView& v, int half_storage, double* partials, double* out,
+                             cudaStream_t st);
+// Sum nblocks x K partials in a fixed order into out[K].
+cudaError_t launch_fold(const double* partials, int nblocks, int K, double* out, cudaStream_t st);
+
+}  // namespace stro

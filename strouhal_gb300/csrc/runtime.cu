@@ -1,0 +1,750 @@
+// Host runtime of the C ABI (include/strouhal_c.h): the GB300 counterpart of
+// the reference's GPU and Simulation classes (Sources/StrouhalCore/Sim.swift).
+//
+// Design (one process, one GPU):
+//   - one CUDA stream per context; every call is stream-ordered and
+//     synchronous at return, like Simulation.run's final wait (Sim.swift:326);
+//   - DDFs live in HBM as 19 planes with a padded plane stride (multiple of 64
+//     elements) so every plane starts 128-byte aligned; the canonical
+//     unpadded layout only exists at the upload/download/digest boundary;
+//   - geometry is precomputed once on the host (Sim.swift:227-255) and packed
+//     into a cell byte (even pass) and a geometry word (odd pass);
+//   - the per-step uniforms, including the cosine ramp (Sim.swift:258-281),
+//     are computed on the host and passed by value to each launch;
+//   - GPU time is accumulated from CUDA events around each run (gpuSeconds).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "lbm_launch.h"
+#include "sha256.h"
+#include "strouhal_c.h"
+
+using namespace stro;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg) {
+    g_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    const int code = (e == cudaErrorMemoryAllocation) ? STRO_ERR_OOM : STRO_ERR_CUDA;
+    return fail(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define STRO_CUDA(expr)                                        \
+    do {                                                       \
+        cudaError_t e_ = (expr);                               \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #expr);    \
+    } while (0)
+
+constexpr int CX[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+constexpr int CY[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1};
+constexpr int CZ[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
+
+uint64_t padded_plane(uint64_t N) { return (N + 63) / 64 * 64; }
+
+}  // namespace
+
+struct stro_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    char name[256] = {0};
+};
+
+struct stro_sim {
+    stro_ctx* ctx = nullptr;
+    int precision = STRO_FP32;
+    int32_t nx = 0, ny = 0, nz = 0;
+    uint64_t N = 0, plane = 0;
+    size_t esize = 4;
+    // Simulation properties (Sim.swift:164-172)
+    float omega = 1.0f, omega_minus = 1.0f;
+    float lid[3] = {0, 0, 0};
+    float uin = 0.0f;
+    int32_t ramp_steps = 0;
+    float force[3] = {0, 0, 0};
+    float c_smago = 0.0f;
+    int inflow_uniform = 0;
+    bool sponge_on = false;
+    float sponge_x0 = 1e9f, sponge_width = 0.0f, sponge_tau = 1.0f;
+    bool wants_forces = false;
+    // host geometry
+    std::vector<uint8_t> flags;
+    std::vector<uint32_t> smask, lmask;
+    std::vector<float> eps;
+    bool any_wall = false, has_eps = false, has_ffield = false;
+    // device buffers
+    void* d_f = nullptr;
+    uint8_t* d_cell = nullptr;
+    uint32_t* d_geo = nullptr;
+    uint32_t* d_lmask = nullptr;
+    float* d_eps = nullptr;
+    float* d_ffield = nullptr;
+    float4* d_moments = nullptr;
+    double* d_partials = nullptr;
+    size_t partials_len = 0;
+    double* d_out = nullptr;
+    // bookkeeping
+    int64_t steps_done = 0;
+    double gpu_seconds = 0.0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    dim3 block{256, 1, 1};
+};
+
+namespace {
+
+bool geo_on(const stro_sim* s) { return s->any_wall || s->has_eps; }
+bool sponge_active(const stro_sim* s) {
+    return s->sponge_on && s->sponge_x0 < float(s->nx - 1);
+}
+bool force_on(const stro_sim* s) {
+    return s->has_ffield || s->force[0] != 0.0f || s->force[1] != 0.0f || s->force[2] != 0.0f;
+}
+bool feat_on(const stro_sim* s) {
+    return s->has_eps || s->c_smago > 0.0f || sponge_active(s) || force_on(s);
+}
+
+dim3 default_block(int nx) {
+    int bx = ((nx + 31) / 32) * 32;
+    if (bx > 256) bx = 256;
+    if (bx < 32) bx = 32;
+    int by = 256 / bx;
+    if (by < 1) by = 1;
+    return dim3(bx, by, 1);
+}
+
+// Cosine ramp factor at step t, Sim.swift:258-266.
+float ramp_factor(const stro_sim* s, int64_t t) {
+    if (s->ramp_steps <= 0) return 1.0f;
+    const double x = std::fmin(1.0, double(t) / double(s->ramp_steps));
+    return 1.0f * float(0.5 * (1.0 - std::cos(3.141592653589793 * x)));
+}
+
+StepArgs step_args(const stro_sim* s, int64_t t) {
+    StepArgs a{};
+    a.f = s->d_f;
+    a.plane = s->plane;
+    a.nx = s->nx; a.ny = s->ny; a.nz = s->nz;
+    a.cell = s->d_cell;
+    a.geo = s->d_geo;
+    a.lmask = s->d_lmask;
+    a.eps = s->d_eps;
+    a.ffield = s->has_ffield ? s->d_ffield : nullptr;
+    a.ffield_plane = uint32_t(s->N);
+    a.omega = s->omega;
+    a.omega_minus = s->omega_minus;
+    const float r = ramp_factor(s, t);
+    a.uin = s->uin * r;
+    a.c_smago = s->c_smago;
+    a.fx = s->force[0]; a.fy = s->force[1]; a.fz = s->force[2];
+    a.ulid_x = s->lid[0] * r; a.ulid_y = s->lid[1] * r; a.ulid_z = s->lid[2] * r;
+    a.inflow_uniform = s->inflow_uniform;
+    if (s->sponge_on) {
+        a.sponge_x0 = s->sponge_x0;
+        a.sponge_inv_w = 1.0f / s->sponge_width;
+        a.sponge_tau = s->sponge_tau;
+    } else {
+        a.sponge_x0 = 1e9f; a.sponge_inv_w = 0.0f; a.sponge_tau = 1.0f;
+    }
+    a.force_on = force_on(s) ? 1 : 0;
+    a.box_x0 = 0; a.box_x1 = -1; a.box_y0 = 0; a.box_y1 = -1;
+    a.partials = s->d_partials;
+    return a;
+}
+
+FieldView field_view(const stro_sim* s) {
+    FieldView v{};
+    v.f = s->d_f;
+    v.plane = s->plane;
+    v.nx = uint32_t(s->nx); v.ny = uint32_t(s->ny); v.nz = uint32_t(s->nz);
+    v.N = uint32_t(s->N);
+    v.cell = geo_on(s) ? s->d_cell : nullptr;
+    v.ffield = s->has_ffield ? s->d_ffield : nullptr;
+    v.fx = s->force[0]; v.fy = s->force[1]; v.fz = s->force[2];
+    return v;
+}
+
+// Neighbour masks (Sim.swift:227-255) and the packed device geometry.
+int upload_geometry(stro_sim* s) {
+    const int nx = s->nx, ny = s->ny, nz = s->nz;
+    const uint64_t N = s->N;
+    s->smask.assign(N, 0u);
+    s->lmask.assign(N, 0u);
+    s->any_wall = false;
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                const uint64_t idx = (uint64_t(z) * ny + y) * nx + x;
+                const uint8_t c = s->flags[idx];
+                if (c != STRO_FLUID) { s->any_wall = true; continue; }
+                uint32_t sm = 0, lm = 0;
+                for (int i = 1; i < 19; ++i) {
+                    const int xn = (x + CX[i] + nx) % nx, yn = (y + CY[i] + ny) % ny,
+                              zn = (z + CZ[i] + nz) % nz;
+                    const uint8_t cn = s->flags[(uint64_t(zn) * ny + yn) * nx + xn];
+                    if (cn == STRO_FLUID) continue;
+                    sm |= 1u << (i - 1);
+                    if (cn == STRO_LID || cn == STRO_INFLOW || cn == STRO_OUTFLOW) lm |= 1u << (i - 1);
+                }
+                s->smask[idx] = sm;
+                s->lmask[idx] = lm;
+            }
+    if (!geo_on(s)) return STRO_OK;
+    std::vector<uint8_t> cell(N);
+    std::vector<uint32_t> geo(N);
+    for (uint64_t n = 0; n < N; ++n) {
+        const uint8_t c = s->flags[n];
+        const bool e = s->has_eps && s->eps[n] != 0.0f && c == STRO_FLUID;
+        cell[n] = uint8_t((c & CELL_TYPE_MASK) | (e ? CELL_EPS_BIT : 0));
+        uint32_t g = s->smask[n];
+        if (e) g |= GEO_EPS;
+        if (s->lmask[n]) g |= GEO_MOVING;
+        if (c != STRO_FLUID) g |= GEO_NONFLUID;
+        geo[n] = g;
+    }
+    if (!s->d_cell) {
+        STRO_CUDA(cudaMalloc(&s->d_cell, N));
+        STRO_CUDA(cudaMalloc(&s->d_geo, N * 4));
+        STRO_CUDA(cudaMalloc(&s->d_lmask, N * 4));
+    }
+    cudaStream_t st = s->ctx->stream;
+    STRO_CUDA(cudaMemcpyAsync(s->d_cell, cell.data(), N, cudaMemcpyHostToDevice, st));
+    STRO_CUDA(cudaMemcpyAsync(s->d_geo, geo.data(), N * 4, cudaMemcpyHostToDevice, st));
+    STRO_CUDA(cudaMemcpyAsync(s->d_lmask, s->lmask.data(), N * 4, cudaMemcpyHostToDevice, st));
+    STRO_CUDA(cudaStreamSynchronize(st));
+    return STRO_OK;
+}
+
+void free_sim(stro_sim* s) {
+    cudaFree(s->d_f);
+    cudaFree(s->d_cell);
+    cudaFree(s->d_geo);
+    cudaFree(s->d_lmask);
+    cudaFree(s->d_eps);
+    cudaFree(s->d_ffield);
+    cudaFree(s->d_moments);
+    cudaFree(s->d_partials);
+    cudaFree(s->d_out);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+}
+
+int launch_one_step(stro_sim* s, int64_t t, bool probe, const int box[4]) {
+    StepArgs a = step_args(s, t);
+    if (probe) {
+        a.box_x0 = box[0]; a.box_x1 = box[1]; a.box_y0 = box[2]; a.box_y1 = box[3];
+    }
+    const cudaError_t e = launch_step(a, s->precision == STRO_FP16S, int(t & 1), geo_on(s) ? 1 : 0,
+                                      feat_on(s), probe, s->block, s->ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "step launch");
+    return STRO_OK;
+}
+
+int run_steps(stro_sim* s, int64_t steps, int64_t probe_step = -1, const int* box = nullptr) {
+    cudaStream_t st = s->ctx->stream;
+    STRO_CUDA(cudaEventRecord(s->ev0, st));
+    for (int64_t k = 0; k < steps; ++k) {
+        const int64_t t = s->steps_done + k;
+        const int rc = launch_one_step(s, t, t == probe_step, box);
+        if (rc != STRO_OK) return rc;
+    }
+    STRO_CUDA(cudaEventRecord(s->ev1, st));
+    STRO_CUDA(cudaEventSynchronize(s->ev1));
+    float ms = 0.0f;
+    STRO_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    s->gpu_seconds += double(ms) * 1e-3;
+    s->steps_done += steps;
+    STRO_CUDA(cudaGetLastError());
+    return STRO_OK;
+}
+
+int ensure_partials(stro_sim* s, size_t doubles) {
+    if (s->partials_len >= doubles) return STRO_OK;
+    cudaFree(s->d_partials);
+    s->d_partials = nullptr;
+    STRO_CUDA(cudaMalloc(&s->d_partials, doubles * sizeof(double)));
+    s->partials_len = doubles;
+    return STRO_OK;
+}
+
+#define CHECK_SIM(s) \
+    if (!(s)) return fail(STRO_ERR_INVALID, "null simulation handle")
+
+}  // namespace
+
+extern "C" {
+
+const char* stro_last_error(void) { return g_error.c_str(); }
+int stro_abi_version(void) { return STRO_ABI_VERSION; }
+
+int stro_ctx_create(int device, stro_ctx** out) {
+    if (!out) return fail(STRO_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return fail(STRO_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (device < 0 || device >= count) return fail(STRO_ERR_INVALID, "device index out of range");
+    STRO_CUDA(cudaSetDevice(device));
+    stro_ctx* c = new (std::nothrow) stro_ctx;
+    if (!c) return fail(STRO_ERR_OOM, "host allocation failed");
+    c->device = device;
+    cudaDeviceProp prop{};
+    cudaError_t e = cudaGetDeviceProperties(&prop, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "context set-up");
+    }
+    c->sm_count = prop.multiProcessorCount;
+    std::snprintf(c->name, sizeof c->name, "%s", prop.name);
+    *out = c;
+    return STRO_OK;
+}
+
+int stro_ctx_destroy(stro_ctx* ctx) {
+    if (!ctx) return STRO_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return STRO_OK;
+}
+
+int stro_ctx_info(stro_ctx* ctx, char* name, size_t name_len, int* sm_count) {
+    if (!ctx) return fail(STRO_ERR_INVALID, "null context");
+    if (name && name_len) std::snprintf(name, name_len, "%s", ctx->name);
+    if (sm_count) *sm_count = ctx->sm_count;
+    return STRO_OK;
+}
+
+int stro_sim_create(stro_ctx* ctx, const stro_sim_desc* d, const uint8_t* flags, stro_sim** out) {
+    if (!ctx || !d || !out) return fail(STRO_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (d->precision != STRO_FP32 && d->precision != STRO_FP16S)
+        return fail(STRO_ERR_INVALID, "precision must be STRO_FP32 or STRO_FP16S");
+    if (d->nx < 1 || d->ny < 1 || d->nz < 1 || d->nx > 65535 * 256 || d->ny > 65535 ||
+        d->nz > 65535)
+        return fail(STRO_ERR_INVALID, "lattice dimensions out of range");
+    const uint64_t N = uint64_t(d->nx) * d->ny * d->nz;
+    if (N >= (1ull << 31) || 19ull * (N + 64) >= (1ull << 40))
+        return fail(STRO_ERR_INVALID, "lattice too large (N must be < 2^31 cells)");
+    if (flags)
+        for (uint64_t n = 0; n < N; ++n)
+            if (flags[n] > STRO_OUTFLOW) return fail(STRO_ERR_INVALID, "flag value out of range");
+    STRO_CUDA(cudaSetDevice(ctx->device));
+    stro_sim* s = new (std::nothrow) stro_sim;
+    if (!s) return fail(STRO_ERR_OOM, "host allocation failed");
+    s->ctx = ctx;
+    s->precision = d->precision;
+    s->nx = d->nx; s->ny = d->ny; s->nz = d->nz;
+    s->N = N;
+    s->plane = padded_plane(N);
+    s->esize = d->precision == STRO_FP16S ? 2 : 4;
+    s->omega = d->omega;
+    s->omega_minus = d->omega_minus;
+    std::memcpy(s->lid, d->lid, sizeof s->lid);
+    s->uin = d->uin;
+    s->ramp_steps = d->ramp_steps;
+    std::memcpy(s->force, d->force, sizeof s->force);
+    s->c_smago = d->c_smago;
+    s->wants_forces = d->wants_forces != 0;
+    s->block = default_block(d->nx);
+    try {
+        s->flags.assign(N, 0);
+        if (flags) std::memcpy(s->flags.data(), flags, N);
+    } catch (const std::bad_alloc&) {
+        delete s;
+        return fail(STRO_ERR_OOM, "host allocation failed");
+    }
+    auto bail = [&](int rc) {
+        free_sim(s);
+        delete s;
+        return rc;
+    };
+    cudaError_t e = cudaMalloc(&s->d_f, 19 * s->plane * s->esize);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "DDF allocation"));
+    // shifted equilibrium at rest is exactly 0 (Sim.swift:225)
+    e = cudaMemsetAsync(s->d_f, 0, 19 * s->plane * s->esize, ctx->stream);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_out, 8 * sizeof(double));
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "simulation set-up"));
+    int rc = upload_geometry(s);
+    if (rc != STRO_OK) return bail(rc);
+    const dim3 grid = dim3((s->nx + s->block.x - 1) / s->block.x,
+                           (s->ny + s->block.y - 1) / s->block.y, s->nz);
+    const size_t step_blocks = size_t(grid.x) * grid.y * grid.z;
+    rc = ensure_partials(s, std::max<size_t>(s->wants_forces ? 3 * step_blocks : 0, 2 * 2048));
+    if (rc != STRO_OK) return bail(rc);
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "simulation set-up"));
+    *out = s;
+    return STRO_OK;
+}
+
+int stro_sim_destroy(stro_sim* s) {
+    if (!s) return STRO_OK;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    free_sim(s);
+    delete s;
+    return STRO_OK;
+}
+
+int stro_sim_set_omega(stro_sim* s, float omega, float omega_minus) {
+    CHECK_SIM(s);
+    s->omega = omega;
+    s->omega_minus = omega_minus;
+    return STRO_OK;
+}
+int stro_sim_set_lid(stro_sim* s, const float lid[3]) {
+    CHECK_SIM(s);
+    if (!lid) return fail(STRO_ERR_INVALID, "null lid");
+    std::memcpy(s->lid, lid, sizeof s->lid);
+    return STRO_OK;
+}
+int stro_sim_set_uin(stro_sim* s, float uin) {
+    CHECK_SIM(s);
+    s->uin = uin;
+    return STRO_OK;
+}
+int stro_sim_set_ramp_steps(stro_sim* s, int32_t r) {
+    CHECK_SIM(s);
+    s->ramp_steps = r;
+    return STRO_OK;
+}
+int stro_sim_set_force(stro_sim* s, const float f[3]) {
+    CHECK_SIM(s);
+    if (!f) return fail(STRO_ERR_INVALID, "null force");
+    std::memcpy(s->force, f, sizeof s->force);
+    return STRO_OK;
+}
+int stro_sim_set_c_smago(stro_sim* s, float c) {
+    CHECK_SIM(s);
+    s->c_smago = c;
+    return STRO_OK;
+}
+int stro_sim_set_inflow_uniform(stro_sim* s, int u) {
+    CHECK_SIM(s);
+    s->inflow_uniform = u ? 1 : 0;
+    return STRO_OK;
+}
+int stro_sim_set_sponge(stro_sim* s, int enabled, float x0, float width, float tau) {
+    CHECK_SIM(s);
+    if (enabled && !(width > 0.0f)) return fail(STRO_ERR_INVALID, "sponge width must be > 0");
+    s->sponge_on = enabled != 0;
+    s->sponge_x0 = enabled ? x0 : 1e9f;
+    s->sponge_width = enabled ? width : 0.0f;
+    s->sponge_tau = enabled ? tau : 1.0f;
+    return STRO_OK;
+}
+
+int stro_sim_set_solid_fractions(stro_sim* s, const float* eps) {
+    CHECK_SIM(s);
+    if (!eps) return fail(STRO_ERR_INVALID, "null eps");
+    cudaSetDevice(s->ctx->device);
+    s->eps.assign(eps, eps + s->N);
+    s->has_eps = true;
+    if (!s->d_eps) STRO_CUDA(cudaMalloc(&s->d_eps, s->N * 4));
+    STRO_CUDA(cudaMemcpyAsync(s->d_eps, eps, s->N * 4, cudaMemcpyHostToDevice, s->ctx->stream));
+    return upload_geometry(s);
+}
+
+int stro_sim_set_force_field(stro_sim* s, const float* fxyz) {
+    CHECK_SIM(s);
+    cudaSetDevice(s->ctx->device);
+    if (!fxyz) {
+        s->has_ffield = false;
+        return STRO_OK;
+    }
+    if (!s->d_ffield) STRO_CUDA(cudaMalloc(&s->d_ffield, 3 * s->N * 4));
+    STRO_CUDA(cudaMemcpyAsync(s->d_ffield, fxyz, 3 * s->N * 4, cudaMemcpyHostToDevice,
+                              s->ctx->stream));
+    STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    s->has_ffield = true;
+    return STRO_OK;
+}
+
+int stro_sim_init_field(stro_sim* s, uint32_t mode, float amplitude) {
+    CHECK_SIM(s);
+    if (mode > 2) return fail(STRO_ERR_INVALID, "init mode must be 0, 1 or 2");
+    cudaSetDevice(s->ctx->device);
+    const float tau = 1.0f / s->omega;
+    STRO_CUDA(launch_init_field(field_view(s), s->precision == STRO_FP16S, mode, amplitude, tau,
+                                s->ctx->stream));
+    STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    return STRO_OK;
+}
+
+int stro_sim_state_bytes(stro_sim* s, size_t* bytes) {
+    CHECK_SIM(s);
+    if (!bytes) return fail(STRO_ERR_INVALID, "null output");
+    *bytes = 19 * s->N * s->esize;
+    return STRO_OK;
+}
+
+int stro_sim_upload_state(stro_sim* s, const void* host, size_t bytes) {
+    CHECK_SIM(s);
+    if (!host || bytes != 19 * s->N * s->esize)
+        return fail(STRO_ERR_INVALID, "state size must be 19*N*element_size bytes");
+    cudaSetDevice(s->ctx->device);
+    STRO_CUDA(cudaMemcpy2DAsync(s->d_f, s->plane * s->esize, host, s->N * s->esize,
+                                s->N * s->esize, 19, cudaMemcpyHostToDevice, s->ctx->stream));
+    STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    return STRO_OK;
+}
+
+int stro_sim_download_state(stro_sim* s, void* host, size_t bytes) {
+    CHECK_SIM(s);
+    if (!host || bytes != 19 * s->N * s->esize)
+        return fail(STRO_ERR_INVALID, "state size must be 19*N*element_size bytes");
+    cudaSetDevice(s->ctx->device);
+    STRO_CUDA(cudaMemcpy2DAsync(host, s->N * s->esize, s->d_f, s->plane * s->esize,
+                                s->N * s->esize, 19, cudaMemcpyDeviceToHost, s->ctx->stream));
+    STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    return STRO_OK;
+}
+
+int stro_sim_run(stro_sim* s, int64_t steps) {
+    CHECK_SIM(s);
+    if (steps < 0) return fail(STRO_ERR_INVALID, "negative step count");
+    if (steps == 0) return STRO_OK;
+    cudaSetDevice(s->ctx->device);
+    return run_steps(s, steps);
+}
+
+int stro_sim_steps_done(stro_sim* s, int64_t* steps) {
+    CHECK_SIM(s);
+    if (!steps) return fail(STRO_ERR_INVALID, "null output");
+    *steps = s->steps_done;
+    return STRO_OK;
+}
+
+int stro_sim_set_steps_done(stro_sim* s, int64_t steps) {
+    CHECK_SIM(s);
+    if (steps < 0) return fail(STRO_ERR_INVALID, "negative step count");
+    s->steps_done = steps;
+    return STRO_OK;
+}
+
+int stro_sim_gpu_seconds(stro_sim* s, double* seconds) {
+    CHECK_SIM(s);
+    if (!seconds) return fail(STRO_ERR_INVALID, "null output");
+    *seconds = s->gpu_seconds;
+    return STRO_OK;
+}
+
+int stro_sim_moments(stro_sim* s, float* out4) {
+    CHECK_SIM(s);
+    if (!out4) return fail(STRO_ERR_INVALID, "null output");
+    if (s->steps_done % 2 != 0)
+        return fail(STRO_ERR_STATE, "moments probe requires even step count");
+    cudaSetDevice(s->ctx->device);
+    if (!s->d_moments) STRO_CUDA(cudaMalloc(&s->d_moments, s->N * sizeof(float4)));
+    STRO_CUDA(launch_moments(field_view(s), s->precision == STRO_FP16S, s->d_moments,
+                             s->ctx->stream));
+    STRO_CUDA(cudaMemcpyAsync(out4, s->d_moments, s->N * sizeof(float4), cudaMemcpyDeviceToHost,
+                              s->ctx->stream));
+    STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    return STRO_OK;
+}
+
+int stro_sim_probe_force(stro_sim* s, int32_t x0, int32_t x1, int32_t y0, int32_t y1,
+                         double out[3]) {
+    CHECK_SIM(s);
+    if (!out) return fail(STRO_ERR_INVALID, "null output");
+    if (!s->wants_forces) return fail(STRO_ERR_STATE, "force probe requires wants_forces");
+    if (s->steps_done % 2 != 0)
+        return fail(STRO_ERR_STATE, "force probe requires even step count");
+    if (x0 < 0 || x1 >= s->nx || y0 < 0 || y1 >= s->ny || x0 > x1 || y0 > y1)
+        return fail(STRO_ERR_INVALID, "force box outside the lattice");
+    cudaSetDevice(s->ctx->device);
+    if (!geo_on(s)) {  // no wall and no solid fraction: nothing exchanges momentum
+        const int rc = run_steps(s, 2);
+        out[0] = out[1] = out[2] = 0.0;
+        return rc;
+    }
+    const int box[4] = {x0, x1, y0, y1};
+    int rc = run_steps(s, 2, s->steps_done + 1, box);
+    if (rc != STRO_OK) return rc;
+    StepArgs a = step_args(s, 0);
+    const dim3 grid = step_grid(a, s->block);
+    const int nblocks = int(grid.x * grid.y * grid.z);
+    STRO_CUDA(launch_fold(s->d_partials, nblocks, 3, s->d_out, s->ctx->stream));
+    STRO_CUDA(cudaMemcpyAsync(out, s->d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                              s->ctx->stream));
+    STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    return STRO_OK;
+}
+
+static int observables(stro_sim* s, double out[2]) {
+    if (s->steps_done % 2 != 0)
+        return fail(STRO_ERR_STATE, "observables require an even step count");
+    cudaSetDevice(s->ctx->device);
+    STRO_CUDA(launch_observables(field_view(s), s->precision == STRO_FP16S, s->omega,
+                                 s->d_partials, s->d_out, s->ctx->stream));
+    STRO_CUDA(cudaMemcpyAsync(out, s->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                              s->ctx->stream));
+    STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    return STRO_OK;
+}
+
+int stro_sim_kinetic_energy(stro_sim* s, double* sum_u2) {
+    CHECK_SIM(s);
+    if (!sum_u2) return fail(STRO_ERR_INVALID, "null output");
+    double o[2];
+    const int rc = observables(s, o);
+    if (rc == STRO_OK) *sum_u2 = o[0];
+    return rc;
+}
+
+int stro_sim_dissipation(stro_sim* s, double* sum_eps) {
+    CHECK_SIM(s);
+    if (!sum_eps) return fail(STRO_ERR_INVALID, "null output");
+    double o[2];
+    const int rc = observables(s, o);
+    if (rc == STRO_OK) *sum_eps = o[1];
+    return rc;
+}
+
+int stro_sim_digest(stro_sim* s, char hex[65]) {
+    CHECK_SIM(s);
+    if (!hex) return fail(STRO_ERR_INVALID, "null output");
+    cudaSetDevice(s->ctx->device);
+    // Stream the planes through a pinned staging buffer in slices.
+    const size_t plane_bytes = s->N * s->esize;
+    const size_t slice = std::min<size_t>(plane_bytes, size_t(64) << 20);
+    void* stage = nullptr;
+    STRO_CUDA(cudaMallocHost(&stage, slice));
+    Sha256 h;
+    for (int i = 0; i < 19; ++i) {
+        const char* src = static_cast<const char*>(s->d_f) + size_t(i) * s->plane * s->esize;
+        for (size_t off = 0; off < plane_bytes; off += slice) {
+            const size_t len = std::min(slice, plane_bytes - off);
+            cudaError_t e = cudaMemcpyAsync(stage, src + off, len, cudaMemcpyDeviceToHost,
+                                            s->ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->ctx->stream);
+            if (e != cudaSuccess) {
+                cudaFreeHost(stage);
+                return cuda_fail(e, "digest download");
+            }
+            h.update(stage, len);
+        }
+    }
+    cudaFreeHost(stage);
+    uint8_t dg[32];
+    h.finish(dg);
+    sha256_hex(dg, hex);
+    return STRO_OK;
+}
+
+int stro_sim_mass(stro_sim* s, double* total) {
+    CHECK_SIM(s);
+    if (!total) return fail(STRO_ERR_INVALID, "null output");
+    cudaSetDevice(s->ctx->device);
+    STRO_CUDA(launch_mass(field_view(s), s->precision == STRO_FP16S, s->d_partials, s->d_out,
+                          s->ctx->stream));
+    STRO_CUDA(cudaMemcpyAsync(total, s->d_out, sizeof(double), cudaMemcpyDeviceToHost,
+                              s->ctx->stream));
+    STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    return STRO_OK;
+}
+
+int stro_sim_check_finite(stro_sim* s, int* all_finite) {
+    CHECK_SIM(s);
+    if (!all_finite) return fail(STRO_ERR_INVALID, "null output");
+    cudaSetDevice(s->ctx->device);
+    double bad = 0.0;
+    STRO_CUDA(launch_nonfinite(field_view(s), s->precision == STRO_FP16S, s->d_partials,
+                               s->d_out, s->ctx->stream));
+    STRO_CUDA(cudaMemcpyAsync(&bad, s->d_out, sizeof(double), cudaMemcpyDeviceToHost,
+                              s->ctx->stream));
+    STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    *all_finite = bad == 0.0 ? 1 : 0;
+    return STRO_OK;
+}
+
+int stro_sha256_hex(const void* data, size_t len, char hex[65]) {
+    if ((!data && len) || !hex) return fail(STRO_ERR_INVALID, "null argument");
+    Sha256 h;
+    h.update(data, len);
+    uint8_t dg[32];
+    h.finish(dg);
+    sha256_hex(dg, hex);
+    return STRO_OK;
+}
+
+int stro_host_alloc(size_t bytes, void** out) {
+    if (!out) return fail(STRO_ERR_INVALID, "null output");
+    *out = nullptr;
+    STRO_CUDA(cudaMallocHost(out, bytes));
+    return STRO_OK;
+}
+
+int stro_host_free(void* ptr) {
+    if (ptr) STRO_CUDA(cudaFreeHost(ptr));
+    return STRO_OK;
+}
+
+// diskSolidFractions, CaseSetups.swift:6-25.
+int stro_disk_solid_fractions(int32_t nx, int32_t ny, double cx, double cy, double r, float* out) {
+    if (!out || nx < 1 || ny < 1) return fail(STRO_ERR_INVALID, "bad disk arguments");
+    std::fill(out, out + size_t(nx) * ny, 0.0f);
+    const double r2 = r * r;
+    const int sub = 16;
+    const int lo = int(cx - r) - 2, hi = int(cx + r) + 2;
+    const int loY = int(cy - r) - 2, hiY = int(cy + r) + 2;
+    for (int y = std::max(0, loY); y <= std::min(ny - 1, hiY); ++y)
+        for (int x = std::max(0, lo); x <= std::min(nx - 1, hi); ++x) {
+            int inside = 0;
+            for (int sy = 0; sy < sub; ++sy)
+                for (int sx = 0; sx < sub; ++sx) {
+                    const double px = double(x) - 0.5 + (double(sx) + 0.5) / double(sub);
+                    const double py = double(y) - 0.5 + (double(sy) + 0.5) / double(sub);
+                    const double dx = px - cx, dy = py - cy;
+                    if (dx * dx + dy * dy <= r2) ++inside;
+                }
+            out[size_t(y) * nx + x] = float(inside) / float(sub * sub);
+        }
+    return STRO_OK;
+}
+
+// sphereSolidFractions, CaseSetups.swift:68-90, with sub^3 samples per cell.
+int stro_sphere_solid_fractions(int32_t nx, int32_t ny, int32_t nz, double cx, double cy,
+                                double cz, double r, int32_t sub, float* out) {
+    if (!out || nx < 1 || ny < 1 || nz < 1 || sub < 1 || sub > 64)
+        return fail(STRO_ERR_INVALID, "bad sphere arguments");
+    std::fill(out, out + size_t(nx) * ny * nz, 0.0f);
+    const double r2 = r * r;
+    for (int z = std::max(0, int(cz - r) - 2); z <= std::min(nz - 1, int(cz + r) + 2); ++z)
+        for (int y = std::max(0, int(cy - r) - 2); y <= std::min(ny - 1, int(cy + r) + 2); ++y)
+            for (int x = std::max(0, int(cx - r) - 2); x <= std::min(nx - 1, int(cx + r) + 2); ++x) {
+                int inside = 0;
+                for (int sz = 0; sz < sub; ++sz)
+                    for (int sy = 0; sy < sub; ++sy)
+                        for (int sx = 0; sx < sub; ++sx) {
+                            const double px = double(x) - 0.5 + (double(sx) + 0.5) / double(sub);
+                            const double py = double(y) - 0.5 + (double(sy) + 0.5) / double(sub);
+                            const double pz = double(z) - 0.5 + (double(sz) + 0.5) / double(sub);
+                            const double dx = px - cx, dy = py - cy, dz = pz - cz;
+                            if (dx * dx + dy * dy + dz * dz <= r2) ++inside;
+                        }
+                out[(size_t(z) * ny + y) * nx + x] = float(inside) / float(sub * sub * sub);
+            }
+    return STRO_OK;
+}
+
+}  // extern "C"
