@@ -138,6 +138,50 @@ int stro_sim_mass(stro_sim* sim, double* total);
 /* 1 if every DDF is finite, else 0 (failure detection, Cases.swift:1250-1252). */
 int stro_sim_check_finite(stro_sim* sim, int* all_finite);
 
+/* Launch shape of the step kernels: bx*by threads (a multiple of 32, at most
+ * 256) per block over an x-y tile. Results do not depend on it. */
+int stro_sim_set_block(stro_sim* sim, int32_t bx, int32_t by);
+int stro_sim_get_block(stro_sim* sim, int32_t* bx, int32_t* by);
+/* Kernel variant: 0 = one cell per thread (all lattices); 1 = FP16 storage,
+ * two x-adjacent cells per thread with half2 accesses (periodic lattices,
+ * nx a multiple of 64; other lattices fall back to variant 0). Results are
+ * identical; FP16 lattices that qualify start with variant 1. */
+int stro_sim_set_variant(stro_sim* sim, int32_t variant);
+int stro_sim_get_variant(stro_sim* sim, int32_t* variant);
+/* Autotuner: times `steps` steps per candidate variant and launch shape on the current
+ * state (saved and restored, stepsDone unchanged) and keeps the fastest. */
+int stro_sim_autotune(stro_sim* sim, int64_t steps, int32_t* bx, int32_t* by, double* glups);
+
+/* ---- batch: many lattices advanced together ------------------------------------
+ * The reference advances credibility-ladder rungs and Mach anchors one after
+ * another on one queue (Ladder.swift:74-121). A batch groups simulations of
+ * one precision on one context and advances them in one launch. */
+typedef struct stro_batch stro_batch;
+enum {
+    STRO_BATCH_PERSISTENT = 0, /* one cooperative persistent kernel, bounded grid barrier, in a CUDA graph */
+    STRO_BATCH_ROUNDS = 1,     /* a CUDA graph of one launch per round */
+    STRO_BATCH_SEQUENTIAL = 2  /* one instance after another, one launch per step */
+};
+int stro_batch_create(stro_ctx* ctx, int32_t count, stro_sim* const* sims, stro_batch** out);
+int stro_batch_destroy(stro_batch* batch);
+int stro_batch_set_mode(stro_batch* batch, int32_t mode);
+int stro_batch_set_tile(stro_batch* batch, int32_t bx, int32_t by);
+/* Polls before a grid-barrier wait gives up with STRO_ERR_TIMEOUT. */
+int stro_batch_set_spin_limit(stro_batch* batch, int64_t polls);
+/* Advance sims[i] by steps[i] steps (DDFs bitwise identical to stro_sim_run).
+ * If log_every != NULL and log_every[i] > 0 (even; sims[i] at an even step
+ * count), sum |u|^2 is sampled before the first step and after every
+ * log_every[i] steps into traces[i * trace_stride + k]; trace_counts[i] gets
+ * the number of samples. */
+int stro_batch_run(stro_batch* batch, const int64_t* steps, const int32_t* log_every,
+                   double* traces, int32_t trace_stride, int32_t* trace_counts);
+int stro_batch_gpu_seconds(stro_batch* batch, double* seconds);
+/* "persistent-graph", "rounds-graph" or "sequential": the path the last run took. */
+int stro_batch_last_path(stro_batch* batch, char* buf, size_t len);
+/* Times each mode and tile shape for `rounds` rounds (states restored) and keeps the fastest. */
+int stro_batch_autotune(stro_batch* batch, int64_t rounds, int32_t* mode, int32_t* bx,
+                        int32_t* by, double* seconds);
+
 /* ---- host utilities ---------------------------------------------------------- */
 /* SHA-256 (FIPS 180-4) of a host buffer as 64 hex chars + NUL: the digest
  * stro_sim_digest computes over the downloaded state, for caller-held copies. */

@@ -99,6 +99,22 @@ def lib():
         "stro_sim_digest": ([_P, ctypes.c_char_p], c_int),
         "stro_sim_mass": ([_P, ctypes.POINTER(c_double)], c_int),
         "stro_sim_check_finite": ([_P, ctypes.POINTER(c_int)], c_int),
+        "stro_sim_set_variant": ([_P, ctypes.c_int32], c_int),
+        "stro_sim_get_variant": ([_P, ctypes.POINTER(ctypes.c_int32)], c_int),
+        "stro_sim_set_block": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
+        "stro_sim_get_block": ([_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)], c_int),
+        "stro_sim_autotune": ([_P, c_i64, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                               ctypes.POINTER(c_double)], c_int),
+        "stro_batch_create": ([_P, ctypes.c_int32, _P, ctypes.POINTER(_P)], c_int),
+        "stro_batch_destroy": ([_P], c_int),
+        "stro_batch_set_mode": ([_P, ctypes.c_int32], c_int),
+        "stro_batch_set_tile": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
+        "stro_batch_set_spin_limit": ([_P, c_i64], c_int),
+        "stro_batch_run": ([_P, _P, _P, _P, ctypes.c_int32, _P], c_int),
+        "stro_batch_gpu_seconds": ([_P, ctypes.POINTER(c_double)], c_int),
+        "stro_batch_last_path": ([_P, ctypes.c_char_p, ctypes.c_size_t], c_int),
+        "stro_batch_autotune": ([_P, c_i64, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                                 ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(c_double)], c_int),
         "stro_sha256_hex": ([_P, ctypes.c_size_t, ctypes.c_char_p], c_int),
         "stro_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(_P)], c_int),
         "stro_host_free": ([_P], c_int),
@@ -408,6 +424,111 @@ class Simulation:
         v = ctypes.c_int()
         _check(lib().stro_sim_check_finite(self._h, ctypes.byref(v)))
         return bool(v.value)
+
+    # -- launch shape ---------------------------------------------------------
+    @property
+    def block(self):
+        bx, by = ctypes.c_int32(), ctypes.c_int32()
+        _check(lib().stro_sim_get_block(self._h, ctypes.byref(bx), ctypes.byref(by)))
+        return bx.value, by.value
+
+    @block.setter
+    def block(self, v):
+        _check(lib().stro_sim_set_block(self._h, int(v[0]), int(v[1])))
+
+    @property
+    def variant(self):
+        v = ctypes.c_int32()
+        _check(lib().stro_sim_get_variant(self._h, ctypes.byref(v)))
+        return v.value
+
+    @variant.setter
+    def variant(self, v):
+        _check(lib().stro_sim_set_variant(self._h, int(v)))
+
+    def autotune(self, steps=20):
+        """Pick the fastest kernel variant and launch shape (state restored); returns (bx, by, GLUPS)."""
+        bx, by, g = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_double()
+        _check(lib().stro_sim_autotune(self._h, int(steps), ctypes.byref(bx), ctypes.byref(by),
+                                       ctypes.byref(g)))
+        return bx.value, by.value, g.value
+
+
+class Batch:
+    """Several simulations of one precision advanced together (stro_batch_*).
+
+    mode: "persistent" (one cooperative kernel in a CUDA graph), "rounds" (a
+    graph of one launch per round) or "sequential" (one instance after another,
+    the reference's order)."""
+
+    MODES = {"persistent": 0, "rounds": 1, "sequential": 2}
+
+    def __init__(self, gpu, sims, mode="persistent"):
+        self.sims = list(sims)
+        arr = (_P * len(self.sims))(*[s._h for s in self.sims])
+        self._h = _P()
+        _check(lib().stro_batch_create(gpu._h, len(self.sims), arr, ctypes.byref(self._h)))
+        self.mode = mode
+
+    @property
+    def mode(self):
+        return self._mode
+
+    @mode.setter
+    def mode(self, m):
+        _check(lib().stro_batch_set_mode(self._h, self.MODES[m]))
+        self._mode = m
+
+    def setTile(self, bx, by):
+        _check(lib().stro_batch_set_tile(self._h, int(bx), int(by)))
+
+    def setSpinLimit(self, polls):
+        _check(lib().stro_batch_set_spin_limit(self._h, int(polls)))
+
+    def run(self, steps, logEvery=None):
+        """Advance sims[i] by steps[i]; returns kinetic-energy traces (lists) or None."""
+        n = len(self.sims)
+        st = np.ascontiguousarray(steps, dtype=np.int64).reshape(n)
+        if logEvery is None:
+            _check(lib().stro_batch_run(self._h, st.ctypes.data, None, None, 0, None))
+            return None
+        le = np.ascontiguousarray(logEvery, dtype=np.int32).reshape(n)
+        stride = int(max(1, max((s // l + 1) if l > 0 else 0 for s, l in zip(st, le))))
+        tr = np.zeros((n, stride), np.float64)
+        cnt = np.zeros(n, np.int32)
+        _check(lib().stro_batch_run(self._h, st.ctypes.data, le.ctypes.data, tr.ctypes.data,
+                                    stride, cnt.ctypes.data))
+        return [tr[i, :cnt[i]].copy() for i in range(n)]
+
+    @property
+    def gpuSeconds(self):
+        v = ctypes.c_double()
+        _check(lib().stro_batch_gpu_seconds(self._h, ctypes.byref(v)))
+        return v.value
+
+    @property
+    def lastPath(self):
+        buf = ctypes.create_string_buffer(64)
+        _check(lib().stro_batch_last_path(self._h, buf, 64))
+        return buf.value.decode()
+
+    def autotune(self, rounds=20):
+        m, bx, by, sec = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_double()
+        _check(lib().stro_batch_autotune(self._h, int(rounds), ctypes.byref(m), ctypes.byref(bx),
+                                         ctypes.byref(by), ctypes.byref(sec)))
+        self._mode = {v: k for k, v in self.MODES.items()}[m.value]
+        return self._mode, bx.value, by.value, sec.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().stro_batch_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def sha256Hex(data):

@@ -1,0 +1,226 @@
+// Batched stepping of many independent lattices of uneven size.
+//
+// The reference runs the rungs of a credibility ladder and its Mach anchors
+// one after another on one queue (Ladder.swift:74-121). Here all instances
+// advance together: every lattice is cut into tiles of one block each, the
+// instances are sorted by step count (longest first) so that the instances
+// still running in round r are a prefix of the list and so are their tiles,
+// and each round processes the active prefix.
+//
+// Two launch forms, both captured in a CUDA graph by the host:
+//   k_batch_persistent  one cooperative launch; blocks loop over rounds and
+//                       meet at a grid barrier between rounds. Every wait is
+//                       bounded: after `spin_limit` polls the block records a
+//                       timeout in the control word and returns, and the other
+//                       blocks leave at their next barrier.
+//   k_batch_round       one launch per round over the active tiles (the graph
+//                       holds the rounds in order; kernel boundaries are the
+//                       barriers).
+// DDFs are read through L2 only inside the persistent kernel: a slot written by
+// another SM in the previous round must not be served from this SM's L1.
+//
+// Optional per-instance kinetic-energy traces are fused into the even pass:
+// on a logging round each tile reduces sum |u|^2 of its cells (FP64, fixed
+// order) into one partial, and the partials of an instance are folded in tile
+// order after the round, so a trace is bitwise reproducible.
+#include "lbm_batch.h"
+#include "lbm_cell.cuh"
+
+namespace stro {
+
+namespace {
+
+__device__ __forceinline__ int find_instance(const BatchArgs& b, uint32_t tile) {
+    int k = 0;
+    while (k + 1 < b.count && b.inst[k + 1].tile_begin <= tile) ++k;
+    return k;
+}
+
+__device__ __forceinline__ uint32_t active_tiles(const BatchArgs& b, int64_t r) {
+    uint32_t tiles = 0;
+    for (int k = 0; k < b.count; ++k) {
+        if (b.inst[k].steps <= r) break;
+        tiles = b.inst[k].tile_begin + b.inst[k].ntiles;
+    }
+    return tiles;
+}
+
+__device__ __forceinline__ bool logs_at(const BatchInstance& I, int64_t r) {
+    return I.log_every > 0 && r < I.steps && (r % I.log_every) == 0 && ((I.t0 + r) & 1) == 0;
+}
+
+template <typename S, int GEO, bool FEAT, bool CG>
+__device__ __forceinline__ void process_tile(const BatchArgs& b, const BatchInstance& I,
+                                             uint32_t tile, int64_t r) {
+    const uint32_t rem = tile - I.tile_begin;
+    const uint32_t bxi = rem % I.tiles_x;
+    const uint32_t t2 = rem / I.tiles_x;
+    const uint32_t byi = t2 % I.tiles_y;
+    const int z = int(t2 / I.tiles_y);
+    const int x = int(bxi * blockDim.x + threadIdx.x);
+    const int y = int(byi * blockDim.y + threadIdx.y);
+    const bool in = x < I.a.nx && y < I.a.ny;
+    if (((I.t0 + r) & 1) == 0) {
+        if (logs_at(I, r)) {
+            float u2 = 0.0f;
+            if (in) even_cell<S, GEO, FEAT, true, CG>(I.a, x, y, z, &u2);
+            double v[1] = {(double)u2};
+            block_reduce_store<1>(v, b.kepart + tile);
+        } else if (in) {
+            even_cell<S, GEO, FEAT, false, CG>(I.a, x, y, z);
+        }
+    } else if (in) {
+        double dummy[3];
+        if (I.ramp != nullptr) {
+            const float rr = I.ramp[r];
+            const WallVel wv(I.uin_target * rr, I.lid_target[0] * rr, I.lid_target[1] * rr,
+                             I.lid_target[2] * rr);
+            odd_cell<S, GEO, FEAT, false, CG>(I.a, wv, x, y, z, dummy);
+        } else {
+            odd_cell<S, GEO, FEAT, false, CG>(I.a, WallVel(I.a), x, y, z, dummy);
+        }
+    }
+}
+
+// Fold the kinetic-energy partials of every instance that logged in round r,
+// in tile order, into its trace. Called by one whole block.
+__device__ void fold_logs(const BatchArgs& b, int64_t r) {
+    for (int k = 0; k < b.count; ++k) {
+        const BatchInstance& I = b.inst[k];
+        if (!logs_at(I, r)) continue;
+        const int64_t s = r / I.log_every;
+        double acc[1] = {0.0};
+        const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+        const int nth = blockDim.x * blockDim.y;
+        for (uint32_t t = tid; t < I.ntiles; t += nth) acc[0] += __ldcg(b.kepart + I.tile_begin + t);
+        __shared__ double folded[1];
+        block_reduce_store<1>(acc, folded);
+        if (tid == 0 && s < I.trace_cap) I.trace[s] = folded[0];
+        __syncthreads();
+    }
+}
+
+// Bounded grid barrier (sense by generation counter). Returns false when any
+// block has recorded a timeout; the caller then returns.
+__device__ bool grid_barrier(BatchCtl* ctl, unsigned& gen, long long spin_limit, int64_t r) {
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        __threadfence();
+        const unsigned nblocks = gridDim.x;
+        if (atomicAdd(&ctl->arrived, 1u) == nblocks - 1) {
+            atomicExch(&ctl->arrived, 0u);
+            __threadfence();
+            atomicExch(&ctl->generation, gen + 1);
+        } else {
+            long long spins = 0;
+            while (atomicAdd(&ctl->generation, 0u) == gen) {
+                if (atomicAdd(&ctl->error, 0) != 0) break;
+                if (++spins > spin_limit) {
+                    if (atomicCAS(&ctl->error, 0, 1) == 0) ctl->error_round = r;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    ++gen;
+    return *((volatile int*)&ctl->error) == 0;
+}
+
+template <typename S, int GEO, bool FEAT>
+__global__ void __launch_bounds__(256) k_batch_persistent(const BatchArgs b) {
+    unsigned gen = 0;
+    for (int64_t r = 0; r < b.max_steps; ++r) {
+        if (blockIdx.x == 0 && r > 0) fold_logs(b, r - 1);
+        const uint32_t tiles = active_tiles(b, r);
+        for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+            const BatchInstance& I = b.inst[find_instance(b, tile)];
+            process_tile<S, GEO, FEAT, true>(b, I, tile, r);
+        }
+        if (!grid_barrier(b.ctl, gen, b.spin_limit, r)) return;
+    }
+    if (blockIdx.x == 0 && b.max_steps > 0) fold_logs(b, b.max_steps - 1);
+}
+
+template <typename S, int GEO, bool FEAT>
+__global__ void __launch_bounds__(256) k_batch_round(const BatchArgs b, int64_t r) {
+    const uint32_t tile = blockIdx.x;
+    const BatchInstance& I = b.inst[find_instance(b, tile)];
+    process_tile<S, GEO, FEAT, false>(b, I, tile, r);
+}
+
+__global__ void __launch_bounds__(256) k_batch_fold(const BatchArgs b, int64_t r) {
+    fold_logs(b, r);
+}
+
+template <typename S, int GEO, bool FEAT>
+const void* persistent_fn() {
+    return reinterpret_cast<const void*>(&k_batch_persistent<S, GEO, FEAT>);
+}
+
+template <typename S>
+const void* pick_persistent(int geo, bool feat) {
+    if (geo) return feat ? persistent_fn<S, 1, true>() : persistent_fn<S, 1, false>();
+    return feat ? persistent_fn<S, 0, true>() : persistent_fn<S, 0, false>();
+}
+
+template <typename S>
+cudaError_t launch_round_typed(const BatchArgs& b, int geo, bool feat, int64_t r, uint32_t tiles,
+                               dim3 block, cudaStream_t st) {
+    if (geo) {
+        if (feat) k_batch_round<S, 1, true><<<tiles, block, 0, st>>>(b, r);
+        else k_batch_round<S, 1, false><<<tiles, block, 0, st>>>(b, r);
+    } else {
+        if (feat) k_batch_round<S, 0, true><<<tiles, block, 0, st>>>(b, r);
+        else k_batch_round<S, 0, false><<<tiles, block, 0, st>>>(b, r);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+const void* batch_persistent_kernel(int half_storage, int geo, bool feat) {
+    return half_storage ? pick_persistent<__half>(geo, feat) : pick_persistent<float>(geo, feat);
+}
+
+cudaError_t launch_batch_persistent(const BatchArgs& b, int half_storage, int geo, bool feat,
+                                    unsigned grid, dim3 block, cudaStream_t st) {
+    const void* fn = batch_persistent_kernel(half_storage, geo, feat);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid, 1, 1);
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void* args[] = {const_cast<BatchArgs*>(&b)};
+    return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
+cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, bool feat, int64_t r,
+                               uint32_t tiles, dim3 block, cudaStream_t st) {
+    if (tiles == 0) return cudaSuccess;
+    return half_storage ? launch_round_typed<__half>(b, geo, feat, r, tiles, block, st)
+                        : launch_round_typed<float>(b, geo, feat, r, tiles, block, st);
+}
+
+cudaError_t launch_batch_fold(const BatchArgs& b, int64_t r, cudaStream_t st) {
+    k_batch_fold<<<1, 256, 0, st>>>(b, r);
+    return cudaGetLastError();
+}
+
+int batch_persistent_blocks_per_sm(int half_storage, int geo, bool feat, dim3 block) {
+    int n = 0;
+    const void* fn = batch_persistent_kernel(half_storage, geo, feat);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, int(block.x * block.y * block.z), 0) !=
+        cudaSuccess)
+        return 0;
+    return n;
+}
+
+}  // namespace stro

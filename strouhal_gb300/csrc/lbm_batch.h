@@ -1,0 +1,52 @@
+// Batched stepping: per-instance descriptors and launchers (lbm_batch.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "lbm_device.cuh"
+
+namespace stro {
+
+// One lattice of a batch. Device-resident, read-only during a launch.
+struct BatchInstance {
+    StepArgs a;               // step arguments (uin/ulid at ramp factor 1 when `ramp` is set)
+    float uin_target;         // unramped targets, used with `ramp`
+    float lid_target[3];
+    const float* ramp;        // ramp factor per round (rounds [0, steps)), or nullptr
+    int64_t t0;               // stepsDone when the batch starts
+    int64_t steps;            // rounds this instance takes part in
+    int32_t log_every;        // log sum |u|^2 every so many rounds (even, 0 = off)
+    int32_t trace_cap;        // capacity of `trace`
+    double* trace;            // kinetic-energy samples: trace[s] at round s * log_every
+    uint32_t tile_begin;      // first tile of this instance in the batch tile list
+    uint32_t ntiles;          // tiles_x * tiles_y * nz
+    uint32_t tiles_x, tiles_y;
+};
+
+// Grid-barrier and error state of the persistent launch (zeroed before each launch).
+struct BatchCtl {
+    unsigned arrived;
+    unsigned generation;
+    int error;                // 1: a barrier wait timed out
+    int pad;
+    long long error_round;
+};
+
+struct BatchArgs {
+    const BatchInstance* inst;  // sorted by `steps`, longest first
+    int32_t count;
+    int64_t max_steps;
+    double* kepart;             // one kinetic-energy partial per tile
+    BatchCtl* ctl;
+    long long spin_limit;       // polls before a barrier wait gives up
+};
+
+cudaError_t launch_batch_persistent(const BatchArgs& b, int half_storage, int geo, bool feat,
+                                    unsigned grid, dim3 block, cudaStream_t st);
+cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, bool feat, int64_t r,
+                               uint32_t tiles, dim3 block, cudaStream_t st);
+cudaError_t launch_batch_fold(const BatchArgs& b, int64_t r, cudaStream_t st);
+int batch_persistent_blocks_per_sm(int half_storage, int geo, bool feat, dim3 block);
+
+}  // namespace stro

@@ -1,0 +1,476 @@
+// Per-cell bodies of the D3Q19 AA step, shared by the single-lattice kernels
+// (lbm_step.cu) and the batched persistent kernel (lbm_batch.cu).
+//
+// Restates the reference's `collide` (Kernels.metal:105-228) and the two
+// branches of its `step` kernel (Kernels.metal:252-354) with the same FP32
+// operation order; see lbm_step.cu for the arithmetic contract.
+#pragma once
+
+#include "lbm_device.cuh"
+
+namespace stro {
+
+__device__ __forceinline__ int wrapi(int v, int n) {  // Kernels.metal:73-77
+    v += (v < 0) ? n : 0;
+    v -= (v >= n) ? n : 0;
+    return v;
+}
+
+// Ramped moving-wall velocities of one step (Sim.swift:270-275).
+struct WallVel {
+    float uin, lx, ly, lz;
+    __device__ __forceinline__ explicit WallVel(const StepArgs& a)
+        : uin(a.uin), lx(a.ulid_x), ly(a.ulid_y), lz(a.ulid_z) {}
+    __device__ __forceinline__ WallVel(float u, float x, float y, float z)
+        : uin(u), lx(x), ly(y), lz(z) {}
+};
+
+// Wall velocity of a moving-wall cell at row wy, Kernels.metal:79-87.
+__device__ __forceinline__ void wall_velocity(uint8_t wf, int wy, const StepArgs& a,
+                                              const WallVel& wv, float& ux, float& uy,
+                                              float& uz) {
+    if (wf == CELL_LID) {
+        ux = wv.lx; uy = wv.ly; uz = wv.lz;
+        return;
+    }
+    uy = 0.0f; uz = 0.0f;
+    if (a.inflow_uniform != 0) { ux = wv.uin; return; }
+    const float H = (float)a.ny - 2.0f;
+    const float yd = (float)wy - 0.5f;
+    ux = fmaxf(4.0f * wv.uin * yd * (H - yd) / (H * H), 0.0f);
+}
+
+// Relaxation of the rest direction and the nine antipodal pairs
+// (Kernels.metal:169-227). FORCE adds the TRT-split Guo source, NT blends with
+// the Noble-Torczynski bounce operator and accumulates its force.
+template <bool FORCE, bool NT>
+__device__ __forceinline__ void relax(float (&fh)[19], float wp, float wm, float rho, float rhom1,
+                                      float ux, float uy, float uz, float u2, float Fx, float Fy,
+                                      float Fz, float eps, float& ntx, float& nty, float& ntz) {
+    const float feq0 = wgt(0) * (rhom1 - 1.5f * rho * u2);
+    float uF = 0.0f, ap = 0.0f, am = 0.0f;
+    if constexpr (FORCE) {
+        uF = ux * Fx + uy * Fy + uz * Fz;
+        ap = 1.0f - 0.5f * wp;
+        am = 1.0f - 0.5f * wm;
+    }
+    float B = 0.0f, omb = 1.0f;
+    if constexpr (!NT) {
+        if constexpr (FORCE) {
+            const float s0 = wgt(0) * ap * (-3.0f * uF);
+            fh[0] = fmaf(wp, feq0 - fh[0], fh[0]) + s0;
+        } else {
+            fh[0] = fmaf(wp, feq0 - fh[0], fh[0]);
+        }
+    } else {
+        const float tw = 1.0f / wp - 0.5f;
+        B = eps * tw / ((1.0f - eps) + tw);
+        omb = 1.0f - B;
+        if constexpr (FORCE) {
+            const float s0 = wgt(0) * ap * (-3.0f * uF);
+            fh[0] += omb * (wp * (feq0 - fh[0]) + s0);
+        } else {
+            fh[0] += omb * (wp * (feq0 - fh[0]));
+        }
+    }
+    const float u2t = 1.5f * u2;
+    sfor<0, 9>([&](auto P) {
+        constexpr int i = 2 * P + 1;
+        constexpr float w = wgt(i);
+        const float cu = 3.0f * cdot<i>(ux, uy, uz);
+        const float feqp = w * (rhom1 + rho * (0.5f * cu * cu - u2t));
+        const float feqm = w * rho * cu;
+        const float fp = 0.5f * (fh[i] + fh[i + 1]);
+        const float fm = 0.5f * (fh[i] - fh[i + 1]);
+        const float dp = wp * (feqp - fp);
+        const float dm = wm * (feqm - fm);
+        float up, um;
+        if constexpr (FORCE) {
+            const float cF = cdot<i>(Fx, Fy, Fz);
+            const float sm = w * am * (3.0f * cF);
+            const float sp = w * ap * (3.0f * cu * cF - 3.0f * uF);
+            up = dp + dm + sp + sm;
+            um = dp - dm + sp - sm;
+        } else {
+            up = dp + dm;
+            um = dp - dm;
+        }
+        if constexpr (!NT) {
+            fh[i] += up;
+            fh[i + 1] += um;
+        } else {
+            const float bounce = B * (fh[i + 1] - fh[i]);
+            fh[i] += omb * up + bounce;
+            fh[i + 1] += omb * um - bounce;
+            if constexpr (dcx(i) > 0) ntx -= 2.0f * bounce;
+            if constexpr (dcx(i) < 0) ntx += 2.0f * bounce;
+            if constexpr (dcy(i) > 0) nty -= 2.0f * bounce;
+            if constexpr (dcy(i) < 0) nty += 2.0f * bounce;
+            if constexpr (dcz(i) > 0) ntz -= 2.0f * bounce;
+            if constexpr (dcz(i) < 0) ntz += 2.0f * bounce;
+        }
+    });
+}
+
+// Collision, Kernels.metal:105-228.
+template <bool FEAT>
+__device__ __forceinline__ void collide(float (&fh)[19], const StepArgs& a, int x, float eps,
+                                        float Fx, float Fy, float Fz, float& ntx, float& nty,
+                                        float& ntz) {
+    float wp = a.omega, wm = a.omega_minus;
+    if constexpr (FEAT) {
+        if ((float)x > a.sponge_x0) {  // viscous sponge, Kernels.metal:112-123
+            const float frac = fminf(((float)x - a.sponge_x0) * a.sponge_inv_w, 1.0f);
+            const float tau0 = 1.0f / wp;
+            const float tauS = tau0 + frac * (a.sponge_tau - tau0);
+            if (a.omega_minus == a.omega) {
+                wp = 1.0f / tauS;
+                wm = wp;
+            } else {
+                const float lambda = (1.0f / wp - 0.5f) * (1.0f / wm - 0.5f);
+                wp = 1.0f / tauS;
+                wm = 1.0f / (0.5f + lambda / (tauS - 0.5f));
+            }
+        }
+    }
+    float rhom1 = fh[0];
+    sfor<1, 19>([&](auto I) { rhom1 += fh[I]; });
+    const float rho = 1.0f + rhom1;
+    const float inv = 1.0f / rho;
+    float px = fh[1], py = fh[3], pz = fh[5];
+    sfor<2, 19>([&](auto I) {
+        constexpr int i = I;
+        if constexpr (dcx(i) > 0) px += fh[i];
+        if constexpr (dcx(i) < 0) px -= fh[i];
+    });
+    sfor<4, 19>([&](auto I) {
+        constexpr int i = I;
+        if constexpr (dcy(i) > 0) py += fh[i];
+        if constexpr (dcy(i) < 0) py -= fh[i];
+    });
+    sfor<6, 19>([&](auto I) {
+        constexpr int i = I;
+        if constexpr (dcz(i) > 0) pz += fh[i];
+        if constexpr (dcz(i) < 0) pz -= fh[i];
+    });
+    float ux, uy, uz;
+    if constexpr (FEAT) {
+        ux = (px + 0.5f * Fx) * inv;
+        uy = (py + 0.5f * Fy) * inv;
+        uz = (pz + 0.5f * Fz) * inv;
+    } else {
+        ux = px * inv;
+        uy = py * inv;
+        uz = pz * inv;
+    }
+    const float u2 = ux * ux + uy * uy + uz * uz;
+
+    if constexpr (FEAT) {
+        if (a.c_smago > 0.0f) {  // Smagorinsky LES, Kernels.metal:140-167
+            float pxx = 0.f, pyy = 0.f, pzz = 0.f, pxy = 0.f, pxz = 0.f, pyz = 0.f;
+            sfor<1, 19>([&](auto I) {
+                constexpr int i = I;
+                constexpr float w = wgt(i);
+                const float cu = 3.0f * cdot<i>(ux, uy, uz);
+                const float feq = w * (rhom1 + rho * (cu + 0.5f * cu * cu - 1.5f * u2));
+                const float d = fh[i] - feq;
+                // first nonzero term of each sum starts it (index 1, 3, 5, 7, 11, 15)
+                if constexpr (dcx(i) != 0) pxx = (i == 1) ? d : pxx + d;
+                if constexpr (dcy(i) != 0) pyy = (i == 3) ? d : pyy + d;
+                if constexpr (dcz(i) != 0) pzz = (i == 5) ? d : pzz + d;
+                if constexpr (dcx(i) * dcy(i) > 0) pxy = (i == 7) ? d : pxy + d;
+                if constexpr (dcx(i) * dcy(i) < 0) pxy -= d;
+                if constexpr (dcx(i) * dcz(i) > 0) pxz = (i == 11) ? d : pxz + d;
+                if constexpr (dcx(i) * dcz(i) < 0) pxz -= d;
+                if constexpr (dcy(i) * dcz(i) > 0) pyz = (i == 15) ? d : pyz + d;
+                if constexpr (dcy(i) * dcz(i) < 0) pyz -= d;
+            });
+            const float Q = sqrtf(pxx * pxx + pyy * pyy + pzz * pzz +
+                                  2.0f * (pxy * pxy + pxz * pxz + pyz * pyz));
+            const float tau0 = 1.0f / wp;
+            const float tauEff =
+                0.5f * (tau0 + sqrtf(tau0 * tau0 + 25.455844f * a.c_smago * Q * inv));
+            if (a.omega_minus == a.omega) {
+                wp = 1.0f / tauEff;
+                wm = wp;
+            } else {
+                const float lambda = (1.0f / wp - 0.5f) * (1.0f / wm - 0.5f);
+                wp = 1.0f / tauEff;
+                wm = 1.0f / (0.5f + lambda / (tauEff - 0.5f));
+            }
+        }
+        if (eps == 0.0f) {
+            if (a.force_on) relax<true, false>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, Fx, Fy, Fz, eps, ntx, nty, ntz);
+            else relax<false, false>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, Fx, Fy, Fz, eps, ntx, nty, ntz);
+        } else {
+            if (a.force_on) relax<true, true>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, Fx, Fy, Fz, eps, ntx, nty, ntz);
+            else relax<false, true>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, Fx, Fy, Fz, eps, ntx, nty, ntz);
+        }
+    } else {
+        relax<false, false>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, 0.f, 0.f, 0.f, 0.f, ntx, nty, ntz);
+    }
+}
+
+template <bool FEAT>
+__device__ __forceinline__ void cell_force(const StepArgs& a, uint32_t n, float& Fx, float& Fy,
+                                           float& Fz) {
+    Fx = a.fx; Fy = a.fy; Fz = a.fz;
+    if constexpr (FEAT) {
+        if (a.ffield != nullptr) {
+            Fx = a.fx + a.ffield[n];
+            Fy = a.fy + a.ffield[a.ffield_plane + n];
+            Fz = a.fz + a.ffield[2u * a.ffield_plane + n];
+        }
+    }
+}
+
+// c_i * v added to (ax, ay, az), zero components skipped.
+template <int I>
+__device__ __forceinline__ void acc_add(float& ax, float& ay, float& az, float v) {
+    if constexpr (dcx(I) > 0) ax += v;
+    if constexpr (dcx(I) < 0) ax -= v;
+    if constexpr (dcy(I) > 0) ay += v;
+    if constexpr (dcy(I) < 0) ay -= v;
+    if constexpr (dcz(I) > 0) az += v;
+    if constexpr (dcz(I) < 0) az -= v;
+}
+template <int I>
+__device__ __forceinline__ void acc_sub(float& ax, float& ay, float& az, float v) {
+    if constexpr (dcx(I) > 0) ax -= v;
+    if constexpr (dcx(I) < 0) ax += v;
+    if constexpr (dcy(I) > 0) ay -= v;
+    if constexpr (dcy(I) < 0) ay += v;
+    if constexpr (dcz(I) > 0) az -= v;
+    if constexpr (dcz(I) < 0) az += v;
+}
+
+// Wrapped neighbour offsets of one cell: the linear offset of x-1, x+1, ...
+struct NbrOffsets {
+    int xm, xp, ym, yp, zm, zp;
+    __device__ __forceinline__ NbrOffsets(int x, int y, int z, int nx, int ny, int nz) {
+        const int nxy = nx * ny;
+        xm = (x == 0) ? nx - 1 : -1;
+        xp = (x == nx - 1) ? -(nx - 1) : 1;
+        ym = (y == 0) ? (ny - 1) * nx : -nx;
+        yp = (y == ny - 1) ? -(ny - 1) * nx : nx;
+        zm = (z == 0) ? (nz - 1) * nxy : -nxy;
+        zp = (z == nz - 1) ? -(nz - 1) * nxy : nxy;
+    }
+    template <int DX, int DY, int DZ>
+    __device__ __forceinline__ int off() const {
+        return (DX > 0 ? xp : (DX < 0 ? xm : 0)) + (DY > 0 ? yp : (DY < 0 ? ym : 0)) +
+               (DZ > 0 ? zp : (DZ < 0 ? zm : 0));
+    }
+};
+
+// Deferred moving-wall corrections of the gathered DDFs, Kernels.metal:292-314.
+template <bool PROBE>
+__device__ __forceinline__ void moving_wall_loads(float (&fh)[19], const StepArgs& a,
+                                                  const WallVel& wv, uint32_t wb, uint32_t lm,
+                                                  int x, int y, int z, float& ax, float& ay,
+                                                  float& az) {
+    sfor<1, 19>([&](auto I) {
+        constexpr int i = I;
+        constexpr int bit = opp(i) - 1;
+        if (((wb >> bit) & 1u) && ((lm >> bit) & 1u)) {
+            const int sy = wrapi(y - dcy(i), a.ny);
+            const uint32_t s = (uint32_t(wrapi(z - dcz(i), a.nz)) * uint32_t(a.ny) + uint32_t(sy)) *
+                                   uint32_t(a.nx) +
+                               uint32_t(wrapi(x - dcx(i), a.nx));
+            const uint8_t wf = a.cell[s] & CELL_TYPE_MASK;
+            if (wf == CELL_OUTFLOW) {
+                fh[i] = -fh[i];
+            } else {
+                float uwx, uwy, uwz;
+                wall_velocity(wf, sy, a, wv, uwx, uwy, uwz);
+                const float corr = 6.0f * wgt(i) * cdot<i>(uwx, uwy, uwz);
+                fh[i] += corr;
+                if constexpr (PROBE) acc_sub<i>(ax, ay, az, corr);
+            }
+        }
+    });
+}
+
+// Scatter with moving-wall corrections, Kernels.metal:317-350.
+template <typename S, bool PROBE>
+__device__ __forceinline__ void moving_wall_stores(const float (&fh)[19], const StepArgs& a,
+                                                   const WallVel& wv, uint32_t n, uint32_t wb,
+                                                   uint32_t lm, int x, int y, int z,
+                                                   const NbrOffsets& nb, float& ax, float& ay,
+                                                   float& az) {
+    S* __restrict__ f = static_cast<S*>(a.f);
+    const uint64_t P = a.plane;
+    sfor<1, 19>([&](auto I) {
+        constexpr int i = I;
+        if (!((wb >> (i - 1)) & 1u)) {
+            store_ddf<S>(f + uint64_t(i) * P + uint32_t(int(n) + nb.template off<dcx(i), dcy(i), dcz(i)>()), fh[i]);
+        } else {
+            float sv = fh[i];
+            float out = sv;
+            if ((lm >> (i - 1)) & 1u) {
+                const int dy = wrapi(y + dcy(i), a.ny);
+                const uint32_t d = (uint32_t(wrapi(z + dcz(i), a.nz)) * uint32_t(a.ny) + uint32_t(dy)) *
+                                       uint32_t(a.nx) +
+                                   uint32_t(wrapi(x + dcx(i), a.nx));
+                const uint8_t wf = a.cell[d] & CELL_TYPE_MASK;
+                if (wf == CELL_OUTFLOW) {
+                    sv = -fh[i];
+                    out = sv;
+                } else {
+                    float uwx, uwy, uwz;
+                    wall_velocity(wf, dy, a, wv, uwx, uwy, uwz);
+                    const float corr = 6.0f * wgt(i) * cdot<i>(uwx, uwy, uwz);
+                    out = sv - corr;
+                }
+            }
+            store_ddf<S>(f + uint64_t(opp(i)) * P + n, out);
+            if constexpr (PROBE) acc_add<i>(ax, ay, az, sv + 2.0f * wgt(i));
+        }
+    });
+}
+
+
+// |u|^2 of a cell's natural-slot DDFs, formed as momentsEven does
+// (Kernels.metal:368-379: division by rho) and as the host energy loop squares
+// it (Cases.swift:1242).
+__device__ __forceinline__ float cell_u2(const float (&fh)[19], float Fx, float Fy, float Fz) {
+    float rhom1 = fh[0];
+    sfor<1, 19>([&](auto I) { rhom1 += fh[I]; });
+    float px = fh[1], py = fh[3], pz = fh[5];
+    sfor<2, 19>([&](auto I) {
+        constexpr int i = I;
+        if constexpr (dcx(i) > 0) px += fh[i];
+        if constexpr (dcx(i) < 0) px -= fh[i];
+    });
+    sfor<4, 19>([&](auto I) {
+        constexpr int i = I;
+        if constexpr (dcy(i) > 0) py += fh[i];
+        if constexpr (dcy(i) < 0) py -= fh[i];
+    });
+    sfor<6, 19>([&](auto I) {
+        constexpr int i = I;
+        if constexpr (dcz(i) > 0) pz += fh[i];
+        if constexpr (dcz(i) < 0) pz -= fh[i];
+    });
+    const float rho = 1.0f + rhom1;
+    const float ux = (px + 0.5f * Fx) / rho, uy = (py + 0.5f * Fy) / rho,
+                uz = (pz + 0.5f * Fz) / rho;
+    return ux * ux + uy * uy + uz * uz;
+}
+
+// Even (in-cell) pass of one cell, Kernels.metal:252-260. Non-fluid cells are
+// skipped. With LOG, u2 receives |u|^2 of the state before the step.
+template <typename S, int GEO, bool FEAT, bool LOG = false, bool CG = false>
+__device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z,
+                                          float* u2 = nullptr) {
+    const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
+    float eps = 0.0f;
+    if constexpr (GEO) {
+        const uint8_t c = a.cell[n];
+        if (c & CELL_TYPE_MASK) return;
+        if constexpr (FEAT) {
+            if (c & CELL_EPS_BIT) eps = a.eps[n];
+        }
+    }
+    S* __restrict__ f = static_cast<S*>(a.f);
+    const uint64_t P = a.plane;
+    float fh[19];
+    sfor<0, 19>([&](auto I) { fh[I] = load_slot<S, CG>(f + uint64_t(I) * P + n); });
+    float Fx = 0.f, Fy = 0.f, Fz = 0.f;
+    cell_force<FEAT>(a, n, Fx, Fy, Fz);
+    if constexpr (LOG) *u2 = cell_u2(fh, Fx, Fy, Fz);
+    float ntx = 0.f, nty = 0.f, ntz = 0.f;
+    collide<FEAT>(fh, a, x, eps, Fx, Fy, Fz, ntx, nty, ntz);
+    store_ddf<S>(f + n, fh[0]);
+    sfor<1, 19>([&](auto I) { store_ddf<S>(f + uint64_t(opp(I)) * P + n, fh[I]); });
+}
+
+// Odd (streaming) pass of one cell with halfway / moving-wall bounce-back,
+// Kernels.metal:261-354. With PROBE the cell's momentum-exchange force is
+// returned in contrib when the cell is a boundary cell inside the probe box.
+template <typename S, int GEO, bool FEAT, bool PROBE, bool CG = false>
+__device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, int x, int y,
+                                         int z, double (&contrib)[3]) {
+    const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
+    uint32_t g = 0;
+    if constexpr (GEO) {
+        g = a.geo[n];
+        if (g & GEO_NONFLUID) return;
+    }
+    S* __restrict__ f = static_cast<S*>(a.f);
+    const uint64_t P = a.plane;
+    const NbrOffsets nb(x, y, z, a.nx, a.ny, a.nz);
+    const uint32_t wb = g & GEO_WALL_BITS;
+    float eps = 0.0f;
+    if constexpr (GEO && FEAT) {
+        if (g & GEO_EPS) eps = a.eps[n];
+    }
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    float fh[19];
+    fh[0] = load_slot<S, CG>(f + n);
+    sfor<1, 19>([&](auto I) {
+        constexpr int i = I;
+        constexpr int o = opp(i);
+        const uint32_t src = uint32_t(int(n) + nb.template off<-dcx(i), -dcy(i), -dcz(i)>());
+        if constexpr (GEO) {
+            const bool bb = (wb >> (o - 1)) & 1u;
+            const uint64_t idx = bb ? (uint64_t(i) * P + n) : (uint64_t(o) * P + src);
+            fh[i] = load_slot<S, CG>(f + idx);
+            if constexpr (PROBE) {
+                if (bb) acc_sub<i>(ax, ay, az, fh[i]);
+            }
+        } else {
+            fh[i] = load_slot<S, CG>(f + uint64_t(o) * P + src);
+        }
+    });
+    uint32_t lm = 0;
+    if constexpr (GEO) {
+        if (g & GEO_MOVING) {
+            lm = a.lmask[n];
+            moving_wall_loads<PROBE>(fh, a, wv, wb, lm, x, y, z, ax, ay, az);
+        }
+    }
+    float Fx = 0.f, Fy = 0.f, Fz = 0.f;
+    cell_force<FEAT>(a, n, Fx, Fy, Fz);
+    float ntx = 0.f, nty = 0.f, ntz = 0.f;
+    collide<FEAT>(fh, a, x, eps, Fx, Fy, Fz, ntx, nty, ntz);
+    if constexpr (PROBE) {
+        ax += ntx;
+        ay += nty;
+        az += ntz;
+    }
+    store_ddf<S>(f + n, fh[0]);
+    if constexpr (GEO) {
+        if (!(g & GEO_MOVING)) {
+            sfor<1, 19>([&](auto I) {
+                constexpr int i = I;
+                constexpr int o = opp(i);
+                const bool bb = (wb >> (i - 1)) & 1u;
+                const uint32_t dst = uint32_t(int(n) + nb.template off<dcx(i), dcy(i), dcz(i)>());
+                const uint64_t idx = bb ? (uint64_t(o) * P + n) : (uint64_t(i) * P + dst);
+                store_ddf<S>(f + idx, fh[i]);
+                if constexpr (PROBE) {
+                    if (bb) acc_add<i>(ax, ay, az, fh[i] + 2.0f * wgt(i));
+                }
+            });
+        } else {
+            moving_wall_stores<S, PROBE>(fh, a, wv, n, wb, lm, x, y, z, nb, ax, ay, az);
+        }
+    } else {
+        sfor<1, 19>([&](auto I) {
+            constexpr int i = I;
+            const uint32_t dst = uint32_t(int(n) + nb.template off<dcx(i), dcy(i), dcz(i)>());
+            store_ddf<S>(f + uint64_t(i) * P + dst, fh[i]);
+        });
+    }
+    if constexpr (PROBE) {
+        if ((wb != 0u || eps > 0.0f) && x >= a.box_x0 && x <= a.box_x1 && y >= a.box_y0 &&
+            y <= a.box_y1) {
+            contrib[0] = (double)ax;
+            contrib[1] = (double)ay;
+            contrib[2] = (double)az;
+        }
+    }
+}
+
+}  // namespace stro

@@ -71,6 +71,18 @@ template <> __device__ __forceinline__ float load_ddf<float>(const float* p) { r
 template <> __device__ __forceinline__ float load_ddf<__half>(const __half* p) {
     return __half2float(*p);
 }
+// Load through L2 only (no L1 allocation): used where another SM may have
+// rewritten the slot since this SM last read it, inside one launch.
+template <typename S> __device__ __forceinline__ float load_ddf_cg(const S* p);
+template <> __device__ __forceinline__ float load_ddf_cg<float>(const float* p) { return __ldcg(p); }
+template <> __device__ __forceinline__ float load_ddf_cg<__half>(const __half* p) {
+    return __half2float(__ldcg(p));
+}
+template <typename S, bool CG>
+__device__ __forceinline__ float load_slot(const S* p) {
+    if constexpr (CG) return load_ddf_cg<S>(p);
+    else return load_ddf<S>(p);
+}
 template <typename S> __device__ __forceinline__ void store_ddf(S* p, float v);
 template <> __device__ __forceinline__ void store_ddf<float>(float* p, float v) { *p = v; }
 template <> __device__ __forceinline__ void store_ddf<__half>(__half* p, float v) {
@@ -140,6 +152,7 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[K], double* out) 
             if (lane == 0) out[k] = s;
         }
     }
+    __syncthreads();  // warp_sums may be reused by the next call
 }
 
 }  // namespace stro

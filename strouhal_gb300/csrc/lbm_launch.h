@@ -14,6 +14,11 @@ cudaError_t launch_step(const StepArgs& a, int half_storage, int parity, int geo
                         bool probe, dim3 block, cudaStream_t st);
 dim3 step_grid(const StepArgs& a, dim3 block);
 
+// FP16 periodic step with x-adjacent cell pairs per thread (lbm_pair.cu).
+// block.x threads cover 2*block.x cells of a row.
+bool pair_step_supported(int half_storage, int geo, bool probe, int nx, uint64_t plane, dim3 block);
+cudaError_t launch_pair_step(const StepArgs& a, int parity, bool feat, dim3 block, cudaStream_t st);
+
 // Fields and reductions (lbm_probe.cu). `plane` is the DDF plane stride in
 // elements, N the cell count. Reductions write per-block FP64 partials to
 // `partials` and then fold them in a fixed order into `out`.

@@ -22,15 +22,26 @@
 #include <string>
 #include <vector>
 
-#include "lbm_launch.h"
+#include "runtime_internal.h"
 #include "sha256.h"
-#include "strouhal_c.h"
 
 using namespace stro;
+using namespace stro::rt;
 
 namespace {
 
 thread_local std::string g_error;
+
+constexpr int CX[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+constexpr int CY[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1};
+constexpr int CZ[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
+
+uint64_t padded_plane(uint64_t N) { return (N + 63) / 64 * 64; }
+
+}  // namespace
+
+namespace stro {
+namespace rt {
 
 int fail(int code, const std::string& msg) {
     g_error = msg;
@@ -42,70 +53,8 @@ int cuda_fail(cudaError_t e, const char* what) {
     return fail(code, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define STRO_CUDA(expr)                                        \
-    do {                                                       \
-        cudaError_t e_ = (expr);                               \
-        if (e_ != cudaSuccess) return cuda_fail(e_, #expr);    \
-    } while (0)
-
-constexpr int CX[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
-constexpr int CY[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1};
-constexpr int CZ[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
-
-uint64_t padded_plane(uint64_t N) { return (N + 63) / 64 * 64; }
-
-}  // namespace
-
-struct stro_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    int sm_count = 0;
-    char name[256] = {0};
-};
-
-struct stro_sim {
-    stro_ctx* ctx = nullptr;
-    int precision = STRO_FP32;
-    int32_t nx = 0, ny = 0, nz = 0;
-    uint64_t N = 0, plane = 0;
-    size_t esize = 4;
-    // Simulation properties (Sim.swift:164-172)
-    float omega = 1.0f, omega_minus = 1.0f;
-    float lid[3] = {0, 0, 0};
-    float uin = 0.0f;
-    int32_t ramp_steps = 0;
-    float force[3] = {0, 0, 0};
-    float c_smago = 0.0f;
-    int inflow_uniform = 0;
-    bool sponge_on = false;
-    float sponge_x0 = 1e9f, sponge_width = 0.0f, sponge_tau = 1.0f;
-    bool wants_forces = false;
-    // host geometry
-    std::vector<uint8_t> flags;
-    std::vector<uint32_t> smask, lmask;
-    std::vector<float> eps;
-    bool any_wall = false, has_eps = false, has_ffield = false;
-    // device buffers
-    void* d_f = nullptr;
-    uint8_t* d_cell = nullptr;
-    uint32_t* d_geo = nullptr;
-    uint32_t* d_lmask = nullptr;
-    float* d_eps = nullptr;
-    float* d_ffield = nullptr;
-    float4* d_moments = nullptr;
-    double* d_partials = nullptr;
-    size_t partials_len = 0;
-    double* d_out = nullptr;
-    // bookkeeping
-    int64_t steps_done = 0;
-    double gpu_seconds = 0.0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    dim3 block{256, 1, 1};
-};
-
-namespace {
-
 bool geo_on(const stro_sim* s) { return s->any_wall || s->has_eps; }
+
 bool sponge_active(const stro_sim* s) {
     return s->sponge_on && s->sponge_x0 < float(s->nx - 1);
 }
@@ -201,7 +150,7 @@ int upload_geometry(stro_sim* s) {
                 s->smask[idx] = sm;
                 s->lmask[idx] = lm;
             }
-    if (!geo_on(s)) return STRO_OK;
+    if (!geo_on(s) && !s->force_geometry) return STRO_OK;
     std::vector<uint8_t> cell(N);
     std::vector<uint32_t> geo(N);
     for (uint64_t n = 0; n < N; ++n) {
@@ -246,8 +195,7 @@ int launch_one_step(stro_sim* s, int64_t t, bool probe, const int box[4]) {
     if (probe) {
         a.box_x0 = box[0]; a.box_x1 = box[1]; a.box_y0 = box[2]; a.box_y1 = box[3];
     }
-    const cudaError_t e = launch_step(a, s->precision == STRO_FP16S, int(t & 1), geo_on(s) ? 1 : 0,
-                                      feat_on(s), probe, s->block, s->ctx->stream);
+    const cudaError_t e = launch_sim_step(s, a, t, probe);
     if (e != cudaSuccess) return cuda_fail(e, "step launch");
     return STRO_OK;
 }
@@ -279,10 +227,47 @@ int ensure_partials(stro_sim* s, size_t doubles) {
     return STRO_OK;
 }
 
+cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool probe) {
+    const int half = s->precision == STRO_FP16S ? 1 : 0;
+    const int geo = geo_on(s) ? 1 : 0;
+    if (s->variant == 1 && pair_step_supported(half, geo, probe, s->nx, s->plane, s->pair_block))
+        return launch_pair_step(a, int(t & 1), feat_on(s), s->pair_block, s->ctx->stream);
+    return launch_step(a, half, int(t & 1), geo, feat_on(s), probe,
+                       probe ? s->probe_block : s->block, s->ctx->stream);
+}
+
+void ctx_retain(stro_ctx* c) { ++c->refs; }
+
+void ctx_release(stro_ctx* c) {
+    if (--c->refs > 0) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int ensure_geometry(stro_sim* s) {
+    if (s->d_cell) return STRO_OK;
+    s->force_geometry = true;
+    return upload_geometry(s);
+}
+
+}  // namespace rt
+}  // namespace stro
+
+int stro::rt::observables(stro_sim* s, double out[2]) {
+    if (s->steps_done % 2 != 0)
+        return fail(STRO_ERR_STATE, "observables require an even step count");
+    cudaSetDevice(s->ctx->device);
+    STRO_CUDA(launch_observables(field_view(s), s->precision == STRO_FP16S, s->omega,
+                                 s->d_partials, s->d_out, s->ctx->stream));
+    STRO_CUDA(cudaMemcpyAsync(out, s->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                              s->ctx->stream));
+    STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    return STRO_OK;
+}
+
 #define CHECK_SIM(s) \
     if (!(s)) return fail(STRO_ERR_INVALID, "null simulation handle")
-
-}  // namespace
 
 extern "C" {
 
@@ -316,10 +301,9 @@ int stro_ctx_create(int device, stro_ctx** out) {
 }
 
 int stro_ctx_destroy(stro_ctx* ctx) {
-    if (!ctx) return STRO_OK;
-    cudaSetDevice(ctx->device);
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
-    delete ctx;
+    if (!ctx || ctx->closed) return STRO_OK;
+    ctx->closed = true;
+    ctx_release(ctx);
     return STRO_OK;
 }
 
@@ -333,6 +317,7 @@ int stro_ctx_info(stro_ctx* ctx, char* name, size_t name_len, int* sm_count) {
 int stro_sim_create(stro_ctx* ctx, const stro_sim_desc* d, const uint8_t* flags, stro_sim** out) {
     if (!ctx || !d || !out) return fail(STRO_ERR_INVALID, "null argument");
     *out = nullptr;
+    if (ctx->closed) return fail(STRO_ERR_INVALID, "context already destroyed");
     if (d->precision != STRO_FP32 && d->precision != STRO_FP16S)
         return fail(STRO_ERR_INVALID, "precision must be STRO_FP32 or STRO_FP16S");
     if (d->nx < 1 || d->ny < 1 || d->nz < 1 || d->nx > 65535 * 256 || d->ny > 65535 ||
@@ -362,6 +347,14 @@ int stro_sim_create(stro_ctx* ctx, const stro_sim_desc* d, const uint8_t* flags,
     s->c_smago = d->c_smago;
     s->wants_forces = d->wants_forces != 0;
     s->block = default_block(d->nx);
+    s->probe_block = s->block;
+    if (d->precision == STRO_FP16S && d->nx % 64 == 0) {
+        // FP16 lattices with whole warps of cell pairs per row default to the pair variant
+        int bxp = std::min(128, d->nx / 2);
+        while ((d->nx / 2) % bxp != 0) bxp -= 32;
+        s->pair_block = dim3(bxp, 256 / bxp, 1);
+        s->variant = 1;
+    }
     try {
         s->flags.assign(N, 0);
         if (flags) std::memcpy(s->flags.data(), flags, N);
@@ -384,23 +377,26 @@ int stro_sim_create(stro_ctx* ctx, const stro_sim_desc* d, const uint8_t* flags,
     if (e != cudaSuccess) return bail(cuda_fail(e, "simulation set-up"));
     int rc = upload_geometry(s);
     if (rc != STRO_OK) return bail(rc);
-    const dim3 grid = dim3((s->nx + s->block.x - 1) / s->block.x,
-                           (s->ny + s->block.y - 1) / s->block.y, s->nz);
+    const dim3 grid = dim3((s->nx + s->probe_block.x - 1) / s->probe_block.x,
+                           (s->ny + s->probe_block.y - 1) / s->probe_block.y, s->nz);
     const size_t step_blocks = size_t(grid.x) * grid.y * grid.z;
     rc = ensure_partials(s, std::max<size_t>(s->wants_forces ? 3 * step_blocks : 0, 2 * 2048));
     if (rc != STRO_OK) return bail(rc);
     e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return bail(cuda_fail(e, "simulation set-up"));
+    ctx_retain(ctx);
     *out = s;
     return STRO_OK;
 }
 
 int stro_sim_destroy(stro_sim* s) {
     if (!s) return STRO_OK;
-    cudaSetDevice(s->ctx->device);
-    cudaStreamSynchronize(s->ctx->stream);
+    stro_ctx* c = s->ctx;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
     free_sim(s);
     delete s;
+    ctx_release(c);
     return STRO_OK;
 }
 
@@ -581,7 +577,7 @@ int stro_sim_probe_force(stro_sim* s, int32_t x0, int32_t x1, int32_t y0, int32_
     int rc = run_steps(s, 2, s->steps_done + 1, box);
     if (rc != STRO_OK) return rc;
     StepArgs a = step_args(s, 0);
-    const dim3 grid = step_grid(a, s->block);
+    const dim3 grid = step_grid(a, s->probe_block);
     const int nblocks = int(grid.x * grid.y * grid.z);
     STRO_CUDA(launch_fold(s->d_partials, nblocks, 3, s->d_out, s->ctx->stream));
     STRO_CUDA(cudaMemcpyAsync(out, s->d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost,
@@ -590,17 +586,6 @@ int stro_sim_probe_force(stro_sim* s, int32_t x0, int32_t x1, int32_t y0, int32_
     return STRO_OK;
 }
 
-static int observables(stro_sim* s, double out[2]) {
-    if (s->steps_done % 2 != 0)
-        return fail(STRO_ERR_STATE, "observables require an even step count");
-    cudaSetDevice(s->ctx->device);
-    STRO_CUDA(launch_observables(field_view(s), s->precision == STRO_FP16S, s->omega,
-                                 s->d_partials, s->d_out, s->ctx->stream));
-    STRO_CUDA(cudaMemcpyAsync(out, s->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost,
-                              s->ctx->stream));
-    STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
-    return STRO_OK;
-}
 
 int stro_sim_kinetic_energy(stro_sim* s, double* sum_u2) {
     CHECK_SIM(s);

@@ -1,0 +1,95 @@
+// Internal state of the C-ABI handles, shared by runtime.cu and batch.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "lbm_launch.h"
+#include "strouhal_c.h"
+
+struct stro_ctx {
+    // Simulations and batches hold a reference; stro_ctx_destroy only marks the
+    // context closed and the last holder frees it, so handles may be released
+    // in any order.
+    int refs = 1;
+    bool closed = false;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    char name[256] = {0};
+};
+
+struct stro_sim {
+    stro_ctx* ctx = nullptr;
+    int precision = STRO_FP32;
+    int32_t nx = 0, ny = 0, nz = 0;
+    uint64_t N = 0, plane = 0;
+    size_t esize = 4;
+    // Simulation properties (Sim.swift:164-172)
+    float omega = 1.0f, omega_minus = 1.0f;
+    float lid[3] = {0, 0, 0};
+    float uin = 0.0f;
+    int32_t ramp_steps = 0;
+    float force[3] = {0, 0, 0};
+    float c_smago = 0.0f;
+    int inflow_uniform = 0;
+    bool sponge_on = false;
+    float sponge_x0 = 1e9f, sponge_width = 0.0f, sponge_tau = 1.0f;
+    bool wants_forces = false;
+    // host geometry
+    std::vector<uint8_t> flags;
+    std::vector<uint32_t> smask, lmask;
+    std::vector<float> eps;
+    bool any_wall = false, has_eps = false, has_ffield = false;
+    bool force_geometry = false;  // device geometry kept even for an all-fluid lattice
+    // device buffers
+    void* d_f = nullptr;
+    uint8_t* d_cell = nullptr;
+    uint32_t* d_geo = nullptr;
+    uint32_t* d_lmask = nullptr;
+    float* d_eps = nullptr;
+    float* d_ffield = nullptr;
+    float4* d_moments = nullptr;
+    double* d_partials = nullptr;
+    size_t partials_len = 0;
+    double* d_out = nullptr;
+    // bookkeeping
+    int64_t steps_done = 0;
+    double gpu_seconds = 0.0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    dim3 block{256, 1, 1};        // launch shape of ordinary steps (autotunable)
+    dim3 probe_block{256, 1, 1};  // fixed shape of force-probe steps: fixes the FP64 sum order
+    int variant = 0;              // 0: one cell per thread; 1: FP16 x-pairs (lbm_pair.cu)
+    dim3 pair_block{128, 2, 1};   // launch shape of the pair variant
+};
+
+namespace stro {
+namespace rt {
+
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+bool geo_on(const stro_sim* s);
+bool feat_on(const stro_sim* s);
+float ramp_factor(const stro_sim* s, int64_t t);
+StepArgs step_args(const stro_sim* s, int64_t t);
+FieldView field_view(const stro_sim* s);
+// Builds the device cell bytes / geometry words even for an all-fluid lattice
+// (needed when the lattice joins a batch that runs the wall-aware kernels).
+int ensure_geometry(stro_sim* s);
+// Launch one lattice step t on the simulation stream (variant and shape of the sim).
+cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool probe);
+void ctx_retain(stro_ctx* c);
+void ctx_release(stro_ctx* c);
+int observables(stro_sim* s, double out[2]);
+
+}  // namespace rt
+}  // namespace stro
+
+#define STRO_CUDA(expr)                                              \
+    do {                                                             \
+        cudaError_t e_ = (expr);                                     \
+        if (e_ != cudaSuccess) return ::stro::rt::cuda_fail(e_, #expr); \
+    } while (0)

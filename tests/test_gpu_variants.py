@@ -1,0 +1,177 @@
+"""GPU tests of the FP16 pair variant, the batched engine and the autotuners.
+
+All of them must leave the lattice arithmetic untouched: DDFs are compared
+value-for-value with the oracle or bitwise with plain stro_sim_run runs."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("nx,ny,nz", [(64, 7, 5), (128, 6, 4), (192, 3, 3)])
+@pytest.mark.parametrize("feature", ["plain", "force", "les", "sponge"])
+def test_pair_variant_matches_oracle(gpu, oracle, nx, ny, nz, feature):
+    import strouhal_gb300 as sg
+
+    po = oracle
+    kw = dict(omega=1.7, omegaMinus=1.3)
+    if feature == "force":
+        kw["force"] = (2e-5, -3e-5, 1e-5)
+    if feature == "les":
+        kw["cSmago"] = 0.01
+    g = sg.Simulation(gpu, precision="fp16s", nx=nx, ny=ny, nz=nz, **kw)
+    o = po.OracleSim(nx, ny, nz, kind=po.KIND_F16, **kw)
+    if feature == "sponge":
+        g.sponge = (nx * 0.6, nx * 0.3, 0.9)
+        o.sponge = (nx * 0.6, nx * 0.3, 0.9)
+    assert g.variant == 1
+    rng = np.random.default_rng(nx * 31 + ny)
+    f0 = (rng.standard_normal((19, nx * ny * nz)) * 0.01).astype(np.float16)
+    g.uploadState(f0)
+    o.f[:] = f0
+    for chunk in (1, 2, 3):
+        g.run(chunk)
+        o.run(chunk)
+        assert np.array_equal(g.downloadState(), o.f), chunk
+    g.close()
+
+
+def test_pair_and_single_variants_agree_bitwise(gpu):
+    import strouhal_gb300 as sg
+
+    sims = []
+    for variant in (0, 1):
+        s = sg.Simulation(gpu, precision="fp16s", nx=128, ny=40, nz=24, omega=1.95)
+        s.variant = variant
+        s.initField(2, 0.05)
+        s.run(11)
+        sims.append(s)
+    assert sims[0].stateDigest == sims[1].stateDigest
+
+
+def _ladder(sg, gpu, precision="fp32"):
+    """Uneven periodic TGV boxes plus a ramped cavity and a channel with NT cells."""
+    sims, steps, logs = [], [], []
+    for n, u0, nsteps, le in [(32, 0.05, 40, 10), (48, 0.025, 62, 0), (16, 0.05, 12, 4),
+                              (64, 0.05, 26, 2)]:
+        L = n / (2 * np.pi)
+        tau = 3 * u0 * L / 1600 + 0.5
+        s = sg.Simulation(gpu, precision=precision, nx=n, ny=n, nz=n, omega=1 / tau)
+        s.initField(2, u0)
+        sims.append(s)
+        steps.append(nsteps)
+        logs.append(le)
+    n = 40
+
+    def cav(x, y, z):
+        if y == n - 1:
+            return sg.Cell.lid
+        if x == 0 or x == n - 1 or y == 0:
+            return sg.Cell.solid
+        return sg.Cell.fluid
+
+    c = sg.Simulation(gpu, precision=precision, nx=n, ny=n, nz=3, omega=1.2, omegaMinus=1.0,
+                      lid=(0.1, 0, 0), rampSteps=30, flags=cav)
+    sims.append(c)
+    steps.append(50)
+    logs.append(10)
+    ch = np.zeros((4, 20, 50), np.uint8)
+    ch[:, 0, :] = ch[:, -1, :] = sg.Cell.solid
+    ch[:, 1:-1, 0] = ch[:, 1:-1, -1] = sg.Cell.inflow
+    d = sg.Simulation(gpu, precision=precision, nx=50, ny=20, nz=4, omega=1.5, omegaMinus=1.2,
+                      uin=0.05, rampSteps=20, force=(1e-5, 0, 0), cSmago=0.01,
+                      flags=ch.reshape(-1))
+    eps = sg.diskSolidFractions(50, 20, 15.5, 9.5, 4.0)
+    d.setSolidFractions(np.tile(eps, 4))
+    d.sponge = (35.0, 10.0, 0.9)
+    sims.append(d)
+    steps.append(33)
+    logs.append(0)
+    return sims, steps, logs
+
+
+@pytest.mark.parametrize("mode", ["persistent", "rounds", "sequential"])
+@pytest.mark.parametrize("precision", ["fp32", "fp16s"])
+def test_batch_matches_independent_runs(gpu, mode, precision):
+    import strouhal_gb300 as sg
+
+    ref, steps, logs = _ladder(sg, gpu, precision)
+    ref_traces = []
+    for s, k, le in zip(ref, steps, logs):
+        tr = []
+        if le:
+            tr.append(s.kineticEnergySum())
+            for _ in range(k // le):
+                s.run(le)
+                tr.append(s.kineticEnergySum())
+            s.run(k - (k // le) * le)
+        else:
+            s.run(k)
+        ref_traces.append(np.array(tr))
+    sims, _, _ = _ladder(sg, gpu, precision)
+    b = sg.Batch(gpu, sims, mode=mode)
+    traces = b.run(steps, logs)
+    assert b.lastPath.startswith({"persistent": "persistent", "rounds": "rounds",
+                                  "sequential": "sequential"}[mode])
+    for s, r, k, tr, rtr in zip(sims, ref, steps, traces, ref_traces):
+        assert s.stepsDone == r.stepsDone == k
+        assert np.array_equal(s.downloadState(), r.downloadState())
+        assert len(tr) == len(rtr)
+        assert np.allclose(tr, rtr, rtol=1e-12, atol=0)
+    # a second run replays the cached graph from the new state
+    steps2 = [6] * len(sims)
+    b.run(steps2)
+    for s, r in zip(sims, ref):
+        r.run(6)
+        assert np.array_equal(s.downloadState(), r.downloadState())
+    b.close()
+
+
+def test_batch_barrier_timeout_is_an_error_status(gpu):
+    """A persistent batch whose barrier waits may poll only once gives up with
+    STRO_ERR_TIMEOUT instead of waiting; the context stays usable."""
+    import strouhal_gb300 as sg
+
+    sims = [sg.Simulation(gpu, nx=96, ny=96, nz=96, omega=1.8) for _ in range(2)]
+    b = sg.Batch(gpu, sims, mode="persistent")
+    b.setSpinLimit(1)
+    with pytest.raises(sg.StrouhalError) as ei:
+        b.run([20, 20])
+    assert ei.value.code == 6
+    b.close()
+    s = sg.Simulation(gpu, nx=16, ny=16, nz=16, omega=1.5)
+    s.initField(2, 0.05)
+    s.run(4)
+    assert s.checkFinite()
+
+
+def test_autotune_restores_state(gpu):
+    import strouhal_gb300 as sg
+
+    for precision in ("fp32", "fp16s"):
+        s = sg.Simulation(gpu, precision=precision, nx=128, ny=64, nz=32, omega=1.9)
+        s.initField(2, 0.05)
+        s.run(3)
+        d0, t0 = s.stateDigest, s.stepsDone
+        bx, by, glups = s.autotune(steps=8)
+        assert bx * by % 32 == 0 and glups > 0
+        assert s.stateDigest == d0 and s.stepsDone == t0
+        ref = sg.Simulation(gpu, precision=precision, nx=128, ny=64, nz=32, omega=1.9)
+        ref.initField(2, 0.05)
+        ref.run(3)
+        s.run(5)
+        ref.run(5)
+        assert s.stateDigest == ref.stateDigest
+
+
+def test_batch_autotune_restores_state(gpu):
+    import strouhal_gb300 as sg
+
+    sims, steps, _ = _ladder(sg, gpu)
+    before = [s.stateDigest for s in sims]
+    b = sg.Batch(gpu, sims)
+    mode, bx, by, sec = b.autotune(rounds=6)
+    assert mode in ("persistent", "rounds") and sec > 0
+    assert [s.stateDigest for s in sims] == before
+    assert all(s.stepsDone == 0 for s in sims)
+    b.close()
