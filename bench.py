@@ -167,6 +167,8 @@ def run_variant(sg, gpu, precision, lam, steps, warmup, dist, clocks=None):
     cells = sim.cells
     # ---- device-timed: kernels only, state resident in HBM
     sim.initField(2, U0)
+    bx, by, _ = sim.autotune(steps=20)  # picks the kernel variant and launch shape (state restored)
+    tuned = {"variant": sim.variant, "block": [bx, by]}
     sim.run(warmup * STEPS_PER_BENCH_STEP)
     sim.kineticEnergySum()
     barrier(dist)
@@ -203,7 +205,8 @@ def run_variant(sg, gpu, precision, lam, steps, warmup, dist, clocks=None):
     host.close()
     sim.close()
     return dict(cells=cells, launches=launches, dev=dev, wall=wall, e2e_wall=e2e_wall,
-                state_bytes=state_bytes, finite=finite, ke_last=logs[-1][0] if logs else None)
+                state_bytes=state_bytes, finite=finite, ke_last=logs[-1][0] if logs else None,
+                tuned=tuned)
 
 
 class _Null:
@@ -330,7 +333,8 @@ def main():
         "roofline": {"bound": "hbm", "achieved": ach16, "peak": peak, "unit": "GB/s",
                      "frac": ach16 / peak, "peak_source": peak_kind,
                      "traffic": None if t16 is None else t16 * head["cells"],
-                     "kernel": "k_step_even/k_step_odd (fp16, periodic, lean)",
+                     "kernel": {0: "k_step_even/k_step_odd", 1: "k_pair_even/k_pair_odd",
+                                2: "k_rows<even>/k_rows<odd>"}[head["tuned"]["variant"]],
                      "alg_bytes_per_cell": ALG_BYTES["fp16s"]},
         "e2e": {"value": e16, "unit": "GLUPS",
                 "h2d_bytes_per_step": head["state_bytes"] / args.steps,
@@ -343,8 +347,9 @@ def main():
                          "roofline": {"achieved": ach32, "peak": peak, "frac": ach32 / peak,
                                       "traffic": None if t32 is None else t32 * trt["cells"],
                                       "alg_bytes_per_cell": ALG_BYTES["fp32"]},
-                         "ms_per_launch": 1e3 * pl32},
-            "fp16s_srt": {"ms_per_launch": 1e3 * pl16, "finite": head["finite"]},
+                         "ms_per_launch": 1e3 * pl32, "tuned": trt["tuned"]},
+            "fp16s_srt": {"ms_per_launch": 1e3 * pl16, "finite": head["finite"],
+                          "tuned": head["tuned"]},
         },
     }
     print(json.dumps(line))

@@ -144,8 +144,10 @@ int stro_sim_set_block(stro_sim* sim, int32_t bx, int32_t by);
 int stro_sim_get_block(stro_sim* sim, int32_t* bx, int32_t* by);
 /* Kernel variant: 0 = one cell per thread (all lattices); 1 = FP16 storage,
  * two x-adjacent cells per thread with half2 accesses (periodic lattices,
- * nx a multiple of 64; other lattices fall back to variant 0). Results are
- * identical; FP16 lattices that qualify start with variant 1. */
+ * nx a multiple of 64); 2 = row streaming: whole rows staged in shared memory
+ * by bulk copies ahead of the compute (periodic lattices, nx*element size a
+ * multiple of 16). A lattice a variant does not apply to runs variant 0.
+ * Results are identical for every variant. */
 int stro_sim_set_variant(stro_sim* sim, int32_t variant);
 int stro_sim_get_variant(stro_sim* sim, int32_t* variant);
 /* Autotuner: times `steps` steps per candidate variant and launch shape on the current

@@ -278,9 +278,10 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
 int tune_sim_shape(stro_sim* s, int64_t steps, int variant, dim3 cand, double* seconds) {
     cudaStream_t st = s->ctx->stream;
     const dim3 saved = s->block, saved_pair = s->pair_block;
-    const int saved_variant = s->variant;
+    const int saved_variant = s->variant, saved_rows = s->rows_threads;
     s->variant = variant;
     if (variant == 1) s->pair_block = cand;
+    else if (variant == 2) s->rows_threads = int(cand.x * cand.y);
     else s->block = cand;
     const int64_t t0 = s->steps_done;
     const double g0 = s->gpu_seconds;
@@ -296,18 +297,26 @@ int tune_sim_shape(stro_sim* s, int64_t steps, int variant, dim3 cand, double* s
     if (e == cudaSuccess) e = cudaEventSynchronize(s->ev1);
     float ms = 0.0f;
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    int err = 0;
+    if (e == cudaSuccess && variant == 2)
+        e = cudaMemcpy(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost);
     s->block = saved;
     s->pair_block = saved_pair;
     s->variant = saved_variant;
+    s->rows_threads = saved_rows;
     s->gpu_seconds = g0;
     if (e != cudaSuccess) return cuda_fail(e, "autotune launch");
+    if (err != 0) {
+        cudaMemset(s->d_error, 0, sizeof(int));
+        return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-streaming step timed out");
+    }
     *seconds = double(ms) * 1e-3;
     return STRO_OK;
 }
 
 const dim3 kShapes[] = {dim3(32, 8, 1), dim3(64, 4, 1), dim3(128, 2, 1), dim3(256, 1, 1),
                         dim3(16, 16, 1), dim3(32, 4, 1), dim3(64, 2, 1), dim3(128, 1, 1),
-                        dim3(16, 8, 1)};
+                        dim3(16, 8, 1), dim3(64, 1, 1), dim3(96, 1, 1), dim3(192, 1, 1)};
 
 }  // namespace
 
@@ -453,7 +462,7 @@ int stro_sim_set_block(stro_sim* s, int32_t bx, int32_t by) {
 
 int stro_sim_set_variant(stro_sim* s, int32_t variant) {
     if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
-    if (variant != 0 && variant != 1) return fail(STRO_ERR_INVALID, "variant must be 0 or 1");
+    if (variant < 0 || variant > 2) return fail(STRO_ERR_INVALID, "variant must be 0, 1 or 2");
     s->variant = variant;
     return STRO_OK;
 }
@@ -486,12 +495,16 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
     int best_variant = 0;
     int rc = e == cudaSuccess ? STRO_OK : cuda_fail(e, "autotune save");
     const int half = s->precision == STRO_FP16S ? 1 : 0;
-    for (int variant : {0, 1}) {
+    for (int variant : {0, 1, 2}) {
         for (const dim3& c : kShapes) {
             if (rc != STRO_OK) break;
             if (variant == 0 && c.x > 32 && int(c.x) > ((s->nx + 31) / 32) * 32) continue;
             if (variant == 1 && !pair_step_supported(half, geo_on(s) ? 1 : 0, false, s->nx,
                                                      s->plane, c))
+                continue;
+            // the row-streaming variant only varies its thread count: one shape per count
+            if (variant == 2 && (c.y != 1 || !rows_step_supported(half, geo_on(s) ? 1 : 0, false,
+                                                                  s->nx, int(c.x))))
                 continue;
             double sec = 0.0;
             rc = tune_sim_shape(s, steps, variant, c, &sec);
@@ -509,6 +522,7 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
     if (e != cudaSuccess) return cuda_fail(e, "autotune restore");
     s->variant = best_variant;
     if (best_variant == 1) s->pair_block = best_shape;
+    else if (best_variant == 2) s->rows_threads = int(best_shape.x);
     else s->block = best_shape;
     if (bx) *bx = int32_t(best_shape.x);
     if (by) *by = int32_t(best_shape.y);

@@ -19,6 +19,13 @@ dim3 step_grid(const StepArgs& a, dim3 block);
 bool pair_step_supported(int half_storage, int geo, bool probe, int nx, uint64_t plane, dim3 block);
 cudaError_t launch_pair_step(const StepArgs& a, int parity, bool feat, dim3 block, cudaStream_t st);
 
+// Row-streaming step (lbm_rows.cu): bulk-copy staging of whole rows in shared
+// memory, `threads` per block, persistent over rows. `error` receives 1 if a
+// bounded wait gave up.
+bool rows_step_supported(int half_storage, int geo, bool probe, int nx, int threads);
+cudaError_t launch_rows_step(const StepArgs& a, int half_storage, int parity, bool feat,
+                             int threads, int sm_count, int* error, cudaStream_t st);
+
 // Fields and reductions (lbm_probe.cu). `plane` is the DDF plane stride in
 // elements, N the cell count. Reductions write per-block FP64 partials to
 // `partials` and then fold them in a fixed order into `out`.

@@ -186,6 +186,7 @@ void free_sim(stro_sim* s) {
     cudaFree(s->d_moments);
     cudaFree(s->d_partials);
     cudaFree(s->d_out);
+    cudaFree(s->d_error);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
 }
@@ -215,6 +216,14 @@ int run_steps(stro_sim* s, int64_t steps, int64_t probe_step = -1, const int* bo
     s->gpu_seconds += double(ms) * 1e-3;
     s->steps_done += steps;
     STRO_CUDA(cudaGetLastError());
+    if (s->variant == 2) {
+        int err = 0;
+        STRO_CUDA(cudaMemcpy(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost));
+        if (err != 0) {
+            cudaMemset(s->d_error, 0, sizeof(int));
+            return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-streaming step timed out");
+        }
+    }
     return STRO_OK;
 }
 
@@ -232,6 +241,9 @@ cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool prob
     const int geo = geo_on(s) ? 1 : 0;
     if (s->variant == 1 && pair_step_supported(half, geo, probe, s->nx, s->plane, s->pair_block))
         return launch_pair_step(a, int(t & 1), feat_on(s), s->pair_block, s->ctx->stream);
+    if (s->variant == 2 && rows_step_supported(half, geo, probe, s->nx, s->rows_threads))
+        return launch_rows_step(a, half, int(t & 1), feat_on(s), s->rows_threads,
+                                s->ctx->sm_count, s->d_error, s->ctx->stream);
     return launch_step(a, half, int(t & 1), geo, feat_on(s), probe,
                        probe ? s->probe_block : s->block, s->ctx->stream);
 }
@@ -372,6 +384,8 @@ int stro_sim_create(stro_ctx* ctx, const stro_sim_desc* d, const uint8_t* flags,
     // shifted equilibrium at rest is exactly 0 (Sim.swift:225)
     e = cudaMemsetAsync(s->d_f, 0, 19 * s->plane * s->esize, ctx->stream);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_out, 8 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_error, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_error, 0, sizeof(int), ctx->stream);
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
     if (e != cudaSuccess) return bail(cuda_fail(e, "simulation set-up"));

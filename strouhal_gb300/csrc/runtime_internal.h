@@ -62,8 +62,11 @@ struct stro_sim {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     dim3 block{256, 1, 1};        // launch shape of ordinary steps (autotunable)
     dim3 probe_block{256, 1, 1};  // fixed shape of force-probe steps: fixes the FP64 sum order
-    int variant = 0;              // 0: one cell per thread; 1: FP16 x-pairs (lbm_pair.cu)
+    int variant = 0;              // 0: one cell per thread; 1: FP16 x-pairs (lbm_pair.cu);
+                                  // 2: row streaming through shared memory (lbm_rows.cu)
     dim3 pair_block{128, 2, 1};   // launch shape of the pair variant
+    int rows_threads = 256;       // threads per block of the row-streaming variant
+    int* d_error = nullptr;       // device error word of the row-streaming variant
 };
 
 namespace stro {

@@ -1,0 +1,48 @@
+"""Time the D3Q19 step for one kernel variant on a periodic Taylor-Green box.
+
+    python -m strouhal_gb300.stepbench --n 256 --precision fp16s --variant 2 --steps 20
+
+Prints one line: lattice, precision, variant, launch shape, ms per step and
+GLUPS (CUDA-event device time of the step launches). Useful for comparing the
+variants on a given lattice and as a fixed command for profilers.
+"""
+import argparse
+import math
+
+import strouhal_gb300 as sg
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=256, help="edge of the cubic lattice")
+    ap.add_argument("--precision", default="fp16s", choices=["fp32", "fp16s"])
+    ap.add_argument("--variant", type=int, default=-1, help="0, 1, 2 or -1 = autotune")
+    ap.add_argument("--trt", action="store_true", help="TRT Lambda=3/16 instead of SRT")
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=4)
+    a = ap.parse_args(argv)
+    n = a.n
+    L = n / (2 * math.pi)
+    tau = 3 * 0.05 * L / 1600 + 0.5
+    wp, wm = sg.trtOmegas(tau, 3.0 / 16.0 if a.trt else None)
+    gpu = sg.GPU(0)
+    s = sg.Simulation(gpu, precision=a.precision, nx=n, ny=n, nz=n, omega=wp, omegaMinus=wm)
+    s.initField(2, 0.05)
+    if a.variant < 0:
+        s.autotune(steps=10)
+    else:
+        s.variant = a.variant
+    s.run(a.warmup)
+    t0 = s.gpuSeconds
+    s.run(a.steps)
+    dt = s.gpuSeconds - t0
+    bx, by = s.block
+    print("lattice %d^3 %s %s variant %d block %dx%d: %.4f ms/step, %.2f GLUPS"
+          % (n, a.precision, "TRT" if a.trt else "SRT", s.variant, bx, by,
+             1e3 * dt / a.steps, s.cells * a.steps / dt / 1e9))
+    s.close()
+    gpu.close()
+
+
+if __name__ == "__main__":
+    main()

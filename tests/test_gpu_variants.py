@@ -8,9 +8,17 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("nx,ny,nz", [(64, 7, 5), (128, 6, 4), (192, 3, 3)])
+VARIANT_CASES = [
+    # (variant, precision, nx, ny, nz)
+    (1, "fp16s", 64, 7, 5), (1, "fp16s", 128, 6, 4), (1, "fp16s", 192, 3, 3),
+    (2, "fp16s", 64, 7, 5), (2, "fp16s", 40, 6, 4), (2, "fp16s", 256, 3, 2), (2, "fp16s", 8, 9, 4),
+    (2, "fp32", 36, 7, 5), (2, "fp32", 128, 5, 3), (2, "fp32", 4, 6, 5),
+]
+
+
+@pytest.mark.parametrize("variant,precision,nx,ny,nz", VARIANT_CASES)
 @pytest.mark.parametrize("feature", ["plain", "force", "les", "sponge"])
-def test_pair_variant_matches_oracle(gpu, oracle, nx, ny, nz, feature):
+def test_variant_matches_oracle(gpu, oracle, variant, precision, nx, ny, nz, feature):
     import strouhal_gb300 as sg
 
     po = oracle
@@ -19,14 +27,15 @@ def test_pair_variant_matches_oracle(gpu, oracle, nx, ny, nz, feature):
         kw["force"] = (2e-5, -3e-5, 1e-5)
     if feature == "les":
         kw["cSmago"] = 0.01
-    g = sg.Simulation(gpu, precision="fp16s", nx=nx, ny=ny, nz=nz, **kw)
-    o = po.OracleSim(nx, ny, nz, kind=po.KIND_F16, **kw)
+    g = sg.Simulation(gpu, precision=precision, nx=nx, ny=ny, nz=nz, **kw)
+    kind = po.KIND_F16 if precision == "fp16s" else po.KIND_F32
+    o = po.OracleSim(nx, ny, nz, kind=kind, **kw)
     if feature == "sponge":
         g.sponge = (nx * 0.6, nx * 0.3, 0.9)
         o.sponge = (nx * 0.6, nx * 0.3, 0.9)
-    assert g.variant == 1
-    rng = np.random.default_rng(nx * 31 + ny)
-    f0 = (rng.standard_normal((19, nx * ny * nz)) * 0.01).astype(np.float16)
+    g.variant = variant
+    rng = np.random.default_rng(nx * 31 + ny + variant)
+    f0 = (rng.standard_normal((19, nx * ny * nz)) * 0.01).astype(o.f.dtype)
     g.uploadState(f0)
     o.f[:] = f0
     for chunk in (1, 2, 3):
@@ -36,17 +45,19 @@ def test_pair_variant_matches_oracle(gpu, oracle, nx, ny, nz, feature):
     g.close()
 
 
-def test_pair_and_single_variants_agree_bitwise(gpu):
+@pytest.mark.parametrize("precision", ["fp16s", "fp32"])
+def test_variants_agree_bitwise(gpu, precision):
     import strouhal_gb300 as sg
 
-    sims = []
-    for variant in (0, 1):
-        s = sg.Simulation(gpu, precision="fp16s", nx=128, ny=40, nz=24, omega=1.95)
+    digests = []
+    for variant in ((0, 1, 2) if precision == "fp16s" else (0, 2)):
+        s = sg.Simulation(gpu, precision=precision, nx=128, ny=40, nz=24, omega=1.95)
         s.variant = variant
         s.initField(2, 0.05)
         s.run(11)
-        sims.append(s)
-    assert sims[0].stateDigest == sims[1].stateDigest
+        digests.append(s.stateDigest)
+        s.close()
+    assert len(set(digests)) == 1
 
 
 def _ladder(sg, gpu, precision="fp32"):
