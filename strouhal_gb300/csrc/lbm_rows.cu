@@ -208,6 +208,7 @@ __global__ void __launch_bounds__(256) k_rows(const StepArgs a, int* error) {
 }
 
 constexpr int kStages = 3;
+constexpr size_t kMaxRowsSmem = 200 * 1024;  // largest stage set the variant accepts
 
 template <typename S>
 size_t rows_smem(int nx) {
@@ -231,26 +232,35 @@ const void* pick(int parity, bool feat) {
 bool rows_step_supported(int half_storage, int geo, bool probe, int nx, int threads) {
     const size_t es = half_storage ? 2 : 4;
     const size_t smem = half_storage ? rows_smem<__half>(nx) : rows_smem<float>(nx);
-    return !geo && !probe && (size_t(nx) * es) % 16 == 0 && smem <= 200 * 1024 && threads >= 32 &&
+    return !geo && !probe && (size_t(nx) * es) % 16 == 0 && smem <= kMaxRowsSmem && threads >= 32 &&
            threads <= 256 && threads % 32 == 0;
 }
 
 // Resident blocks per SM of one kernel at one (threads, smem), cached: the
-// attribute call and the occupancy query cost host time on every launch.
+// attribute call and the occupancy query cost host time on every launch. The
+// dynamic shared-memory limit of a kernel is raised once to kMaxRowsSmem, so a
+// cached entry stays valid whatever size another lattice asked for since.
 int rows_blocks_per_sm(const void* fn, int threads, size_t smem, cudaError_t* err) {
     struct Entry { const void* fn; int threads; size_t smem; int per_sm; };
-    static thread_local Entry cache[16];
+    static thread_local Entry cache[32];
     static thread_local int used = 0;
+    static thread_local const void* raised[16];
+    static thread_local int nraised = 0;
     for (int k = 0; k < used; ++k)
         if (cache[k].fn == fn && cache[k].threads == threads && cache[k].smem == smem)
             return cache[k].per_sm;
-    *err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (*err != cudaSuccess) return 0;
+    bool is_raised = false;
+    for (int k = 0; k < nraised; ++k) is_raised = is_raised || raised[k] == fn;
+    if (!is_raised) {
+        *err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(kMaxRowsSmem));
+        if (*err != cudaSuccess) return 0;
+        if (nraised < 16) raised[nraised++] = fn;
+    }
     int per_sm = 0;
     *err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
     if (*err != cudaSuccess) return 0;
-    const int slot = used < 16 ? used++ : int((reinterpret_cast<uintptr_t>(fn) >> 4) & 15);
-    cache[slot] = Entry{fn, threads, smem, per_sm};
+    if (used < 32) cache[used++] = Entry{fn, threads, smem, per_sm};
     return per_sm;
 }
 
