@@ -184,6 +184,30 @@ int stro_batch_last_path(stro_batch* batch, char* buf, size_t len);
 int stro_batch_autotune(stro_batch* batch, int64_t rounds, int32_t* mode, int32_t* bx,
                         int32_t* by, double* seconds);
 
+/* No counterpart in the reference. Kinetic-energy and dissipation sums (as
+ * stro_sim_kinetic_energy / stro_sim_dissipation) of a DDF state the CALLER
+ * holds in device memory, for callers that must not allocate: a framework
+ * whose own allocator owns the device memory, a real-time loop that cannot
+ * afford the implicit synchronisation of cudaMalloc, or code running while a
+ * stream is captured. This call allocates nothing. Its scratch is a 32 KB
+ * array in the library's device module, present on every GPU that loads the
+ * library until exit.
+ *   f            device pointer: 19 planes, plane i at f + i*plane_stride elements
+ *                (FP32 or FP16 per `precision`)
+ *   cell_types   optional device array of N cell codes (0 = fluid; other cells
+ *                are skipped); NULL = all fluid
+ *   force        host pointer to the uniform force (half-force shift of u); NULL = 0
+ *   out          device pointer to 2 doubles: sum |u|^2, sum 2 nu S:S (nu from omega)
+ *   stream       cudaStream_t (NULL = default stream); the call only enqueues work
+ * Lattices up to N < 2^31 cells are accepted; larger ones are rejected with
+ * STRO_ERR_INVALID. The first call on a device looks up the scratch address
+ * on that device (with it current); make that first call before any stream
+ * capture. All calls share the scratch array, so calls whose work overlaps on
+ * the GPU (two streams at once) race: order them on one stream. */
+int stro_observables_noalloc(const void* f, int32_t precision, int32_t nx, int32_t ny, int32_t nz,
+                             uint64_t plane_stride, const uint8_t* cell_types, float omega,
+                             const float force[3], double* out, void* stream);
+
 /* ---- host utilities ---------------------------------------------------------- */
 /* SHA-256 (FIPS 180-4) of a host buffer as 64 hex chars + NUL: the digest
  * stro_sim_digest computes over the downloaded state, for caller-held copies. */

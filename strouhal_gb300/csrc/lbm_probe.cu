@@ -254,3 +254,87 @@ cudaError_t launch_nonfinite(const FieldView& v, int half_storage, double* parti
 }
 
 }  // namespace stro
+
+// ---------------------------------------------------------------------------
+// Allocation-free observables for callers that cannot allocate device memory.
+//
+// Some hosts of this library must not call cudaMalloc while they step a
+// lattice. One example is a framework whose caching allocator already owns
+// the HBM. Another is a real-time loop, where cudaMalloc may synchronise the
+// device and stall the loop. A third is code that runs while a stream is
+// being captured. Such callers hold the DDF state in memory they own and want
+// the kinetic-energy and dissipation sums of it. stro_observables_noalloc runs
+// the same reduction kernels as stro_sim_kinetic_energy / stro_sim_dissipation
+// and allocates nothing itself. Its per-block partial sums go to the
+// file-scope array below. The module holds that array on every GPU that loads
+// the library, until the process exits.
+#include <mutex>
+
+#include "runtime_internal.h"
+
+namespace {
+
+constexpr int kNoAllocMaxBlocks = 2048;  // = the most blocks reduction_blocks() ever uses
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxBlocks * 2];  // 32 KB
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the host-side symbol is only a stand-in, not a device address).
+int noalloc_scratch(double** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return stro::rt::cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return stro::rt::fail(STRO_ERR_INVALID, "device index beyond the scratch table");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        if (e != cudaSuccess) return stro::rt::cuda_fail(e, "cudaGetSymbolAddress");
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = static_cast<double*>(g_noalloc_ptr[dev]);
+    return STRO_OK;
+}
+
+}  // namespace
+
+extern "C" int stro_observables_noalloc(const void* f, int32_t precision, int32_t nx, int32_t ny,
+                                        int32_t nz, uint64_t plane_stride,
+                                        const uint8_t* cell_types, float omega,
+                                        const float force[3], double* out, void* stream) {
+    using stro::rt::fail;
+    if (!f || !out) return fail(STRO_ERR_INVALID, "state and output pointers are required");
+    if (precision != STRO_FP32 && precision != STRO_FP16S)
+        return fail(STRO_ERR_INVALID, "precision must be STRO_FP32 or STRO_FP16S");
+    if (nx < 1 || ny < 1 || nz < 1) return fail(STRO_ERR_INVALID, "lattice dimensions must be >= 1");
+    const uint64_t N = uint64_t(nx) * uint64_t(ny) * uint64_t(nz);
+    if (N >= (1ull << 31)) return fail(STRO_ERR_INVALID, "lattice too large (N must be < 2^31 cells)");
+    if (plane_stride < N) return fail(STRO_ERR_INVALID, "plane stride must be at least nx*ny*nz");
+    const int nb = stro::reduction_blocks(N);
+    if (nb > kNoAllocMaxBlocks)
+        return fail(STRO_ERR_INVALID, "reduction needs more partials than the scratch array holds");
+    double* scratch = nullptr;
+    const int rc = noalloc_scratch(&scratch);
+    if (rc != STRO_OK) return rc;
+    stro::FieldView v{};
+    v.f = const_cast<void*>(f);
+    v.plane = plane_stride;
+    v.nx = uint32_t(nx); v.ny = uint32_t(ny); v.nz = uint32_t(nz);
+    v.N = uint32_t(N);
+    v.cell = cell_types;
+    v.ffield = nullptr;
+    v.fx = force ? force[0] : 0.0f;
+    v.fy = force ? force[1] : 0.0f;
+    v.fz = force ? force[2] : 0.0f;
+    // Every block writes its own partials before the fold reads them, so nothing in
+    // the scratch array has to start at zero; what a previous call left there is
+    // simply overwritten.
+    const cudaError_t e = stro::launch_observables(v, precision == STRO_FP16S, omega, scratch, out,
+                                                   static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return stro::rt::cuda_fail(e, "observables launch");
+    return STRO_OK;
+}
