@@ -208,6 +208,28 @@ int stro_observables_noalloc(const void* f, int32_t precision, int32_t nx, int32
                              uint64_t plane_stride, const uint8_t* cell_types, float omega,
                              const float force[3], double* out, void* stream);
 
+/* ---- discrete adjoint -------------------------------------------------------------
+ * No reference counterpart (the reference has no adjoint). Objective over the
+ * window [t0, t0 + steps) from the simulation's current state:
+ *   J = mean over the odd steps t of dir . F_box(t),
+ * F_box = the momentum-exchange force of the odd pass over the cells the
+ * reference's probeForce would sum (box x0..x1, y0..y1 inclusive, all z;
+ * Sim.swift:359-372): with dir = (1,0,0) the time-averaged drag.
+ * stro_adj_forward runs the window (advancing the simulation) and keeps
+ * `checkpoints` states on the device; stro_adj_backward recomputes between
+ * checkpoints and returns dJ/d eps (N floats: Noble-Torczynski cells, 0 where
+ * eps = 0) and dJ/d F_field (3 planes of N floats, the per-cell Guo force). */
+typedef struct stro_adjoint stro_adjoint;
+int stro_adj_create(stro_sim* sim, const double dir[3], const int32_t box[4], int64_t steps,
+                    int32_t checkpoints, stro_adjoint** out);
+int stro_adj_destroy(stro_adjoint* adj);
+int stro_adj_forward(stro_adjoint* adj, double* J);
+int stro_adj_backward(stro_adjoint* adj, float* grad_eps, float* grad_force);
+/* Device seconds of the last forward, of the recomputation and of the adjoint
+ * steps, and the number of adjoint steps run. */
+int stro_adj_stats(stro_adjoint* adj, double* forward_s, double* recompute_s, double* adjoint_s,
+                   int64_t* adjoint_steps);
+
 /* ---- host utilities ---------------------------------------------------------- */
 /* SHA-256 (FIPS 180-4) of a host buffer as 64 hex chars + NUL: the digest
  * stro_sim_digest computes over the downloaded state, for caller-held copies. */

@@ -18,6 +18,8 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
+#include <vector>
+#include <algorithm>
 
 namespace {
 
@@ -43,12 +45,77 @@ struct Params {
 };
 static_assert(sizeof(Params) == 80, "Params layout");
 
+// Math through unqualified calls, so a dual-number type can supply its own.
+using std::fma;
+using std::fmax;
+using std::fmin;
+using std::sqrt;
+template <class R> inline R Sqrt(R a) { return sqrt(a); }
+template <class R> inline R Fma(R a, R b, R c) { return fma(a, b, c); }
+template <class R> inline R Fmin(R a, R b) { return fmin(a, b); }
+template <class R> inline R Fmax(R a, R b) { return fmax(a, b); }
+
+// Forward-mode dual number with K derivative lanes, in double. Instantiating
+// the restated kernel arithmetic on it gives the exact local Jacobian of a
+// cell update (used by the FP64 adjoint below).
+template <int K> struct Dual {
+    double v;
+    double d[K];
+    Dual() : v(0.0) { for (int k = 0; k < K; ++k) d[k] = 0.0; }
+    Dual(double x) : v(x) { for (int k = 0; k < K; ++k) d[k] = 0.0; }  // NOLINT: implicit
+    static Dual var(double x, int lane) {
+        Dual r(x);
+        r.d[lane] = 1.0;
+        return r;
+    }
+};
+template <int K> inline Dual<K> operator+(const Dual<K>& a, const Dual<K>& b) {
+    Dual<K> r(a.v + b.v);
+    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] + b.d[k];
+    return r;
+}
+template <int K> inline Dual<K> operator-(const Dual<K>& a, const Dual<K>& b) {
+    Dual<K> r(a.v - b.v);
+    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] - b.d[k];
+    return r;
+}
+template <int K> inline Dual<K> operator-(const Dual<K>& a) {
+    Dual<K> r(-a.v);
+    for (int k = 0; k < K; ++k) r.d[k] = -a.d[k];
+    return r;
+}
+template <int K> inline Dual<K> operator*(const Dual<K>& a, const Dual<K>& b) {
+    Dual<K> r(a.v * b.v);
+    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+    return r;
+}
+template <int K> inline Dual<K> operator/(const Dual<K>& a, const Dual<K>& b) {
+    Dual<K> r(a.v / b.v);
+    for (int k = 0; k < K; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) / b.v;
+    return r;
+}
+template <int K> inline Dual<K>& operator+=(Dual<K>& a, const Dual<K>& b) { return a = a + b; }
+template <int K> inline Dual<K>& operator-=(Dual<K>& a, const Dual<K>& b) { return a = a - b; }
+template <int K> inline bool operator==(const Dual<K>& a, const Dual<K>& b) { return a.v == b.v; }
+template <int K> inline bool operator>(const Dual<K>& a, const Dual<K>& b) { return a.v > b.v; }
+template <int K> inline bool operator<(const Dual<K>& a, const Dual<K>& b) { return a.v < b.v; }
+template <int K> inline Dual<K> sqrt(const Dual<K>& a) {
+    Dual<K> r(std::sqrt(a.v));
+    const double g = r.v > 0.0 ? 0.5 / r.v : 0.0;  // subgradient 0 at the kink
+    for (int k = 0; k < K; ++k) r.d[k] = g * a.d[k];
+    return r;
+}
+template <int K> inline Dual<K> fma(const Dual<K>& a, const Dual<K>& b, const Dual<K>& c) {
+    return a * b + c;
+}
+template <int K> inline Dual<K> fmin(const Dual<K>& a, const Dual<K>& b) { return b.v < a.v ? b : a; }
+template <int K> inline Dual<K> fmax(const Dual<K>& a, const Dual<K>& b) { return b.v > a.v ? b : a; }
+
 template <class R> inline R weight(int i) {
     return i == 0 ? R(1) / R(3) : (i < 7 ? R(1) / R(18) : R(1) / R(36));
 }
-template <class R> inline R smagConst();  // 18*sqrt(2), Kernels.metal:156-157
+template <class R> inline R smagConst() { return R(18.0 * std::sqrt(2.0)); }  // Kernels.metal:156-157
 template <> inline float smagConst<float>() { return 25.455844f; }
-template <> inline double smagConst<double>() { return 18.0 * std::sqrt(2.0); }
 
 // sum_k c_k * v_k over the three components, in x,y,z order, skipping zero
 // coefficients (value-identical to the reference's (float)Cx*vx + ... form).
@@ -81,7 +148,7 @@ template <class R> inline V3<R> wall_velocity(uint8_t wf, int wy, const Params& 
     const R H = R(p.ny) - R(2);
     const R yd = R(wy) - R(0.5);
     const R prof = R(4) * R(p.uin) * yd * (H - yd) / (H * H);
-    return {std::fmax(prof, R(0)), R(0), R(0)};
+    return {Fmax(prof, R(0)), R(0), R(0)};
 }
 
 // TRT + Guo + sponge + Smagorinsky + Noble-Torczynski collision on shifted
@@ -91,7 +158,7 @@ template <class R>
 void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt[3]) {
     R wp = R(p.omega), wm = R(p.omegaMinus);
     if (R(x) > R(p.spongeX0)) {  // sponge, Kernels.metal:112-123
-        const R frac = std::fmin((R(x) - R(p.spongeX0)) * R(p.spongeInvW), R(1));
+        const R frac = Fmin((R(x) - R(p.spongeX0)) * R(p.spongeInvW), R(1));
         const R tau0 = R(1) / wp;
         const R tauS = tau0 + frac * (R(p.spongeTau) - tau0);
         if (p.omegaMinus == p.omega) {
@@ -145,11 +212,11 @@ void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt
             acc(pxz, sxz, CX[i] * CZ[i], d);
             acc(pyz, syz, CY[i] * CZ[i], d);
         }
-        const R Q = std::sqrt(pxx * pxx + pyy * pyy + pzz * pzz +
-                              R(2) * (pxy * pxy + pxz * pxz + pyz * pyz));
+        const R Q = Sqrt(pxx * pxx + pyy * pyy + pzz * pzz +
+                         R(2) * (pxy * pxy + pxz * pxz + pyz * pyz));
         const R tau0 = R(1) / wp;
         const R tauEff =
-            R(0.5) * (tau0 + std::sqrt(tau0 * tau0 + smagConst<R>() * R(p.cSmago) * Q * inv));
+            R(0.5) * (tau0 + Sqrt(tau0 * tau0 + smagConst<R>() * R(p.cSmago) * Q * inv));
         if (p.omegaMinus == p.omega) {
             wp = R(1) / tauEff;
             wm = wp;
@@ -168,7 +235,7 @@ void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt
     const R s0 = w0 * ap * (R(-3) * uF);
 
     if (eps == R(0)) {  // Kernels.metal:177-199 (bit-compatible golden path)
-        fh[0] = std::fma(wp, feq0 - fh[0], fh[0]) + s0;
+        fh[0] = Fma(wp, feq0 - fh[0], fh[0]) + s0;
         for (int i = 1; i < 19; i += 2) {
             const R w = weight<R>(i);
             const R cu = R(3) * cdot<R>(i, ux, uy, uz);
@@ -231,43 +298,65 @@ template <class R> inline void cell_force(const Params& p, const float* ffield, 
     }
 }
 
-// One thread of the `step` kernel, Kernels.metal:230-355. FOut is float for
-// the FP32-arithmetic instances and double for the FP64 oracle.
-template <class R, class S, class FOut>
-void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMaskBuf,
-               const uint32_t* lMaskBuf, const Params& p, FOut* force, const float* epsBuf,
-               const float* ffield, size_t n) {
-    const size_t N = A.N;
-    if (flags && flags[n] != FLUID) return;
-    const R eps = (p.useEps != 0u && epsBuf) ? R(epsBuf[n]) : R(0);
+// Slots one cell reads and writes in one pass of the AA pattern
+// (Kernels.metal:252-350): value fh_i comes from rd[i] and the post-collision
+// value of direction i goes to wr[i]. In both passes the two sets coincide,
+// which is what makes the update in place.
+struct CellSlots {
+    size_t rd[19];
+    size_t wr[19];
+};
+
+inline void cell_slots(const Params& p, uint32_t sMask, size_t N, size_t n, int x, int y, int z,
+                       CellSlots& c) {
     const int nx = int(p.nx), ny = int(p.ny), nz = int(p.nz);
-    const int x = int(n % p.nx);
-    const int t = int(n / p.nx);
-    const int y = t % ny;
-    const int z = t / ny;
-    R F[3];
-    cell_force<R>(p, ffield, N, n, F);
+    c.rd[0] = c.wr[0] = n;
+    for (int i = 1; i < 19; ++i) {
+        if (p.parity == 0u) {
+            c.rd[i] = size_t(i) * N + n;
+            c.wr[i] = size_t(OPP[i]) * N + n;
+            continue;
+        }
+        if ((sMask >> (OPP[i] - 1)) & 1u) {
+            c.rd[i] = size_t(i) * N + n;
+        } else {
+            const int sx = wrap(x - CX[i], nx), sy = wrap(y - CY[i], ny), sz = wrap(z - CZ[i], nz);
+            c.rd[i] = size_t(OPP[i]) * N + (size_t(sz) * ny + sy) * nx + sx;
+        }
+        if ((sMask >> (i - 1)) & 1u) {
+            c.wr[i] = size_t(OPP[i]) * N + n;
+        } else {
+            const int dx = wrap(x + CX[i], nx), dy = wrap(y + CY[i], ny), dz = wrap(z + CZ[i], nz);
+            c.wr[i] = size_t(i) * N + (size_t(dz) * ny + dy) * nx + dx;
+        }
+    }
+}
+
+// Local update of one fluid cell from the 19 values it read (in[i] from slot
+// rd[i]): out[i] is stored to slot wr[i]; a[] receives the cell's
+// momentum-exchange force and force_out tells whether the reference writes it
+// (Kernels.metal:240-354, same order of operations).
+template <class R>
+void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_t lMask, int x,
+                  int y, int z, const R in[19], R eps, const R F[3], R out[19], R a[3],
+                  bool& force_out) {
+    const int nx = int(p.nx), ny = int(p.ny), nz = int(p.nz);
     R fh[19];
+    for (int i = 0; i < 19; ++i) fh[i] = in[i];
     R rho = R(1);
     R nt[3] = {R(0), R(0), R(0)};
-
+    a[0] = a[1] = a[2] = R(0);
+    force_out = false;
     if (p.parity == 0u) {  // even: in-cell pass
-        for (int i = 0; i < 19; ++i) fh[i] = A.ld(i, n);
         collide<R>(fh, p, x, eps, F, rho, nt);
-        A.st(0, n, fh[0]);
-        for (int i = 1; i < 19; ++i) A.st(OPP[i], n, fh[i]);
-        if (p.writeForce != 0u && eps > R(0) && force) {
-            force[4 * n + 0] = FOut(nt[0]);
-            force[4 * n + 1] = FOut(nt[1]);
-            force[4 * n + 2] = FOut(nt[2]);
-            force[4 * n + 3] = FOut(0);
+        for (int i = 0; i < 19; ++i) out[i] = fh[i];
+        if (p.writeForce != 0u && eps > R(0)) {
+            a[0] = nt[0]; a[1] = nt[1]; a[2] = nt[2];
+            force_out = true;
         }
         return;
     }
     // odd: streaming pass with walls
-    const uint32_t sMask = sMaskBuf ? sMaskBuf[n] : 0u;
-    const uint32_t lMask = lMaskBuf ? lMaskBuf[n] : 0u;
-    R a[3] = {R(0), R(0), R(0)};
     auto acc_sub = [&](int i, R v) {  // a -= c_i * v
         const int c[3] = {CX[i], CY[i], CZ[i]};
         for (int k = 0; k < 3; ++k)
@@ -279,17 +368,11 @@ void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMask
             if (c[k] != 0) a[k] = c[k] > 0 ? a[k] + v : a[k] - v;
     };
     uint32_t deferred = 0;
-    fh[0] = A.ld(0, n);
     for (int i = 1; i < 19; ++i) {
         const int srcBit = OPP[i] - 1;
         if ((sMask >> srcBit) & 1u) {
-            fh[i] = A.ld(i, n);
             if ((lMask >> srcBit) & 1u) deferred |= (1u << i);
             if (p.writeForce != 0u) acc_sub(i, fh[i]);
-        } else {
-            const int sx = wrap(x - CX[i], nx), sy = wrap(y - CY[i], ny), sz = wrap(z - CZ[i], nz);
-            const size_t s = (size_t(sz) * ny + sy) * nx + sx;
-            fh[i] = A.ld(OPP[i], s);
         }
     }
     if (deferred != 0u) {
@@ -313,7 +396,7 @@ void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMask
     a[0] += nt[0];
     a[1] += nt[1];
     a[2] += nt[2];
-    A.st(0, n, fh[0]);
+    out[0] = fh[0];
     for (int i = 1; i < 19; ++i) {
         const int dstBit = i - 1;
         if ((sMask >> dstBit) & 1u) {
@@ -334,15 +417,40 @@ void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMask
                 }
             }
             const R sv = sign * fh[i];
-            A.st(OPP[i], n, has_corr ? sv - corr : sv);
+            out[i] = has_corr ? sv - corr : sv;
             if (p.writeForce != 0u) acc_add(i, sv + R(2) * weight<R>(i));
         } else {
-            const int dx = wrap(x + CX[i], nx), dy = wrap(y + CY[i], ny), dz = wrap(z + CZ[i], nz);
-            const size_t d = (size_t(dz) * ny + dy) * nx + dx;
-            A.st(i, d, fh[i]);
+            out[i] = fh[i];
         }
     }
-    if (p.writeForce != 0u && (sMask != 0u || eps > R(0)) && force) {
+    force_out = p.writeForce != 0u && (sMask != 0u || eps > R(0));
+}
+
+// One thread of the `step` kernel, Kernels.metal:230-355. FOut is float for
+// the FP32-arithmetic instances and double for the FP64 oracle.
+template <class R, class S, class FOut>
+void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMaskBuf,
+               const uint32_t* lMaskBuf, const Params& p, FOut* force, const float* epsBuf,
+               const float* ffield, size_t n) {
+    const size_t N = A.N;
+    if (flags && flags[n] != FLUID) return;
+    const R eps = (p.useEps != 0u && epsBuf) ? R(epsBuf[n]) : R(0);
+    const int x = int(n % p.nx);
+    const int t = int(n / p.nx);
+    const int y = t % int(p.ny);
+    const int z = t / int(p.ny);
+    R F[3];
+    cell_force<R>(p, ffield, N, n, F);
+    const uint32_t sMask = (p.parity != 0u && sMaskBuf) ? sMaskBuf[n] : 0u;
+    const uint32_t lMask = (p.parity != 0u && lMaskBuf) ? lMaskBuf[n] : 0u;
+    CellSlots c;
+    cell_slots(p, sMask, N, n, x, y, z, c);
+    R in[19], out[19], a[3];
+    for (int i = 0; i < 19; ++i) in[i] = R(A.f[c.rd[i]]);
+    bool fo = false;
+    cell_compute<R>(p, flags, sMask, lMask, x, y, z, in, eps, F, out, a, fo);
+    for (int i = 0; i < 19; ++i) A.f[c.wr[i]] = S(out[i]);
+    if (fo && force) {
         force[4 * n + 0] = FOut(a[0]);
         force[4 * n + 1] = FOut(a[1]);
         force[4 * n + 2] = FOut(a[2]);
@@ -548,6 +656,107 @@ int orc_init_field(int kind, void* f, uint32_t nx, uint32_t ny, uint32_t nz, uin
         case 2: init_all<double, double>(f, nx, ny, nz, mode, amplitude, tau); return 0;
     }
     return 1;
+}
+
+// FP64 discrete adjoint of the time-averaged momentum-exchange force, by
+// forward-mode automatic differentiation of the restated step (Dual<23>).
+//   J = (1/K) sum over the K odd steps t of dir . F_box(t),
+// F_box(t) = sum of the per-cell force of the odd pass (the reference's force
+// probe, Kernels.metal:263-353) over cells with box[0] <= x <= box[1],
+// box[2] <= y <= box[3], all z. params: `steps` consecutive 80-byte Params
+// (writeForce is set here on odd steps). f0: initial state, 19*N doubles.
+// Outputs J and, when not null, dJ/d eps (N) and dJ/d F_field (3 planes of N).
+int orc_adjoint_force(const double* f0, const uint8_t* flags, const uint32_t* solid_mask,
+                      const uint32_t* lid_mask, const void* params, int steps, const float* eps,
+                      const float* ffield, const int box[4], const double dir[3], double* J_out,
+                      double* grad_eps, double* grad_f) {
+    if (steps <= 0) return 1;
+    std::vector<Params> P(steps);
+    std::memcpy(P.data(), params, sizeof(Params) * steps);
+    const Params& p0 = P[0];
+    const size_t N = size_t(p0.nx) * p0.ny * p0.nz;
+    int K = 0;
+    for (int t = 0; t < steps; ++t) {
+        P[t].writeForce = P[t].parity;
+        K += P[t].parity ? 1 : 0;
+    }
+    const double w = K > 0 ? 1.0 / K : 0.0;
+    std::vector<std::vector<double>> states(steps, std::vector<double>(19 * N));
+    std::vector<double> A(f0, f0 + 19 * N);
+    double J = 0.0;
+    auto cell_ctx = [&](const Params& p, size_t n, int& x, int& y, int& z, uint32_t& sm,
+                        uint32_t& lm) {
+        x = int(n % p.nx);
+        const int t = int(n / p.nx);
+        y = t % int(p.ny);
+        z = t / int(p.ny);
+        sm = (p.parity != 0u && solid_mask) ? solid_mask[n] : 0u;
+        lm = (p.parity != 0u && lid_mask) ? lid_mask[n] : 0u;
+    };
+    auto in_box = [&](int x, int y) {
+        return x >= box[0] && x <= box[1] && y >= box[2] && y <= box[3];
+    };
+    for (int t = 0; t < steps; ++t) {  // forward, every input state kept
+        const Params& p = P[t];
+        states[t] = A;
+        for (size_t n = 0; n < N; ++n) {
+            if (flags && flags[n] != FLUID) continue;
+            int x, y, z;
+            uint32_t sm, lm;
+            cell_ctx(p, n, x, y, z, sm, lm);
+            CellSlots c;
+            cell_slots(p, sm, N, n, x, y, z, c);
+            double in[19], out[19], a[3], F[3];
+            for (int i = 0; i < 19; ++i) in[i] = A[c.rd[i]];
+            cell_force<double>(p, ffield, N, n, F);
+            const double e = (p.useEps && eps) ? double(eps[n]) : 0.0;
+            bool fo = false;
+            cell_compute<double>(p, flags, sm, lm, x, y, z, in, e, F, out, a, fo);
+            for (int i = 0; i < 19; ++i) A[c.wr[i]] = out[i];
+            if (p.parity && fo && in_box(x, y))
+                J += w * (dir[0] * a[0] + dir[1] * a[1] + dir[2] * a[2]);
+        }
+    }
+    *J_out = J;
+    if (grad_eps) std::fill(grad_eps, grad_eps + N, 0.0);
+    if (grad_f) std::fill(grad_f, grad_f + 3 * N, 0.0);
+    std::vector<double> lam(19 * N, 0.0);
+    typedef Dual<23> D;
+    for (int t = steps - 1; t >= 0; --t) {  // reverse
+        const Params& p = P[t];
+        const std::vector<double>& S = states[t];
+        for (size_t n = 0; n < N; ++n) {
+            if (flags && flags[n] != FLUID) continue;
+            int x, y, z;
+            uint32_t sm, lm;
+            cell_ctx(p, n, x, y, z, sm, lm);
+            CellSlots c;
+            cell_slots(p, sm, N, n, x, y, z, c);
+            D in[19], out[19], a[3], F[3];
+            for (int i = 0; i < 19; ++i) in[i] = D::var(S[c.rd[i]], i);
+            double Fv[3];
+            cell_force<double>(p, ffield, N, n, Fv);
+            for (int k = 0; k < 3; ++k) F[k] = D::var(Fv[k], 20 + k);
+            const D e = D::var((p.useEps && eps) ? double(eps[n]) : 0.0, 19);
+            bool fo = false;
+            cell_compute<D>(p, flags, sm, lm, x, y, z, in, e, F, out, a, fo);
+            double mu[19];
+            for (int j = 0; j < 19; ++j) mu[j] = lam[c.wr[j]];
+            const bool obj = p.parity && fo && in_box(x, y);
+            double g[23];
+            for (int k = 0; k < 23; ++k) {
+                double acc = 0.0;
+                for (int j = 0; j < 19; ++j) acc += mu[j] * out[j].d[k];
+                if (obj) acc += w * (dir[0] * a[0].d[k] + dir[1] * a[1].d[k] + dir[2] * a[2].d[k]);
+                g[k] = acc;
+            }
+            for (int i = 0; i < 19; ++i) lam[c.rd[i]] = g[i];
+            if (grad_eps) grad_eps[n] += g[19];
+            if (grad_f)
+                for (int k = 0; k < 3; ++k) grad_f[k * N + n] += g[20 + k];
+        }
+    }
+    return 0;
 }
 
 // Sum of all 19*N shifted DDFs in index order, in double (Sim.swift:447-458).

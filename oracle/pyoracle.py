@@ -53,6 +53,8 @@ def lib():
         L.orc_init_field.argtypes = [ctypes.c_int, _P, ctypes.c_uint32, ctypes.c_uint32,
                                      ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
                                      ctypes.c_float]
+        L.orc_adjoint_force.argtypes = [_P, _P, _P, _P, _P, ctypes.c_int, _P, _P, _P, _P, _P, _P,
+                                        _P]
         L.orc_mass.argtypes = [ctypes.c_int, _P, ctypes.c_size_t]
         L.orc_mass.restype = ctypes.c_double
         _lib = L
@@ -241,6 +243,27 @@ class OracleSim:
             return float(np.sum(m[:, 0] * m[:, 0] + m[:, 1] * m[:, 1] + m[:, 2] * m[:, 2]))
         u2 = (m[:, 0] * m[:, 0] + m[:, 1] * m[:, 1]) + m[:, 2] * m[:, 2]
         return float(np.sum(u2.astype(np.float64)))
+
+    def adjointForce(self, steps, box, direction=(1.0, 0.0, 0.0), grads=True):
+        """FP64 adjoint of J = mean over the odd steps of direction . F_box.
+
+        Runs the window [stepsDone, stepsDone + steps) from the current state in
+        FP64 (the state itself is not advanced). Returns (J, dJ/deps, dJ/dF) with
+        dJ/dF of shape (3, N); the gradients are None when grads=False."""
+        f0 = np.ascontiguousarray(self.f, dtype=np.float64)
+        P = b"".join(self.params(self.stepsDone + t) for t in range(int(steps)))
+        box = (ctypes.c_int * 4)(int(box[0][0]), int(box[0][1]), int(box[1][0]), int(box[1][1]))
+        d3 = (ctypes.c_double * 3)(*[float(v) for v in direction])
+        J = ctypes.c_double()
+        ge = np.zeros(self.N) if grads else None
+        gf = np.zeros((3, self.N)) if grads else None
+        rc = lib().orc_adjoint_force(_ptr(f0), _ptr(self.flags), _ptr(self.solidMask),
+                                     _ptr(self.lidMask), P, int(steps), _ptr(self.eps),
+                                     _ptr(self.forceField), box, d3, ctypes.byref(J), _ptr(ge),
+                                     _ptr(gf))
+        if rc != 0:
+            raise RuntimeError("orc_adjoint_force failed")
+        return J.value, ge, gf
 
     def massSum(self):
         return float(lib().orc_mass(self.kind, _ptr(self.f), self.f.size))

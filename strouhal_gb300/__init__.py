@@ -115,6 +115,12 @@ def lib():
         "stro_batch_last_path": ([_P, ctypes.c_char_p, ctypes.c_size_t], c_int),
         "stro_batch_autotune": ([_P, c_i64, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
                                  ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(c_double)], c_int),
+        "stro_adj_create": ([_P, _P, _P, c_i64, ctypes.c_int32, ctypes.POINTER(_P)], c_int),
+        "stro_adj_destroy": ([_P], c_int),
+        "stro_adj_forward": ([_P, ctypes.POINTER(c_double)], c_int),
+        "stro_adj_backward": ([_P, _P, _P], c_int),
+        "stro_adj_stats": ([_P, ctypes.POINTER(c_double), ctypes.POINTER(c_double),
+                            ctypes.POINTER(c_double), ctypes.POINTER(c_i64)], c_int),
         "stro_sha256_hex": ([_P, ctypes.c_size_t, ctypes.c_char_p], c_int),
         "stro_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(_P)], c_int),
         "stro_host_free": ([_P], c_int),
@@ -522,6 +528,53 @@ class Batch:
     def close(self):
         if getattr(self, "_h", None):
             lib().stro_batch_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Adjoint:
+    """Discrete adjoint of the time-averaged force over a window (stro_adj_*).
+
+    J = mean over the odd steps of direction . F_box, F_box the force the
+    probe box sums. forward() advances the simulation through the window and
+    returns J; backward() returns (dJ/d eps, dJ/d F_field) as float32 arrays of
+    shapes (N,) and (3, N)."""
+
+    def __init__(self, sim, steps, box, direction=(1.0, 0.0, 0.0), checkpoints=8):
+        self.sim = sim
+        d3 = (ctypes.c_double * 3)(*[float(v) for v in direction])
+        b4 = (ctypes.c_int32 * 4)(int(box[0][0]), int(box[0][1]), int(box[1][0]), int(box[1][1]))
+        self._h = _P()
+        _check(lib().stro_adj_create(sim._h, d3, b4, int(steps), int(checkpoints),
+                                     ctypes.byref(self._h)))
+
+    def forward(self):
+        J = ctypes.c_double()
+        _check(lib().stro_adj_forward(self._h, ctypes.byref(J)))
+        return J.value
+
+    def backward(self):
+        N = self.sim.cells
+        ge = np.zeros(N, np.float32)
+        gf = np.zeros((3, N), np.float32)
+        _check(lib().stro_adj_backward(self._h, ge.ctypes.data, gf.ctypes.data))
+        return ge, gf
+
+    def stats(self):
+        f, r, a, k = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int64()
+        _check(lib().stro_adj_stats(self._h, ctypes.byref(f), ctypes.byref(r), ctypes.byref(a),
+                                    ctypes.byref(k)))
+        return {"forward_s": f.value, "recompute_s": r.value, "adjoint_s": a.value,
+                "adjoint_steps": k.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().stro_adj_destroy(self._h)
             self._h = _P()
 
     def __del__(self):

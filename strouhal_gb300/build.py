@@ -20,7 +20,7 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIBNAME = "libstrouhal_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-SOURCES = ["lbm_step.cu", "lbm_pair.cu", "lbm_rows.cu", "lbm_probe.cu", "lbm_batch.cu", "runtime.cu", "batch.cu", "sha256.cpp"]
+SOURCES = ["lbm_step.cu", "lbm_pair.cu", "lbm_rows.cu", "lbm_probe.cu", "lbm_batch.cu", "lbm_adjoint.cu", "runtime.cu", "batch.cu", "adjoint.cu", "sha256.cpp"]
 
 
 def nvcc():

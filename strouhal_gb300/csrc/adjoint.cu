@@ -1,0 +1,253 @@
+// Host side of the discrete adjoint (C ABI stro_adj_*): checkpointed forward,
+// recomputation between checkpoints, reverse sweep.
+//
+// The tape is the schedule kept here: the window [t0, t0 + steps), the
+// checkpoint states saved every `seg` steps on the device during the forward
+// run, and the per-step uniforms (ramp) rebuilt from the step index. The
+// backward sweep walks the segments last to first: it restores a segment's
+// checkpoint, recomputes the segment forward while keeping every input state
+// on the device, then runs the adjoint steps of the segment in reverse.
+// Memory: checkpoints + one segment of states + the FP32 adjoint array.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "lbm_adjoint.h"
+#include "runtime_internal.h"
+
+using namespace stro;
+using namespace stro::rt;
+
+struct stro_adjoint {
+    stro_sim* sim = nullptr;
+    double dir[3] = {1.0, 0.0, 0.0};
+    int box[4] = {0, 0, 0, 0};
+    int64_t steps = 0, t0 = 0, seg = 0;
+    int32_t ncheck = 0;
+    bool forward_done = false;
+    size_t state_bytes = 0;
+    void* d_check = nullptr;   // ncheck states
+    void* d_seg = nullptr;     // seg states
+    float* d_lam = nullptr;
+    float* d_geps = nullptr;
+    float* d_gf = nullptr;
+    double* d_forces = nullptr;  // 3 doubles per odd step
+    int64_t nodd = 0;
+    double J = 0.0;
+    double fwd_seconds = 0.0, recompute_seconds = 0.0, adjoint_seconds = 0.0;
+    int64_t adjoint_launches = 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+
+namespace {
+
+void adj_free(stro_adjoint* a) {
+    cudaFree(a->d_check);
+    cudaFree(a->d_seg);
+    cudaFree(a->d_lam);
+    cudaFree(a->d_geps);
+    cudaFree(a->d_gf);
+    cudaFree(a->d_forces);
+    if (a->e0) cudaEventDestroy(a->e0);
+    if (a->e1) cudaEventDestroy(a->e1);
+}
+
+char* state_at(void* base, size_t bytes, int64_t k) { return static_cast<char*>(base) + bytes * k; }
+
+int timed(stro_adjoint* a, double* acc, int rc_in) {
+    (void)rc_in;
+    cudaStream_t st = a->sim->ctx->stream;
+    STRO_CUDA(cudaEventRecord(a->e1, st));
+    STRO_CUDA(cudaEventSynchronize(a->e1));
+    float ms = 0.f;
+    STRO_CUDA(cudaEventElapsedTime(&ms, a->e0, a->e1));
+    *acc += double(ms) * 1e-3;
+    return STRO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int stro_adj_create(stro_sim* s, const double dir[3], const int32_t box[4], int64_t steps,
+                    int32_t checkpoints, stro_adjoint** out) {
+    if (!s || !dir || !box || !out) return fail(STRO_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (steps < 1) return fail(STRO_ERR_INVALID, "the window needs at least one step");
+    if (checkpoints < 1) checkpoints = 1;
+    if (checkpoints > steps) checkpoints = int32_t(steps);
+    if (box[0] < 0 || box[1] >= s->nx || box[2] < 0 || box[3] >= s->ny || box[0] > box[1] ||
+        box[2] > box[3])
+        return fail(STRO_ERR_INVALID, "force box outside the lattice");
+    cudaSetDevice(s->ctx->device);
+    stro_adjoint* a = new (std::nothrow) stro_adjoint;
+    if (!a) return fail(STRO_ERR_OOM, "host allocation failed");
+    a->sim = s;
+    std::memcpy(a->dir, dir, sizeof a->dir);
+    std::memcpy(a->box, box, sizeof a->box);
+    a->steps = steps;
+    a->ncheck = checkpoints;
+    a->seg = (steps + checkpoints - 1) / checkpoints;
+    a->state_bytes = 19 * s->plane * s->esize;
+    const uint64_t N = s->N;
+    cudaError_t e = cudaMalloc(&a->d_check, a->state_bytes * size_t(a->ncheck));
+    if (e == cudaSuccess) e = cudaMalloc(&a->d_seg, a->state_bytes * size_t(a->seg));
+    if (e == cudaSuccess) e = cudaMalloc(&a->d_lam, 19 * s->plane * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&a->d_geps, N * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&a->d_gf, 3 * N * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&a->d_forces, size_t(steps / 2 + 2) * 3 * sizeof(double));
+    if (e == cudaSuccess) e = cudaEventCreate(&a->e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&a->e1);
+    if (e != cudaSuccess) {
+        adj_free(a);
+        delete a;
+        return cuda_fail(e, "adjoint buffers");
+    }
+    *out = a;
+    return STRO_OK;
+}
+
+int stro_adj_destroy(stro_adjoint* a) {
+    if (!a) return STRO_OK;
+    cudaSetDevice(a->sim->ctx->device);
+    cudaStreamSynchronize(a->sim->ctx->stream);
+    adj_free(a);
+    delete a;
+    return STRO_OK;
+}
+
+int stro_adj_forward(stro_adjoint* a, double* J) {
+    if (!a || !J) return fail(STRO_ERR_INVALID, "null argument");
+    stro_sim* s = a->sim;
+    cudaSetDevice(s->ctx->device);
+    cudaStream_t st = s->ctx->stream;
+    a->t0 = s->steps_done;
+    a->nodd = 0;
+    const bool geo = geo_on(s);
+    if (geo) {
+        const dim3 g = step_grid(step_args(s, 0), s->probe_block);
+        const size_t need = size_t(3) * g.x * g.y * g.z;
+        if (s->partials_len < need) {
+            cudaFree(s->d_partials);
+            s->d_partials = nullptr;
+            s->partials_len = 0;
+            STRO_CUDA(cudaMalloc(&s->d_partials, need * sizeof(double)));
+            s->partials_len = need;
+        }
+    }
+    STRO_CUDA(cudaEventRecord(a->e0, st));
+    for (int64_t k = 0; k < a->steps; ++k) {
+        const int64_t t = a->t0 + k;
+        if (k % a->seg == 0)
+            STRO_CUDA(cudaMemcpyAsync(state_at(a->d_check, a->state_bytes, k / a->seg), s->d_f,
+                                      a->state_bytes, cudaMemcpyDeviceToDevice, st));
+        StepArgs sa = step_args(s, t);
+        const bool odd = (t & 1) != 0;
+        const bool probe = odd && geo;
+        if (probe) {
+            sa.box_x0 = a->box[0]; sa.box_x1 = a->box[1];
+            sa.box_y0 = a->box[2]; sa.box_y1 = a->box[3];
+        }
+        STRO_CUDA(launch_sim_step(s, sa, t, probe));
+        if (odd) {
+            if (probe) {
+                const dim3 g = step_grid(sa, s->probe_block);
+                STRO_CUDA(launch_fold(s->d_partials, int(g.x * g.y * g.z), 3,
+                                      a->d_forces + 3 * a->nodd, st));
+            } else {
+                STRO_CUDA(cudaMemsetAsync(a->d_forces + 3 * a->nodd, 0, 3 * sizeof(double), st));
+            }
+            ++a->nodd;
+        }
+    }
+    int rc = timed(a, &a->fwd_seconds, STRO_OK);
+    if (rc != STRO_OK) return rc;
+    std::vector<double> forces(size_t(3 * a->nodd));
+    if (a->nodd)
+        STRO_CUDA(cudaMemcpy(forces.data(), a->d_forces, forces.size() * sizeof(double),
+                             cudaMemcpyDeviceToHost));
+    double sum = 0.0;
+    for (int64_t j = 0; j < a->nodd; ++j)
+        sum += a->dir[0] * forces[3 * j] + a->dir[1] * forces[3 * j + 1] +
+               a->dir[2] * forces[3 * j + 2];
+    a->J = a->nodd ? sum / double(a->nodd) : 0.0;
+    s->steps_done += a->steps;
+    a->forward_done = true;
+    *J = a->J;
+    return STRO_OK;
+}
+
+int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
+    if (!a) return fail(STRO_ERR_INVALID, "null adjoint handle");
+    if (!a->forward_done) return fail(STRO_ERR_STATE, "stro_adj_forward must run first");
+    stro_sim* s = a->sim;
+    cudaSetDevice(s->ctx->device);
+    cudaStream_t st = s->ctx->stream;
+    const uint64_t N = s->N;
+    const int half = s->precision == STRO_FP16S ? 1 : 0;
+    const int geo = geo_on(s) ? 1 : 0;
+    STRO_CUDA(cudaMemsetAsync(a->d_lam, 0, 19 * s->plane * sizeof(float), st));
+    STRO_CUDA(cudaMemsetAsync(a->d_geps, 0, N * sizeof(float), st));
+    STRO_CUDA(cudaMemsetAsync(a->d_gf, 0, 3 * N * sizeof(float), st));
+    const float w = a->nodd ? float(1.0 / double(a->nodd)) : 0.0f;
+    const dim3 ablock(32, 4, 1);
+    void* live = s->d_f;  // the forward kernels step the buffer a StepArgs points to
+    for (int32_t c = a->ncheck - 1; c >= 0; --c) {
+        const int64_t k0 = int64_t(c) * a->seg;
+        const int64_t len = std::min<int64_t>(a->seg, a->steps - k0);
+        if (len <= 0) continue;
+        // recompute the segment, keeping the input state of every step
+        STRO_CUDA(cudaEventRecord(a->e0, st));
+        STRO_CUDA(cudaMemcpyAsync(state_at(a->d_seg, a->state_bytes, 0),
+                                  state_at(a->d_check, a->state_bytes, c), a->state_bytes,
+                                  cudaMemcpyDeviceToDevice, st));
+        for (int64_t k = 1; k < len; ++k) {
+            void* cur = state_at(a->d_seg, a->state_bytes, k);
+            STRO_CUDA(cudaMemcpyAsync(cur, state_at(a->d_seg, a->state_bytes, k - 1),
+                                      a->state_bytes, cudaMemcpyDeviceToDevice, st));
+            StepArgs sa = step_args(s, a->t0 + k0 + k - 1);
+            sa.f = cur;
+            STRO_CUDA(launch_sim_step(s, sa, a->t0 + k0 + k - 1, false));
+        }
+        int rc = timed(a, &a->recompute_seconds, STRO_OK);
+        if (rc != STRO_OK) return rc;
+        // adjoint steps of the segment, last to first
+        STRO_CUDA(cudaEventRecord(a->e0, st));
+        for (int64_t k = len - 1; k >= 0; --k) {
+            const int64_t t = a->t0 + k0 + k;
+            AdjArgs g{};
+            g.a = step_args(s, t);
+            g.a.f = state_at(a->d_seg, a->state_bytes, k);
+            g.lam = a->d_lam;
+            g.grad_eps = a->d_geps;
+            g.grad_f = a->d_gf;
+            g.obj_w = (t & 1) ? w : 0.0f;
+            for (int q = 0; q < 3; ++q) g.dir[q] = float(a->dir[q]);
+            std::memcpy(g.box, a->box, sizeof g.box);
+            g.force_terms = 1;
+            STRO_CUDA(launch_adjoint_step(g, half, int(t & 1), geo, ablock, st));
+            ++a->adjoint_launches;
+        }
+        rc = timed(a, &a->adjoint_seconds, STRO_OK);
+        if (rc != STRO_OK) return rc;
+    }
+    (void)live;
+    if (grad_eps)
+        STRO_CUDA(cudaMemcpy(grad_eps, a->d_geps, N * sizeof(float), cudaMemcpyDeviceToHost));
+    if (grad_force)
+        STRO_CUDA(cudaMemcpy(grad_force, a->d_gf, 3 * N * sizeof(float), cudaMemcpyDeviceToHost));
+    return STRO_OK;
+}
+
+int stro_adj_stats(stro_adjoint* a, double* forward_s, double* recompute_s, double* adjoint_s,
+                   int64_t* adjoint_steps) {
+    if (!a) return fail(STRO_ERR_INVALID, "null adjoint handle");
+    if (forward_s) *forward_s = a->fwd_seconds;
+    if (recompute_s) *recompute_s = a->recompute_seconds;
+    if (adjoint_s) *adjoint_s = a->adjoint_seconds;
+    if (adjoint_steps) *adjoint_steps = a->adjoint_launches;
+    return STRO_OK;
+}
+
+}  // extern "C"

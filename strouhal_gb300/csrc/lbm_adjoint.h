@@ -1,0 +1,24 @@
+// Discrete adjoint step (lbm_adjoint.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "lbm_device.cuh"
+
+namespace stro {
+
+struct AdjArgs {
+    StepArgs a;         // forward arguments of the step; a.f = the stored input state of the step
+    float* lam;         // adjoint of the state, 19 planes, plane stride a.plane (FP32)
+    float* grad_eps;    // dJ/d eps (N), or null
+    float* grad_f;      // dJ/d F_field (3 planes of a.ffield_plane), or null
+    float obj_w;        // weight of this step's force in J (odd steps), 0 = none
+    float dir[3];       // force direction of the objective
+    int box[4];         // x0, x1, y0, y1 (inclusive) of the force box
+    int force_terms;    // differentiate the Guo source terms
+};
+
+cudaError_t launch_adjoint_step(const AdjArgs& g, int half_storage, int parity, int geo, dim3 block,
+                                cudaStream_t st);
+
+}  // namespace stro
