@@ -1,0 +1,493 @@
+"""Case runners over the C ABI for the workloads the step is judged on.
+
+Each function restates a host-side procedure of the reference's gate suite
+(Sources/strouhal/Cases.swift, Sources/StrouhalCore/CaseSetups.swift) on top
+of strouhal_gb300.Simulation and returns plain measurements (dicts of floats
+and lists). The thresholds and published reference values the reference
+compares against are applied by the tests, not here.
+
+    python -m strouhal_gb300.cases <name> [--out results.json]
+
+names: poiseuille, tg_order, cavity, dfg2, dfg2_adjoint, tgv, sphere,
+sphere_adjoint, ladder.
+"""
+import argparse
+import json
+import math
+import time
+
+import numpy as np
+
+import strouhal_gb300 as sg
+
+
+# --------------------------------------------------------------- Poiseuille
+def poiseuille(gpu, H=64, precision="fp32"):
+    """Body-force channel with TRT Lambda=3/16 (Cases.swift:286-317): max
+    |u - u_exact| / u_max over the profile after 6 diffusive times."""
+    tau = 0.8
+    nu = (tau - 0.5) / 3.0
+    umax = 0.05
+    F = 8.0 * nu * umax / (H * H)
+    wp, wm = sg.trtOmegas(tau, 3.0 / 16.0)
+    ny = H + 2
+    flags = np.zeros((1, ny, 16), np.uint8)
+    flags[:, 0, :] = flags[:, -1, :] = sg.Cell.solid
+    s = sg.Simulation(gpu, precision=precision, nx=16, ny=ny, nz=1, omega=wp, omegaMinus=wm,
+                      force=(F, 0.0, 0.0), flags=flags.reshape(-1))
+    steps = (int(6.0 * H * H / nu) + 1) & ~1
+    s.run(steps)
+    m = s.probeMoments()
+    errs = []
+    for j in range(1, H + 1):
+        yd = j - 0.5
+        exact = F / (2.0 * nu) * yd * (H - yd)
+        errs.append(abs(float(m[j * 16 + 8, 0]) - exact) / umax)
+    s.close()
+    return {"H": H, "steps": steps, "max_err": max(errs), "wall_err": max(errs[0], errs[-1]),
+            "center_err": max(errs[H // 2 - 1], errs[H // 2])}
+
+
+# ------------------------------------------------------- Taylor-Green order
+def tg_order(gpu, sizes=(32, 64, 128), u0base=0.20, precision="fp32"):
+    """2-D Taylor-Green decay under diffusive scaling (Cases.swift:329-370)."""
+    nu = 0.02
+    wp, wm = sg.trtOmegas(3.0 * nu + 0.5, 0.25)
+    errors = []
+    for N in sizes:
+        u0 = u0base * 32.0 / N
+        k = 2.0 * math.pi / N
+        steps = int(math.log(2.0) / (2.0 * nu * k * k)) & ~1
+        s = sg.Simulation(gpu, precision=precision, nx=N, ny=N, nz=1, omega=wp, omegaMinus=wm)
+        s.initField(1, u0)
+        s.run(steps)
+        m = s.probeMoments().reshape(N, N, 4)
+        decay = math.exp(-2.0 * nu * k * k * steps)
+        xa = (np.arange(N) + 0.5)[None, :]
+        ya = (np.arange(N) + 0.5)[:, None]
+        ue = u0 * decay * np.sin(k * xa) * np.cos(k * ya)
+        ve = -u0 * decay * np.cos(k * xa) * np.sin(k * ya)
+        du = m[:, :, 0].astype(np.float64) - ue
+        dv = m[:, :, 1].astype(np.float64) - ve
+        errors.append(math.sqrt(float(np.sum(du * du + dv * dv)) / (2 * N * N)) / (u0 * decay))
+        s.close()
+    orders = [math.log2(errors[i - 1] / errors[i]) for i in range(1, len(errors))]
+    return {"sizes": list(sizes), "errors": errors, "orders": orders, "min_order": min(orders)}
+
+
+# ------------------------------------------------------------------- cavity
+def cavity(gpu, n=128, re=100.0, steps=20000, lam=None, ulid=0.1, ramp=5000, nz=3,
+           precision="fp32"):
+    """Lid-driven cavity: n x n interior, 1-cell frame, lid at the top moving
+    +x, periodic z (Cases.swift:167-215 set-up). Returns the centreline
+    profiles u(y)/u_lid on the vertical and v(x)/u_lid on the horizontal
+    centreline (each averaged over the two centre columns / rows, z = 0), at
+    physical coordinates (i - 0.5)/n, plus the digest and mass drift."""
+    nx = ny = n + 2
+    nu = ulid * n / re
+    wp, wm = sg.trtOmegas(3.0 * nu + 0.5, lam)
+    flags = np.zeros((nz, ny, nx), np.uint8)
+    flags[:, :, 0] = flags[:, :, -1] = flags[:, 0, :] = sg.Cell.solid
+    flags[:, -1, :] = sg.Cell.lid
+    s = sg.Simulation(gpu, precision=precision, nx=nx, ny=ny, nz=nz, omega=wp, omegaMinus=wm,
+                      lid=(ulid, 0.0, 0.0), rampSteps=ramp, flags=flags.reshape(-1))
+    m0 = s.massSum()
+    t0 = time.perf_counter()
+    s.run(steps)
+    wall = time.perf_counter() - t0
+    m = s.probeMoments().reshape(nz, ny, nx, 4)[0]
+    c0, c1 = n // 2, n // 2 + 1
+    u = [(float(m[j, c0, 0]) + float(m[j, c1, 0])) / 2.0 / ulid for j in range(1, n + 1)]
+    v = [(float(m[c0, i, 1]) + float(m[c1, i, 1])) / 2.0 / ulid for i in range(1, n + 1)]
+    out = {"n": n, "re": re, "steps": steps, "srt": lam is None, "coords": [(i - 0.5) / n
+                                                                            for i in range(1, n + 1)],
+           "u_centerline": u, "v_centerline": v, "digest": s.stateDigest,
+           "mass_drift": s.massSum() - m0, "gpu_seconds": s.gpuSeconds, "wall_seconds": wall}
+    s.close()
+    return out
+
+
+def ghia_rms(rec, table_u, table_v):
+    """Centreline RMS against a table of (coordinate, value) pairs, linear
+    interpolation between the two bracketing nodes (Cases.swift:220-270)."""
+    n = rec["n"]
+
+    def interp(coord, vals):
+        sx = coord * n + 0.5
+        k0 = min(max(int(math.floor(sx)), 1), n - 1)
+        frac = sx - k0
+        return vals[k0 - 1] * (1 - frac) + vals[k0] * frac
+
+    d = [interp(y, rec["u_centerline"]) - r for y, r in table_u]
+    d += [interp(x, rec["v_centerline"]) - r for x, r in table_v]
+    return math.sqrt(sum(x * x for x in d) / len(d)), max(abs(x) for x in d)
+
+
+# ------------------------------------------------------------ DFG 2D-2 (C3)
+def dfg2(gpu, D=64, uin_max=0.06, nz=3, transient=None, sample_cycles=22, stride=26,
+         sponge_d=3, sponge_tau=1.0, ramp=24000, precision="fp32", max_steps=None):
+    """Cylinder channel with Noble-Torczynski walls (Cases.swift:840-951,
+    CaseSetups.swift:29-65): C_D and C_L sampled every `stride` steps by the
+    two-step force probe, Strouhal number from the upward zero crossings of
+    C_L, peaks and cycle means over complete cycles."""
+    nx = 22 * D + 2
+    ny = int(4.1 * D) + 2
+    umean = uin_max * 2.0 / 3.0
+    nu = umean * D / 100.0
+    wp, wm = sg.trtOmegas(3.0 * nu + 0.5, 3.0 / 16.0)
+    cx = cy = 0.5 + 2.0 * D
+    flags = np.zeros((nz, ny, nx), np.uint8)
+    flags[:, 0, :] = flags[:, -1, :] = sg.Cell.solid
+    flags[:, 1:-1, 0] = flags[:, 1:-1, -1] = sg.Cell.inflow
+    s = sg.Simulation(gpu, precision=precision, nx=nx, ny=ny, nz=nz, omega=wp, omegaMinus=wm,
+                      uin=uin_max, rampSteps=ramp, wantsForces=True, flags=flags.reshape(-1))
+    s.setSolidFractions(np.tile(sg.diskSolidFractions(nx, ny, cx, cy, D / 2.0), nz))
+    s.sponge = (float(nx - 1 - sponge_d * D), float(sponge_d * D), sponge_tau)
+    box_x = (int(cx) - D // 2 - 3, int(cx) + D // 2 + 3)
+    box_y = (int(cy) - D // 2 - 3, int(cy) + D // 2 + 3)
+    if transient is None:
+        transient = (int(60000 * 0.075 / uin_max) + 1) & ~1
+    t0 = time.perf_counter()
+    s.run(transient)
+    period = D / (0.30 * umean)
+    samples = int(period * sample_cycles / stride) + 64
+    if max_steps is not None:
+        samples = min(samples, max(1, (max_steps - transient) // stride))
+    norm = umean * umean * D * nz  # force per unit depth: the z extent holds nz cells
+    cd, cl, t = [], [], []
+    for _ in range(samples):
+        s.run(stride - 2)
+        f = s.probeForce(box_x, box_y)
+        cd.append(2.0 * f[0] / norm)
+        cl.append(2.0 * f[1] / norm)
+        t.append(s.stepsDone)
+    wall = time.perf_counter() - t0
+    stats = cycle_stats(t, cd, cl, D, umean)
+    out = {"D": D, "nx": nx, "ny": ny, "nz": nz, "uin_max": uin_max, "steps": s.stepsDone,
+           "stride": stride, "t": t, "cd": cd, "cl": cl, "digest": s.stateDigest,
+           "gpu_seconds": s.gpuSeconds, "wall_seconds": wall,
+           "cells": nx * ny * nz}
+    out.update(stats)
+    s.close()
+    return out
+
+
+def cycle_stats(t, cd, cl, D, umean):
+    """Strouhal number, peaks and batch-mean C_D over complete C_L cycles."""
+    cross = []
+    for k in range(1, len(cl)):
+        if cl[k - 1] < 0 <= cl[k]:
+            frac = -cl[k - 1] / (cl[k] - cl[k - 1])
+            cross.append(t[k - 1] + frac * (t[k] - t[k - 1]))
+    cycles = max(len(cross) - 1, 0)
+    st, maxcd, maxcl, means = 0.0, 0.0, float("-inf"), []
+    if cycles >= 2:
+        st = D / ((cross[-1] - cross[0]) / cycles * umean)
+        for c in range(cycles):
+            sel = [k for k in range(len(cl)) if cross[c] <= t[k] < cross[c + 1]]
+            if sel:
+                maxcd = max(maxcd, max(cd[k] for k in sel))
+                maxcl = max(maxcl, max(cl[k] for k in sel))
+                means.append(sum(cd[k] for k in sel) / len(sel))
+    mean, ci = 0.0, 0.0
+    if len(means) >= 4:
+        mean = sum(means) / len(means)
+        sd = math.sqrt(sum((m - mean) ** 2 for m in means) / (len(means) - 1))
+        ci = 1.96 * sd / math.sqrt(len(means))
+    return {"strouhal": st, "max_cd": maxcd, "max_cl": maxcl, "mean_cd": mean,
+            "mean_cd_ci95": ci, "cycles": cycles}
+
+
+# --------------------------------------------------------------- TGV (C2)
+def tgv(gpu, n=256, u0=0.05, t_end=20.0, precision="fp16s", lam=None, log_every=100,
+        re=1600.0):
+    """3-D Taylor-Green vortex at Re=1600 (Cases.swift:1217-1282, with the
+    logging cadence of the workload): kinetic energy E = sum|u|^2/(2 N u0^2)
+    and the strain-rate dissipation every `log_every` steps, dissipation also
+    as -dE/dt* by central differences, peak refined by a parabola. A run that
+    goes non-finite stops and reports the time."""
+    L = n / (2.0 * math.pi)
+    nu = u0 * L / re
+    tau = 3.0 * nu + 0.5
+    wp, wm = sg.trtOmegas(tau, lam)
+    s = sg.Simulation(gpu, precision=precision, nx=n, ny=n, nz=n, omega=wp, omegaMinus=wm)
+    s.initField(2, u0)
+    s.autotune(steps=10)
+    tc = L / u0
+    total = int(round(t_end * tc))
+    total -= total % log_every
+    N = s.cells
+    times, E, eps_s = [], [], []
+    nonfinite = None
+    t0 = time.perf_counter()
+    while True:
+        ke = s.kineticEnergySum()
+        ds = s.dissipationSum()
+        times.append(s.stepsDone / tc)
+        E.append(ke / (2.0 * N * u0 * u0))
+        eps_s.append(ds * L / (N * u0 ** 3))
+        if not math.isfinite(ke):
+            nonfinite = times[-1]
+            break
+        if s.stepsDone >= total:
+            break
+        s.run(log_every)
+    wall = time.perf_counter() - t0
+    eps_fd = [-(E[j + 1] - E[j - 1]) / (times[j + 1] - times[j - 1]) for j in range(1, len(E) - 1)]
+    t_fd = times[1:-1]
+    peak_t, peak_e = float("nan"), float("nan")
+    if len(eps_fd) >= 3:
+        k = int(np.argmax(eps_fd))
+        peak_t, peak_e = t_fd[k], eps_fd[k]
+        if 0 < k < len(eps_fd) - 1:
+            y0, y1, y2 = eps_fd[k - 1], eps_fd[k], eps_fd[k + 1]
+            den = y0 - 2 * y1 + y2
+            if abs(den) > 1e-12:
+                dd = 0.5 * (y0 - y2) / den
+                peak_t = t_fd[k] + dd * (t_fd[1] - t_fd[0])
+                peak_e = y1 - 0.25 * (y0 - y2) * dd
+    out = {"n": n, "u0": u0, "tau": tau, "precision": precision,
+           "collision": "SRT" if lam is None else "TRT Lambda=%g" % lam, "steps": s.stepsDone,
+           "steps_per_tstar": tc, "t": times, "E": E, "eps_strain": eps_s, "t_fd": t_fd,
+           "eps_fd": eps_fd, "peak_t": peak_t, "peak_eps": peak_e, "nonfinite_at": nonfinite,
+           "gpu_seconds": s.gpuSeconds, "wall_seconds": wall,
+           "glups": N * s.stepsDone / max(s.gpuSeconds, 1e-30) / 1e9, "variant": s.variant}
+    s.close()
+    return out
+
+
+# ------------------------------------------------------------- sphere (C5)
+def sphere(gpu, nx=512, ny=256, nz=256, D=48, center=(128.0, 128.0, 128.0), u=0.05, re=300.0,
+           cs=0.1, steps=50000, probe_every=500, ramp=8000, sponge=True, precision="fp16s",
+           sub=8):
+    """3-D sphere wake with LES (workload set-up from CaseSetups.swift:95-134):
+    uniform-inflow velocity walls at x = 0 and x = nx-1, periodic y and z,
+    Noble-Torczynski sphere from 8^3 subcell sampling, Smagorinsky
+    cSmago = Cs^2, Guo force field present and zero. Drag coefficient
+    2 F_x / (u^2 pi D^2 / 4) every `probe_every` steps."""
+    nu = u * D / re
+    wp, _ = sg.trtOmegas(3.0 * nu + 0.5, None)
+    flags = np.zeros((nz, ny, nx), np.uint8)
+    flags[:, :, 0] = flags[:, :, -1] = sg.Cell.inflow
+    s = sg.Simulation(gpu, precision=precision, nx=nx, ny=ny, nz=nz, omega=wp, uin=u,
+                      rampSteps=ramp, cSmago=cs * cs, wantsForces=True, flags=flags.reshape(-1))
+    s.inflowUniform = True
+    cx, cy, cz = center
+    s.setSolidFractions(sg.sphereSolidFractions(nx, ny, nz, cx, cy, cz, D / 2.0, sub))
+    s.setForceField(np.zeros((3, nx * ny * nz), np.float32))
+    if sponge:
+        s.sponge = (float(nx - 1 - D), float(D), 1.0)
+    bx = (int(cx) - D // 2 - 3, int(cx) + D // 2 + 3)
+    byr = (int(cy) - D // 2 - 3, int(cy) + D // 2 + 3)
+    area = u * u * math.pi * D * D / 4.0
+    t, cd = [], []
+    t0 = time.perf_counter()
+    while s.stepsDone + probe_every <= steps:
+        s.run(probe_every - 2)
+        f = s.probeForce(bx, byr)
+        t.append(s.stepsDone)
+        cd.append(2.0 * f[0] / area)
+    wall = time.perf_counter() - t0
+    out = {"nx": nx, "ny": ny, "nz": nz, "D": D, "re": re, "steps": s.stepsDone, "t": t,
+           "cd": cd, "finite": s.checkFinite(), "gpu_seconds": s.gpuSeconds,
+           "wall_seconds": wall, "glups": s.cells * s.stepsDone / max(s.gpuSeconds, 1e-30) / 1e9}
+    s.close()
+    return out
+
+
+# ---------------------------------------------------------- ladder (C4)
+def ladder_instances(count=32, seed=1234, edges=(32, 48, 64, 96, 128, 160),
+                     machs=(0.05, 0.025), t_star=5.0):
+    """Seed-fixed TGV rungs: (edge, u0, steps, log_every)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(rng.choice(edges))
+        u0 = float(rng.choice(machs))
+        L = n / (2.0 * math.pi)
+        tc = L / u0
+        steps = int(round(t_star * tc)) & ~1
+        log_every = max(2, int(tc * 0.1) & ~1)
+        out.append((n, u0, steps, log_every))
+    return out
+
+
+def ladder(gpu, count=32, seed=1234, precision="fp32", modes=("persistent", "sequential"),
+           t_star=5.0):
+    """32 periodic TGV instances of uneven size and Mach number, FP32 SRT,
+    Re = 1600, 5 convective times each, kinetic-energy traces every 0.1 t*;
+    wall time of the batched launch against instance-after-instance."""
+    inst = ladder_instances(count, seed, t_star=t_star)
+    results = {"instances": [{"n": n, "u0": u0, "steps": k, "log_every": le}
+                             for n, u0, k, le in inst],
+               "cell_updates": sum(n ** 3 * k for n, _, k, _ in inst)}
+    traces = {}
+    for mode in modes:
+        sims = []
+        for n, u0, k, le in inst:
+            L = n / (2.0 * math.pi)
+            wp, wm = sg.trtOmegas(3.0 * u0 * L / 1600.0 + 0.5, None)
+            s = sg.Simulation(gpu, precision=precision, nx=n, ny=n, nz=n, omega=wp, omegaMinus=wm)
+            s.initField(2, u0)
+            sims.append(s)
+        b = sg.Batch(gpu, sims, mode=mode)
+        t0 = time.perf_counter()
+        tr = b.run([k for _, _, k, _ in inst], [le for _, _, _, le in inst])
+        wall = time.perf_counter() - t0
+        results[mode] = {"wall_seconds": wall, "gpu_seconds": b.gpuSeconds, "path": b.lastPath,
+                         "glups": results["cell_updates"] / wall / 1e9,
+                         "digests": [s.stateDigest[:16] for s in sims]}
+        traces[mode] = tr
+        b.close()
+        for s in sims:
+            s.close()
+    if len(modes) >= 2:
+        a, b = modes[0], modes[1]
+        results["speedup"] = results[b]["wall_seconds"] / results[a]["wall_seconds"]
+        results["identical_states"] = results[a]["digests"] == results[b]["digests"]
+        results["max_trace_rel_diff"] = max(
+            float(np.max(np.abs(x - y) / np.maximum(np.abs(y), 1e-300)))
+            for x, y in zip(traces[a], traces[b]))
+    results["traces"] = {m: [list(map(float, t)) for t in traces[m]] for m in traces}
+    return results
+
+
+# ------------------------------------------------------------ adjoints
+def _dfg2_sim(gpu, D, uin_max, nz, precision, ramp, sponge_d=3, sponge_tau=1.0):
+    nx = 22 * D + 2
+    ny = int(4.1 * D) + 2
+    umean = uin_max * 2.0 / 3.0
+    wp, wm = sg.trtOmegas(3.0 * (umean * D / 100.0) + 0.5, 3.0 / 16.0)
+    cx = cy = 0.5 + 2.0 * D
+    flags = np.zeros((nz, ny, nx), np.uint8)
+    flags[:, 0, :] = flags[:, -1, :] = sg.Cell.solid
+    flags[:, 1:-1, 0] = flags[:, 1:-1, -1] = sg.Cell.inflow
+    s = sg.Simulation(gpu, precision=precision, nx=nx, ny=ny, nz=nz, omega=wp, omegaMinus=wm,
+                      uin=uin_max, rampSteps=ramp, wantsForces=True, flags=flags.reshape(-1))
+    eps = np.tile(sg.diskSolidFractions(nx, ny, cx, cy, D / 2.0), nz)
+    s.setSolidFractions(eps)
+    s.sponge = (float(nx - 1 - sponge_d * D), float(sponge_d * D), sponge_tau)
+    box = ((int(cx) - D // 2 - 3, int(cx) + D // 2 + 3), (int(cy) - D // 2 - 3, int(cy) + D // 2 + 3))
+    return s, eps, box, umean
+
+
+def dfg2_adjoint(gpu, D=64, uin_max=0.06, nz=3, total=200000, window=10000, checkpoints=20,
+                 fd_cells=8, fd_h=0.02, seed=7, precision="fp32", ramp=24000):
+    """Adjoint of the time-averaged C_D over the last `window` steps of the
+    cylinder run with respect to the solid-fraction field (20 checkpoints),
+    checked by central differences of the same FP32 forward on `fd_cells`
+    random boundary cells with 0 < eps < 1. Also times forward and backward."""
+    s, eps, box, umean = _dfg2_sim(gpu, D, uin_max, nz, precision, ramp)
+    s.run(total - window)
+    start = s.downloadState()
+    t_start = s.stepsDone
+    norm = 2.0 / (umean * umean * D * nz)  # C_D = norm * F_x
+    adj = sg.Adjoint(s, window, box, checkpoints=checkpoints)
+    t0 = time.perf_counter()
+    J = adj.forward()
+    t1 = time.perf_counter()
+    ge, _ = adj.backward()
+    t2 = time.perf_counter()
+    st = adj.stats()
+    adj.close()
+    rng = np.random.default_rng(seed)
+    cand = np.flatnonzero((eps > 0.05) & (eps < 0.95))
+    cells = rng.choice(cand, size=min(fd_cells, cand.size), replace=False)
+    fd = []
+    for n in cells:
+        vals = []
+        for sgn in (1.0, -1.0):
+            e = eps.copy()
+            e[n] = np.float32(e[n] + sgn * fd_h)
+            s.setSolidFractions(e)
+            s.uploadState(start)
+            s.stepsDone = t_start
+            a2 = sg.Adjoint(s, window, box, checkpoints=1)
+            vals.append(a2.forward())
+            a2.close()
+        h_eff = float(np.float32(eps[n] + fd_h)) - float(np.float32(eps[n] - fd_h))
+        fd.append({"cell": int(n), "eps": float(eps[n]), "adjoint": float(ge[n]) * norm,
+                   "fd": (vals[0] - vals[1]) / h_eff * norm})
+    s.setSolidFractions(eps)
+    fwd_step = st["forward_s"] / window
+    out = {"D": D, "window": window, "checkpoints": checkpoints, "mean_cd": J * norm,
+           "fd": fd, "forward_seconds": st["forward_s"], "recompute_seconds": st["recompute_s"],
+           "adjoint_seconds": st["adjoint_s"], "wall_forward": t1 - t0, "wall_backward": t2 - t1,
+           "adjoint_step_over_forward_step": st["adjoint_s"] / window / fwd_step,
+           "backward_over_forward": (st["recompute_s"] + st["adjoint_s"]) / st["forward_s"]}
+    s.close()
+    return out
+
+
+def sphere_adjoint(gpu, nx=512, ny=256, nz=256, D=48, u=0.05, re=300.0, cs=0.1, spinup=4000,
+                   window=2000, checkpoints=45, precision="fp16s"):
+    """Adjoint of the mean drag over `window` steps of the sphere wake with
+    respect to the Guo force field, sqrt(window) checkpoints: gradient
+    statistics and the forward / backward device time."""
+    nu = u * D / re
+    wp, _ = sg.trtOmegas(3.0 * nu + 0.5, None)
+    flags = np.zeros((nz, ny, nx), np.uint8)
+    flags[:, :, 0] = flags[:, :, -1] = sg.Cell.inflow
+    s = sg.Simulation(gpu, precision=precision, nx=nx, ny=ny, nz=nz, omega=wp, uin=u,
+                      rampSteps=min(8000, spinup), cSmago=cs * cs, wantsForces=True,
+                      flags=flags.reshape(-1))
+    s.inflowUniform = True
+    cx, cy, cz = 128.0, ny / 2.0, nz / 2.0
+    s.setSolidFractions(sg.sphereSolidFractions(nx, ny, nz, cx, cy, cz, D / 2.0, 8))
+    s.setForceField(np.zeros((3, nx * ny * nz), np.float32))
+    s.sponge = (float(nx - 1 - D), float(D), 1.0)
+    box = ((int(cx) - D // 2 - 3, int(cx) + D // 2 + 3), (int(cy) - D // 2 - 3, int(cy) + D // 2 + 3))
+    s.run(spinup)
+    adj = sg.Adjoint(s, window, box, checkpoints=checkpoints)
+    J = adj.forward()
+    _, gf = adj.backward()
+    st = adj.stats()
+    adj.close()
+    area = u * u * math.pi * D * D / 4.0
+    mag = np.sqrt((gf.astype(np.float64) ** 2).sum(0))
+    out = {"lattice": [nx, ny, nz], "window": window, "checkpoints": checkpoints,
+           "mean_cd": 2.0 * J / area, "grad_norm": float(np.linalg.norm(mag)),
+           "grad_max_cell": int(np.argmax(mag)), "grad_finite": bool(np.isfinite(gf).all()),
+           "forward_seconds": st["forward_s"], "recompute_seconds": st["recompute_s"],
+           "adjoint_seconds": st["adjoint_s"],
+           "adjoint_step_over_forward_step": st["adjoint_s"] / st["forward_s"],
+           "backward_over_forward": (st["recompute_s"] + st["adjoint_s"]) / st["forward_s"]}
+    s.close()
+    return out
+
+
+CASES = {"poiseuille": poiseuille, "tg_order": tg_order, "cavity": cavity, "dfg2": dfg2,
+         "dfg2_adjoint": dfg2_adjoint, "tgv": tgv, "sphere": sphere,
+         "sphere_adjoint": sphere_adjoint, "ladder": ladder}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("name", choices=sorted(CASES))
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--set", action="append", default=[],
+                    help="key=value overrides of the case function's arguments")
+    a = ap.parse_args(argv)
+    kw = {}
+    for item in a.set:
+        k, v = item.split("=", 1)
+        try:
+            kw[k] = json.loads(v)
+        except ValueError:
+            kw[k] = v
+    gpu = sg.GPU(0)
+    t0 = time.perf_counter()
+    res = CASES[a.name](gpu, **kw)
+    res["case"] = a.name
+    res["elapsed_seconds"] = time.perf_counter() - t0
+    text = json.dumps(res)
+    if a.out:
+        with open(a.out, "w") as fh:
+            fh.write(text)
+    summary = {k: v for k, v in res.items() if not isinstance(v, (list, dict))}
+    print(json.dumps(summary))
+    gpu.close()
+
+
+if __name__ == "__main__":
+    main()

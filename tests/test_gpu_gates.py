@@ -1,0 +1,90 @@
+"""Physics gates of the reference's suite (Sources/strouhal/Cases.swift) run
+through the C ABI on the GPU, and the precision study against the FP64 oracle.
+
+Thresholds are the reference's own: Poiseuille max relative error <= 3e-5
+(Cases.swift:313), Taylor-Green minimum observed order >= 1.9
+(Cases.swift:365), bitwise replay of an unsteady run (Cases.swift:989-999)."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _record(name, data):
+    """Keep measured values for the record when STRO_RESULTS_DIR is set."""
+    d = os.environ.get("STRO_RESULTS_DIR")
+    if d:
+        os.makedirs(d, exist_ok=True)
+        with open(os.path.join(d, name + ".json"), "w") as fh:
+            json.dump(data, fh)
+
+
+def test_poiseuille_exact(gpu):
+    from strouhal_gb300 import cases
+
+    r = cases.poiseuille(gpu, H=64)
+    _record("poiseuille", r)
+    assert r["max_err"] <= 3e-5, r
+
+
+def test_taylor_green_order(gpu):
+    from strouhal_gb300 import cases
+
+    r = cases.tg_order(gpu)
+    _record("tg_order", r)
+    assert r["min_order"] >= 1.9, r
+
+
+def test_unsteady_run_replays_bitwise(gpu):
+    """A short cylinder run with its probe schedule twice: identical digests."""
+    from strouhal_gb300 import cases
+
+    a = cases.dfg2(gpu, D=20, transient=2000, sample_cycles=1, stride=26, max_steps=3000)
+    b = cases.dfg2(gpu, D=20, transient=2000, sample_cycles=1, stride=26, max_steps=3000)
+    assert a["digest"] == b["digest"]
+    assert a["cd"] == b["cd"] and a["cl"] == b["cl"]
+
+
+def test_precision_per_observable(gpu, oracle):
+    """FP16-storage SRT and FP32-storage TRT against the FP64 oracle on a 48^3
+    Taylor-Green box over one convective time: relative error of the kinetic
+    energy and of the DDFs at every 20 steps."""
+    import strouhal_gb300 as sg
+
+    po = oracle
+    n, u0 = 48, 0.05
+    L = n / (2.0 * math.pi)
+    tau = 3.0 * u0 * L / 1600.0 + 0.5
+    steps = int(round(L / u0))
+    steps -= steps % 20
+    table = {"n": n, "u0": u0, "tau": tau, "steps": steps, "runs": []}
+    for precision, lam in (("fp16s", None), ("fp32", 3.0 / 16.0)):
+        wp, wm = sg.trtOmegas(tau, lam)
+        g = sg.Simulation(gpu, precision=precision, nx=n, ny=n, nz=n, omega=wp, omegaMinus=wm)
+        o = po.OracleSim(n, n, n, omega=wp, omegaMinus=wm, kind=po.KIND_F64, threads=16)
+        o.initField(2, u0)
+        g.uploadState(o.f.astype(np.float16 if precision == "fp16s" else np.float32))
+        rows = []
+        while True:
+            mo = o.probeMoments()
+            ke_o = float(np.sum(mo[:, 0] ** 2 + mo[:, 1] ** 2 + mo[:, 2] ** 2))
+            ke_g = g.kineticEnergySum()
+            ddf = float(np.linalg.norm(g.downloadState().astype(np.float64) - o.f) /
+                        np.linalg.norm(o.f))
+            rows.append({"step": g.stepsDone, "ke_rel": abs(ke_g - ke_o) / ke_o, "ddf_rel": ddf})
+            if g.stepsDone >= steps:
+                break
+            g.run(20)
+            o.run(20)
+        table["runs"].append({"precision": precision, "rows": rows})
+        g.close()
+        worst_ke = max(r["ke_rel"] for r in rows)
+        if precision == "fp32":
+            assert worst_ke < 1e-5 and rows[2]["ddf_rel"] < 1e-5, rows
+        else:
+            assert worst_ke < 5e-3 and rows[2]["ddf_rel"] < 2e-3, rows
+    _record("precision_tgv48", table)
