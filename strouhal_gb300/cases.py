@@ -312,8 +312,8 @@ def ladder_instances(count=32, seed=1234, edges=(32, 48, 64, 96, 128, 160),
     return out
 
 
-def ladder(gpu, count=32, seed=1234, precision="fp32", modes=("persistent", "sequential"),
-           t_star=5.0):
+def ladder(gpu, count=32, seed=1234, precision="fp32",
+           modes=("persistent", "rounds", "sequential"), t_star=5.0, tune=True):
     """32 periodic TGV instances of uneven size and Mach number, FP32 SRT,
     Re = 1600, 5 convective times each, kinetic-energy traces every 0.1 t*;
     wall time of the batched launch against instance-after-instance."""
@@ -331,23 +331,32 @@ def ladder(gpu, count=32, seed=1234, precision="fp32", modes=("persistent", "seq
             s.initField(2, u0)
             sims.append(s)
         b = sg.Batch(gpu, sims, mode=mode)
+        tuned = None
+        if tune and mode != "sequential":
+            chosen, bx, by, _ = b.autotune(rounds=40)  # tile shape (and mode), states restored
+            b.mode = mode
+            tuned = [bx, by]
         t0 = time.perf_counter()
         tr = b.run([k for _, _, k, _ in inst], [le for _, _, _, le in inst])
         wall = time.perf_counter() - t0
         results[mode] = {"wall_seconds": wall, "gpu_seconds": b.gpuSeconds, "path": b.lastPath,
+                         "tile": tuned,
                          "glups": results["cell_updates"] / wall / 1e9,
                          "digests": [s.stateDigest[:16] for s in sims]}
         traces[mode] = tr
         b.close()
         for s in sims:
             s.close()
-    if len(modes) >= 2:
-        a, b = modes[0], modes[1]
-        results["speedup"] = results[b]["wall_seconds"] / results[a]["wall_seconds"]
-        results["identical_states"] = results[a]["digests"] == results[b]["digests"]
-        results["max_trace_rel_diff"] = max(
-            float(np.max(np.abs(x - y) / np.maximum(np.abs(y), 1e-300)))
-            for x, y in zip(traces[a], traces[b]))
+    if "sequential" in modes:
+        seq = results["sequential"]["wall_seconds"]
+        for m in modes:
+            if m == "sequential":
+                continue
+            results[m]["speedup_vs_sequential"] = seq / results[m]["wall_seconds"]
+            results[m]["identical_states"] = results[m]["digests"] == results["sequential"]["digests"]
+            results[m]["max_trace_rel_diff"] = max(
+                float(np.max(np.abs(x - y) / np.maximum(np.abs(y), 1e-300)))
+                for x, y in zip(traces[m], traces["sequential"]))
     results["traces"] = {m: [list(map(float, t)) for t in traces[m]] for m in traces}
     return results
 
@@ -479,6 +488,8 @@ def main(argv=None):
     t0 = time.perf_counter()
     res = CASES[a.name](gpu, **kw)
     res["case"] = a.name
+    res["command"] = "python -m strouhal_gb300.cases " + " ".join(argv if argv is not None
+                                                                 else __import__("sys").argv[1:])
     res["elapsed_seconds"] = time.perf_counter() - t0
     text = json.dumps(res)
     if a.out:

@@ -7,7 +7,8 @@
 // backward sweep walks the segments last to first: it restores a segment's
 // checkpoint, recomputes the segment forward while keeping every input state
 // on the device, then runs the adjoint steps of the segment in reverse.
-// Memory: checkpoints + one segment of states + the FP32 adjoint array.
+// Memory: checkpoints + one segment of states (allocated by the first
+// backward sweep) + the FP32 adjoint array.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -92,7 +93,6 @@ int stro_adj_create(stro_sim* s, const double dir[3], const int32_t box[4], int6
     a->state_bytes = 19 * s->plane * s->esize;
     const uint64_t N = s->N;
     cudaError_t e = cudaMalloc(&a->d_check, a->state_bytes * size_t(a->ncheck));
-    if (e == cudaSuccess) e = cudaMalloc(&a->d_seg, a->state_bytes * size_t(a->seg));
     if (e == cudaSuccess) e = cudaMalloc(&a->d_lam, 19 * s->plane * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&a->d_geps, N * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&a->d_gf, 3 * N * sizeof(float));
@@ -186,6 +186,8 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
     cudaStream_t st = s->ctx->stream;
     const uint64_t N = s->N;
     const int half = s->precision == STRO_FP16S ? 1 : 0;
+    if (!a->d_seg)  // the segment of recomputed states is only needed by the reverse sweep
+        STRO_CUDA(cudaMalloc(&a->d_seg, a->state_bytes * size_t(a->seg)));
     const int geo = geo_on(s) ? 1 : 0;
     STRO_CUDA(cudaMemsetAsync(a->d_lam, 0, 19 * s->plane * sizeof(float), st));
     STRO_CUDA(cudaMemsetAsync(a->d_geps, 0, N * sizeof(float), st));
@@ -219,6 +221,7 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
             AdjArgs g{};
             g.a = step_args(s, t);
             g.a.f = state_at(a->d_seg, a->state_bytes, k);
+            g.a.ffield_plane = uint32_t(N);
             g.lam = a->d_lam;
             g.grad_eps = a->d_geps;
             g.grad_f = a->d_gf;

@@ -78,10 +78,10 @@ bool batch_geo(const stro_batch* b) {
         if (geo_on(s)) return true;
     return false;
 }
-bool batch_feat(const stro_batch* b) {
-    for (auto* s : b->sims)
-        if (feat_on(s)) return true;
-    return false;
+int batch_feat(const stro_batch* b) {
+    int level = 0;
+    for (auto* s : b->sims) level = std::max(level, feat_on(s));
+    return level;
 }
 
 // The reference's order: instance after instance, step after step.
@@ -120,7 +120,7 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
     const size_t n = b->sims.size();
     cudaStream_t st = b->ctx->stream;
     const int geo = batch_geo(b) ? 1 : 0;
-    const bool feat = batch_feat(b);
+    const int feat = batch_feat(b);
     if (geo)
         for (auto* s : b->sims) {
             const int rc = ensure_geometry(s);

@@ -49,7 +49,7 @@ __device__ __forceinline__ bool logs_at(const BatchInstance& I, int64_t r) {
     return I.log_every > 0 && r < I.steps && (r % I.log_every) == 0 && ((I.t0 + r) & 1) == 0;
 }
 
-template <typename S, int GEO, bool FEAT, bool CG>
+template <typename S, int GEO, int FEAT, bool CG>
 __device__ __forceinline__ void process_tile(const BatchArgs& b, const BatchInstance& I,
                                              uint32_t tile, int64_t r) {
     const uint32_t rem = tile - I.tile_begin;
@@ -129,7 +129,7 @@ __device__ bool grid_barrier(BatchCtl* ctl, unsigned& gen, long long spin_limit,
     return *((volatile int*)&ctl->error) == 0;
 }
 
-template <typename S, int GEO, bool FEAT>
+template <typename S, int GEO, int FEAT>
 __global__ void __launch_bounds__(256) k_batch_persistent(const BatchArgs b) {
     unsigned gen = 0;
     for (int64_t r = 0; r < b.max_steps; ++r) {
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(256) k_batch_persistent(const BatchArgs b) {
     if (blockIdx.x == 0 && b.max_steps > 0) fold_logs(b, b.max_steps - 1);
 }
 
-template <typename S, int GEO, bool FEAT>
+template <typename S, int GEO, int FEAT>
 __global__ void __launch_bounds__(256) k_batch_round(const BatchArgs b, int64_t r) {
     const uint32_t tile = blockIdx.x;
     const BatchInstance& I = b.inst[find_instance(b, tile)];
@@ -155,37 +155,42 @@ __global__ void __launch_bounds__(256) k_batch_fold(const BatchArgs b, int64_t r
     fold_logs(b, r);
 }
 
-template <typename S, int GEO, bool FEAT>
+template <typename S, int GEO, int FEAT>
 const void* persistent_fn() {
     return reinterpret_cast<const void*>(&k_batch_persistent<S, GEO, FEAT>);
 }
 
 template <typename S>
-const void* pick_persistent(int geo, bool feat) {
-    if (geo) return feat ? persistent_fn<S, 1, true>() : persistent_fn<S, 1, false>();
-    return feat ? persistent_fn<S, 0, true>() : persistent_fn<S, 0, false>();
+const void* pick_persistent(int geo, int feat) {
+    if (geo)
+        return feat == 2 ? persistent_fn<S, 1, 2>()
+                         : (feat == 1 ? persistent_fn<S, 1, 1>() : persistent_fn<S, 1, 0>());
+    return feat == 2 ? persistent_fn<S, 0, 2>()
+                     : (feat == 1 ? persistent_fn<S, 0, 1>() : persistent_fn<S, 0, 0>());
 }
 
 template <typename S>
-cudaError_t launch_round_typed(const BatchArgs& b, int geo, bool feat, int64_t r, uint32_t tiles,
+cudaError_t launch_round_typed(const BatchArgs& b, int geo, int feat, int64_t r, uint32_t tiles,
                                dim3 block, cudaStream_t st) {
     if (geo) {
-        if (feat) k_batch_round<S, 1, true><<<tiles, block, 0, st>>>(b, r);
-        else k_batch_round<S, 1, false><<<tiles, block, 0, st>>>(b, r);
+        if (feat == 2) k_batch_round<S, 1, 2><<<tiles, block, 0, st>>>(b, r);
+        else if (feat == 1) k_batch_round<S, 1, 1><<<tiles, block, 0, st>>>(b, r);
+        else k_batch_round<S, 1, 0><<<tiles, block, 0, st>>>(b, r);
     } else {
-        if (feat) k_batch_round<S, 0, true><<<tiles, block, 0, st>>>(b, r);
-        else k_batch_round<S, 0, false><<<tiles, block, 0, st>>>(b, r);
+        if (feat == 2) k_batch_round<S, 0, 2><<<tiles, block, 0, st>>>(b, r);
+        else if (feat == 1) k_batch_round<S, 0, 1><<<tiles, block, 0, st>>>(b, r);
+        else k_batch_round<S, 0, 0><<<tiles, block, 0, st>>>(b, r);
     }
     return cudaGetLastError();
 }
 
 }  // namespace
 
-const void* batch_persistent_kernel(int half_storage, int geo, bool feat) {
+const void* batch_persistent_kernel(int half_storage, int geo, int feat) {
     return half_storage ? pick_persistent<__half>(geo, feat) : pick_persistent<float>(geo, feat);
 }
 
-cudaError_t launch_batch_persistent(const BatchArgs& b, int half_storage, int geo, bool feat,
+cudaError_t launch_batch_persistent(const BatchArgs& b, int half_storage, int geo, int feat,
                                     unsigned grid, dim3 block, cudaStream_t st) {
     const void* fn = batch_persistent_kernel(half_storage, geo, feat);
     cudaLaunchConfig_t cfg = {};
@@ -202,7 +207,7 @@ cudaError_t launch_batch_persistent(const BatchArgs& b, int half_storage, int ge
     return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
-cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, bool feat, int64_t r,
+cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, int feat, int64_t r,
                                uint32_t tiles, dim3 block, cudaStream_t st) {
     if (tiles == 0) return cudaSuccess;
     return half_storage ? launch_round_typed<__half>(b, geo, feat, r, tiles, block, st)
@@ -214,7 +219,7 @@ cudaError_t launch_batch_fold(const BatchArgs& b, int64_t r, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-int batch_persistent_blocks_per_sm(int half_storage, int geo, bool feat, dim3 block) {
+int batch_persistent_blocks_per_sm(int half_storage, int geo, int feat, dim3 block) {
     int n = 0;
     const void* fn = batch_persistent_kernel(half_storage, geo, feat);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, int(block.x * block.y * block.z), 0) !=

@@ -42,11 +42,11 @@ struct BatchArgs {
     long long spin_limit;       // polls before a barrier wait gives up
 };
 
-cudaError_t launch_batch_persistent(const BatchArgs& b, int half_storage, int geo, bool feat,
+cudaError_t launch_batch_persistent(const BatchArgs& b, int half_storage, int geo, int feat,
                                     unsigned grid, dim3 block, cudaStream_t st);
-cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, bool feat, int64_t r,
+cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, int feat, int64_t r,
                                uint32_t tiles, dim3 block, cudaStream_t st);
 cudaError_t launch_batch_fold(const BatchArgs& b, int64_t r, cudaStream_t st);
-int batch_persistent_blocks_per_sm(int half_storage, int geo, bool feat, dim3 block);
+int batch_persistent_blocks_per_sm(int half_storage, int geo, int feat, dim3 block);
 
 }  // namespace stro

@@ -113,7 +113,7 @@ __device__ __forceinline__ void relax(float (&fh)[19], float wp, float wm, float
 }
 
 // Collision, Kernels.metal:105-228.
-template <bool FEAT>
+template <int FEAT>
 __device__ __forceinline__ void collide(float (&fh)[19], const StepArgs& a, int x, float eps,
                                         float Fx, float Fy, float Fz, float& ntx, float& nty,
                                         float& ntz) {
@@ -165,7 +165,7 @@ __device__ __forceinline__ void collide(float (&fh)[19], const StepArgs& a, int 
     }
     const float u2 = ux * ux + uy * uy + uz * uz;
 
-    if constexpr (FEAT) {
+    if constexpr (FEAT == 2) {
         if (a.c_smago > 0.0f) {  // Smagorinsky LES, Kernels.metal:140-167
             float pxx = 0.f, pyy = 0.f, pzz = 0.f, pxy = 0.f, pxz = 0.f, pyz = 0.f;
             sfor<1, 19>([&](auto I) {
@@ -199,6 +199,8 @@ __device__ __forceinline__ void collide(float (&fh)[19], const StepArgs& a, int 
                 wm = 1.0f / (0.5f + lambda / (tauEff - 0.5f));
             }
         }
+    }
+    if constexpr (FEAT) {
         if (eps == 0.0f) {
             if (a.force_on) relax<true, false>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, Fx, Fy, Fz, eps, ntx, nty, ntz);
             else relax<false, false>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, Fx, Fy, Fz, eps, ntx, nty, ntz);
@@ -211,7 +213,7 @@ __device__ __forceinline__ void collide(float (&fh)[19], const StepArgs& a, int 
     }
 }
 
-template <bool FEAT>
+template <int FEAT>
 __device__ __forceinline__ void cell_force(const StepArgs& a, uint32_t n, float& Fx, float& Fy,
                                            float& Fz) {
     Fx = a.fx; Fy = a.fy; Fz = a.fz;
@@ -360,7 +362,7 @@ __device__ __forceinline__ float cell_u2(const float (&fh)[19], float Fx, float 
 
 // Even (in-cell) pass of one cell, Kernels.metal:252-260. Non-fluid cells are
 // skipped. With LOG, u2 receives |u|^2 of the state before the step.
-template <typename S, int GEO, bool FEAT, bool LOG = false, bool CG = false>
+template <typename S, int GEO, int FEAT, bool LOG = false, bool CG = false>
 __device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z,
                                           float* u2 = nullptr) {
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
@@ -388,7 +390,7 @@ __device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z
 // Odd (streaming) pass of one cell with halfway / moving-wall bounce-back,
 // Kernels.metal:261-354. With PROBE the cell's momentum-exchange force is
 // returned in contrib when the cell is a boundary cell inside the probe box.
-template <typename S, int GEO, bool FEAT, bool PROBE, bool CG = false>
+template <typename S, int GEO, int FEAT, bool PROBE, bool CG = false>
 __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, int x, int y,
                                          int z, double (&contrib)[3]) {
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);

@@ -10,20 +10,20 @@ namespace stro {
 
 // One AA pass over the lattice. block.x * block.y must be a multiple of 32
 // and at most 256; the grid is (ceil(nx/bx), ceil(ny/by), nz).
-cudaError_t launch_step(const StepArgs& a, int half_storage, int parity, int geo, bool feat,
+cudaError_t launch_step(const StepArgs& a, int half_storage, int parity, int geo, int feat,
                         bool probe, dim3 block, cudaStream_t st);
 dim3 step_grid(const StepArgs& a, dim3 block);
 
 // FP16 periodic step with x-adjacent cell pairs per thread (lbm_pair.cu).
 // block.x threads cover 2*block.x cells of a row.
 bool pair_step_supported(int half_storage, int geo, bool probe, int nx, uint64_t plane, dim3 block);
-cudaError_t launch_pair_step(const StepArgs& a, int parity, bool feat, dim3 block, cudaStream_t st);
+cudaError_t launch_pair_step(const StepArgs& a, int parity, int feat, dim3 block, cudaStream_t st);
 
 // Row-streaming step (lbm_rows.cu): bulk-copy staging of whole rows in shared
 // memory, `threads` per block, persistent over rows. `error` receives 1 if a
 // bounded wait gave up.
 bool rows_step_supported(int half_storage, int geo, bool probe, int nx, int threads);
-cudaError_t launch_rows_step(const StepArgs& a, int half_storage, int parity, bool feat,
+cudaError_t launch_rows_step(const StepArgs& a, int half_storage, int parity, int feat,
                              int threads, int sm_count, int* error, cudaStream_t st);
 
 // Fields and reductions (lbm_probe.cu). `plane` is the DDF plane stride in

@@ -32,7 +32,7 @@ __device__ __forceinline__ int wrap_x(int v, int nx) {
     return v;
 }
 
-template <bool FEAT>
+template <int FEAT>
 __global__ void __launch_bounds__(256, 2) k_pair_even(const StepArgs a) {
     const int x = 2 * int(blockIdx.x * blockDim.x + threadIdx.x);
     const int y = int(blockIdx.y * blockDim.y + threadIdx.y);
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256, 2) k_pair_even(const StepArgs a) {
     sfor<1, 19>([&](auto I) { f2[uint64_t(opp(I)) * P2 + n2] = __floats2half2_rn(A[I], B[I]); });
 }
 
-template <bool FEAT>
+template <int FEAT>
 __global__ void __launch_bounds__(256, 2) k_pair_odd(const StepArgs a) {
     const int lane = int(threadIdx.x & 31u);
     const int x = 2 * int(blockIdx.x * blockDim.x + threadIdx.x);
@@ -145,15 +145,17 @@ bool pair_step_supported(int half_storage, int geo, bool probe, int nx, uint64_t
            (nx / 2) % int(block.x) == 0 && block.x * block.y <= 256;
 }
 
-cudaError_t launch_pair_step(const StepArgs& a, int parity, bool feat, dim3 block, cudaStream_t st) {
+cudaError_t launch_pair_step(const StepArgs& a, int parity, int feat, dim3 block, cudaStream_t st) {
     const dim3 grid(unsigned(a.nx / 2) / block.x, (unsigned(a.ny) + block.y - 1) / block.y,
                     unsigned(a.nz));
     if (parity == 0) {
-        if (feat) k_pair_even<true><<<grid, block, 0, st>>>(a);
-        else k_pair_even<false><<<grid, block, 0, st>>>(a);
+        if (feat == 2) k_pair_even<2><<<grid, block, 0, st>>>(a);
+        else if (feat == 1) k_pair_even<1><<<grid, block, 0, st>>>(a);
+        else k_pair_even<0><<<grid, block, 0, st>>>(a);
     } else {
-        if (feat) k_pair_odd<true><<<grid, block, 0, st>>>(a);
-        else k_pair_odd<false><<<grid, block, 0, st>>>(a);
+        if (feat == 2) k_pair_odd<2><<<grid, block, 0, st>>>(a);
+        else if (feat == 1) k_pair_odd<1><<<grid, block, 0, st>>>(a);
+        else k_pair_odd<0><<<grid, block, 0, st>>>(a);
     }
     return cudaGetLastError();
 }

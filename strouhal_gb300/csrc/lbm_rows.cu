@@ -107,7 +107,7 @@ __device__ __forceinline__ void issue_row(const StepArgs& a, uint32_t row, S* bu
     });
 }
 
-template <typename S, int PARITY, bool FEAT, int NSTAGE>
+template <typename S, int PARITY, int FEAT, int NSTAGE>
 __global__ void __launch_bounds__(256) k_rows(const StepArgs a, int* error) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t nx = uint32_t(a.nx), ny = uint32_t(a.ny), nz = uint32_t(a.nz);
@@ -216,15 +216,16 @@ size_t rows_smem(int nx) {
     return kStages * stage_bytes + kStages * sizeof(uint64_t);
 }
 
-template <typename S, int PARITY, bool FEAT>
+template <typename S, int PARITY, int FEAT>
 const void* rows_fn() {
     return reinterpret_cast<const void*>(&k_rows<S, PARITY, FEAT, kStages>);
 }
 
 template <typename S>
-const void* pick(int parity, bool feat) {
-    if (parity == 0) return feat ? rows_fn<S, 0, true>() : rows_fn<S, 0, false>();
-    return feat ? rows_fn<S, 1, true>() : rows_fn<S, 1, false>();
+const void* pick(int parity, int feat) {
+    if (parity == 0)
+        return feat == 2 ? rows_fn<S, 0, 2>() : (feat == 1 ? rows_fn<S, 0, 1>() : rows_fn<S, 0, 0>());
+    return feat == 2 ? rows_fn<S, 1, 2>() : (feat == 1 ? rows_fn<S, 1, 1>() : rows_fn<S, 1, 0>());
 }
 
 }  // namespace
@@ -264,7 +265,7 @@ int rows_blocks_per_sm(const void* fn, int threads, size_t smem, cudaError_t* er
     return per_sm;
 }
 
-cudaError_t launch_rows_step(const StepArgs& a, int half_storage, int parity, bool feat,
+cudaError_t launch_rows_step(const StepArgs& a, int half_storage, int parity, int feat,
                              int threads, int sm_count, int* error, cudaStream_t st) {
     const void* fn = half_storage ? pick<__half>(parity, feat) : pick<float>(parity, feat);
     const size_t smem = half_storage ? rows_smem<__half>(a.nx) : rows_smem<float>(a.nx);

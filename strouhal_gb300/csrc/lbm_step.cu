@@ -27,7 +27,7 @@
 namespace stro {
 
 // ---------------------------------------------------------------- kernels
-template <typename S, int GEO, bool FEAT>
+template <typename S, int GEO, int FEAT>
 __global__ void __launch_bounds__(256) k_step_even(const StepArgs a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(256) k_step_even(const StepArgs a) {
     even_cell<S, GEO, FEAT>(a, x, y, blockIdx.z);
 }
 
-template <typename S, int GEO, bool FEAT, bool PROBE>
+template <typename S, int GEO, int FEAT, bool PROBE>
 __global__ void __launch_bounds__(256) k_step_odd(const StepArgs a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -52,34 +52,32 @@ __global__ void __launch_bounds__(256) k_step_odd(const StepArgs a) {
 }
 
 // ----------------------------------------------------------------- launcher
-template <typename S>
-static cudaError_t launch_typed(const StepArgs& a, int parity, int geo, bool feat, bool probe,
-                                dim3 grid, dim3 block, cudaStream_t st) {
+template <typename S, int FEAT>
+static void launch_level(const StepArgs& a, int parity, int geo, bool probe, dim3 grid, dim3 block,
+                         cudaStream_t st) {
     if (parity == 0) {
-        if (geo) {
-            if (feat) k_step_even<S, 1, true><<<grid, block, 0, st>>>(a);
-            else k_step_even<S, 1, false><<<grid, block, 0, st>>>(a);
-        } else {
-            if (feat) k_step_even<S, 0, true><<<grid, block, 0, st>>>(a);
-            else k_step_even<S, 0, false><<<grid, block, 0, st>>>(a);
-        }
+        if (geo) k_step_even<S, 1, FEAT><<<grid, block, 0, st>>>(a);
+        else k_step_even<S, 0, FEAT><<<grid, block, 0, st>>>(a);
+    } else if (probe) {
+        k_step_odd<S, 1, FEAT, true><<<grid, block, 0, st>>>(a);
+    } else if (geo) {
+        k_step_odd<S, 1, FEAT, false><<<grid, block, 0, st>>>(a);
     } else {
-        if (probe) {
-            if (!geo) return cudaErrorInvalidValue;
-            if (feat) k_step_odd<S, 1, true, true><<<grid, block, 0, st>>>(a);
-            else k_step_odd<S, 1, false, true><<<grid, block, 0, st>>>(a);
-        } else if (geo) {
-            if (feat) k_step_odd<S, 1, true, false><<<grid, block, 0, st>>>(a);
-            else k_step_odd<S, 1, false, false><<<grid, block, 0, st>>>(a);
-        } else {
-            if (feat) k_step_odd<S, 0, true, false><<<grid, block, 0, st>>>(a);
-            else k_step_odd<S, 0, false, false><<<grid, block, 0, st>>>(a);
-        }
+        k_step_odd<S, 0, FEAT, false><<<grid, block, 0, st>>>(a);
     }
+}
+
+template <typename S>
+static cudaError_t launch_typed(const StepArgs& a, int parity, int geo, int feat, bool probe,
+                                dim3 grid, dim3 block, cudaStream_t st) {
+    if (probe && (parity == 0 || !geo)) return cudaErrorInvalidValue;
+    if (feat == 2) launch_level<S, 2>(a, parity, geo, probe, grid, block, st);
+    else if (feat == 1) launch_level<S, 1>(a, parity, geo, probe, grid, block, st);
+    else launch_level<S, 0>(a, parity, geo, probe, grid, block, st);
     return cudaGetLastError();
 }
 
-cudaError_t launch_step(const StepArgs& a, int half_storage, int parity, int geo, bool feat,
+cudaError_t launch_step(const StepArgs& a, int half_storage, int parity, int geo, int feat,
                         bool probe, dim3 block, cudaStream_t st) {
     const dim3 grid((a.nx + block.x - 1) / block.x, (a.ny + block.y - 1) / block.y, a.nz);
     if (half_storage) return launch_typed<__half>(a, parity, geo, feat, probe, grid, block, st);

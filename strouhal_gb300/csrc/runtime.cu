@@ -59,10 +59,12 @@ bool sponge_active(const stro_sim* s) {
     return s->sponge_on && s->sponge_x0 < float(s->nx - 1);
 }
 bool force_on(const stro_sim* s) {
-    return s->has_ffield || s->force[0] != 0.0f || s->force[1] != 0.0f || s->force[2] != 0.0f;
+    return (s->has_ffield && s->ffield_nonzero) || s->force[0] != 0.0f || s->force[1] != 0.0f ||
+           s->force[2] != 0.0f;
 }
-bool feat_on(const stro_sim* s) {
-    return s->has_eps || s->c_smago > 0.0f || sponge_active(s) || force_on(s);
+int feat_on(const stro_sim* s) {
+    if (s->c_smago > 0.0f) return 2;  // features with the Smagorinsky block compiled in
+    return (s->has_eps || sponge_active(s) || force_on(s)) ? 1 : 0;
 }
 
 dim3 default_block(int nx) {
@@ -90,7 +92,7 @@ StepArgs step_args(const stro_sim* s, int64_t t) {
     a.geo = s->d_geo;
     a.lmask = s->d_lmask;
     a.eps = s->d_eps;
-    a.ffield = s->has_ffield ? s->d_ffield : nullptr;
+    a.ffield = (s->has_ffield && s->ffield_nonzero) ? s->d_ffield : nullptr;
     a.ffield_plane = uint32_t(s->N);
     a.omega = s->omega;
     a.omega_minus = s->omega_minus;
@@ -485,6 +487,10 @@ int stro_sim_set_force_field(stro_sim* s, const float* fxyz) {
                               s->ctx->stream));
     STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
     s->has_ffield = true;
+    // An all-zero field adds exact zeros to the uniform force: the step skips the
+    // field (and, with no uniform force, the Guo terms), with identical results.
+    s->ffield_nonzero = false;
+    for (uint64_t k = 0; k < 3 * s->N && !s->ffield_nonzero; ++k) s->ffield_nonzero = fxyz[k] != 0.0f;
     return STRO_OK;
 }
 

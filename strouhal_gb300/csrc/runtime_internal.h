@@ -44,6 +44,7 @@ struct stro_sim {
     std::vector<uint32_t> smask, lmask;
     std::vector<float> eps;
     bool any_wall = false, has_eps = false, has_ffield = false;
+    bool ffield_nonzero = false;  // a zero field leaves the step's arithmetic unchanged
     bool force_geometry = false;  // device geometry kept even for an all-fluid lattice
     // device buffers
     void* d_f = nullptr;
@@ -75,7 +76,8 @@ namespace rt {
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
 bool geo_on(const stro_sim* s);
-bool feat_on(const stro_sim* s);
+// Feature level of the step kernels: 0 lean, 1 sponge / force / NT, 2 also LES.
+int feat_on(const stro_sim* s);
 float ramp_factor(const stro_sim* s, int64_t t);
 StepArgs step_args(const stro_sim* s, int64_t t);
 FieldView field_view(const stro_sim* s);
