@@ -146,10 +146,17 @@ int stro_sim_get_block(stro_sim* sim, int32_t* bx, int32_t* by);
  * two x-adjacent cells per thread with half2 accesses (periodic lattices,
  * nx a multiple of 64); 2 = row streaming: whole rows staged in shared memory
  * by bulk copies ahead of the compute (periodic lattices, nx*element size a
- * multiple of 16). A lattice a variant does not apply to runs variant 0.
+ * multiple of 16); 3 = one cell per thread with registers capped at 64 for
+ * more warps in flight (periodic lattices, blocks of at most 128 threads).
+ * A lattice a variant does not apply to runs variant 0.
  * Results are identical for every variant. */
 int stro_sim_set_variant(stro_sim* sim, int32_t variant);
 int stro_sim_get_variant(stro_sim* sim, int32_t* variant);
+/* Walled lattices run their bulk blocks (cells with no wall neighbour and no
+ * solid fraction) with the wall-free kernels and only the boundary blocks
+ * with the wall-aware ones (default on); 0 runs the wall-aware kernels on
+ * every block. Results are identical either way. */
+int stro_sim_set_block_split(stro_sim* sim, int32_t enabled);
 /* Autotuner: times `steps` steps per candidate variant and launch shape on the current
  * state (saved and restored, stepsDone unchanged) and keeps the fastest. */
 int stro_sim_autotune(stro_sim* sim, int64_t steps, int32_t* bx, int32_t* by, double* glups);

@@ -100,6 +100,7 @@ def lib():
         "stro_sim_mass": ([_P, ctypes.POINTER(c_double)], c_int),
         "stro_sim_check_finite": ([_P, ctypes.POINTER(c_int)], c_int),
         "stro_sim_set_variant": ([_P, ctypes.c_int32], c_int),
+        "stro_sim_set_block_split": ([_P, ctypes.c_int32], c_int),
         "stro_sim_get_variant": ([_P, ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_set_block": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
         "stro_sim_get_block": ([_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)], c_int),
@@ -451,6 +452,10 @@ class Simulation:
     @variant.setter
     def variant(self, v):
         _check(lib().stro_sim_set_variant(self._h, int(v)))
+
+    def setBlockSplit(self, enabled):
+        """Bulk blocks of a walled lattice on the wall-free kernels (default True)."""
+        _check(lib().stro_sim_set_block_split(self._h, int(bool(enabled))))
 
     def autotune(self, steps=20):
         """Pick the fastest kernel variant and launch shape (state restored); returns (bx, by, GLUPS)."""

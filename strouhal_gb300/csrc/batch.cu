@@ -282,7 +282,7 @@ int tune_sim_shape(stro_sim* s, int64_t steps, int variant, dim3 cand, double* s
     s->variant = variant;
     if (variant == 1) s->pair_block = cand;
     else if (variant == 2) s->rows_threads = int(cand.x * cand.y);
-    else s->block = cand;
+    else s->block = cand;  // variants 0 and 3
     const int64_t t0 = s->steps_done;
     const double g0 = s->gpu_seconds;
     // warm-up pair, then the timed steps
@@ -462,8 +462,14 @@ int stro_sim_set_block(stro_sim* s, int32_t bx, int32_t by) {
 
 int stro_sim_set_variant(stro_sim* s, int32_t variant) {
     if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
-    if (variant < 0 || variant > 2) return fail(STRO_ERR_INVALID, "variant must be 0, 1 or 2");
+    if (variant < 0 || variant > 3) return fail(STRO_ERR_INVALID, "variant must be 0..3");
     s->variant = variant;
+    return STRO_OK;
+}
+
+int stro_sim_set_block_split(stro_sim* s, int32_t enabled) {
+    if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
+    s->split = enabled != 0;
     return STRO_OK;
 }
 
@@ -495,10 +501,17 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
     int best_variant = 0;
     int rc = e == cudaSuccess ? STRO_OK : cuda_fail(e, "autotune save");
     const int half = s->precision == STRO_FP16S ? 1 : 0;
-    for (int variant : {0, 1, 2}) {
+    const bool saved_split = s->split;
+    bool best_split = saved_split;
+    for (int split : {1, 0}) {
+    if (!split && !geo_on(s)) break;  // the split only exists for walled lattices
+    s->split = split != 0;
+    for (int variant : {0, 1, 2, 3}) {
         for (const dim3& c : kShapes) {
             if (rc != STRO_OK) break;
-            if (variant == 0 && c.x > 32 && int(c.x) > ((s->nx + 31) / 32) * 32) continue;
+            if ((variant == 0 || variant == 3) && c.x > 32 && int(c.x) > ((s->nx + 31) / 32) * 32)
+                continue;
+            if (variant == 3 && (geo_on(s) || c.x * c.y > 128)) continue;
             if (variant == 1 && !pair_step_supported(half, geo_on(s) ? 1 : 0, false, s->nx,
                                                      s->plane, c))
                 continue;
@@ -512,9 +525,12 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
                 best = sec;
                 best_shape = c;
                 best_variant = variant;
+                best_split = s->split;
             }
         }
     }
+    }
+    s->split = best_split;
     e = cudaMemcpyAsync(s->d_f, saved, bytes, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     cudaFree(saved);

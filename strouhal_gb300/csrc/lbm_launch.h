@@ -14,6 +14,19 @@ cudaError_t launch_step(const StepArgs& a, int half_storage, int parity, int geo
                         bool probe, dim3 block, cudaStream_t st);
 dim3 step_grid(const StepArgs& a, dim3 block);
 
+// Register-capped one-cell kernels for periodic lattices (block <= 128 threads).
+cudaError_t launch_step_capped(const StepArgs& a, int half_storage, int parity, int feat,
+                               dim3 block, cudaStream_t st);
+
+// One pass split over two block lists of the (bx,by) grid: `bulk` blocks
+// (every cell fluid, no wall neighbour, no solid fraction) run the wall-free
+// kernels at feature level feat_bulk, `edge` blocks the wall-aware kernels at
+// feat_edge. Each cell touches only its own slots, so the two launches are
+// independent.
+cudaError_t launch_step_split(const StepArgs& a, int half_storage, int parity, int feat_bulk,
+                              int feat_edge, dim3 block, const uint32_t* bulk, uint32_t nbulk,
+                              const uint32_t* edge, uint32_t nedge, cudaStream_t st);
+
 // FP16 periodic step with x-adjacent cell pairs per thread (lbm_pair.cu).
 // block.x threads cover 2*block.x cells of a row.
 bool pair_step_supported(int half_storage, int geo, bool probe, int nx, uint64_t plane, dim3 block);

@@ -51,6 +51,111 @@ __global__ void __launch_bounds__(256) k_step_odd(const StepArgs a) {
     }
 }
 
+// Register-capped periodic kernels (64 registers, up to 8 blocks of 128 per
+// SM): more warps in flight for the latency-bound FP16 case, at the price of
+// a few spilled bytes. Same per-cell code.
+template <typename S, int FEAT>
+__global__ void __launch_bounds__(128, 8) k_step_even_capped(const StepArgs a) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= a.nx || y >= a.ny) return;
+    even_cell<S, 0, FEAT>(a, x, y, blockIdx.z);
+}
+
+template <typename S, int FEAT>
+__global__ void __launch_bounds__(128, 8) k_step_odd_capped(const StepArgs a) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= a.nx || y >= a.ny) return;
+    double contrib[3];
+    odd_cell<S, 0, FEAT, false>(a, WallVel(a), x, y, blockIdx.z, contrib);
+}
+
+template <typename S, int FEAT>
+static void launch_capped_level(const StepArgs& a, int parity, dim3 grid, dim3 block,
+                                cudaStream_t st) {
+    if (parity == 0) k_step_even_capped<S, FEAT><<<grid, block, 0, st>>>(a);
+    else k_step_odd_capped<S, FEAT><<<grid, block, 0, st>>>(a);
+}
+
+cudaError_t launch_step_capped(const StepArgs& a, int half_storage, int parity, int feat,
+                               dim3 block, cudaStream_t st) {
+    if (block.x * block.y > 128) return cudaErrorInvalidValue;
+    const dim3 grid((a.nx + block.x - 1) / block.x, (a.ny + block.y - 1) / block.y, a.nz);
+    if (half_storage) {
+        if (feat == 2) launch_capped_level<__half, 2>(a, parity, grid, block, st);
+        else if (feat == 1) launch_capped_level<__half, 1>(a, parity, grid, block, st);
+        else launch_capped_level<__half, 0>(a, parity, grid, block, st);
+    } else {
+        if (feat == 2) launch_capped_level<float, 2>(a, parity, grid, block, st);
+        else if (feat == 1) launch_capped_level<float, 1>(a, parity, grid, block, st);
+        else launch_capped_level<float, 0>(a, parity, grid, block, st);
+    }
+    return cudaGetLastError();
+}
+
+// Block-list launches: block i of the grid processes lattice block list[i]
+// (linear index bx + gx * (by + gy * bz)). Used to run the bulk of a walled
+// lattice with the wall-free kernels and only its boundary blocks with the
+// wall-aware ones.
+__device__ __forceinline__ void list_block(const uint32_t* list, uint32_t gx, uint32_t gy,
+                                           int& x, int& y, int& z) {
+    const uint32_t blk = list[blockIdx.x];
+    const uint32_t t = blk / gx;
+    x = int((blk - t * gx) * blockDim.x + threadIdx.x);
+    y = int((t % gy) * blockDim.y + threadIdx.y);
+    z = int(t / gy);
+}
+
+template <typename S, int GEO, int FEAT>
+__global__ void __launch_bounds__(256) k_list_even(const StepArgs a, const uint32_t* list,
+                                                   uint32_t gx, uint32_t gy) {
+    int x, y, z;
+    list_block(list, gx, gy, x, y, z);
+    if (x >= a.nx || y >= a.ny) return;
+    even_cell<S, GEO, FEAT>(a, x, y, z);
+}
+
+template <typename S, int GEO, int FEAT>
+__global__ void __launch_bounds__(256) k_list_odd(const StepArgs a, const uint32_t* list,
+                                                  uint32_t gx, uint32_t gy) {
+    int x, y, z;
+    list_block(list, gx, gy, x, y, z);
+    if (x >= a.nx || y >= a.ny) return;
+    double contrib[3];
+    odd_cell<S, GEO, FEAT, false>(a, WallVel(a), x, y, z, contrib);
+}
+
+template <typename S, int GEO, int FEAT>
+static void launch_list(const StepArgs& a, int parity, const uint32_t* list, uint32_t count,
+                        dim3 block, cudaStream_t st) {
+    if (count == 0) return;
+    const uint32_t gx = (a.nx + block.x - 1) / block.x, gy = (a.ny + block.y - 1) / block.y;
+    if (parity == 0) k_list_even<S, GEO, FEAT><<<count, block, 0, st>>>(a, list, gx, gy);
+    else k_list_odd<S, GEO, FEAT><<<count, block, 0, st>>>(a, list, gx, gy);
+}
+
+template <typename S, int GEO>
+static void launch_list_level(const StepArgs& a, int parity, int feat, const uint32_t* list,
+                              uint32_t count, dim3 block, cudaStream_t st) {
+    if (feat == 2) launch_list<S, GEO, 2>(a, parity, list, count, block, st);
+    else if (feat == 1) launch_list<S, GEO, 1>(a, parity, list, count, block, st);
+    else launch_list<S, GEO, 0>(a, parity, list, count, block, st);
+}
+
+cudaError_t launch_step_split(const StepArgs& a, int half_storage, int parity, int feat_bulk,
+                              int feat_edge, dim3 block, const uint32_t* bulk, uint32_t nbulk,
+                              const uint32_t* edge, uint32_t nedge, cudaStream_t st) {
+    if (half_storage) {
+        launch_list_level<__half, 0>(a, parity, feat_bulk, bulk, nbulk, block, st);
+        launch_list_level<__half, 1>(a, parity, feat_edge, edge, nedge, block, st);
+    } else {
+        launch_list_level<float, 0>(a, parity, feat_bulk, bulk, nbulk, block, st);
+        launch_list_level<float, 1>(a, parity, feat_edge, edge, nedge, block, st);
+    }
+    return cudaGetLastError();
+}
+
 // ----------------------------------------------------------------- launcher
 template <typename S, int FEAT>
 static void launch_level(const StepArgs& a, int parity, int geo, bool probe, dim3 grid, dim3 block,

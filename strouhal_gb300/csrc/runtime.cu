@@ -175,6 +175,9 @@ int upload_geometry(stro_sim* s) {
     STRO_CUDA(cudaMemcpyAsync(s->d_geo, geo.data(), N * 4, cudaMemcpyHostToDevice, st));
     STRO_CUDA(cudaMemcpyAsync(s->d_lmask, s->lmask.data(), N * 4, cudaMemcpyHostToDevice, st));
     STRO_CUDA(cudaStreamSynchronize(st));
+    s->cell_host.swap(cell);
+    s->geo_host.swap(geo);
+    ++s->geo_version;
     return STRO_OK;
 }
 
@@ -189,6 +192,7 @@ void free_sim(stro_sim* s) {
     cudaFree(s->d_partials);
     cudaFree(s->d_out);
     cudaFree(s->d_error);
+    cudaFree(s->d_blocks);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
 }
@@ -238,11 +242,63 @@ int ensure_partials(stro_sim* s, size_t doubles) {
     return STRO_OK;
 }
 
+// Bulk / boundary block lists for the current block shape (rebuilt when the
+// shape or the geometry changes). A block is bulk when every cell it covers is
+// fluid with no wall neighbour, no moving wall nearby and no solid fraction.
+static int ensure_block_lists(stro_sim* s) {
+    if (s->lists_version == s->geo_version && s->lists_block.x == s->block.x &&
+        s->lists_block.y == s->block.y)
+        return STRO_OK;
+    const uint32_t bx = s->block.x, by = s->block.y;
+    const uint32_t gx = (uint32_t(s->nx) + bx - 1) / bx, gy = (uint32_t(s->ny) + by - 1) / by;
+    const uint64_t nblocks = uint64_t(gx) * gy * uint64_t(s->nz);
+    std::vector<uint32_t> bulk, edge;
+    bulk.reserve(nblocks);
+    for (uint64_t b = 0; b < nblocks; ++b) {
+        const uint32_t bxi = uint32_t(b % gx), t = uint32_t(b / gx), byi = t % gy, z = t / gy;
+        bool is_bulk = true;
+        for (uint32_t yy = byi * by; yy < std::min<uint32_t>((byi + 1) * by, s->ny) && is_bulk; ++yy) {
+            const uint64_t row = (uint64_t(z) * s->ny + yy) * s->nx;
+            for (uint32_t xx = bxi * bx; xx < std::min<uint32_t>((bxi + 1) * bx, s->nx); ++xx)
+                if (s->cell_host[row + xx] != 0 || s->geo_host[row + xx] != 0) {
+                    is_bulk = false;
+                    break;
+                }
+        }
+        (is_bulk ? bulk : edge).push_back(uint32_t(b));
+    }
+    cudaFree(s->d_blocks);
+    s->d_blocks = nullptr;
+    STRO_CUDA(cudaMalloc(&s->d_blocks, std::max<size_t>(nblocks, 1) * sizeof(uint32_t)));
+    bulk.insert(bulk.end(), edge.begin(), edge.end());
+    STRO_CUDA(cudaMemcpy(s->d_blocks, bulk.data(), nblocks * sizeof(uint32_t),
+                         cudaMemcpyHostToDevice));
+    s->nbulk = uint32_t(nblocks - edge.size());
+    s->nedge = uint32_t(edge.size());
+    s->lists_block = s->block;
+    s->lists_version = s->geo_version;
+    return STRO_OK;
+}
+
+// Feature level of wall-free cells (no solid fraction among them).
+static int bulk_feat(const stro_sim* s) {
+    if (s->c_smago > 0.0f) return 2;
+    return (sponge_active(s) || force_on(s)) ? 1 : 0;
+}
+
 cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool probe) {
     const int half = s->precision == STRO_FP16S ? 1 : 0;
     const int geo = geo_on(s) ? 1 : 0;
+    if (geo && !probe && s->variant == 0 && s->split && s->geo_host.size() == s->N) {
+        if (ensure_block_lists(s) != STRO_OK) return cudaErrorMemoryAllocation;
+        return launch_step_split(a, half, int(t & 1), bulk_feat(s), feat_on(s), s->block,
+                                 s->d_blocks, s->nbulk, s->d_blocks + s->nbulk, s->nedge,
+                                 s->ctx->stream);
+    }
     if (s->variant == 1 && pair_step_supported(half, geo, probe, s->nx, s->plane, s->pair_block))
         return launch_pair_step(a, int(t & 1), feat_on(s), s->pair_block, s->ctx->stream);
+    if (s->variant == 3 && !geo && !probe && s->block.x * s->block.y <= 128)
+        return launch_step_capped(a, half, int(t & 1), feat_on(s), s->block, s->ctx->stream);
     if (s->variant == 2 && rows_step_supported(half, geo, probe, s->nx, s->rows_threads))
         return launch_rows_step(a, half, int(t & 1), feat_on(s), s->rows_threads,
                                 s->ctx->sm_count, s->d_error, s->ctx->stream);

@@ -43,6 +43,8 @@ struct stro_sim {
     std::vector<uint8_t> flags;
     std::vector<uint32_t> smask, lmask;
     std::vector<float> eps;
+    std::vector<uint8_t> cell_host;   // packed cell bytes, as on the device
+    std::vector<uint32_t> geo_host;   // packed geometry words, as on the device
     bool any_wall = false, has_eps = false, has_ffield = false;
     bool ffield_nonzero = false;  // a zero field leaves the step's arithmetic unchanged
     bool force_geometry = false;  // device geometry kept even for an all-fluid lattice
@@ -68,6 +70,13 @@ struct stro_sim {
     dim3 pair_block{128, 2, 1};   // launch shape of the pair variant
     int rows_threads = 256;       // threads per block of the row-streaming variant
     int* d_error = nullptr;       // device error word of the row-streaming variant
+    // bulk / boundary block lists of a walled lattice for the current block shape
+    bool split = true;
+    uint32_t* d_blocks = nullptr;  // bulk blocks first, then edge blocks
+    uint32_t nbulk = 0, nedge = 0;
+    dim3 lists_block{0, 0, 0};
+    uint64_t lists_version = ~0ull;
+    uint64_t geo_version = 0;      // bumped whenever the device geometry changes
 };
 
 namespace stro {

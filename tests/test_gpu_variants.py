@@ -13,6 +13,7 @@ VARIANT_CASES = [
     (1, "fp16s", 64, 7, 5), (1, "fp16s", 128, 6, 4), (1, "fp16s", 192, 3, 3),
     (2, "fp16s", 64, 7, 5), (2, "fp16s", 40, 6, 4), (2, "fp16s", 256, 3, 2), (2, "fp16s", 8, 9, 4),
     (2, "fp32", 36, 7, 5), (2, "fp32", 128, 5, 3), (2, "fp32", 4, 6, 5),
+    (3, "fp16s", 37, 7, 5), (3, "fp32", 64, 6, 4),
 ]
 
 
@@ -34,6 +35,8 @@ def test_variant_matches_oracle(gpu, oracle, variant, precision, nx, ny, nz, fea
         g.sponge = (nx * 0.6, nx * 0.3, 0.9)
         o.sponge = (nx * 0.6, nx * 0.3, 0.9)
     g.variant = variant
+    if variant == 3:
+        g.block = (32, 4)
     rng = np.random.default_rng(nx * 31 + ny + variant)
     f0 = (rng.standard_normal((19, nx * ny * nz)) * 0.01).astype(o.f.dtype)
     g.uploadState(f0)
@@ -50,14 +53,42 @@ def test_variants_agree_bitwise(gpu, precision):
     import strouhal_gb300 as sg
 
     digests = []
-    for variant in ((0, 1, 2) if precision == "fp16s" else (0, 2)):
+    for variant in ((0, 1, 2, 3) if precision == "fp16s" else (0, 2, 3)):
         s = sg.Simulation(gpu, precision=precision, nx=128, ny=40, nz=24, omega=1.95)
         s.variant = variant
+        if variant == 3:
+            s.block = (64, 2)
         s.initField(2, 0.05)
         s.run(11)
         digests.append(s.stateDigest)
         s.close()
     assert len(set(digests)) == 1
+
+
+@pytest.mark.parametrize("precision", ["fp16s", "fp32"])
+def test_block_split_is_bitwise_neutral(gpu, precision):
+    """Walled lattice with a Noble-Torczynski body, LES and a sponge: the
+    bulk/boundary split and the single wall-aware kernel give identical states."""
+    import strouhal_gb300 as sg
+
+    nx, ny, nz = 96, 40, 24
+    flags = np.zeros((nz, ny, nx), np.uint8)
+    flags[:, :, 0] = flags[:, :, -1] = sg.Cell.inflow
+    flags[:, 0, :] = sg.Cell.solid
+    eps = sg.sphereSolidFractions(nx, ny, nz, 30.5, 20.0, 12.0, 6.0, 4)
+    digests = []
+    for split in (True, False):
+        s = sg.Simulation(gpu, precision=precision, nx=nx, ny=ny, nz=nz, omega=1.8, uin=0.05,
+                          rampSteps=10, cSmago=0.01, flags=flags.reshape(-1))
+        s.inflowUniform = True
+        s.setSolidFractions(eps)
+        s.sponge = (70.0, 20.0, 1.0)
+        s.setBlockSplit(split)
+        s.initField(2, 0.02)
+        s.run(13)
+        digests.append(s.stateDigest)
+        s.close()
+    assert digests[0] == digests[1]
 
 
 def _ladder(sg, gpu, precision="fp32"):
