@@ -41,6 +41,9 @@ U0 = 0.05
 RE = 1600.0
 STEPS_PER_BENCH_STEP = 100
 ALG_BYTES = {"fp32": 152, "fp16s": 76}  # 19 reads + 19 writes per cell per step
+# Kernels of each launch variant (stro_sim_set_variant), named as in the launch list.
+KERNEL_NAMES = {0: "k_step_even/k_step_odd", 1: "k_pair_even/k_pair_odd",
+                2: "k_rows<even>/k_rows<odd>", 3: "k_step_even_capped/k_step_odd_capped"}
 
 
 def tgv_params(n=N_EDGE, u0=U0, re=RE):
@@ -333,8 +336,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": ach16, "peak": peak, "unit": "GB/s",
                      "frac": ach16 / peak, "peak_source": peak_kind,
                      "traffic": None if t16 is None else t16 * head["cells"],
-                     "kernel": {0: "k_step_even/k_step_odd", 1: "k_pair_even/k_pair_odd",
-                                2: "k_rows<even>/k_rows<odd>"}[head["tuned"]["variant"]],
+                     "kernel": KERNEL_NAMES.get(head["tuned"]["variant"], "unknown"),
                      "alg_bytes_per_cell": ALG_BYTES["fp16s"]},
         "e2e": {"value": e16, "unit": "GLUPS",
                 "h2d_bytes_per_step": head["state_bytes"] / args.steps,

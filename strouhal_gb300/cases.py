@@ -259,7 +259,7 @@ def tgv(gpu, n=256, u0=0.05, t_end=20.0, precision="fp16s", lam=None, log_every=
 # ------------------------------------------------------------- sphere (C5)
 def sphere(gpu, nx=512, ny=256, nz=256, D=48, center=(128.0, 128.0, 128.0), u=0.05, re=300.0,
            cs=0.1, steps=50000, probe_every=500, ramp=8000, sponge=True, precision="fp16s",
-           sub=8):
+           sub=8, tune=True):
     """3-D sphere wake with LES (workload set-up from CaseSetups.swift:95-134):
     uniform-inflow velocity walls at x = 0 and x = nx-1, periodic y and z,
     Noble-Torczynski sphere from 8^3 subcell sampling, Smagorinsky
@@ -280,6 +280,8 @@ def sphere(gpu, nx=512, ny=256, nz=256, D=48, center=(128.0, 128.0, 128.0), u=0.
     bx = (int(cx) - D // 2 - 3, int(cx) + D // 2 + 3)
     byr = (int(cy) - D // 2 - 3, int(cy) + D // 2 + 3)
     area = u * u * math.pi * D * D / 4.0
+    if tune:
+        s.autotune(steps=10)  # launch shape and bulk/boundary split (state restored)
     t, cd = [], []
     t0 = time.perf_counter()
     while s.stepsDone + probe_every <= steps:
@@ -290,7 +292,8 @@ def sphere(gpu, nx=512, ny=256, nz=256, D=48, center=(128.0, 128.0, 128.0), u=0.
     wall = time.perf_counter() - t0
     out = {"nx": nx, "ny": ny, "nz": nz, "D": D, "re": re, "steps": s.stepsDone, "t": t,
            "cd": cd, "finite": s.checkFinite(), "gpu_seconds": s.gpuSeconds,
-           "wall_seconds": wall, "glups": s.cells * s.stepsDone / max(s.gpuSeconds, 1e-30) / 1e9}
+           "wall_seconds": wall, "glups": s.cells * s.stepsDone / max(s.gpuSeconds, 1e-30) / 1e9,
+           "variant": s.variant, "block": list(s.block)}
     s.close()
     return out
 

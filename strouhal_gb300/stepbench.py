@@ -16,7 +16,9 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=256, help="edge of the cubic lattice")
     ap.add_argument("--precision", default="fp16s", choices=["fp32", "fp16s"])
-    ap.add_argument("--variant", type=int, default=-1, help="0, 1, 2 or -1 = autotune")
+    ap.add_argument("--variant", type=int, default=-1, help="0, 1, 2, 3 or -1 = autotune")
+    ap.add_argument("--block", type=int, nargs=2, default=None, metavar=("BX", "BY"),
+                    help="launch shape of variants 0 and 3")
     ap.add_argument("--trt", action="store_true", help="TRT Lambda=3/16 instead of SRT")
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=4)
@@ -32,6 +34,8 @@ def main(argv=None):
         s.autotune(steps=10)
     else:
         s.variant = a.variant
+        if a.block:
+            s.block = tuple(a.block)
     s.run(a.warmup)
     t0 = s.gpuSeconds
     s.run(a.steps)
