@@ -144,14 +144,32 @@ int stro_sim_set_block(stro_sim* sim, int32_t bx, int32_t by);
 int stro_sim_get_block(stro_sim* sim, int32_t* bx, int32_t* by);
 /* Kernel variant: 0 = one cell per thread (all lattices); 1 = FP16 storage,
  * two x-adjacent cells per thread with half2 accesses (periodic lattices,
- * nx a multiple of 64); 2 = row streaming: whole rows staged in shared memory
- * by bulk copies ahead of the compute (periodic lattices, nx*element size a
- * multiple of 16); 3 = one cell per thread with registers capped at 64 for
+ * nx a multiple of 64); 2 = row staging: tiles of whole rows move through
+ * shared memory by bulk loads ahead of the compute and bulk stores after it
+ * (periodic lattices, nx*element size a multiple of 16, ny a multiple of the
+ * rows per tile); 3 = one cell per thread with registers capped at 64 for
  * more warps in flight (periodic lattices, blocks of at most 128 threads).
  * A lattice a variant does not apply to runs variant 0.
  * Results are identical for every variant. */
 int stro_sim_set_variant(stro_sim* sim, int32_t variant);
 int stro_sim_get_variant(stro_sim* sim, int32_t* variant);
+/* Arithmetic of the step. STRO_ARITH_REFERENCE (default) evaluates the
+ * reference's collision expressions as written (Kernels.metal:105-228), equal
+ * in value to the reference kernel in FP32. STRO_ARITH_FUSED evaluates the
+ * same collision in an algebraically equal form with fused multiply-adds,
+ * pair sums for the moments and shared weight products: about a quarter
+ * fewer instructions per cell, results differ from the reference
+ * arithmetic in the last bits and stay within the FP64 oracle's tolerances.
+ * It has no reference counterpart. Batches and adjoints require
+ * STRO_ARITH_REFERENCE. */
+enum { STRO_ARITH_REFERENCE = 0, STRO_ARITH_FUSED = 1 };
+int stro_sim_set_arithmetic(stro_sim* sim, int32_t arith);
+int stro_sim_get_arithmetic(stro_sim* sim, int32_t* arith);
+/* Launch shape of variant 2: `threads` computing threads per block (a
+ * multiple of 32, at most 256; one more warp issues the copies) and `rows`
+ * lattice rows per tile (1 to 8). */
+int stro_sim_set_rows_tile(stro_sim* sim, int32_t threads, int32_t rows);
+int stro_sim_get_rows_tile(stro_sim* sim, int32_t* threads, int32_t* rows);
 /* Walled lattices run their bulk blocks (cells with no wall neighbour and no
  * solid fraction) with the wall-free kernels and only the boundary blocks
  * with the wall-aware ones (default on); 0 runs the wall-aware kernels on

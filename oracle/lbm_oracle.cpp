@@ -7,6 +7,9 @@
 //   <float, float>     value-identical to the reference kernel at FPXX=float
 //   <float, _Float16>  value-identical to the reference kernel at FPXX=half
 //   <double, double>   the FP64 oracle (same algorithm, double throughout)
+// and, with FUSED, the library's fused-multiply-add arithmetic (an
+// algebraically equal form of the same collision that the reference does not
+// have): kinds 3 and 4 below, FP32 arithmetic over FP32 and FP16 storage.
 // "Value-identical" means equal as IEEE numbers (+0 == -0): terms whose lattice
 // coefficient is 0 are skipped, which can only change the sign of a zero.
 // The <float,*> instances are pinned against the reference's own kernel source
@@ -155,6 +158,10 @@ template <class R> inline V3<R> wall_velocity(uint8_t wf, int wy, const Params& 
 // DDFs, Kernels.metal:105-228. F is the cell's body force (the reference's
 // uniform force plus the optional per-cell field extension).
 template <class R>
+void relax_fused(R* fh, R wp, R wm, R rho, R rhom1, R ux, R uy, R uz, R u2, const R F[3], R eps,
+                 R nt[3]);
+
+template <class R, bool FUSED = false>
 void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt[3]) {
     R wp = R(p.omega), wm = R(p.omegaMinus);
     if (R(x) > R(p.spongeX0)) {  // sponge, Kernels.metal:112-123
@@ -187,10 +194,18 @@ void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt
             started[k] = true;
         }
     }
-    const R ux = (pc[0] + R(0.5) * F[0]) * inv;
-    const R uy = (pc[1] + R(0.5) * F[1]) * inv;
-    const R uz = (pc[2] + R(0.5) * F[2]) * inv;
-    const R u2 = ux * ux + uy * uy + uz * uz;
+    R ux, uy, uz, u2;
+    if (!FUSED) {
+        ux = (pc[0] + R(0.5) * F[0]) * inv;
+        uy = (pc[1] + R(0.5) * F[1]) * inv;
+        uz = (pc[2] + R(0.5) * F[2]) * inv;
+        u2 = ux * ux + uy * uy + uz * uz;
+    } else {
+        ux = Fma(R(0.5), F[0], pc[0]) * inv;
+        uy = Fma(R(0.5), F[1], pc[1]) * inv;
+        uz = Fma(R(0.5), F[2], pc[2]) * inv;
+        u2 = Fma(uz, uz, Fma(uy, uy, ux * ux));
+    }
 
     if (R(p.cSmago) > R(0)) {  // Smagorinsky, Kernels.metal:140-167
         R pxx = 0, pyy = 0, pzz = 0, pxy = 0, pxz = 0, pyz = 0;
@@ -227,6 +242,10 @@ void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt
         }
     }
 
+    if (FUSED) {
+        relax_fused<R>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, F, eps, nt);
+        return;
+    }
     const R uF = ux * F[0] + uy * F[1] + uz * F[2];
     const R ap = R(1) - R(0.5) * wp;
     const R am = R(1) - R(0.5) * wm;
@@ -276,6 +295,67 @@ void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt
         const int c[3] = {CX[i], CY[i], CZ[i]};
         for (int k = 0; k < 3; ++k)
             if (c[k] != 0) nt[k] -= R(2 * c[k]) * bounce;
+    }
+}
+
+// The fused relaxation, operation for operation as the GPU's fused mode:
+//   feq+ = fma(w rho, fma(4.5 cd, cd, -1.5 u2), w (rho-1)),  feq- = (w rho)(3 cd)
+//   A = fma(-1/2, f_i + f_j, feq+),  B = fma(-1/2, f_i - f_j, feq-)
+//   f_i' = fma(w+, A, fma(w-, B, f_i + (s+ + s-))),
+//   f_j' = fma(w+, A, fma(-w-, B, f_j + (s+ - s-)))
+// with cd = c_i . u, j = opp(i), s+/s- the split Guo source terms; partially
+// saturated cells blend with the Noble-Torczynski bounce operator as in
+// Kernels.metal:201-227. Same steps as relax_fused in lbm_cell.cuh.
+template <class R>
+void relax_fused(R* fh, R wp, R wm, R rho, R rhom1, R ux, R uy, R uz, R u2, const R F[3], R eps,
+                 R nt[3]) {
+    const R u2t = R(1.5) * u2;
+    const R w0 = weight<R>(0), ws = weight<R>(1), wl = weight<R>(7);
+    const R wr0 = w0 * rho, wm0 = w0 * rhom1;
+    const R wrs = ws * rho, wms = ws * rhom1;
+    const R wrl = wl * rho, wml = wl * rhom1;
+    const R feq0 = Fma(-wr0, u2t, wm0);
+    const R uF = Fma(uz, F[2], Fma(uy, F[1], ux * F[0]));
+    const R ap = Fma(R(-0.5), wp, R(1));
+    const R am = Fma(R(-0.5), wm, R(1));
+    const R aps = ws * ap, apl = wl * ap, ams = ws * am, aml = wl * am;
+    const R s0 = w0 * ap * (R(-3) * uF);
+    const bool nt_cell = !(eps == R(0));
+    R B = R(0), omb = R(1);
+    if (!nt_cell) {
+        fh[0] = Fma(wp, feq0 - fh[0], fh[0]) + s0;
+    } else {
+        const R tw = R(1) / wp - R(0.5);
+        B = eps * tw / ((R(1) - eps) + tw);
+        omb = R(1) - B;
+        fh[0] = Fma(omb, Fma(wp, feq0 - fh[0], s0), fh[0]);
+    }
+    for (int i = 1; i < 19; i += 2) {
+        const bool lng = i >= 7;
+        const R wr = lng ? wrl : wrs, wmr = lng ? wml : wms;
+        const R cd = cdot<R>(i, ux, uy, uz);
+        const R X = Fma(R(4.5) * cd, cd, -u2t);
+        const R feqp = Fma(wr, X, wmr);
+        const R feqm = wr * (R(3) * cd);
+        const R A = Fma(R(-0.5), fh[i] + fh[i + 1], feqp);
+        const R Bm = Fma(R(-0.5), fh[i] - fh[i + 1], feqm);
+        const R cF = cdot<R>(i, F[0], F[1], F[2]);
+        const R sm = (lng ? aml : ams) * (R(3) * cF);
+        const R sp = (lng ? apl : aps) * (R(3) * Fma(R(3) * cd, cF, -uF));
+        const R spp = sp + sm, spm = sp - sm;
+        if (!nt_cell) {
+            fh[i] = Fma(wp, A, Fma(wm, Bm, fh[i] + spp));
+            fh[i + 1] = Fma(wp, A, Fma(-wm, Bm, fh[i + 1] + spm));
+        } else {
+            const R up = Fma(wp, A, Fma(wm, Bm, spp));
+            const R um = Fma(wp, A, Fma(-wm, Bm, spm));
+            const R bounce = B * (fh[i + 1] - fh[i]);
+            fh[i] = Fma(omb, up, bounce) + fh[i];
+            fh[i + 1] = Fma(omb, um, -bounce) + fh[i + 1];
+            const int c[3] = {CX[i], CY[i], CZ[i]};
+            for (int k = 0; k < 3; ++k)
+                if (c[k] != 0) nt[k] -= R(2 * c[k]) * bounce;
+        }
     }
 }
 
@@ -336,7 +416,7 @@ inline void cell_slots(const Params& p, uint32_t sMask, size_t N, size_t n, int 
 // rd[i]): out[i] is stored to slot wr[i]; a[] receives the cell's
 // momentum-exchange force and force_out tells whether the reference writes it
 // (Kernels.metal:240-354, same order of operations).
-template <class R>
+template <class R, bool FUSED = false>
 void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_t lMask, int x,
                   int y, int z, const R in[19], R eps, const R F[3], R out[19], R a[3],
                   bool& force_out) {
@@ -348,7 +428,7 @@ void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_
     a[0] = a[1] = a[2] = R(0);
     force_out = false;
     if (p.parity == 0u) {  // even: in-cell pass
-        collide<R>(fh, p, x, eps, F, rho, nt);
+        collide<R, FUSED>(fh, p, x, eps, F, rho, nt);
         for (int i = 0; i < 19; ++i) out[i] = fh[i];
         if (p.writeForce != 0u && eps > R(0)) {
             a[0] = nt[0]; a[1] = nt[1]; a[2] = nt[2];
@@ -392,7 +472,7 @@ void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_
             }
         }
     }
-    collide<R>(fh, p, x, eps, F, rho, nt);
+    collide<R, FUSED>(fh, p, x, eps, F, rho, nt);
     a[0] += nt[0];
     a[1] += nt[1];
     a[2] += nt[2];
@@ -428,7 +508,7 @@ void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_
 
 // One thread of the `step` kernel, Kernels.metal:230-355. FOut is float for
 // the FP32-arithmetic instances and double for the FP64 oracle.
-template <class R, class S, class FOut>
+template <class R, class S, class FOut, bool FUSED>
 void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMaskBuf,
                const uint32_t* lMaskBuf, const Params& p, FOut* force, const float* epsBuf,
                const float* ffield, size_t n) {
@@ -448,7 +528,7 @@ void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMask
     R in[19], out[19], a[3];
     for (int i = 0; i < 19; ++i) in[i] = R(A.f[c.rd[i]]);
     bool fo = false;
-    cell_compute<R>(p, flags, sMask, lMask, x, y, z, in, eps, F, out, a, fo);
+    cell_compute<R, FUSED>(p, flags, sMask, lMask, x, y, z, in, eps, F, out, a, fo);
     for (int i = 0; i < 19; ++i) A.f[c.wr[i]] = S(out[i]);
     if (fo && force) {
         force[4 * n + 0] = FOut(a[0]);
@@ -458,7 +538,7 @@ void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMask
     }
 }
 
-template <class R, class S, class FOut>
+template <class R, class S, class FOut, bool FUSED = false>
 void step_all(void* f, const uint8_t* flags, const uint32_t* sm, const uint32_t* lm,
               const Params& p, FOut* force, const float* eps, const float* ffield, int threads) {
     const size_t N = size_t(p.nx) * p.ny * p.nz;
@@ -467,7 +547,7 @@ void step_all(void* f, const uint8_t* flags, const uint32_t* sm, const uint32_t*
     // same thread, so cells may be processed in any order or in parallel.
 #pragma omp parallel for schedule(static) num_threads(threads > 0 ? threads : 1) if (threads > 1)
     for (long long n = 0; n < (long long)N; ++n)
-        step_cell<R, S, FOut>(A, flags, sm, lm, p, force, eps, ffield, size_t(n));
+        step_cell<R, S, FOut, FUSED>(A, flags, sm, lm, p, force, eps, ffield, size_t(n));
 }
 
 // momentsEven, Kernels.metal:359-380 (division by rho, not by a reciprocal).
@@ -556,7 +636,9 @@ void init_all(void* fv, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t mode, fl
 
 extern "C" {
 
-// kind: 0 = <float,float>, 1 = <float,_Float16>, 2 = <double,double>.
+// kind: 0 = <float,float>, 1 = <float,_Float16>, 2 = <double,double>;
+// orc_step also takes 3 = <float,float> and 4 = <float,_Float16> in the fused
+// arithmetic.
 
 // Neighbour masks, Sim.swift:227-255: bit i-1 of solid_mask is set when the
 // neighbour at n + c_i is not fluid; lid_mask marks the moving-wall subset.
@@ -630,6 +712,13 @@ int orc_step(int kind, void* f, const uint8_t* flags, const uint32_t* solid_mask
                 return 0;
         case 2: step_all<double, double, double>(f, flags, solid_mask, lid_mask, p,
                                                  static_cast<double*>(force), eps, ffield, threads);
+                return 0;
+        case 3: step_all<float, float, float, true>(f, flags, solid_mask, lid_mask, p,
+                                                    static_cast<float*>(force), eps, ffield, threads);
+                return 0;
+        case 4: step_all<float, _Float16, float, true>(f, flags, solid_mask, lid_mask, p,
+                                                       static_cast<float*>(force), eps, ffield,
+                                                       threads);
                 return 0;
     }
     return 1;

@@ -22,6 +22,8 @@ from . import build_oracle as _build
 
 KIND_F32, KIND_F16, KIND_F64 = 0, 1, 2
 _DTYPES = {KIND_F32: np.float32, KIND_F16: np.float16, KIND_F64: np.float64}
+# step kinds of the fused-multiply-add arithmetic over FP32 / FP16 storage
+_FUSED_STEP_KIND = {KIND_F32: 3, KIND_F16: 4}
 
 CX = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0])
 CY = np.array([0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1])
@@ -39,7 +41,9 @@ def lib():
     global _lib
     if _lib is None:
         path = _build.oracle_lib_path()
-        if not os.path.exists(path):
+        src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lbm_oracle.cpp")
+        if not os.path.exists(path) or (os.path.exists(src) and
+                                        os.path.getmtime(src) > os.path.getmtime(path)):
             _build.build_oracle()
         L = ctypes.CDLL(path)
         L.orc_masks.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P]
@@ -113,10 +117,16 @@ class OracleSim:
 
     def __init__(self, nx, ny, nz, omega, omegaMinus=None, lid=(0.0, 0.0, 0.0), uin=0.0,
                  rampSteps=0, force=(0.0, 0.0, 0.0), cSmago=0.0, wantsForces=False,
-                 flags=None, kind=KIND_F32, backend="oracle", threads=1):
+                 flags=None, kind=KIND_F32, backend="oracle", threads=1, arithmetic="reference"):
         self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
         self.N = self.nx * self.ny * self.nz
         self.kind = kind
+        if arithmetic not in ("reference", "fused"):
+            raise ValueError("arithmetic must be 'reference' or 'fused'")
+        if arithmetic == "fused" and (kind not in _FUSED_STEP_KIND or backend != "oracle"):
+            raise ValueError("the fused arithmetic exists for FP32 arithmetic in the oracle only")
+        self.arithmetic = arithmetic
+        self.step_kind = _FUSED_STEP_KIND[kind] if arithmetic == "fused" else kind
         self.backend = backend
         self.threads = threads
         if backend == "ref" and kind == KIND_F64:
@@ -196,9 +206,12 @@ class OracleSim:
                                    _ptr(self.solidMask), _ptr(self.lidMask), p, _ptr(force),
                                    _ptr(eps))
             else:
-                lib().orc_step(self.kind, _ptr(self.f), _ptr(self.flags), _ptr(self.solidMask),
-                               _ptr(self.lidMask), p, _ptr(self.forceBuf), _ptr(eps),
-                               _ptr(self.forceField), self.threads)
+                rc = lib().orc_step(self.step_kind, _ptr(self.f), _ptr(self.flags),
+                                    _ptr(self.solidMask), _ptr(self.lidMask), p,
+                                    _ptr(self.forceBuf), _ptr(eps), _ptr(self.forceField),
+                                    self.threads)
+                if rc != 0:
+                    raise RuntimeError("orc_step rejected kind %d" % self.step_kind)
             self.stepsDone += 1
 
     # -- probes ---------------------------------------------------------------

@@ -38,6 +38,10 @@ class Precision(str, enum.Enum):
         return 4 if self is Precision.fp32 else 2
 
 
+# Arithmetic of the step, indexed by STRO_ARITH_* (see Simulation.arithmetic).
+ARITHMETICS = ("reference", "fused")
+
+
 class Cell(enum.IntEnum):
     """Sim.swift:46-52."""
     fluid = 0
@@ -100,6 +104,10 @@ def lib():
         "stro_sim_mass": ([_P, ctypes.POINTER(c_double)], c_int),
         "stro_sim_check_finite": ([_P, ctypes.POINTER(c_int)], c_int),
         "stro_sim_set_variant": ([_P, ctypes.c_int32], c_int),
+        "stro_sim_set_rows_tile": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
+        "stro_sim_set_arithmetic": ([_P, ctypes.c_int32], c_int),
+        "stro_sim_get_arithmetic": ([_P, ctypes.POINTER(ctypes.c_int32)], c_int),
+        "stro_sim_get_rows_tile": ([_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_set_block_split": ([_P, ctypes.c_int32], c_int),
         "stro_sim_get_variant": ([_P, ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_set_block": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
@@ -209,7 +217,8 @@ class Simulation:
 
     def __init__(self, gpu, precision=Precision.fp32, nx=1, ny=1, nz=1, omega=1.0,
                  omegaMinus=None, lid=(0.0, 0.0, 0.0), uin=0.0, rampSteps=0,
-                 force=(0.0, 0.0, 0.0), cSmago=0.0, wantsForces=False, flags=None):
+                 force=(0.0, 0.0, 0.0), cSmago=0.0, wantsForces=False, flags=None,
+                 arithmetic="reference"):
         self.gpu = gpu
         self.precision = Precision(precision)
         self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
@@ -238,6 +247,8 @@ class Simulation:
         self._cSmago = float(np.float32(cSmago))
         self._inflowUniform = False
         self._sponge = None
+        if arithmetic != "reference":
+            self.arithmetic = arithmetic
 
     # -- lifetime ----------------------------------------------------------
     def close(self):
@@ -452,6 +463,31 @@ class Simulation:
     @variant.setter
     def variant(self, v):
         _check(lib().stro_sim_set_variant(self._h, int(v)))
+
+    @property
+    def arithmetic(self):
+        """'reference' (the reference's expressions as written) or 'fused'
+        (fused multiply-adds, fewer instructions; stro_sim_set_arithmetic)."""
+        v = ctypes.c_int32()
+        _check(lib().stro_sim_get_arithmetic(self._h, ctypes.byref(v)))
+        return ARITHMETICS[v.value]
+
+    @arithmetic.setter
+    def arithmetic(self, v):
+        if v not in ARITHMETICS:
+            raise ValueError("arithmetic must be one of %s" % (ARITHMETICS,))
+        _check(lib().stro_sim_set_arithmetic(self._h, ARITHMETICS.index(v)))
+
+    @property
+    def rowsTile(self):
+        """(threads per block, lattice rows per tile) of the row-staged variant 2."""
+        t, r = ctypes.c_int32(), ctypes.c_int32()
+        _check(lib().stro_sim_get_rows_tile(self._h, ctypes.byref(t), ctypes.byref(r)))
+        return t.value, r.value
+
+    @rowsTile.setter
+    def rowsTile(self, v):
+        _check(lib().stro_sim_set_rows_tile(self._h, int(v[0]), int(v[1])))
 
     def setBlockSplit(self, enabled):
         """Bulk blocks of a walled lattice on the wall-free kernels (default True)."""

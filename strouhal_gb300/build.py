@@ -20,7 +20,24 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIBNAME = "libstrouhal_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-SOURCES = ["lbm_step.cu", "lbm_pair.cu", "lbm_rows.cu", "lbm_probe.cu", "lbm_batch.cu", "lbm_adjoint.cu", "runtime.cu", "batch.cu", "adjoint.cu", "sha256.cpp"]
+# (source, object name, extra flags). The step and row-staged kernels are
+# compiled once per arithmetic: the reference's expressions as written
+# (STRO_ARITH=0) and the fused-multiply-add collision (STRO_ARITH=1).
+SOURCES = [
+    ("lbm_step.cu", "lbm_step.o", ["-DSTRO_ARITH=0"]),
+    ("lbm_step.cu", "lbm_step_fused.o", ["-DSTRO_ARITH=1"]),
+    ("lbm_rows.cu", "lbm_rows.o", ["-DSTRO_ARITH=0"]),
+    ("lbm_rows.cu", "lbm_rows_fused.o", ["-DSTRO_ARITH=1"]),
+    ("lbm_pair.cu", "lbm_pair.o", ["-DSTRO_ARITH=0"]),
+    ("lbm_pair.cu", "lbm_pair_fused.o", ["-DSTRO_ARITH=1"]),
+    ("lbm_probe.cu", "lbm_probe.o", []),
+    ("lbm_batch.cu", "lbm_batch.o", []),
+    ("lbm_adjoint.cu", "lbm_adjoint.o", []),
+    ("runtime.cu", "runtime.o", []),
+    ("batch.cu", "batch.o", []),
+    ("adjoint.cu", "adjoint.o", []),
+    ("sha256.cpp", "sha256.o", []),
+]
 
 
 def nvcc():
@@ -54,12 +71,13 @@ def _stale(obj, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def _compile(src, verbose_ptxas):
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+def _compile(entry, verbose_ptxas):
+    src, objname, extra = entry
+    obj = os.path.join(BUILD, objname)
     deps = [src, __file__] + _headers()
     if not verbose_ptxas and not _stale(obj, deps):
         return obj, ""
-    cmd = [nvcc()] + _flags(verbose_ptxas) + ["-c", src, "-o", obj]
+    cmd = [nvcc()] + _flags(verbose_ptxas) + extra + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("compile failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
@@ -70,7 +88,7 @@ def build(verbose_ptxas=False, jobs=None):
     """Compile and link the library; returns its path."""
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
-    srcs = [os.path.join(CSRC, s) for s in SOURCES]
+    srcs = [(os.path.join(CSRC, s), o, x) for s, o, x in SOURCES]
     with cf.ThreadPoolExecutor(max_workers=jobs or len(srcs)) as ex:
         results = list(ex.map(lambda s: _compile(s, verbose_ptxas), srcs))
     objs = [o for o, _ in results]

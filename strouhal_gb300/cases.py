@@ -316,11 +316,13 @@ def ladder_instances(count=32, seed=1234, edges=(32, 48, 64, 96, 128, 160),
 
 
 def ladder(gpu, count=32, seed=1234, precision="fp32",
-           modes=("persistent", "rounds", "sequential"), t_star=5.0, tune=True):
+           modes=("persistent", "rounds", "sequential"), t_star=5.0, tune=True,
+           edges=(32, 48, 64, 96, 128, 160)):
     """32 periodic TGV instances of uneven size and Mach number, FP32 SRT,
     Re = 1600, 5 convective times each, kinetic-energy traces every 0.1 t*;
-    wall time of the batched launch against instance-after-instance."""
-    inst = ladder_instances(count, seed, t_star=t_star)
+    wall time of the batched launch against instance-after-instance.
+    `edges` is the set the lattice edges are drawn from."""
+    inst = ladder_instances(count, seed, edges=tuple(edges), t_star=t_star)
     results = {"instances": [{"n": n, "u0": u0, "steps": k, "log_every": le}
                              for n, u0, k, le in inst],
                "cell_updates": sum(n ** 3 * k for n, _, k, _ in inst)}

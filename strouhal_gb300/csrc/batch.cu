@@ -278,11 +278,17 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
 int tune_sim_shape(stro_sim* s, int64_t steps, int variant, dim3 cand, double* seconds) {
     cudaStream_t st = s->ctx->stream;
     const dim3 saved = s->block, saved_pair = s->pair_block;
-    const int saved_variant = s->variant, saved_rows = s->rows_threads;
+    const int saved_variant = s->variant, saved_rows = s->rows_threads,
+              saved_tile = s->rows_per_tile;
     s->variant = variant;
-    if (variant == 1) s->pair_block = cand;
-    else if (variant == 2) s->rows_threads = int(cand.x * cand.y);
-    else s->block = cand;  // variants 0 and 3
+    if (variant == 1) {
+        s->pair_block = cand;
+    } else if (variant == 2) {  // (threads, rows per tile)
+        s->rows_threads = int(cand.x);
+        s->rows_per_tile = int(cand.y);
+    } else {
+        s->block = cand;  // variants 0 and 3
+    }
     const int64_t t0 = s->steps_done;
     const double g0 = s->gpu_seconds;
     // warm-up pair, then the timed steps
@@ -304,11 +310,12 @@ int tune_sim_shape(stro_sim* s, int64_t steps, int variant, dim3 cand, double* s
     s->pair_block = saved_pair;
     s->variant = saved_variant;
     s->rows_threads = saved_rows;
+    s->rows_per_tile = saved_tile;
     s->gpu_seconds = g0;
     if (e != cudaSuccess) return cuda_fail(e, "autotune launch");
     if (err != 0) {
         cudaMemset(s->d_error, 0, sizeof(int));
-        return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-streaming step timed out");
+        return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-staged step timed out");
     }
     *seconds = double(ms) * 1e-3;
     return STRO_OK;
@@ -317,6 +324,9 @@ int tune_sim_shape(stro_sim* s, int64_t steps, int variant, dim3 cand, double* s
 const dim3 kShapes[] = {dim3(32, 8, 1), dim3(64, 4, 1), dim3(128, 2, 1), dim3(256, 1, 1),
                         dim3(16, 16, 1), dim3(32, 4, 1), dim3(64, 2, 1), dim3(128, 1, 1),
                         dim3(16, 8, 1), dim3(64, 1, 1), dim3(96, 1, 1), dim3(192, 1, 1)};
+// (threads, rows per tile) of the row-staged variant
+const dim3 kRowShapes[] = {dim3(128, 1, 1), dim3(256, 1, 1), dim3(128, 2, 1), dim3(256, 2, 1),
+                           dim3(256, 4, 1), dim3(64, 1, 1)};
 
 }  // namespace
 
@@ -330,6 +340,8 @@ int stro_batch_create(stro_ctx* ctx, int32_t count, stro_sim* const* sims, stro_
         if (sims[i]->ctx != ctx) return fail(STRO_ERR_INVALID, "batch spans contexts");
         if (sims[i]->precision != sims[0]->precision)
             return fail(STRO_ERR_INVALID, "batch mixes precisions");
+        if (sims[i]->arith != STRO_ARITH_REFERENCE)
+            return fail(STRO_ERR_INVALID, "batches run the reference arithmetic only");
         for (int32_t j = 0; j < i; ++j)
             if (sims[j] == sims[i]) return fail(STRO_ERR_INVALID, "simulation listed twice");
     }
@@ -401,6 +413,8 @@ int stro_batch_run(stro_batch* b, const int64_t* steps, const int32_t* log_every
     const size_t n = b->sims.size();
     for (size_t i = 0; i < n; ++i) {
         if (steps[i] < 0) return fail(STRO_ERR_INVALID, "negative step count");
+        if (b->sims[i]->arith != STRO_ARITH_REFERENCE)
+            return fail(STRO_ERR_INVALID, "batches run the reference arithmetic only");
         if (log_every && log_every[i] != 0) {
             if (log_every[i] < 0 || log_every[i] % 2 != 0)
                 return fail(STRO_ERR_INVALID, "log_every must be even");
@@ -473,6 +487,36 @@ int stro_sim_set_block_split(stro_sim* s, int32_t enabled) {
     return STRO_OK;
 }
 
+int stro_sim_set_arithmetic(stro_sim* s, int32_t arith) {
+    if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
+    if (arith != STRO_ARITH_REFERENCE && arith != STRO_ARITH_FUSED)
+        return fail(STRO_ERR_INVALID, "arithmetic must be STRO_ARITH_REFERENCE or STRO_ARITH_FUSED");
+    s->arith = arith;
+    return STRO_OK;
+}
+
+int stro_sim_get_arithmetic(stro_sim* s, int32_t* arith) {
+    if (!s || !arith) return fail(STRO_ERR_INVALID, "null argument");
+    *arith = s->arith;
+    return STRO_OK;
+}
+
+int stro_sim_set_rows_tile(stro_sim* s, int32_t threads, int32_t rows) {
+    if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
+    if (threads < 32 || threads > 256 || threads % 32 != 0 || rows < 1 || rows > 8)
+        return fail(STRO_ERR_INVALID, "rows tile: threads a multiple of 32 up to 256, 1 to 8 rows");
+    s->rows_threads = threads;
+    s->rows_per_tile = rows;
+    return STRO_OK;
+}
+
+int stro_sim_get_rows_tile(stro_sim* s, int32_t* threads, int32_t* rows) {
+    if (!s || !threads || !rows) return fail(STRO_ERR_INVALID, "null argument");
+    *threads = s->rows_threads;
+    *rows = s->rows_per_tile;
+    return STRO_OK;
+}
+
 int stro_sim_get_variant(stro_sim* s, int32_t* variant) {
     if (!s || !variant) return fail(STRO_ERR_INVALID, "null argument");
     *variant = s->variant;
@@ -503,32 +547,36 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
     const int half = s->precision == STRO_FP16S ? 1 : 0;
     const bool saved_split = s->split;
     bool best_split = saved_split;
+    const int geo = geo_on(s) ? 1 : 0;
     for (int split : {1, 0}) {
-    if (!split && !geo_on(s)) break;  // the split only exists for walled lattices
-    s->split = split != 0;
-    for (int variant : {0, 1, 2, 3}) {
-        for (const dim3& c : kShapes) {
-            if (rc != STRO_OK) break;
-            if ((variant == 0 || variant == 3) && c.x > 32 && int(c.x) > ((s->nx + 31) / 32) * 32)
-                continue;
-            if (variant == 3 && (geo_on(s) || c.x * c.y > 128)) continue;
-            if (variant == 1 && !pair_step_supported(half, geo_on(s) ? 1 : 0, false, s->nx,
-                                                     s->plane, c))
-                continue;
-            // the row-streaming variant only varies its thread count: one shape per count
-            if (variant == 2 && (c.y != 1 || !rows_step_supported(half, geo_on(s) ? 1 : 0, false,
-                                                                  s->nx, int(c.x))))
-                continue;
-            double sec = 0.0;
-            rc = tune_sim_shape(s, steps, variant, c, &sec);
-            if (rc == STRO_OK && sec < best) {
-                best = sec;
-                best_shape = c;
-                best_variant = variant;
-                best_split = s->split;
+        if (!split && !geo) break;  // the split only exists for walled lattices
+        s->split = split != 0;
+        for (int variant : {0, 1, 2, 3}) {
+            const dim3* shapes = variant == 2 ? kRowShapes : kShapes;
+            const size_t nshapes = variant == 2 ? sizeof(kRowShapes) / sizeof(dim3)
+                                                : sizeof(kShapes) / sizeof(dim3);
+            for (size_t q = 0; q < nshapes && rc == STRO_OK; ++q) {
+                const dim3 c = shapes[q];
+                if ((variant == 0 || variant == 3) && c.x > 32 &&
+                    int(c.x) > ((s->nx + 31) / 32) * 32)
+                    continue;
+                if (variant == 3 && (geo || c.x * c.y > 128)) continue;
+                if (variant == 1 && !exact::kPair.supported(half, geo, false, s->nx, s->plane, c))
+                    continue;
+                if (variant == 2 && !exact::kRows.supported(half, geo, false, s->nx, s->ny,
+                                                            int(c.x), int(c.y)))
+                    continue;
+                if (variant != 0 && split == 0) continue;  // the split only changes variant 0
+                double sec = 0.0;
+                rc = tune_sim_shape(s, steps, variant, c, &sec);
+                if (rc == STRO_OK && sec < best) {
+                    best = sec;
+                    best_shape = c;
+                    best_variant = variant;
+                    best_split = s->split;
+                }
             }
         }
-    }
     }
     s->split = best_split;
     e = cudaMemcpyAsync(s->d_f, saved, bytes, cudaMemcpyDeviceToDevice, st);
@@ -538,8 +586,12 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
     if (e != cudaSuccess) return cuda_fail(e, "autotune restore");
     s->variant = best_variant;
     if (best_variant == 1) s->pair_block = best_shape;
-    else if (best_variant == 2) s->rows_threads = int(best_shape.x);
-    else s->block = best_shape;
+    else if (best_variant == 2) {
+        s->rows_threads = int(best_shape.x);
+        s->rows_per_tile = int(best_shape.y);
+    } else {
+        s->block = best_shape;
+    }
     if (bx) *bx = int32_t(best_shape.x);
     if (by) *by = int32_t(best_shape.y);
     if (glups) *glups = double(s->N) * double(steps) / best / 1e9;

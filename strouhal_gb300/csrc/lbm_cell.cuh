@@ -112,8 +112,102 @@ __device__ __forceinline__ void relax(float (&fh)[19], float wp, float wm, float
     });
 }
 
+// Relaxation in the fused arithmetic (ARITH_FUSED): the same collision as
+// relax() written with fused multiply-adds and shared per-weight products:
+//   feq+ = fma(w rho, fma(4.5 cd, cd, -1.5 u2), w (rho-1)),  feq- = (w rho)(3 cd)
+//   A = fma(-1/2, f_i + f_j, feq+),  B = fma(-1/2, f_i - f_j, feq-)
+//   f_i' = fma(w+, A, fma(w-, B, f_i)),  f_j' = fma(w+, A, fma(-w-, B, f_j))
+// with cd = c_i . u, j = opp(i). Equal to relax() in exact arithmetic; the
+// oracle evaluates the identical operation sequence (orc kinds 3 and 4).
+template <bool FORCE, bool NT>
+__device__ __forceinline__ void relax_fused(float (&fh)[19], float wp, float wm, float rho,
+                                            float rhom1, float ux, float uy, float uz, float u2,
+                                            float Fx, float Fy, float Fz, float eps, float& ntx,
+                                            float& nty, float& ntz) {
+    const float u2t = 1.5f * u2;
+    const float wr0 = wgt(0) * rho, wm0 = wgt(0) * rhom1;
+    const float wrs = wgt(1) * rho, wms = wgt(1) * rhom1;
+    const float wrl = wgt(7) * rho, wml = wgt(7) * rhom1;
+    const float feq0 = fmaf(-wr0, u2t, wm0);
+    float uF = 0.0f, ap = 0.0f, am = 0.0f, aps = 0.0f, apl = 0.0f, ams = 0.0f, aml = 0.0f;
+    if constexpr (FORCE) {
+        uF = fmaf(uz, Fz, fmaf(uy, Fy, ux * Fx));
+        ap = fmaf(-0.5f, wp, 1.0f);
+        am = fmaf(-0.5f, wm, 1.0f);
+        aps = wgt(1) * ap; apl = wgt(7) * ap;
+        ams = wgt(1) * am; aml = wgt(7) * am;
+    }
+    float B = 0.0f, omb = 1.0f;
+    if constexpr (!NT) {
+        if constexpr (FORCE) {
+            const float s0 = wgt(0) * ap * (-3.0f * uF);
+            fh[0] = fmaf(wp, feq0 - fh[0], fh[0]) + s0;
+        } else {
+            fh[0] = fmaf(wp, feq0 - fh[0], fh[0]);
+        }
+    } else {
+        const float tw = 1.0f / wp - 0.5f;
+        B = eps * tw / ((1.0f - eps) + tw);
+        omb = 1.0f - B;
+        if constexpr (FORCE) {
+            const float s0 = wgt(0) * ap * (-3.0f * uF);
+            fh[0] = fmaf(omb, fmaf(wp, feq0 - fh[0], s0), fh[0]);
+        } else {
+            fh[0] = fmaf(omb, wp * (feq0 - fh[0]), fh[0]);
+        }
+    }
+    sfor<0, 9>([&](auto P) {
+        constexpr int i = 2 * P + 1;
+        constexpr bool lng = i >= 7;
+        const float wr = lng ? wrl : wrs, wmr = lng ? wml : wms;
+        const float cd = cdot<i>(ux, uy, uz);
+        const float X = fmaf(4.5f * cd, cd, -u2t);
+        const float feqp = fmaf(wr, X, wmr);
+        const float feqm = wr * (3.0f * cd);
+        const float A = fmaf(-0.5f, fh[i] + fh[i + 1], feqp);
+        const float Bm = fmaf(-0.5f, fh[i] - fh[i + 1], feqm);
+        float spp = 0.0f, spm = 0.0f;
+        if constexpr (FORCE) {
+            const float cF = cdot<i>(Fx, Fy, Fz);
+            const float sm = (lng ? aml : ams) * (3.0f * cF);
+            const float sp = (lng ? apl : aps) * (3.0f * fmaf(3.0f * cd, cF, -uF));
+            spp = sp + sm;
+            spm = sp - sm;
+        }
+        if constexpr (!NT) {
+            if constexpr (FORCE) {
+                fh[i] = fmaf(wp, A, fmaf(wm, Bm, fh[i] + spp));
+                fh[i + 1] = fmaf(wp, A, fmaf(-wm, Bm, fh[i + 1] + spm));
+            } else {
+                fh[i] = fmaf(wp, A, fmaf(wm, Bm, fh[i]));
+                fh[i + 1] = fmaf(wp, A, fmaf(-wm, Bm, fh[i + 1]));
+            }
+        } else {
+            const float up = fmaf(wp, A, FORCE ? fmaf(wm, Bm, spp) : wm * Bm);
+            const float um = fmaf(wp, A, FORCE ? fmaf(-wm, Bm, spm) : -(wm * Bm));
+            const float bounce = B * (fh[i + 1] - fh[i]);
+            fh[i] = fmaf(omb, up, bounce) + fh[i];
+            fh[i + 1] = fmaf(omb, um, -bounce) + fh[i + 1];
+            if constexpr (dcx(i) > 0) ntx -= 2.0f * bounce;
+            if constexpr (dcx(i) < 0) ntx += 2.0f * bounce;
+            if constexpr (dcy(i) > 0) nty -= 2.0f * bounce;
+            if constexpr (dcy(i) < 0) nty += 2.0f * bounce;
+            if constexpr (dcz(i) > 0) ntz -= 2.0f * bounce;
+            if constexpr (dcz(i) < 0) ntz += 2.0f * bounce;
+        }
+    });
+}
+
+// Arithmetic of the step: ARITH_REFERENCE evaluates the reference's
+// expressions as written (value-identical to Kernels.metal in FP32);
+// ARITH_FUSED keeps the moments' summation order and evaluates the velocity,
+// |u|^2 and the relaxation with fused multiply-adds and shared weight
+// products (fewer instructions, rounding differs at the last-bit level).
+constexpr int ARITH_REFERENCE = 0;
+constexpr int ARITH_FUSED = 1;
+
 // Collision, Kernels.metal:105-228.
-template <int FEAT>
+template <int FEAT, int ARITH = ARITH_REFERENCE>
 __device__ __forceinline__ void collide(float (&fh)[19], const StepArgs& a, int x, float eps,
                                         float Fx, float Fy, float Fz, float& ntx, float& nty,
                                         float& ntz) {
@@ -135,8 +229,6 @@ __device__ __forceinline__ void collide(float (&fh)[19], const StepArgs& a, int 
     }
     float rhom1 = fh[0];
     sfor<1, 19>([&](auto I) { rhom1 += fh[I]; });
-    const float rho = 1.0f + rhom1;
-    const float inv = 1.0f / rho;
     float px = fh[1], py = fh[3], pz = fh[5];
     sfor<2, 19>([&](auto I) {
         constexpr int i = I;
@@ -153,17 +245,26 @@ __device__ __forceinline__ void collide(float (&fh)[19], const StepArgs& a, int 
         if constexpr (dcz(i) > 0) pz += fh[i];
         if constexpr (dcz(i) < 0) pz -= fh[i];
     });
+    const float rho = 1.0f + rhom1;
+    const float inv = 1.0f / rho;
     float ux, uy, uz;
     if constexpr (FEAT) {
-        ux = (px + 0.5f * Fx) * inv;
-        uy = (py + 0.5f * Fy) * inv;
-        uz = (pz + 0.5f * Fz) * inv;
+        if constexpr (ARITH == ARITH_REFERENCE) {
+            ux = (px + 0.5f * Fx) * inv;
+            uy = (py + 0.5f * Fy) * inv;
+            uz = (pz + 0.5f * Fz) * inv;
+        } else {
+            ux = fmaf(0.5f, Fx, px) * inv;
+            uy = fmaf(0.5f, Fy, py) * inv;
+            uz = fmaf(0.5f, Fz, pz) * inv;
+        }
     } else {
         ux = px * inv;
         uy = py * inv;
         uz = pz * inv;
     }
-    const float u2 = ux * ux + uy * uy + uz * uz;
+    const float u2 = ARITH == ARITH_REFERENCE ? ux * ux + uy * uy + uz * uz
+                                              : fmaf(uz, uz, fmaf(uy, uy, ux * ux));
 
     if constexpr (FEAT == 2) {
         if (a.c_smago > 0.0f) {  // Smagorinsky LES, Kernels.metal:140-167
@@ -200,16 +301,27 @@ __device__ __forceinline__ void collide(float (&fh)[19], const StepArgs& a, int 
             }
         }
     }
+    auto relax_any = [&](auto force, auto nt) {
+        constexpr bool FO = decltype(force)::value, NO = decltype(nt)::value;
+        if constexpr (ARITH == ARITH_REFERENCE)
+            relax<FO, NO>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, Fx, Fy, Fz, eps, ntx, nty, ntz);
+        else
+            relax_fused<FO, NO>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, Fx, Fy, Fz, eps, ntx, nty,
+                                ntz);
+    };
+    using T = std::true_type;
+    using F = std::false_type;
     if constexpr (FEAT) {
         if (eps == 0.0f) {
-            if (a.force_on) relax<true, false>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, Fx, Fy, Fz, eps, ntx, nty, ntz);
-            else relax<false, false>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, Fx, Fy, Fz, eps, ntx, nty, ntz);
+            if (a.force_on) relax_any(T{}, F{});
+            else relax_any(F{}, F{});
         } else {
-            if (a.force_on) relax<true, true>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, Fx, Fy, Fz, eps, ntx, nty, ntz);
-            else relax<false, true>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, Fx, Fy, Fz, eps, ntx, nty, ntz);
+            if (a.force_on) relax_any(T{}, T{});
+            else relax_any(F{}, T{});
         }
     } else {
-        relax<false, false>(fh, wp, wm, rho, rhom1, ux, uy, uz, u2, 0.f, 0.f, 0.f, 0.f, ntx, nty, ntz);
+        Fx = Fy = Fz = 0.0f;
+        relax_any(F{}, F{});
     }
 }
 
@@ -362,7 +474,8 @@ __device__ __forceinline__ float cell_u2(const float (&fh)[19], float Fx, float 
 
 // Even (in-cell) pass of one cell, Kernels.metal:252-260. Non-fluid cells are
 // skipped. With LOG, u2 receives |u|^2 of the state before the step.
-template <typename S, int GEO, int FEAT, bool LOG = false, bool CG = false>
+template <typename S, int GEO, int FEAT, bool LOG = false, bool CG = false,
+          int ARITH = ARITH_REFERENCE>
 __device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z,
                                           float* u2 = nullptr) {
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
@@ -382,7 +495,7 @@ __device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z
     cell_force<FEAT>(a, n, Fx, Fy, Fz);
     if constexpr (LOG) *u2 = cell_u2(fh, Fx, Fy, Fz);
     float ntx = 0.f, nty = 0.f, ntz = 0.f;
-    collide<FEAT>(fh, a, x, eps, Fx, Fy, Fz, ntx, nty, ntz);
+    collide<FEAT, ARITH>(fh, a, x, eps, Fx, Fy, Fz, ntx, nty, ntz);
     store_ddf<S>(f + n, fh[0]);
     sfor<1, 19>([&](auto I) { store_ddf<S>(f + uint64_t(opp(I)) * P + n, fh[I]); });
 }
@@ -390,7 +503,8 @@ __device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z
 // Odd (streaming) pass of one cell with halfway / moving-wall bounce-back,
 // Kernels.metal:261-354. With PROBE the cell's momentum-exchange force is
 // returned in contrib when the cell is a boundary cell inside the probe box.
-template <typename S, int GEO, int FEAT, bool PROBE, bool CG = false>
+template <typename S, int GEO, int FEAT, bool PROBE, bool CG = false,
+          int ARITH = ARITH_REFERENCE>
 __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, int x, int y,
                                          int z, double (&contrib)[3]) {
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
@@ -435,7 +549,7 @@ __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, i
     float Fx = 0.f, Fy = 0.f, Fz = 0.f;
     cell_force<FEAT>(a, n, Fx, Fy, Fz);
     float ntx = 0.f, nty = 0.f, ntz = 0.f;
-    collide<FEAT>(fh, a, x, eps, Fx, Fy, Fz, ntx, nty, ntz);
+    collide<FEAT, ARITH>(fh, a, x, eps, Fx, Fy, Fz, ntx, nty, ntz);
     if constexpr (PROBE) {
         ax += ntx;
         ay += nty;

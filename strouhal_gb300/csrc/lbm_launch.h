@@ -8,36 +8,62 @@
 
 namespace stro {
 
-// One AA pass over the lattice. block.x * block.y must be a multiple of 32
-// and at most 256; the grid is (ceil(nx/bx), ceil(ny/by), nz).
-cudaError_t launch_step(const StepArgs& a, int half_storage, int parity, int geo, int feat,
+// Grid of the one-cell kernels: (ceil(nx/bx), ceil(ny/by), nz).
+inline dim3 step_grid(const StepArgs& a, dim3 block) {
+    return dim3((a.nx + block.x - 1) / block.x, (a.ny + block.y - 1) / block.y, a.nz);
+}
+
+// Launchers of the step kernels (lbm_step.cu), one table per arithmetic:
+// exact::kStep (the reference's expressions as written) and fused::kStep
+// (the fused-multiply-add collision).
+struct StepLaunchers {
+    // One AA pass over the lattice. block.x * block.y must be a multiple of 32
+    // and at most 256; the grid is step_grid(a, block).
+    cudaError_t (*step)(const StepArgs& a, int half_storage, int parity, int geo, int feat,
                         bool probe, dim3 block, cudaStream_t st);
-dim3 step_grid(const StepArgs& a, dim3 block);
+    // Register-capped one-cell kernels for periodic lattices (block <= 128 threads).
+    cudaError_t (*capped)(const StepArgs& a, int half_storage, int parity, int feat, dim3 block,
+                          cudaStream_t st);
+    // One pass split over two block lists of the (bx,by) grid: `bulk` blocks
+    // (every cell fluid, no wall neighbour, no solid fraction) run the
+    // wall-free kernels at feature level feat_bulk, `edge` blocks the
+    // wall-aware kernels at feat_edge. Each cell touches only its own slots,
+    // so the two launches are independent.
+    cudaError_t (*split)(const StepArgs& a, int half_storage, int parity, int feat_bulk,
+                         int feat_edge, dim3 block, const uint32_t* bulk, uint32_t nbulk,
+                         const uint32_t* edge, uint32_t nedge, cudaStream_t st);
+};
 
-// Register-capped one-cell kernels for periodic lattices (block <= 128 threads).
-cudaError_t launch_step_capped(const StepArgs& a, int half_storage, int parity, int feat,
-                               dim3 block, cudaStream_t st);
-
-// One pass split over two block lists of the (bx,by) grid: `bulk` blocks
-// (every cell fluid, no wall neighbour, no solid fraction) run the wall-free
-// kernels at feature level feat_bulk, `edge` blocks the wall-aware kernels at
-// feat_edge. Each cell touches only its own slots, so the two launches are
-// independent.
-cudaError_t launch_step_split(const StepArgs& a, int half_storage, int parity, int feat_bulk,
-                              int feat_edge, dim3 block, const uint32_t* bulk, uint32_t nbulk,
-                              const uint32_t* edge, uint32_t nedge, cudaStream_t st);
+// Row-staged step (lbm_rows.cu): tiles of `rows` whole lattice rows move
+// through shared memory by bulk loads and bulk stores, `threads` computing
+// threads per block plus one copy warp, persistent over tiles. `error`
+// receives 1 if a bounded wait gave up.
+struct RowsLaunchers {
+    bool (*supported)(int half_storage, int geo, bool probe, int nx, int ny, int threads,
+                      int rows);
+    cudaError_t (*launch)(const StepArgs& a, int half_storage, int parity, int feat, int threads,
+                          int rows, int sm_count, int* error, cudaStream_t st);
+};
 
 // FP16 periodic step with x-adjacent cell pairs per thread (lbm_pair.cu).
 // block.x threads cover 2*block.x cells of a row.
-bool pair_step_supported(int half_storage, int geo, bool probe, int nx, uint64_t plane, dim3 block);
-cudaError_t launch_pair_step(const StepArgs& a, int parity, int feat, dim3 block, cudaStream_t st);
+struct PairLaunchers {
+    bool (*supported)(int half_storage, int geo, bool probe, int nx, uint64_t plane, dim3 block);
+    cudaError_t (*launch)(const StepArgs& a, int parity, int feat, dim3 block, cudaStream_t st);
+};
 
-// Row-streaming step (lbm_rows.cu): bulk-copy staging of whole rows in shared
-// memory, `threads` per block, persistent over rows. `error` receives 1 if a
-// bounded wait gave up.
-bool rows_step_supported(int half_storage, int geo, bool probe, int nx, int threads);
-cudaError_t launch_rows_step(const StepArgs& a, int half_storage, int parity, int feat,
-                             int threads, int sm_count, int* error, cudaStream_t st);
+namespace exact {
+extern const StepLaunchers kStep;
+extern const RowsLaunchers kRows;
+extern const PairLaunchers kPair;
+}  // namespace exact
+namespace fused {
+extern const StepLaunchers kStep;
+extern const RowsLaunchers kRows;
+extern const PairLaunchers kPair;
+}  // namespace fused
+
+
 
 // Fields and reductions (lbm_probe.cu). `plane` is the DDF plane stride in
 // elements, N the cell count. Reductions write per-block FP64 partials to

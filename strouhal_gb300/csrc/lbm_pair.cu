@@ -1,10 +1,17 @@
 // FP16-storage step with two x-adjacent cells per thread (periodic lattices).
 //
 // With binary16 DDFs a one-cell thread keeps only 19 x 2 bytes in flight per
-// pass, which leaves the step latency-bound. Here each thread owns the cell
-// pair (x, x+1), x even, and moves both cells' DDFs as one 4-byte half2 per
-// direction (packed conversions, half the load/store instructions). A warp
-// covers 64 consecutive cells of one row.
+// pass and every load is a 2-byte request; the memory system then delivers
+// well below its copy bandwidth however many threads are resident. Here each
+// thread owns the cell pair (x, x+1), x even, and moves both cells' DDFs as
+// one 4-byte half2 per direction. A warp covers 64 consecutive cells of one
+// row.
+//
+// Registers: only one cell's 19 FP32 values are live at a time. After the
+// loads, cell x takes the low halves as FP32 while the high halves (cell
+// x+1) are repacked two directions per register (10 registers); cell x's
+// results are packed the same way before cell x+1 is collided. This keeps
+// the working set near 19 + 10 registers plus the collision's temporaries.
 //
 // Even pass: all accesses are aligned half2.
 // Odd pass: directions with c_x = 0 stay aligned half2. For c_x = +1 the
@@ -17,12 +24,25 @@
 // neighbouring warp's pair. Every slot is still read and written exactly once.
 //
 // The per-cell arithmetic is the shared collide(), so results are identical to
-// the one-cell kernels. Requirements (checked by the host): FP16 storage, no
-// walls or solid fractions, nx a multiple of 64, even plane stride.
+// the one-cell kernels of the same arithmetic. Compiled twice like
+// lbm_step.cu: STRO_ARITH=0 (stro::exact) and 1 (stro::fused); each copy
+// exports one PairLaunchers table. Requirements (checked by the host): FP16
+// storage, no walls or solid fractions, nx a multiple of 64, even plane
+// stride, block.x a multiple of 32 dividing nx/2, at most 256 threads.
 #include "lbm_cell.cuh"
 #include "lbm_launch.h"
 
+#ifndef STRO_ARITH
+#define STRO_ARITH 0
+#endif
+#if STRO_ARITH == 0
+#define STRO_ARITH_NS exact
+#else
+#define STRO_ARITH_NS fused
+#endif
+
 namespace stro {
+namespace STRO_ARITH_NS {
 
 namespace {
 
@@ -32,8 +52,65 @@ __device__ __forceinline__ int wrap_x(int v, int nx) {
     return v;
 }
 
+// Scheduling fence: the packed values pass through an empty asm statement, so
+// the compiler must finish everything that produces `done` before it and may
+// start anything that consumes `next` only after it. Without it the two
+// cells' collisions are interleaved and both sets of 19 values stay live.
+__device__ __forceinline__ void order_cells(__half2 (&done)[10], __half2 (&next)[10]) {
+    sfor<0, 10>([&](auto K) {
+        uint32_t& d = *reinterpret_cast<uint32_t*>(&done[K]);
+        uint32_t& n = *reinterpret_cast<uint32_t*>(&next[K]);
+        asm volatile("" : "+r"(d), "+r"(n));
+    });
+}
+
 template <int FEAT>
-__global__ void __launch_bounds__(256, 2) k_pair_even(const StepArgs a) {
+__device__ __forceinline__ void collide_cell(float (&fh)[19], const StepArgs& a, int x,
+                                             uint32_t n) {
+    float Fx = 0.f, Fy = 0.f, Fz = 0.f;
+    cell_force<FEAT>(a, n, Fx, Fy, Fz);
+    float ntx = 0.f, nty = 0.f, ntz = 0.f;
+    collide<FEAT, STRO_ARITH>(fh, a, x, 0.0f, Fx, Fy, Fz, ntx, nty, ntz);
+}
+
+// Collide both cells of the packed pairs v[i] = (cell x, cell x+1). On
+// return ao[k] holds cell x's post-collision directions (2k, 2k+1) packed,
+// and fh cell x+1's post-collision values.
+template <int FEAT>
+__device__ __forceinline__ void collide_pair(const __half2 (&v)[19], __half2 (&ao)[10],
+                                             float (&fh)[19], const StepArgs& a, int x,
+                                             uint32_t n) {
+    __half2 bi[10];  // cell x+1's inputs, two directions per register
+    sfor<0, 9>([&](auto K) { bi[K] = __halves2half2(__high2half(v[2 * K]), __high2half(v[2 * K + 1])); });
+    bi[9] = __halves2half2(__high2half(v[18]), __high2half(v[18]));
+    sfor<0, 19>([&](auto I) { fh[I] = __low2float(v[I]); });
+    collide_cell<FEAT>(fh, a, x, n);
+    sfor<0, 9>([&](auto K) { ao[K] = __floats2half2_rn(fh[2 * K], fh[2 * K + 1]); });
+    ao[9] = __floats2half2_rn(fh[18], fh[18]);
+    order_cells(ao, bi);
+    sfor<0, 19>([&](auto I) {
+        fh[I] = (I & 1) ? __high2float(bi[I / 2]) : __low2float(bi[I / 2]);
+    });
+    collide_cell<FEAT>(fh, a, x + 1, n + 1);
+}
+
+// The pointer passes through an empty asm statement: addresses formed from it
+// afterwards cannot reuse the ones formed before, so the 19 load addresses
+// (two registers each) are not kept alive across the collision for the stores.
+template <typename P>
+__device__ __forceinline__ void forget(P& p) {
+    asm volatile("" : "+l"(p));
+}
+__device__ __forceinline__ void forget_int(int& v) { asm volatile("" : "+r"(v)); }
+
+// Cell x's post-collision direction i from the packed results.
+template <int I>
+__device__ __forceinline__ __half out_lo(const __half2 (&ao)[10]) {
+    return (I & 1) ? __high2half(ao[I / 2]) : __low2half(ao[I / 2]);
+}
+
+template <int FEAT>
+__global__ void __launch_bounds__(256, FEAT == 2 ? 2 : 4) k_pair_even(const StepArgs a) {
     const int x = 2 * int(blockIdx.x * blockDim.x + threadIdx.x);
     const int y = int(blockIdx.y * blockDim.y + threadIdx.y);
     const int z = int(blockIdx.z);
@@ -42,24 +119,63 @@ __global__ void __launch_bounds__(256, 2) k_pair_even(const StepArgs a) {
     __half2* __restrict__ f2 = static_cast<__half2*>(a.f);
     const uint64_t P2 = a.plane / 2;
     const uint32_t n2 = n / 2;
-    float A[19], B[19];
+    __half2 v[19];
+    sfor<0, 19>([&](auto I) { v[I] = f2[uint64_t(I) * P2 + n2]; });
+    __half2 ao[10];
+    float fh[19];
+    collide_pair<FEAT>(v, ao, fh, a, x, n);
+    forget(f2);
+    // direction i of both cells goes to slot opp(i)
     sfor<0, 19>([&](auto I) {
-        const float2 v = __half22float2(f2[uint64_t(I) * P2 + n2]);
-        A[I] = v.x;
-        B[I] = v.y;
+        f2[uint64_t(opp(I)) * P2 + n2] = __halves2half2(out_lo<I>(ao), __float2half_rn(fh[I]));
     });
-    float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
-    float FAx = 0.f, FAy = 0.f, FAz = 0.f, FBx = 0.f, FBy = 0.f, FBz = 0.f;
-    cell_force<FEAT>(a, n, FAx, FAy, FAz);
-    cell_force<FEAT>(a, n + 1, FBx, FBy, FBz);
-    collide<FEAT>(A, a, x, 0.0f, FAx, FAy, FAz, ax, ay, az);
-    collide<FEAT>(B, a, x + 1, 0.0f, FBx, FBy, FBz, bx, by, bz);
-    f2[n2] = __floats2half2_rn(A[0], B[0]);
-    sfor<1, 19>([&](auto I) { f2[uint64_t(opp(I)) * P2 + n2] = __floats2half2_rn(A[I], B[I]); });
+}
+
+// Odd-pass stores of a cell pair. The indices are formed again from (x, y, z)
+// after an opaque asm statement, so the gather's neighbour offsets do not
+// stay in registers across the two collisions.
+__device__ __forceinline__ void scatter_pair(const StepArgs& a, const __half2 (&ao)[10],
+                                             const float (&fh)[19], int x, int y, int z) {
+    forget_int(x);
+    forget_int(y);
+    forget_int(z);
+    const int lane = int(threadIdx.x & 31u);
+    const int nx = a.nx;
+    const int xw = x - 2 * lane;
+    const int x_left = wrap_x(xw - 1, nx);
+    const int x_right = wrap_x(xw + 64, nx);
+    const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(nx) + uint32_t(x);
+    const NbrOffsets nb(x, y, z, nx, a.ny, a.nz);
+    __half2* __restrict__ f2 = static_cast<__half2*>(a.f);
+    __half* __restrict__ f1 = static_cast<__half*>(a.f);
+    const uint64_t P = a.plane;
+    const uint64_t P2 = P / 2;
+    f2[n / 2] = __halves2half2(out_lo<0>(ao), __float2half_rn(fh[0]));
+    sfor<1, 19>([&](auto I) {
+        constexpr int i = I;
+        // destination row of direction i (y, z shifted by +c_i), same x
+        const uint32_t d = uint32_t(int(n) + nb.template off<0, dcy(i), dcz(i)>());
+        const uint64_t base = uint64_t(i) * P;
+        const __half ah = out_lo<i>(ao);           // cell x, direction i
+        const __half bh = __float2half_rn(fh[i]);  // cell x+1, direction i
+        if constexpr (dcx(i) == 0) {
+            f2[uint64_t(i) * P2 + d / 2] = __halves2half2(ah, bh);
+        } else if constexpr (dcx(i) > 0) {  // destinations x+1, x+2
+            const __half lo = __shfl_up_sync(0xffffffffu, bh, 1);
+            if (lane != 0) f2[uint64_t(i) * P2 + d / 2] = __halves2half2(lo, ah);
+            else f1[base + d + 1] = ah;
+            if (lane == 31) f1[base + (d - uint32_t(x) + uint32_t(x_right))] = bh;
+        } else {  // destinations x-1, x
+            const __half hi = __shfl_down_sync(0xffffffffu, ah, 1);
+            if (lane != 31) f2[uint64_t(i) * P2 + d / 2] = __halves2half2(bh, hi);
+            else f1[base + d] = bh;
+            if (lane == 0) f1[base + (d - uint32_t(x) + uint32_t(x_left))] = ah;
+        }
+    });
 }
 
 template <int FEAT>
-__global__ void __launch_bounds__(256, 2) k_pair_odd(const StepArgs a) {
+__global__ void __launch_bounds__(256, FEAT == 2 ? 2 : 4) k_pair_odd(const StepArgs a) {
     const int lane = int(threadIdx.x & 31u);
     const int x = 2 * int(blockIdx.x * blockDim.x + threadIdx.x);
     const int y = int(blockIdx.y * blockDim.y + threadIdx.y);
@@ -75,66 +191,33 @@ __global__ void __launch_bounds__(256, 2) k_pair_odd(const StepArgs a) {
     __half* __restrict__ f1 = static_cast<__half*>(a.f);
     const uint64_t P = a.plane;
     const uint64_t P2 = P / 2;
-    float A[19], B[19];
-    {
-        const float2 v = __half22float2(f2[n / 2]);
-        A[0] = v.x;
-        B[0] = v.y;
-    }
+    __half2 v[19];
+    v[0] = f2[n / 2];
     sfor<1, 19>([&](auto I) {
         constexpr int i = I;
         constexpr int o = opp(i);
         // source row of direction i (y, z shifted by -c_i), same x
         const uint32_t r = uint32_t(int(n) + nb.template off<0, -dcy(i), -dcz(i)>());
-        const float2 v = __half22float2(f2[uint64_t(o) * P2 + r / 2]);
+        const __half2 w = f2[uint64_t(o) * P2 + r / 2];
         if constexpr (dcx(i) == 0) {
-            A[i] = v.x;
-            B[i] = v.y;
+            v[i] = w;
         } else if constexpr (dcx(i) > 0) {  // sources x-1, x
-            B[i] = v.x;
-            const float left = __shfl_up_sync(0xffffffffu, v.y, 1);
-            A[i] = lane == 0 ? __half2float(f1[uint64_t(o) * P + (r - uint32_t(x) + uint32_t(x_left))])
-                             : left;
+            const __half2 left = __shfl_up_sync(0xffffffffu, w, 1);
+            const __half lo = lane == 0 ? f1[uint64_t(o) * P + (r - uint32_t(x) + uint32_t(x_left))]
+                                        : __high2half(left);
+            v[i] = __halves2half2(lo, __low2half(w));
         } else {  // sources x+1, x+2
-            A[i] = v.y;
-            const float right = __shfl_down_sync(0xffffffffu, v.x, 1);
-            B[i] = lane == 31
-                       ? __half2float(f1[uint64_t(o) * P + (r - uint32_t(x) + uint32_t(x_right))])
-                       : right;
+            const __half2 right = __shfl_down_sync(0xffffffffu, w, 1);
+            const __half hi = lane == 31
+                                  ? f1[uint64_t(o) * P + (r - uint32_t(x) + uint32_t(x_right))]
+                                  : __low2half(right);
+            v[i] = __halves2half2(__high2half(w), hi);
         }
     });
-    float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
-    float FAx = 0.f, FAy = 0.f, FAz = 0.f, FBx = 0.f, FBy = 0.f, FBz = 0.f;
-    cell_force<FEAT>(a, n, FAx, FAy, FAz);
-    cell_force<FEAT>(a, n + 1, FBx, FBy, FBz);
-    collide<FEAT>(A, a, x, 0.0f, FAx, FAy, FAz, ax, ay, az);
-    collide<FEAT>(B, a, x + 1, 0.0f, FBx, FBy, FBz, bx, by, bz);
-    f2[n / 2] = __floats2half2_rn(A[0], B[0]);
-    sfor<1, 19>([&](auto I) {
-        constexpr int i = I;
-        // destination row of direction i (y, z shifted by +c_i), same x
-        const uint32_t d = uint32_t(int(n) + nb.template off<0, dcy(i), dcz(i)>());
-        const uint64_t base = uint64_t(i) * P;
-        if constexpr (dcx(i) == 0) {
-            f2[uint64_t(i) * P2 + d / 2] = __floats2half2_rn(A[i], B[i]);
-        } else if constexpr (dcx(i) > 0) {  // destinations x+1, x+2
-            const float lo = __shfl_up_sync(0xffffffffu, B[i], 1);
-            if (lane != 0) {
-                f2[uint64_t(i) * P2 + d / 2] = __floats2half2_rn(lo, A[i]);
-            } else {
-                f1[base + d + 1] = __float2half_rn(A[i]);
-            }
-            if (lane == 31) f1[base + (d - uint32_t(x) + uint32_t(x_right))] = __float2half_rn(B[i]);
-        } else {  // destinations x-1, x
-            const float hi = __shfl_down_sync(0xffffffffu, A[i], 1);
-            if (lane != 31) {
-                f2[uint64_t(i) * P2 + d / 2] = __floats2half2_rn(B[i], hi);
-            } else {
-                f1[base + d] = __float2half_rn(B[i]);
-            }
-            if (lane == 0) f1[base + (d - uint32_t(x) + uint32_t(x_left))] = __float2half_rn(A[i]);
-        }
-    });
+    __half2 ao[10];
+    float fh[19];
+    collide_pair<FEAT>(v, ao, fh, a, x, n);
+    scatter_pair(a, ao, fh, x, y, z);
 }
 
 }  // namespace
@@ -160,4 +243,7 @@ cudaError_t launch_pair_step(const StepArgs& a, int parity, int feat, dim3 block
     return cudaGetLastError();
 }
 
+const PairLaunchers kPair = {&pair_step_supported, &launch_pair_step};
+
+}  // namespace STRO_ARITH_NS
 }  // namespace stro

@@ -21,10 +21,25 @@
 //          1 all features, each behind a uniform or per-cell branch.
 //   PROBE  odd pass with momentum-exchange force accumulation, reduced per
 //          block in FP64 in a fixed order (no per-cell force buffer).
+//
+// The file is compiled twice: with STRO_ARITH=0 (namespace stro::exact, the
+// reference arithmetic above) and with STRO_ARITH=1 (namespace stro::fused,
+// the fused-multiply-add collision of lbm_cell.cuh). Each copy exports its
+// launchers through one StepLaunchers table.
 #include "lbm_cell.cuh"
 #include "lbm_launch.h"
 
+#ifndef STRO_ARITH
+#define STRO_ARITH 0
+#endif
+#if STRO_ARITH == 0
+#define STRO_ARITH_NS exact
+#else
+#define STRO_ARITH_NS fused
+#endif
+
 namespace stro {
+namespace STRO_ARITH_NS {
 
 // ---------------------------------------------------------------- kernels
 template <typename S, int GEO, int FEAT>
@@ -32,7 +47,7 @@ __global__ void __launch_bounds__(256) k_step_even(const StepArgs a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= a.nx || y >= a.ny) return;
-    even_cell<S, GEO, FEAT>(a, x, y, blockIdx.z);
+    even_cell<S, GEO, FEAT, false, false, STRO_ARITH>(a, x, y, blockIdx.z);
 }
 
 template <typename S, int GEO, int FEAT, bool PROBE>
@@ -42,10 +57,10 @@ __global__ void __launch_bounds__(256) k_step_odd(const StepArgs a) {
     double contrib[3] = {0.0, 0.0, 0.0};
     if constexpr (!PROBE) {
         if (x >= a.nx || y >= a.ny) return;
-        odd_cell<S, GEO, FEAT, false>(a, WallVel(a), x, y, blockIdx.z, contrib);
+        odd_cell<S, GEO, FEAT, false, false, STRO_ARITH>(a, WallVel(a), x, y, blockIdx.z, contrib);
     } else {
         if (x < a.nx && y < a.ny)
-            odd_cell<S, GEO, FEAT, true>(a, WallVel(a), x, y, blockIdx.z, contrib);
+            odd_cell<S, GEO, FEAT, true, false, STRO_ARITH>(a, WallVel(a), x, y, blockIdx.z, contrib);
         const uint32_t blk = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
         block_reduce_store<3>(contrib, a.partials + 3u * blk);
     }
@@ -59,7 +74,7 @@ __global__ void __launch_bounds__(128, 8) k_step_even_capped(const StepArgs a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= a.nx || y >= a.ny) return;
-    even_cell<S, 0, FEAT>(a, x, y, blockIdx.z);
+    even_cell<S, 0, FEAT, false, false, STRO_ARITH>(a, x, y, blockIdx.z);
 }
 
 template <typename S, int FEAT>
@@ -68,7 +83,7 @@ __global__ void __launch_bounds__(128, 8) k_step_odd_capped(const StepArgs a) {
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= a.nx || y >= a.ny) return;
     double contrib[3];
-    odd_cell<S, 0, FEAT, false>(a, WallVel(a), x, y, blockIdx.z, contrib);
+    odd_cell<S, 0, FEAT, false, false, STRO_ARITH>(a, WallVel(a), x, y, blockIdx.z, contrib);
 }
 
 template <typename S, int FEAT>
@@ -113,7 +128,7 @@ __global__ void __launch_bounds__(256) k_list_even(const StepArgs a, const uint3
     int x, y, z;
     list_block(list, gx, gy, x, y, z);
     if (x >= a.nx || y >= a.ny) return;
-    even_cell<S, GEO, FEAT>(a, x, y, z);
+    even_cell<S, GEO, FEAT, false, false, STRO_ARITH>(a, x, y, z);
 }
 
 template <typename S, int GEO, int FEAT>
@@ -123,7 +138,7 @@ __global__ void __launch_bounds__(256) k_list_odd(const StepArgs a, const uint32
     list_block(list, gx, gy, x, y, z);
     if (x >= a.nx || y >= a.ny) return;
     double contrib[3];
-    odd_cell<S, GEO, FEAT, false>(a, WallVel(a), x, y, z, contrib);
+    odd_cell<S, GEO, FEAT, false, false, STRO_ARITH>(a, WallVel(a), x, y, z, contrib);
 }
 
 template <typename S, int GEO, int FEAT>
@@ -189,8 +204,7 @@ cudaError_t launch_step(const StepArgs& a, int half_storage, int parity, int geo
     return launch_typed<float>(a, parity, geo, feat, probe, grid, block, st);
 }
 
-dim3 step_grid(const StepArgs& a, dim3 block) {
-    return dim3((a.nx + block.x - 1) / block.x, (a.ny + block.y - 1) / block.y, a.nz);
-}
+const StepLaunchers kStep = {&launch_step, &launch_step_capped, &launch_step_split};
 
+}  // namespace STRO_ARITH_NS
 }  // namespace stro

@@ -289,21 +289,25 @@ static int bulk_feat(const stro_sim* s) {
 cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool probe) {
     const int half = s->precision == STRO_FP16S ? 1 : 0;
     const int geo = geo_on(s) ? 1 : 0;
+    const bool fused = s->arith == STRO_ARITH_FUSED;
+    const StepLaunchers& L = fused ? fused::kStep : exact::kStep;
+    const RowsLaunchers& R = fused ? fused::kRows : exact::kRows;
     if (geo && !probe && s->variant == 0 && s->split && s->geo_host.size() == s->N) {
         if (ensure_block_lists(s) != STRO_OK) return cudaErrorMemoryAllocation;
-        return launch_step_split(a, half, int(t & 1), bulk_feat(s), feat_on(s), s->block,
-                                 s->d_blocks, s->nbulk, s->d_blocks + s->nbulk, s->nedge,
-                                 s->ctx->stream);
+        return L.split(a, half, int(t & 1), bulk_feat(s), feat_on(s), s->block, s->d_blocks,
+                       s->nbulk, s->d_blocks + s->nbulk, s->nedge, s->ctx->stream);
     }
-    if (s->variant == 1 && pair_step_supported(half, geo, probe, s->nx, s->plane, s->pair_block))
-        return launch_pair_step(a, int(t & 1), feat_on(s), s->pair_block, s->ctx->stream);
+    const PairLaunchers& PL = fused ? fused::kPair : exact::kPair;
+    if (s->variant == 1 && PL.supported(half, geo, probe, s->nx, s->plane, s->pair_block))
+        return PL.launch(a, int(t & 1), feat_on(s), s->pair_block, s->ctx->stream);
     if (s->variant == 3 && !geo && !probe && s->block.x * s->block.y <= 128)
-        return launch_step_capped(a, half, int(t & 1), feat_on(s), s->block, s->ctx->stream);
-    if (s->variant == 2 && rows_step_supported(half, geo, probe, s->nx, s->rows_threads))
-        return launch_rows_step(a, half, int(t & 1), feat_on(s), s->rows_threads,
-                                s->ctx->sm_count, s->d_error, s->ctx->stream);
-    return launch_step(a, half, int(t & 1), geo, feat_on(s), probe,
-                       probe ? s->probe_block : s->block, s->ctx->stream);
+        return L.capped(a, half, int(t & 1), feat_on(s), s->block, s->ctx->stream);
+    if (s->variant == 2 &&
+        R.supported(half, geo, probe, s->nx, s->ny, s->rows_threads, s->rows_per_tile))
+        return R.launch(a, half, int(t & 1), feat_on(s), s->rows_threads, s->rows_per_tile,
+                        s->ctx->sm_count, s->d_error, s->ctx->stream);
+    return L.step(a, half, int(t & 1), geo, feat_on(s), probe, probe ? s->probe_block : s->block,
+                  s->ctx->stream);
 }
 
 void ctx_retain(stro_ctx* c) { ++c->refs; }

@@ -66,9 +66,12 @@ struct stro_sim {
     dim3 block{256, 1, 1};        // launch shape of ordinary steps (autotunable)
     dim3 probe_block{256, 1, 1};  // fixed shape of force-probe steps: fixes the FP64 sum order
     int variant = 0;              // 0: one cell per thread; 1: FP16 x-pairs (lbm_pair.cu);
-                                  // 2: row streaming through shared memory (lbm_rows.cu)
+                                  // 2: rows staged through shared memory (lbm_rows.cu)
+                                  // 3: register-capped one cell per thread
     dim3 pair_block{128, 2, 1};   // launch shape of the pair variant
-    int rows_threads = 256;       // threads per block of the row-streaming variant
+    int rows_threads = 256;       // threads per block of the row-staged variant
+    int rows_per_tile = 1;        // lattice rows per tile of the row-staged variant
+    int arith = 0;                // STRO_ARITH_REFERENCE or STRO_ARITH_FUSED
     int* d_error = nullptr;       // device error word of the row-streaming variant
     // bulk / boundary block lists of a walled lattice for the current block shape
     bool split = true;

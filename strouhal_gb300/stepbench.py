@@ -18,8 +18,10 @@ def main(argv=None):
     ap.add_argument("--precision", default="fp16s", choices=["fp32", "fp16s"])
     ap.add_argument("--variant", type=int, default=-1, help="0, 1, 2, 3 or -1 = autotune")
     ap.add_argument("--block", type=int, nargs=2, default=None, metavar=("BX", "BY"),
-                    help="launch shape of variants 0 and 3")
+                    help="launch shape of variants 0 and 3; threads and rows per tile of variant 2")
     ap.add_argument("--trt", action="store_true", help="TRT Lambda=3/16 instead of SRT")
+    ap.add_argument("--arith", default="reference", choices=["reference", "fused"],
+                    help="step arithmetic (stro_sim_set_arithmetic)")
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=4)
     a = ap.parse_args(argv)
@@ -28,21 +30,24 @@ def main(argv=None):
     tau = 3 * 0.05 * L / 1600 + 0.5
     wp, wm = sg.trtOmegas(tau, 3.0 / 16.0 if a.trt else None)
     gpu = sg.GPU(0)
-    s = sg.Simulation(gpu, precision=a.precision, nx=n, ny=n, nz=n, omega=wp, omegaMinus=wm)
+    s = sg.Simulation(gpu, precision=a.precision, nx=n, ny=n, nz=n, omega=wp, omegaMinus=wm,
+                      arithmetic=a.arith)
     s.initField(2, 0.05)
     if a.variant < 0:
         s.autotune(steps=10)
     else:
         s.variant = a.variant
-        if a.block:
+        if a.block and a.variant == 2:
+            s.rowsTile = tuple(a.block)
+        elif a.block:
             s.block = tuple(a.block)
     s.run(a.warmup)
     t0 = s.gpuSeconds
     s.run(a.steps)
     dt = s.gpuSeconds - t0
-    bx, by = s.block
-    print("lattice %d^3 %s %s variant %d block %dx%d: %.4f ms/step, %.2f GLUPS"
-          % (n, a.precision, "TRT" if a.trt else "SRT", s.variant, bx, by,
+    bx, by = s.rowsTile if s.variant == 2 else s.block
+    print("lattice %d^3 %s %s %s variant %d block %dx%d: %.4f ms/step, %.2f GLUPS"
+          % (n, a.precision, "TRT" if a.trt else "SRT", a.arith, s.variant, bx, by,
              1e3 * dt / a.steps, s.cells * a.steps / dt / 1e9))
     s.close()
     gpu.close()

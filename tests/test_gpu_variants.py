@@ -9,17 +9,22 @@ pytestmark = pytest.mark.gpu
 
 
 VARIANT_CASES = [
-    # (variant, precision, nx, ny, nz)
-    (1, "fp16s", 64, 7, 5), (1, "fp16s", 128, 6, 4), (1, "fp16s", 192, 3, 3),
-    (2, "fp16s", 64, 7, 5), (2, "fp16s", 40, 6, 4), (2, "fp16s", 256, 3, 2), (2, "fp16s", 8, 9, 4),
-    (2, "fp32", 36, 7, 5), (2, "fp32", 128, 5, 3), (2, "fp32", 4, 6, 5),
-    (3, "fp16s", 37, 7, 5), (3, "fp32", 64, 6, 4),
+    # (variant, precision, nx, ny, nz, launch shape: block of variants 0/1/3,
+    #  (threads, rows per tile) of variant 2)
+    (1, "fp16s", 64, 7, 5, None), (1, "fp16s", 128, 6, 4, None), (1, "fp16s", 192, 3, 3, None),
+    (2, "fp16s", 64, 7, 5, (256, 1)), (2, "fp16s", 40, 6, 4, (128, 2)),
+    (2, "fp16s", 256, 3, 2, (256, 1)), (2, "fp16s", 256, 4, 2, (224, 2)),
+    (2, "fp16s", 256, 4, 3, (256, 4)), (2, "fp16s", 256, 2, 3, (64, 1)),
+    (2, "fp16s", 8, 9, 4, (32, 3)), (2, "fp16s", 24, 1, 3, (64, 1)),
+    (2, "fp32", 36, 7, 5, (64, 1)), (2, "fp32", 128, 6, 3, (96, 2)), (2, "fp32", 4, 6, 5, (32, 6)),
+    (2, "fp32", 256, 4, 2, (256, 2)),
+    (3, "fp16s", 37, 7, 5, (32, 4)), (3, "fp32", 64, 6, 4, (32, 4)),
 ]
 
 
-@pytest.mark.parametrize("variant,precision,nx,ny,nz", VARIANT_CASES)
+@pytest.mark.parametrize("variant,precision,nx,ny,nz,shape", VARIANT_CASES)
 @pytest.mark.parametrize("feature", ["plain", "force", "les", "sponge"])
-def test_variant_matches_oracle(gpu, oracle, variant, precision, nx, ny, nz, feature):
+def test_variant_matches_oracle(gpu, oracle, variant, precision, nx, ny, nz, shape, feature):
     import strouhal_gb300 as sg
 
     po = oracle
@@ -35,8 +40,10 @@ def test_variant_matches_oracle(gpu, oracle, variant, precision, nx, ny, nz, fea
         g.sponge = (nx * 0.6, nx * 0.3, 0.9)
         o.sponge = (nx * 0.6, nx * 0.3, 0.9)
     g.variant = variant
-    if variant == 3:
-        g.block = (32, 4)
+    if variant == 2:
+        g.rowsTile = shape
+    elif shape is not None:
+        g.block = shape
     rng = np.random.default_rng(nx * 31 + ny + variant)
     f0 = (rng.standard_normal((19, nx * ny * nz)) * 0.01).astype(o.f.dtype)
     g.uploadState(f0)
@@ -53,11 +60,15 @@ def test_variants_agree_bitwise(gpu, precision):
     import strouhal_gb300 as sg
 
     digests = []
-    for variant in ((0, 1, 2, 3) if precision == "fp16s" else (0, 2, 3)):
+    for variant, shape in ([(0, None), (1, None), (2, (256, 1)), (2, (256, 2)), (3, (64, 2))]
+                           if precision == "fp16s" else
+                           [(0, None), (2, (128, 1)), (2, (256, 4)), (3, (64, 2))]):
         s = sg.Simulation(gpu, precision=precision, nx=128, ny=40, nz=24, omega=1.95)
         s.variant = variant
-        if variant == 3:
-            s.block = (64, 2)
+        if variant == 2:
+            s.rowsTile = shape
+        elif shape is not None:
+            s.block = shape
         s.initField(2, 0.05)
         s.run(11)
         digests.append(s.stateDigest)
