@@ -41,9 +41,10 @@ U0 = 0.05
 RE = 1600.0
 STEPS_PER_BENCH_STEP = 100
 ALG_BYTES = {"fp32": 152, "fp16s": 76}  # 19 reads + 19 writes per cell per step
-# Kernels of each launch variant (stro_sim_set_variant), named as in the launch list.
-KERNEL_NAMES = {0: "k_step_even/k_step_odd", 1: "k_pair_even/k_pair_odd",
-                2: "k_rows<even>/k_rows<odd>", 3: "k_step_even_capped/k_step_odd_capped"}
+# Kernels of each launch path (Simulation.lastPath), named as in the launch list.
+KERNEL_NAMES = {"cell": "k_step_even/k_step_odd", "pair": "k_pair_even/k_pair_odd",
+                "rows": "k_rows<even>/k_rows<odd>",
+                "capped": "k_step_even_capped/k_step_odd_capped"}
 
 
 def tgv_params(n=N_EDGE, u0=U0, re=RE):
@@ -64,16 +65,17 @@ def measured_peak():
 
 
 def profile_traffic():
-    """DRAM bytes per cell per launch from the committed ncu summary, if any."""
+    """DRAM bytes per cell per launch (read + write, mean of the even and odd
+    pass) from the committed ncu summary: {(precision, path): bytes}."""
     path = os.path.join(ROOT, "profiles", "lbm_step_tgv256_ncu.md")
     out = {}
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_cell"):
-                # traffic_bytes_per_cell <variant> <bytes>
-                _, var, val = line.split()
-                out[var] = float(val)
-    except OSError:
+                # traffic_bytes_per_cell <precision> <path> <bytes>
+                _, prec, kpath, val = line.split()
+                out[(prec, kpath)] = float(val)
+    except (OSError, ValueError):
         pass
     return out
 
@@ -162,17 +164,19 @@ def allreduce(dist, value, op):
     return float(t.item())
 
 
-def run_variant(sg, gpu, precision, lam, steps, warmup, dist, clocks=None):
+def run_variant(sg, gpu, precision, lam, steps, warmup, dist, clocks=None, arithmetic="reference"):
     n = N_EDGE
     L, nu, tau = tgv_params()
     wp, wm = sg.trtOmegas(tau, lam)
-    sim = sg.Simulation(gpu, precision=precision, nx=n, ny=n, nz=n, omega=wp, omegaMinus=wm)
+    sim = sg.Simulation(gpu, precision=precision, nx=n, ny=n, nz=n, omega=wp, omegaMinus=wm,
+                        arithmetic=arithmetic)
     cells = sim.cells
     # ---- device-timed: kernels only, state resident in HBM
     sim.initField(2, U0)
     bx, by, _ = sim.autotune(steps=20)  # picks the kernel variant and launch shape (state restored)
-    tuned = {"variant": sim.variant, "block": [bx, by]}
     sim.run(warmup * STEPS_PER_BENCH_STEP)
+    tuned = {"variant": sim.variant, "shape": [bx, by], "path": sim.lastPath,
+             "arithmetic": sim.arithmetic}
     sim.kineticEnergySum()
     barrier(dist)
     t0 = sim.gpuSeconds
@@ -295,7 +299,11 @@ def main():
 
     gpu = sg.GPU(local)
     clocks = ClockSampler(local)
-    head = run_variant(sg, gpu, "fp16s", None, args.steps, args.warmup, dist, clocks)
+    # headline: FP16-storage SRT in the fused arithmetic (within the FP64 oracle's
+    # tolerances, bit-exact against the oracle's fused arithmetic)
+    head = run_variant(sg, gpu, "fp16s", None, args.steps, args.warmup, dist, clocks,
+                       arithmetic="fused")
+    ref16 = run_variant(sg, gpu, "fp16s", None, args.steps, args.warmup, dist)
     trt = run_variant(sg, gpu, "fp32", 3.0 / 16.0, args.steps, args.warmup, dist)
     peak, peak_kind = measured_peak()
     traffic = profile_traffic()
@@ -310,6 +318,7 @@ def main():
         return glups, total / e2e_wall / 1e9, per_launch, ach
 
     g16, e16, pl16, ach16 = summarise(head, "fp16s")
+    gr16, er16, plr16, achr16 = summarise(ref16, "fp16s")
     g32, e32, pl32, ach32 = summarise(trt, "fp32")
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -320,8 +329,9 @@ def main():
             cpu = {"value": None, "unit": "GLUPS", "error": str(exc)[:200]}
     if rank != 0:
         return 0
-    t16 = traffic.get("fp16s_srt")
-    t32 = traffic.get("fp32_trt")
+    t16 = traffic.get(("fp16s", head["tuned"]["path"]))
+    tr16 = traffic.get(("fp16s", ref16["tuned"]["path"]))
+    t32 = traffic.get(("fp32", trt["tuned"]["path"]))
     line = {
         "metric": "D3Q19 TGV Re=1600 256^3 step throughput (GLUPS)",
         "value": g16, "unit": "GLUPS", "n_gpus": ws, "steps": args.steps,
@@ -330,13 +340,14 @@ def main():
         "dtype": "f32",
         "data": "synthetic (analytic Taylor-Green initial field)",
         "config": {"workload": "TGV Re=1600 periodic 256^3, FP16-storage SRT, u0=0.05",
+                   "arithmetic": "fused (fused multiply-add form of the reference collision)",
                    "lattice": [N_EDGE] * 3, "lattice_steps_per_step": STEPS_PER_BENCH_STEP,
                    "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "inputs larger than L2 (state 637 MB fp16 / 1.27 GB fp32)"},
         "roofline": {"bound": "hbm", "achieved": ach16, "peak": peak, "unit": "GB/s",
                      "frac": ach16 / peak, "peak_source": peak_kind,
                      "traffic": None if t16 is None else t16 * head["cells"],
-                     "kernel": KERNEL_NAMES.get(head["tuned"]["variant"], "unknown"),
+                     "kernel": KERNEL_NAMES.get(head["tuned"]["path"], "unknown"),
                      "alg_bytes_per_cell": ALG_BYTES["fp16s"]},
         "e2e": {"value": e16, "unit": "GLUPS",
                 "h2d_bytes_per_step": head["state_bytes"] / args.steps,
@@ -345,9 +356,17 @@ def main():
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
         "variants": {
+            "fp16s_srt_reference_arith": {
+                "value": gr16, "unit": "GLUPS", "e2e": er16,
+                "roofline": {"achieved": achr16, "peak": peak, "frac": achr16 / peak,
+                             "traffic": None if tr16 is None else tr16 * ref16["cells"],
+                             "kernel": KERNEL_NAMES.get(ref16["tuned"]["path"], "unknown"),
+                             "alg_bytes_per_cell": ALG_BYTES["fp16s"]},
+                "ms_per_launch": 1e3 * plr16, "tuned": ref16["tuned"]},
             "fp32_trt": {"value": g32, "unit": "GLUPS", "e2e": e32,
                          "roofline": {"achieved": ach32, "peak": peak, "frac": ach32 / peak,
                                       "traffic": None if t32 is None else t32 * trt["cells"],
+                                      "kernel": KERNEL_NAMES.get(trt["tuned"]["path"], "unknown"),
                                       "alg_bytes_per_cell": ALG_BYTES["fp32"]},
                          "ms_per_launch": 1e3 * pl32, "tuned": trt["tuned"]},
             "fp16s_srt": {"ms_per_launch": 1e3 * pl16, "finite": head["finite"],

@@ -165,6 +165,15 @@ int stro_sim_get_variant(stro_sim* sim, int32_t* variant);
 enum { STRO_ARITH_REFERENCE = 0, STRO_ARITH_FUSED = 1 };
 int stro_sim_set_arithmetic(stro_sim* sim, int32_t arith);
 int stro_sim_get_arithmetic(stro_sim* sim, int32_t* arith);
+/* Launch shape of variant 1: bx threads (a multiple of 32 dividing nx/2, at
+ * most 256) covering 2*bx cells of one row; by must be 1. */
+int stro_sim_set_pair_block(stro_sim* sim, int32_t bx, int32_t by);
+int stro_sim_get_pair_block(stro_sim* sim, int32_t* bx, int32_t* by);
+/* Kernel path of the latest step launch: "cell" (one cell per thread),
+ * "split" (bulk / boundary block lists), "pair", "rows", "capped" or "probe";
+ * "" before the first step. A lattice a variant does not apply to reports the
+ * path that ran instead. */
+int stro_sim_last_path(stro_sim* sim, char* buf, size_t len);
 /* Launch shape of variant 2: `threads` computing threads per block (a
  * multiple of 32, at most 256; one more warp issues the copies) and `rows`
  * lattice rows per tile (1 to 8). */

@@ -106,6 +106,9 @@ def lib():
         "stro_sim_set_variant": ([_P, ctypes.c_int32], c_int),
         "stro_sim_set_rows_tile": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
         "stro_sim_set_arithmetic": ([_P, ctypes.c_int32], c_int),
+        "stro_sim_set_pair_block": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
+        "stro_sim_get_pair_block": ([_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)], c_int),
+        "stro_sim_last_path": ([_P, ctypes.c_char_p, ctypes.c_size_t], c_int),
         "stro_sim_get_arithmetic": ([_P, ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_get_rows_tile": ([_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_set_block_split": ([_P, ctypes.c_int32], c_int),
@@ -477,6 +480,24 @@ class Simulation:
         if v not in ARITHMETICS:
             raise ValueError("arithmetic must be one of %s" % (ARITHMETICS,))
         _check(lib().stro_sim_set_arithmetic(self._h, ARITHMETICS.index(v)))
+
+    @property
+    def pairBlock(self):
+        """(bx, 1): launch shape of the FP16 pair variant 1."""
+        bx, by = ctypes.c_int32(), ctypes.c_int32()
+        _check(lib().stro_sim_get_pair_block(self._h, ctypes.byref(bx), ctypes.byref(by)))
+        return bx.value, by.value
+
+    @pairBlock.setter
+    def pairBlock(self, v):
+        _check(lib().stro_sim_set_pair_block(self._h, int(v[0]), int(v[1])))
+
+    @property
+    def lastPath(self):
+        """Kernel path of the latest step launch (stro_sim_last_path)."""
+        buf = ctypes.create_string_buffer(32)
+        _check(lib().stro_sim_last_path(self._h, buf, 32))
+        return buf.value.decode()
 
     @property
     def rowsTile(self):

@@ -323,7 +323,8 @@ int tune_sim_shape(stro_sim* s, int64_t steps, int variant, dim3 cand, double* s
 
 const dim3 kShapes[] = {dim3(32, 8, 1), dim3(64, 4, 1), dim3(128, 2, 1), dim3(256, 1, 1),
                         dim3(16, 16, 1), dim3(32, 4, 1), dim3(64, 2, 1), dim3(128, 1, 1),
-                        dim3(16, 8, 1), dim3(64, 1, 1), dim3(96, 1, 1), dim3(192, 1, 1)};
+                        dim3(16, 8, 1), dim3(64, 1, 1), dim3(96, 1, 1), dim3(192, 1, 1),
+                        dim3(32, 1, 1)};
 // (threads, rows per tile) of the row-staged variant
 const dim3 kRowShapes[] = {dim3(128, 1, 1), dim3(256, 1, 1), dim3(128, 2, 1), dim3(256, 2, 1),
                            dim3(256, 4, 1), dim3(64, 1, 1)};
@@ -484,6 +485,27 @@ int stro_sim_set_variant(stro_sim* s, int32_t variant) {
 int stro_sim_set_block_split(stro_sim* s, int32_t enabled) {
     if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
     s->split = enabled != 0;
+    return STRO_OK;
+}
+
+int stro_sim_set_pair_block(stro_sim* s, int32_t bx, int32_t by) {
+    if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
+    if (bx < 32 || bx > 256 || bx % 32 != 0 || by != 1)
+        return fail(STRO_ERR_INVALID, "pair block: bx a multiple of 32 up to 256, by = 1");
+    s->pair_block = dim3(bx, by, 1);
+    return STRO_OK;
+}
+
+int stro_sim_get_pair_block(stro_sim* s, int32_t* bx, int32_t* by) {
+    if (!s || !bx || !by) return fail(STRO_ERR_INVALID, "null argument");
+    *bx = int32_t(s->pair_block.x);
+    *by = int32_t(s->pair_block.y);
+    return STRO_OK;
+}
+
+int stro_sim_last_path(stro_sim* s, char* buf, size_t len) {
+    if (!s || !buf || !len) return fail(STRO_ERR_INVALID, "null argument");
+    std::snprintf(buf, len, "%s", s->last_path);
     return STRO_OK;
 }
 

@@ -472,6 +472,17 @@ __device__ __forceinline__ float cell_u2(const float (&fh)[19], float Fx, float 
     return ux * ux + uy * uy + uz * uz;
 }
 
+// Register pressure fence: the pointer passes through an empty asm
+// statement, so addresses formed from it afterwards are computed afresh
+// instead of being kept alive from the loads. In both AA passes the stores go
+// to the very slots the loads came from, and keeping those 19 addresses (two
+// registers each) across the collision would cost more registers than
+// recomputing them costs instructions.
+template <typename P>
+__device__ __forceinline__ void forget_ptr(P& p) {
+    asm volatile("" : "+l"(p));
+}
+
 // Even (in-cell) pass of one cell, Kernels.metal:252-260. Non-fluid cells are
 // skipped. With LOG, u2 receives |u|^2 of the state before the step.
 template <typename S, int GEO, int FEAT, bool LOG = false, bool CG = false,
@@ -496,6 +507,7 @@ __device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z
     if constexpr (LOG) *u2 = cell_u2(fh, Fx, Fy, Fz);
     float ntx = 0.f, nty = 0.f, ntz = 0.f;
     collide<FEAT, ARITH>(fh, a, x, eps, Fx, Fy, Fz, ntx, nty, ntz);
+    forget_ptr(f);
     store_ddf<S>(f + n, fh[0]);
     sfor<1, 19>([&](auto I) { store_ddf<S>(f + uint64_t(opp(I)) * P + n, fh[I]); });
 }
@@ -555,6 +567,7 @@ __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, i
         ay += nty;
         az += ntz;
     }
+    forget_ptr(f);
     store_ddf<S>(f + n, fh[0]);
     if constexpr (GEO) {
         if (!(g & GEO_MOVING)) {

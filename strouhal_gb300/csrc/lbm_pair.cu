@@ -28,7 +28,10 @@
 // lbm_step.cu: STRO_ARITH=0 (stro::exact) and 1 (stro::fused); each copy
 // exports one PairLaunchers table. Requirements (checked by the host): FP16
 // storage, no walls or solid fractions, nx a multiple of 64, even plane
-// stride, block.x a multiple of 32 dividing nx/2, at most 256 threads.
+// stride, 19 planes below 2^32 elements (32-bit element indices), blocks of
+// one row (block.y = 1, so y and z come from the block index and the
+// neighbour-row offsets are block-uniform), block.x a multiple of 32 dividing
+// nx/2, at most 256 threads.
 #include "lbm_cell.cuh"
 #include "lbm_launch.h"
 
@@ -102,6 +105,7 @@ __device__ __forceinline__ void forget(P& p) {
     asm volatile("" : "+l"(p));
 }
 __device__ __forceinline__ void forget_int(int& v) { asm volatile("" : "+r"(v)); }
+__device__ __forceinline__ void forget_u32(uint32_t& v) { asm volatile("" : "+r"(v)); }
 
 // Cell x's post-collision direction i from the packed results.
 template <int I>
@@ -112,64 +116,83 @@ __device__ __forceinline__ __half out_lo(const __half2 (&ao)[10]) {
 template <int FEAT>
 __global__ void __launch_bounds__(256, FEAT == 2 ? 2 : 4) k_pair_even(const StepArgs a) {
     const int x = 2 * int(blockIdx.x * blockDim.x + threadIdx.x);
-    const int y = int(blockIdx.y * blockDim.y + threadIdx.y);
+    const int y = int(blockIdx.y);  // one row per block: y and z are block-uniform
     const int z = int(blockIdx.z);
-    if (y >= a.ny) return;
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
-    __half2* __restrict__ f2 = static_cast<__half2*>(a.f);
-    const uint64_t P2 = a.plane / 2;
-    const uint32_t n2 = n / 2;
+    // per-thread base pointer plus block-uniform plane offsets (32-bit: 19
+    // planes < 2^32 elements)
+    __half2* __restrict__ f2n = static_cast<__half2*>(a.f) + n / 2;
+    const uint32_t P2 = uint32_t(a.plane / 2);
     __half2 v[19];
-    sfor<0, 19>([&](auto I) { v[I] = f2[uint64_t(I) * P2 + n2]; });
+    sfor<0, 19>([&](auto I) { v[I] = f2n[uint32_t(I) * P2]; });
     __half2 ao[10];
     float fh[19];
     collide_pair<FEAT>(v, ao, fh, a, x, n);
-    forget(f2);
+    forget(f2n);
     // direction i of both cells goes to slot opp(i)
     sfor<0, 19>([&](auto I) {
-        f2[uint64_t(opp(I)) * P2 + n2] = __halves2half2(out_lo<I>(ao), __float2half_rn(fh[I]));
+        f2n[uint32_t(opp(I)) * P2] = __halves2half2(out_lo<I>(ao), __float2half_rn(fh[I]));
     });
 }
 
-// Odd-pass stores of a cell pair. The indices are formed again from (x, y, z)
-// after an opaque asm statement, so the gather's neighbour offsets do not
-// stay in registers across the two collisions.
+// Row indices (z * ny + y) of the block's row and its neighbour rows. One
+// row per block, so every value here is block-uniform.
+struct PairRows {
+    uint32_t ym, y0, yp, zm, z0, zp, ny;
+    __device__ __forceinline__ PairRows(const StepArgs& a) {
+        ny = uint32_t(a.ny);
+        const uint32_t y = blockIdx.y, z = blockIdx.z, nz = uint32_t(a.nz);
+        y0 = y;
+        ym = (y == 0) ? ny - 1 : y - 1;
+        yp = (y == ny - 1) ? 0 : y + 1;
+        z0 = z;
+        zm = (z == 0) ? nz - 1 : z - 1;
+        zp = (z == nz - 1) ? 0 : z + 1;
+    }
+    // row of the cell at (y + dy, z + dz)
+    template <int DY, int DZ>
+    __device__ __forceinline__ uint32_t row() const {
+        return (DZ > 0 ? zp : (DZ < 0 ? zm : z0)) * ny + (DY > 0 ? yp : (DY < 0 ? ym : y0));
+    }
+};
+
+// Odd-pass stores of a cell pair. Addresses are a per-thread base pointer
+// (the x part, formed again from x after an opaque asm statement so nothing
+// of the gather stays in registers across the collisions) plus a
+// block-uniform plane-and-row offset.
 __device__ __forceinline__ void scatter_pair(const StepArgs& a, const __half2 (&ao)[10],
-                                             const float (&fh)[19], int x, int y, int z) {
+                                             const float (&fh)[19], int x) {
     forget_int(x);
-    forget_int(y);
-    forget_int(z);
     const int lane = int(threadIdx.x & 31u);
-    const int nx = a.nx;
+    const uint32_t nx = uint32_t(a.nx), hnx = nx / 2;
     const int xw = x - 2 * lane;
-    const int x_left = wrap_x(xw - 1, nx);
-    const int x_right = wrap_x(xw + 64, nx);
-    const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(nx) + uint32_t(x);
-    const NbrOffsets nb(x, y, z, nx, a.ny, a.nz);
-    __half2* __restrict__ f2 = static_cast<__half2*>(a.f);
-    __half* __restrict__ f1 = static_cast<__half*>(a.f);
-    const uint64_t P = a.plane;
-    const uint64_t P2 = P / 2;
-    f2[n / 2] = __halves2half2(out_lo<0>(ao), __float2half_rn(fh[0]));
+    const PairRows rows(a);
+    const uint32_t P = uint32_t(a.plane), P2 = P / 2;
+    __half2* __restrict__ f2x = static_cast<__half2*>(a.f) + x / 2;
+    __half* __restrict__ f1x = static_cast<__half*>(a.f) + x;
+    __half* __restrict__ f1l = static_cast<__half*>(a.f) + wrap_x(xw - 1, int(nx));
+    __half* __restrict__ f1r = static_cast<__half*>(a.f) + wrap_x(xw + 64, int(nx));
+    f2x[rows.row<0, 0>() * hnx] = __halves2half2(out_lo<0>(ao), __float2half_rn(fh[0]));
     sfor<1, 19>([&](auto I) {
         constexpr int i = I;
-        // destination row of direction i (y, z shifted by +c_i), same x
-        const uint32_t d = uint32_t(int(n) + nb.template off<0, dcy(i), dcz(i)>());
-        const uint64_t base = uint64_t(i) * P;
-        const __half ah = out_lo<i>(ao);           // cell x, direction i
-        const __half bh = __float2half_rn(fh[i]);  // cell x+1, direction i
+        // destination row of direction i (y, z shifted by +c_i)
+        const uint32_t R = rows.row<dcy(i), dcz(i)>();
+        const uint32_t w2 = uint32_t(i) * P2 + R * hnx;  // word offset of the row start
+        const uint32_t w1 = uint32_t(i) * P + R * nx;    // element offset of the row start
+        const __half ah = out_lo<i>(ao);                 // cell x, direction i
+        const __half bh = __float2half_rn(fh[i]);        // cell x+1, direction i
         if constexpr (dcx(i) == 0) {
-            f2[uint64_t(i) * P2 + d / 2] = __halves2half2(ah, bh);
+            f2x[w2] = __halves2half2(ah, bh);
         } else if constexpr (dcx(i) > 0) {  // destinations x+1, x+2
             const __half lo = __shfl_up_sync(0xffffffffu, bh, 1);
-            if (lane != 0) f2[uint64_t(i) * P2 + d / 2] = __halves2half2(lo, ah);
-            else f1[base + d + 1] = ah;
-            if (lane == 31) f1[base + (d - uint32_t(x) + uint32_t(x_right))] = bh;
+            if (lane != 0) f2x[w2] = __halves2half2(lo, ah);
+            else f1x[w1 + 1] = ah;
+            if (lane == 31) f1r[w1] = bh;
         } else {  // destinations x-1, x
             const __half hi = __shfl_down_sync(0xffffffffu, ah, 1);
-            if (lane != 31) f2[uint64_t(i) * P2 + d / 2] = __halves2half2(bh, hi);
-            else f1[base + d] = bh;
-            if (lane == 0) f1[base + (d - uint32_t(x) + uint32_t(x_left))] = ah;
+            if (lane != 31) f2x[w2] = __halves2half2(bh, hi);
+            else f1x[w1] = bh;
+            if (lane == 0) f1l[w1] = ah;
         }
     });
 }
@@ -178,46 +201,38 @@ template <int FEAT>
 __global__ void __launch_bounds__(256, FEAT == 2 ? 2 : 4) k_pair_odd(const StepArgs a) {
     const int lane = int(threadIdx.x & 31u);
     const int x = 2 * int(blockIdx.x * blockDim.x + threadIdx.x);
-    const int y = int(blockIdx.y * blockDim.y + threadIdx.y);
-    const int z = int(blockIdx.z);
-    if (y >= a.ny) return;  // whole warps share y: no shuffle loses a lane
-    const int nx = a.nx;
-    const int xw = x - 2 * lane;              // first cell of this warp
-    const int x_left = wrap_x(xw - 1, nx);    // element left of the warp
-    const int x_right = wrap_x(xw + 64, nx);  // element right of the warp
-    const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(nx) + uint32_t(x);
-    const NbrOffsets nb(x, y, z, nx, a.ny, a.nz);
-    __half2* __restrict__ f2 = static_cast<__half2*>(a.f);
-    __half* __restrict__ f1 = static_cast<__half*>(a.f);
-    const uint64_t P = a.plane;
-    const uint64_t P2 = P / 2;
+    const uint32_t nx = uint32_t(a.nx), hnx = nx / 2;
+    const int xw = x - 2 * lane;  // first cell of this warp
+    const PairRows rows(a);
+    const uint32_t P = uint32_t(a.plane), P2 = P / 2;
+    const __half2* __restrict__ f2x = static_cast<const __half2*>(a.f) + x / 2;
+    const __half* __restrict__ f1l = static_cast<const __half*>(a.f) + wrap_x(xw - 1, int(nx));
+    const __half* __restrict__ f1r = static_cast<const __half*>(a.f) + wrap_x(xw + 64, int(nx));
     __half2 v[19];
-    v[0] = f2[n / 2];
+    v[0] = f2x[rows.row<0, 0>() * hnx];
     sfor<1, 19>([&](auto I) {
         constexpr int i = I;
         constexpr int o = opp(i);
         // source row of direction i (y, z shifted by -c_i), same x
-        const uint32_t r = uint32_t(int(n) + nb.template off<0, -dcy(i), -dcz(i)>());
-        const __half2 w = f2[uint64_t(o) * P2 + r / 2];
+        const uint32_t R = rows.row<-dcy(i), -dcz(i)>();
+        const __half2 w = f2x[uint32_t(o) * P2 + R * hnx];
         if constexpr (dcx(i) == 0) {
             v[i] = w;
         } else if constexpr (dcx(i) > 0) {  // sources x-1, x
             const __half2 left = __shfl_up_sync(0xffffffffu, w, 1);
-            const __half lo = lane == 0 ? f1[uint64_t(o) * P + (r - uint32_t(x) + uint32_t(x_left))]
-                                        : __high2half(left);
+            const __half lo = lane == 0 ? f1l[uint32_t(o) * P + R * nx] : __high2half(left);
             v[i] = __halves2half2(lo, __low2half(w));
         } else {  // sources x+1, x+2
             const __half2 right = __shfl_down_sync(0xffffffffu, w, 1);
-            const __half hi = lane == 31
-                                  ? f1[uint64_t(o) * P + (r - uint32_t(x) + uint32_t(x_right))]
-                                  : __low2half(right);
+            const __half hi = lane == 31 ? f1r[uint32_t(o) * P + R * nx] : __low2half(right);
             v[i] = __halves2half2(__high2half(w), hi);
         }
     });
+    const uint32_t n = rows.row<0, 0>() * nx + uint32_t(x);
     __half2 ao[10];
     float fh[19];
     collide_pair<FEAT>(v, ao, fh, a, x, n);
-    scatter_pair(a, ao, fh, x, y, z);
+    scatter_pair(a, ao, fh, x);
 }
 
 }  // namespace
@@ -225,12 +240,12 @@ __global__ void __launch_bounds__(256, FEAT == 2 ? 2 : 4) k_pair_odd(const StepA
 bool pair_step_supported(int half_storage, int geo, bool probe, int nx, uint64_t plane,
                          dim3 block) {
     return half_storage && !geo && !probe && nx % 64 == 0 && plane % 2 == 0 && block.x % 32 == 0 &&
-           (nx / 2) % int(block.x) == 0 && block.x * block.y <= 256;
+           (nx / 2) % int(block.x) == 0 && block.y == 1 && block.x <= 256 &&
+           19 * plane < (uint64_t(1) << 32);  // element indices fit 32 bits
 }
 
 cudaError_t launch_pair_step(const StepArgs& a, int parity, int feat, dim3 block, cudaStream_t st) {
-    const dim3 grid(unsigned(a.nx / 2) / block.x, (unsigned(a.ny) + block.y - 1) / block.y,
-                    unsigned(a.nz));
+    const dim3 grid(unsigned(a.nx / 2) / block.x, unsigned(a.ny), unsigned(a.nz));
     if (parity == 0) {
         if (feat == 2) k_pair_even<2><<<grid, block, 0, st>>>(a);
         else if (feat == 1) k_pair_even<1><<<grid, block, 0, st>>>(a);

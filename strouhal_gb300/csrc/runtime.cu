@@ -294,18 +294,26 @@ cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool prob
     const RowsLaunchers& R = fused ? fused::kRows : exact::kRows;
     if (geo && !probe && s->variant == 0 && s->split && s->geo_host.size() == s->N) {
         if (ensure_block_lists(s) != STRO_OK) return cudaErrorMemoryAllocation;
+        s->last_path = "split";
         return L.split(a, half, int(t & 1), bulk_feat(s), feat_on(s), s->block, s->d_blocks,
                        s->nbulk, s->d_blocks + s->nbulk, s->nedge, s->ctx->stream);
     }
     const PairLaunchers& PL = fused ? fused::kPair : exact::kPair;
-    if (s->variant == 1 && PL.supported(half, geo, probe, s->nx, s->plane, s->pair_block))
+    if (s->variant == 1 && PL.supported(half, geo, probe, s->nx, s->plane, s->pair_block)) {
+        s->last_path = "pair";
         return PL.launch(a, int(t & 1), feat_on(s), s->pair_block, s->ctx->stream);
-    if (s->variant == 3 && !geo && !probe && s->block.x * s->block.y <= 128)
+    }
+    if (s->variant == 3 && !geo && !probe && s->block.x * s->block.y <= 128) {
+        s->last_path = "capped";
         return L.capped(a, half, int(t & 1), feat_on(s), s->block, s->ctx->stream);
+    }
     if (s->variant == 2 &&
-        R.supported(half, geo, probe, s->nx, s->ny, s->rows_threads, s->rows_per_tile))
+        R.supported(half, geo, probe, s->nx, s->ny, s->rows_threads, s->rows_per_tile)) {
+        s->last_path = "rows";
         return R.launch(a, half, int(t & 1), feat_on(s), s->rows_threads, s->rows_per_tile,
                         s->ctx->sm_count, s->d_error, s->ctx->stream);
+    }
+    s->last_path = probe ? "probe" : "cell";
     return L.step(a, half, int(t & 1), geo, feat_on(s), probe, probe ? s->probe_block : s->block,
                   s->ctx->stream);
 }
@@ -424,9 +432,9 @@ int stro_sim_create(stro_ctx* ctx, const stro_sim_desc* d, const uint8_t* flags,
     s->probe_block = s->block;
     if (d->precision == STRO_FP16S && d->nx % 64 == 0) {
         // FP16 lattices with whole warps of cell pairs per row default to the pair variant
-        int bxp = std::min(128, d->nx / 2);
+        int bxp = std::min(256, d->nx / 2);
         while ((d->nx / 2) % bxp != 0) bxp -= 32;
-        s->pair_block = dim3(bxp, 256 / bxp, 1);
+        s->pair_block = dim3(bxp, 1, 1);
         s->variant = 1;
     }
     try {

@@ -68,7 +68,8 @@ struct stro_sim {
     int variant = 0;              // 0: one cell per thread; 1: FP16 x-pairs (lbm_pair.cu);
                                   // 2: rows staged through shared memory (lbm_rows.cu)
                                   // 3: register-capped one cell per thread
-    dim3 pair_block{128, 2, 1};   // launch shape of the pair variant
+    dim3 pair_block{32, 1, 1};    // launch shape of the pair variant (one row per block)
+    const char* last_path = "";   // kernel path of the latest step launch (test hook)
     int rows_threads = 256;       // threads per block of the row-staged variant
     int rows_per_tile = 1;        // lattice rows per tile of the row-staged variant
     int arith = 0;                // STRO_ARITH_REFERENCE or STRO_ARITH_FUSED

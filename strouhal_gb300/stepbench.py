@@ -18,7 +18,7 @@ def main(argv=None):
     ap.add_argument("--precision", default="fp16s", choices=["fp32", "fp16s"])
     ap.add_argument("--variant", type=int, default=-1, help="0, 1, 2, 3 or -1 = autotune")
     ap.add_argument("--block", type=int, nargs=2, default=None, metavar=("BX", "BY"),
-                    help="launch shape of variants 0 and 3; threads and rows per tile of variant 2")
+                    help="launch shape of variants 0, 1 and 3; threads and rows per tile of variant 2")
     ap.add_argument("--trt", action="store_true", help="TRT Lambda=3/16 instead of SRT")
     ap.add_argument("--arith", default="reference", choices=["reference", "fused"],
                     help="step arithmetic (stro_sim_set_arithmetic)")
@@ -39,15 +39,17 @@ def main(argv=None):
         s.variant = a.variant
         if a.block and a.variant == 2:
             s.rowsTile = tuple(a.block)
+        elif a.block and a.variant == 1:
+            s.pairBlock = tuple(a.block)
         elif a.block:
             s.block = tuple(a.block)
     s.run(a.warmup)
     t0 = s.gpuSeconds
     s.run(a.steps)
     dt = s.gpuSeconds - t0
-    bx, by = s.rowsTile if s.variant == 2 else s.block
-    print("lattice %d^3 %s %s %s variant %d block %dx%d: %.4f ms/step, %.2f GLUPS"
-          % (n, a.precision, "TRT" if a.trt else "SRT", a.arith, s.variant, bx, by,
+    bx, by = {1: s.pairBlock, 2: s.rowsTile}.get(s.variant, s.block)
+    print("lattice %d^3 %s %s %s variant %d (%s) block %dx%d: %.4f ms/step, %.2f GLUPS"
+          % (n, a.precision, "TRT" if a.trt else "SRT", a.arith, s.variant, s.lastPath, bx, by,
              1e3 * dt / a.steps, s.cells * a.steps / dt / 1e9))
     s.close()
     gpu.close()

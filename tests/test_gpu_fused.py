@@ -92,6 +92,8 @@ def test_fused_variants_match_fused_oracle(gpu, oracle, variant, shape, kind, fe
         g.run(chunk)
         o.run(chunk)
         assert np.array_equal(g.downloadState(), o.f), chunk
+    expect = {0: "cell", 1: "pair" if kind == 1 else "cell", 2: "rows", 3: "capped"}[variant]
+    assert g.lastPath == expect, g.lastPath
     g.close()
 
 

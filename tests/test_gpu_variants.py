@@ -11,7 +11,9 @@ pytestmark = pytest.mark.gpu
 VARIANT_CASES = [
     # (variant, precision, nx, ny, nz, launch shape: block of variants 0/1/3,
     #  (threads, rows per tile) of variant 2)
-    (1, "fp16s", 64, 7, 5, None), (1, "fp16s", 128, 6, 4, None), (1, "fp16s", 192, 3, 3, None),
+    (1, "fp16s", 64, 7, 5, (32, 1)), (1, "fp16s", 128, 6, 4, (64, 1)),
+    (1, "fp16s", 192, 3, 3, (96, 1)), (1, "fp16s", 256, 3, 2, (128, 1)),
+    (1, "fp16s", 512, 2, 2, (256, 1)), (1, "fp16s", 128, 5, 3, None),
     (2, "fp16s", 64, 7, 5, (256, 1)), (2, "fp16s", 40, 6, 4, (128, 2)),
     (2, "fp16s", 256, 3, 2, (256, 1)), (2, "fp16s", 256, 4, 2, (224, 2)),
     (2, "fp16s", 256, 4, 3, (256, 4)), (2, "fp16s", 256, 2, 3, (64, 1)),
@@ -20,6 +22,9 @@ VARIANT_CASES = [
     (2, "fp32", 256, 4, 2, (256, 2)),
     (3, "fp16s", 37, 7, 5, (32, 4)), (3, "fp32", 64, 6, 4, (32, 4)),
 ]
+
+
+PATHS = {0: "cell", 1: "pair", 2: "rows", 3: "capped"}
 
 
 @pytest.mark.parametrize("variant,precision,nx,ny,nz,shape", VARIANT_CASES)
@@ -42,6 +47,8 @@ def test_variant_matches_oracle(gpu, oracle, variant, precision, nx, ny, nz, sha
     g.variant = variant
     if variant == 2:
         g.rowsTile = shape
+    elif variant == 1 and shape is not None:
+        g.pairBlock = shape
     elif shape is not None:
         g.block = shape
     rng = np.random.default_rng(nx * 31 + ny + variant)
@@ -52,6 +59,7 @@ def test_variant_matches_oracle(gpu, oracle, variant, precision, nx, ny, nz, sha
         g.run(chunk)
         o.run(chunk)
         assert np.array_equal(g.downloadState(), o.f), chunk
+    assert g.lastPath == PATHS[variant], g.lastPath  # the variant's own kernel ran
     g.close()
 
 
@@ -71,6 +79,7 @@ def test_variants_agree_bitwise(gpu, precision):
             s.block = shape
         s.initField(2, 0.05)
         s.run(11)
+        assert s.lastPath == PATHS[variant], (variant, s.lastPath)
         digests.append(s.stateDigest)
         s.close()
     assert len(set(digests)) == 1
