@@ -121,6 +121,18 @@ def test_batched_ladder_reproduces_sequential():
             assert r[mode]["max_trace_rel_diff"] < 1e-12
 
 
+def test_batched_small_rungs_beat_sequential():
+    """Rungs too small to fill the GPU alone (edges 16-32): one batched launch
+    per round against per-rung launches; identical states and traces."""
+    r = rec("ladder_small")
+    assert max(i["n"] for i in r["instances"]) <= 32
+    for mode in ("persistent", "rounds"):
+        assert r[mode]["identical_states"]
+        assert r[mode]["max_trace_rel_diff"] < 1e-12
+    assert max(r["persistent"]["speedup_vs_sequential"],
+               r["rounds"]["speedup_vs_sequential"]) >= 3.0
+
+
 def test_adjoint_cost_and_gradients():
     r = rec("sphere_adjoint")
     assert r["grad_finite"]
