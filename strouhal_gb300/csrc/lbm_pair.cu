@@ -16,12 +16,14 @@
 // Even pass: all accesses are aligned half2.
 // Odd pass: directions with c_x = 0 stay aligned half2. For c_x = +1 the
 // sources are x-1 and x: the thread loads the aligned pair (x, x+1) of the
-// source row and takes x-1 from the lane below (shfl.up); lane 0 reads the one
-// element left of the warp (wrapping at x = 0) directly. c_x = -1 mirrors this
-// with shfl.down and lane 31. Stores are the transpose: each lane writes the
-// aligned pair it covers with the value shuffled in from its neighbour, and
-// the lane at the warp edge writes the single element that belongs to the
-// neighbouring warp's pair. Every slot is still read and written exactly once.
+// source row and the aligned pair (x-2, x-1) to its left (wrapping at the row
+// start) and keeps one half of each; c_x = -1 mirrors this with (x+2, x+3).
+// The second word is the neighbouring thread's own word, so it is served by
+// L1 and costs no DRAM traffic. The x-shifted results are stored as two 2-byte
+// stores per thread (cell x to x+c_x, cell x+1 to x+1+c_x, wrapping at the
+// row ends): wide loads matter for bandwidth, store width does not. No lane
+// exchange and no warp-edge special case. Every slot is still written exactly
+// once.
 //
 // The per-cell arithmetic is the shared collide(), so results are identical to
 // the one-cell kernels of the same arithmetic. Compiled twice like
@@ -163,51 +165,50 @@ struct PairRows {
 __device__ __forceinline__ void scatter_pair(const StepArgs& a, const __half2 (&ao)[10],
                                              const float (&fh)[19], int x) {
     forget_int(x);
-    const int lane = int(threadIdx.x & 31u);
     const uint32_t nx = uint32_t(a.nx), hnx = nx / 2;
-    const int xw = x - 2 * lane;
     const PairRows rows(a);
     const uint32_t P = uint32_t(a.plane), P2 = P / 2;
     __half2* __restrict__ f2x = static_cast<__half2*>(a.f) + x / 2;
-    __half* __restrict__ f1x = static_cast<__half*>(a.f) + x;
-    __half* __restrict__ f1l = static_cast<__half*>(a.f) + wrap_x(xw - 1, int(nx));
-    __half* __restrict__ f1r = static_cast<__half*>(a.f) + wrap_x(xw + 64, int(nx));
+    __half* __restrict__ f1 = static_cast<__half*>(a.f);
+    // x-shifted destinations of the two cells (periodic in x): x-1 and x+2 wrap
+    __half* __restrict__ f1m = f1 + wrap_x(x - 1, int(nx));  // cell x,   c_x = -1
+    __half* __restrict__ f1a = f1 + (x + 1);                 // cell x,   c_x = +1
+    __half* __restrict__ f1b = f1 + x;                       // cell x+1, c_x = -1
+    __half* __restrict__ f1p = f1 + wrap_x(x + 2, int(nx));  // cell x+1, c_x = +1
     f2x[rows.row<0, 0>() * hnx] = __halves2half2(out_lo<0>(ao), __float2half_rn(fh[0]));
     sfor<1, 19>([&](auto I) {
         constexpr int i = I;
         // destination row of direction i (y, z shifted by +c_i)
         const uint32_t R = rows.row<dcy(i), dcz(i)>();
-        const uint32_t w2 = uint32_t(i) * P2 + R * hnx;  // word offset of the row start
-        const uint32_t w1 = uint32_t(i) * P + R * nx;    // element offset of the row start
-        const __half ah = out_lo<i>(ao);                 // cell x, direction i
-        const __half bh = __float2half_rn(fh[i]);        // cell x+1, direction i
+        const __half ah = out_lo<i>(ao);           // cell x, direction i
+        const __half bh = __float2half_rn(fh[i]);  // cell x+1, direction i
         if constexpr (dcx(i) == 0) {
-            f2x[w2] = __halves2half2(ah, bh);
-        } else if constexpr (dcx(i) > 0) {  // destinations x+1, x+2
-            const __half lo = __shfl_up_sync(0xffffffffu, bh, 1);
-            if (lane != 0) f2x[w2] = __halves2half2(lo, ah);
-            else f1x[w1 + 1] = ah;
-            if (lane == 31) f1r[w1] = bh;
-        } else {  // destinations x-1, x
-            const __half hi = __shfl_down_sync(0xffffffffu, ah, 1);
-            if (lane != 31) f2x[w2] = __halves2half2(bh, hi);
-            else f1x[w1] = bh;
-            if (lane == 0) f1l[w1] = ah;
+            f2x[uint32_t(i) * P2 + R * hnx] = __halves2half2(ah, bh);
+        } else {
+            // two 2-byte stores: the warp's stores of one direction fill a
+            // contiguous 64-element span between them, no lane exchange
+            const uint32_t w1 = uint32_t(i) * P + R * nx;  // element offset of the row start
+            if constexpr (dcx(i) > 0) {
+                f1a[w1] = ah;
+                f1p[w1] = bh;
+            } else {
+                f1m[w1] = ah;
+                f1b[w1] = bh;
+            }
         }
     });
 }
 
 template <int FEAT>
 __global__ void __launch_bounds__(256, FEAT == 2 ? 2 : 4) k_pair_odd(const StepArgs a) {
-    const int lane = int(threadIdx.x & 31u);
     const int x = 2 * int(blockIdx.x * blockDim.x + threadIdx.x);
     const uint32_t nx = uint32_t(a.nx), hnx = nx / 2;
-    const int xw = x - 2 * lane;  // first cell of this warp
     const PairRows rows(a);
-    const uint32_t P = uint32_t(a.plane), P2 = P / 2;
-    const __half2* __restrict__ f2x = static_cast<const __half2*>(a.f) + x / 2;
-    const __half* __restrict__ f1l = static_cast<const __half*>(a.f) + wrap_x(xw - 1, int(nx));
-    const __half* __restrict__ f1r = static_cast<const __half*>(a.f) + wrap_x(xw + 64, int(nx));
+    const uint32_t P2 = uint32_t(a.plane) / 2;
+    const __half2* __restrict__ f2 = static_cast<const __half2*>(a.f);
+    const __half2* __restrict__ f2x = f2 + x / 2;
+    const __half2* __restrict__ f2l = f2 + wrap_x(x - 2, int(nx)) / 2;  // word (x-2, x-1)
+    const __half2* __restrict__ f2r = f2 + wrap_x(x + 2, int(nx)) / 2;  // word (x+2, x+3)
     __half2 v[19];
     v[0] = f2x[rows.row<0, 0>() * hnx];
     sfor<1, 19>([&](auto I) {
@@ -215,17 +216,14 @@ __global__ void __launch_bounds__(256, FEAT == 2 ? 2 : 4) k_pair_odd(const StepA
         constexpr int o = opp(i);
         // source row of direction i (y, z shifted by -c_i), same x
         const uint32_t R = rows.row<-dcy(i), -dcz(i)>();
-        const __half2 w = f2x[uint32_t(o) * P2 + R * hnx];
+        const uint32_t w2 = uint32_t(o) * P2 + R * hnx;
+        const __half2 w = f2x[w2];
         if constexpr (dcx(i) == 0) {
             v[i] = w;
         } else if constexpr (dcx(i) > 0) {  // sources x-1, x
-            const __half2 left = __shfl_up_sync(0xffffffffu, w, 1);
-            const __half lo = lane == 0 ? f1l[uint32_t(o) * P + R * nx] : __high2half(left);
-            v[i] = __halves2half2(lo, __low2half(w));
+            v[i] = __halves2half2(__high2half(f2l[w2]), __low2half(w));
         } else {  // sources x+1, x+2
-            const __half2 right = __shfl_down_sync(0xffffffffu, w, 1);
-            const __half hi = lane == 31 ? f1r[uint32_t(o) * P + R * nx] : __low2half(right);
-            v[i] = __halves2half2(__high2half(w), hi);
+            v[i] = __halves2half2(__high2half(w), __low2half(f2r[w2]));
         }
     });
     const uint32_t n = rows.row<0, 0>() * nx + uint32_t(x);
