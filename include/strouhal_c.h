@@ -280,6 +280,27 @@ int stro_disk_solid_fractions(int32_t nx, int32_t ny, double cx, double cy, doub
 int stro_sphere_solid_fractions(int32_t nx, int32_t ny, int32_t nz, double cx, double cy,
                                 double cz, double r, int32_t sub, float* out);
 
+/* ---- triangle meshes (StlVoxels.swift) ---------------------------------------
+ * StlMesh(binarySTL:) (StlVoxels.swift:11-43): the triangle count of a binary
+ * STL, then the triangles (count x 9 floats: three vertices) and the bounds
+ * (min xyz, max xyz). Errors as the reference: "STL too short", "ASCII STL not
+ * supported (binary only)", "STL truncated (or ASCII; binary only)". */
+int stro_stl_triangle_count(const uint8_t* data, size_t len, uint32_t* count);
+int stro_stl_parse(const uint8_t* data, size_t len, float* tris, float bounds[6]);
+/* sphereSTLData (StlVoxels.swift:120-143): a lat-long sphere as binary STL.
+ * With out = NULL only *len (the byte count) is returned. */
+int stro_sphere_stl(float radius, int32_t segments, int32_t rings, uint8_t* out, size_t cap,
+                    size_t* len);
+/* meshSolidFractions (StlVoxels.swift:52-117) on the GPU: Noble-Torczynski
+ * fractions of a closed mesh by parity ray casting along +x with 2x2 sub-rays
+ * per cell; lattice coordinates = vertex * scale + offset (cell centres at
+ * integers). eps: host array of nx*ny*nz floats. seconds (optional): device
+ * time of the ray kernel. Fails if one sub-ray crosses the mesh more than 128
+ * times. */
+int stro_mesh_solid_fractions(stro_ctx* ctx, const float* tris, uint32_t ntri, int32_t nx,
+                              int32_t ny, int32_t nz, float scale, const float offset[3],
+                              float* eps, double* seconds);
+
 #ifdef __cplusplus
 }
 #endif

@@ -848,6 +848,82 @@ int orc_adjoint_force(const double* f0, const uint8_t* flags, const uint32_t* so
     return 0;
 }
 
+// Noble-Torczynski solid fractions of a closed triangle mesh by parity ray
+// casting along +x, StlVoxels.swift:52-117: 2x2 sub-rays per (y, z) cell,
+// exact interior x-spans, coverage accumulated per sub-ray in (sy, sz) order,
+// clamped to 1. tris: ntri x 9 floats (three vertices, mesh coordinates);
+// lattice coordinates are vertex * scale + offset, cell centres at integers.
+// FP32 throughout, operations in the reference's order (no contraction).
+// Returns 0.
+int orc_mesh_solid_fractions(const float* tris, int ntri, int nx, int ny, int nz, float scale,
+                             const float offset[3], float* eps) {
+    struct P3 { float x, y, z; };
+    std::vector<P3> t(size_t(ntri) * 3);
+    for (size_t k = 0; k < t.size(); ++k) {
+        t[k].x = tris[3 * k + 0] * scale + offset[0];
+        t[k].y = tris[3 * k + 1] * scale + offset[1];
+        t[k].z = tris[3 * k + 2] * scale + offset[2];
+    }
+    std::vector<std::vector<int>> buckets(size_t(ny) * nz);
+    for (int i = 0; i < ntri; ++i) {
+        const P3 &a = t[3 * i], &b = t[3 * i + 1], &c = t[3 * i + 2];
+        const int ylo = std::max(0, int(std::floor(std::min(std::min(a.y, b.y), c.y) - 0.5f)));
+        const int yhi = std::min(ny - 1, int(std::ceil(std::max(std::max(a.y, b.y), c.y) + 0.5f)));
+        const int zlo = std::max(0, int(std::floor(std::min(std::min(a.z, b.z), c.z) - 0.5f)));
+        const int zhi = std::min(nz - 1, int(std::ceil(std::max(std::max(a.z, b.z), c.z) + 0.5f)));
+        if (ylo > yhi || zlo > zhi) continue;
+        for (int z = zlo; z <= zhi; ++z)
+            for (int y = ylo; y <= yhi; ++y) buckets[size_t(z) * ny + y].push_back(i);
+    }
+    std::fill(eps, eps + size_t(nx) * ny * nz, 0.0f);
+    const int sub = 2;
+    std::vector<float> xs;
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y) {
+            const std::vector<int>& cands = buckets[size_t(z) * ny + y];
+            if (cands.empty()) continue;
+            for (int sy = 0; sy < sub; ++sy)
+                for (int sz = 0; sz < sub; ++sz) {
+                    const float ry = float(y) - 0.5f + (float(sy) + 0.5f) / float(sub);
+                    const float rz = float(z) - 0.5f + (float(sz) + 0.5f) / float(sub);
+                    xs.clear();
+                    for (int i : cands) {
+                        const P3 &a = t[3 * i], &b = t[3 * i + 1], &c = t[3 * i + 2];
+                        const float d1x = b.y - a.y, d1y = b.z - a.z;
+                        const float d2x = c.y - a.y, d2y = c.z - a.z;
+                        const float denom = d1x * d2y - d1y * d2x;
+                        if (std::fabs(denom) < 1e-12f) continue;  // ray-parallel triangle
+                        const float px = ry - a.y, py = rz - a.z;
+                        const float u = (px * d2y - py * d2x) / denom;
+                        const float v = (d1x * py - d1y * px) / denom;
+                        if (u < 0.0f || v < 0.0f || u + v > 1.0f) continue;
+                        xs.push_back(a.x + u * (b.x - a.x) + v * (c.x - a.x));
+                    }
+                    if (xs.size() < 2) continue;
+                    std::sort(xs.begin(), xs.end());
+                    size_t k = 0;
+                    while (k + 1 < xs.size()) {
+                        if (xs[k + 1] - xs[k] < 1e-5f) {  // grazing hit
+                            k += 1;
+                            continue;
+                        }
+                        const float x0 = xs[k], x1 = xs[k + 1];
+                        k += 2;
+                        const int c0 = std::max(0, int(std::floor(x0 + 0.5f)));
+                        const int c1 = std::min(nx - 1, int(std::floor(x1 + 0.5f)));
+                        for (int x = c0; x <= c1; ++x) {
+                            const float lo = float(x) - 0.5f, hi = float(x) + 0.5f;
+                            const float cover = std::min(x1, hi) - std::max(x0, lo);
+                            if (cover > 0.0f)
+                                eps[(size_t(z) * ny + y) * nx + x] += cover / float(sub * sub);
+                        }
+                    }
+                }
+        }
+    for (size_t i = 0; i < size_t(nx) * ny * nz; ++i) eps[i] = std::min(eps[i], 1.0f);
+    return 0;
+}
+
 // Sum of all 19*N shifted DDFs in index order, in double (Sim.swift:447-458).
 double orc_mass(int kind, const void* f, size_t count) {
     double total = 0.0;

@@ -60,6 +60,8 @@ def lib():
         L.orc_adjoint_force.argtypes = [_P, _P, _P, _P, _P, ctypes.c_int, _P, _P, _P, _P, _P, _P,
                                         _P]
         L.orc_mass.argtypes = [ctypes.c_int, _P, ctypes.c_size_t]
+        L.orc_mesh_solid_fractions.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_int, ctypes.c_float, _P, _P]
         L.orc_mass.restype = ctypes.c_double
         _lib = L
     return _lib
@@ -284,3 +286,14 @@ class OracleSim:
     @property
     def stateDigest(self):
         return hashlib.sha256(self.f.tobytes()).hexdigest()
+
+
+def mesh_solid_fractions(tris, nx, ny, nz, scale, offset):
+    """Restatement of meshSolidFractions (StlVoxels.swift:52-117); tris is a
+    (count, 3, 3) array of mesh-space vertices."""
+    t = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 9)
+    off = np.ascontiguousarray(offset, dtype=np.float32).reshape(3)
+    out = np.zeros(int(nx) * int(ny) * int(nz), np.float32)
+    lib().orc_mesh_solid_fractions(_ptr(t) if t.size else None, t.shape[0], nx, ny, nz,
+                                   float(np.float32(scale)), _ptr(off), _ptr(out))
+    return out

@@ -138,6 +138,13 @@ def lib():
         "stro_host_free": ([_P], c_int),
         "stro_disk_solid_fractions": ([ctypes.c_int32, ctypes.c_int32, c_double, c_double,
                                        c_double, _P], c_int),
+        "stro_stl_triangle_count": ([_P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint32)], c_int),
+        "stro_stl_parse": ([_P, ctypes.c_size_t, _P, _P], c_int),
+        "stro_sphere_stl": ([c_float, ctypes.c_int32, ctypes.c_int32, _P, ctypes.c_size_t,
+                             ctypes.POINTER(ctypes.c_size_t)], c_int),
+        "stro_mesh_solid_fractions": ([_P, _P, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.c_int32, c_float, _P, _P,
+                                       ctypes.POINTER(c_double)], c_int),
         "stro_sphere_solid_fractions": ([ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                          c_double, c_double, c_double, c_double, ctypes.c_int32,
                                          _P], c_int),
@@ -689,3 +696,44 @@ def sphereSolidFractions(nx, ny, nz, cx, cy, cz, r, sub=8):
     out = np.zeros(nx * ny * nz, np.float32)
     _check(lib().stro_sphere_solid_fractions(nx, ny, nz, cx, cy, cz, r, sub, out.ctypes.data))
     return out
+
+
+class StlMesh:
+    """Binary-STL triangle soup (StlVoxels.swift:6-43): `triangles` is a
+    (count, 3, 3) float32 array of vertices, `boundsMin` / `boundsMax` the
+    componentwise bounds."""
+
+    def __init__(self, binarySTL):
+        data = bytes(binarySTL)
+        buf = ctypes.create_string_buffer(data, len(data))
+        n = ctypes.c_uint32()
+        _check(lib().stro_stl_triangle_count(buf, len(data), ctypes.byref(n)))
+        tris = np.zeros((n.value, 3, 3), np.float32)
+        bounds = np.zeros(6, np.float32)
+        _check(lib().stro_stl_parse(buf, len(data), tris.ctypes.data, bounds.ctypes.data))
+        self.triangles = tris
+        self.boundsMin = bounds[:3].copy()
+        self.boundsMax = bounds[3:].copy()
+
+
+def sphereSTLData(radius, segments=48, rings=24):
+    """StlVoxels.swift:120-143: a lat-long sphere as binary STL bytes."""
+    n = ctypes.c_size_t()
+    _check(lib().stro_sphere_stl(radius, segments, rings, None, 0, ctypes.byref(n)))
+    out = ctypes.create_string_buffer(n.value)
+    _check(lib().stro_sphere_stl(radius, segments, rings, out, n.value, ctypes.byref(n)))
+    return out.raw
+
+
+def meshSolidFractions(gpu, mesh, nx, ny, nz, scale, offset, timing=False):
+    """StlVoxels.swift:52-117 on the GPU. `mesh` is an StlMesh or a (count, 3, 3)
+    triangle array; returns nx*ny*nz float32 fractions (and the device seconds
+    of the ray kernel with timing=True)."""
+    tris = np.ascontiguousarray(getattr(mesh, "triangles", mesh), dtype=np.float32).reshape(-1, 9)
+    off = np.ascontiguousarray(offset, dtype=np.float32).reshape(3)
+    out = np.zeros(int(nx) * int(ny) * int(nz), np.float32)
+    sec = ctypes.c_double()
+    _check(lib().stro_mesh_solid_fractions(gpu._h, tris.ctypes.data if tris.size else None,
+                                           tris.shape[0], nx, ny, nz, scale, off.ctypes.data,
+                                           out.ctypes.data, ctypes.byref(sec)))
+    return (out, sec.value) if timing else out

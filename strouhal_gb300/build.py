@@ -36,6 +36,7 @@ SOURCES = [
     ("runtime.cu", "runtime.o", []),
     ("batch.cu", "batch.o", []),
     ("adjoint.cu", "adjoint.o", []),
+    ("voxel.cu", "voxel.o", []),
     ("sha256.cpp", "sha256.o", []),
 ]
 

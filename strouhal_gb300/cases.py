@@ -12,6 +12,7 @@ names: poiseuille, tg_order, cavity, dfg2, dfg2_adjoint, tgv, sphere,
 sphere_adjoint, ladder.
 """
 import argparse
+import hashlib
 import json
 import math
 import time
@@ -366,6 +367,31 @@ def ladder(gpu, count=32, seed=1234, precision="fp32",
     return results
 
 
+# ------------------------------------------------------ STL voxelizer
+def stl_voxelize(gpu, nx=512, ny=256, nz=256, D=48, segments=256, rings=128, repeats=3):
+    """meshSolidFractions (StlVoxels.swift:52-117) on the GPU for the sphere
+    wake's body: a lat-long sphere STL of diameter D cells centred at
+    (128, ny/2, nz/2) of the 512x256x256 lattice. Reports the device time of
+    the ray kernel, the end-to-end call time (host bucketing and transfers
+    included), and the volume against the analytic sphere."""
+    mesh = sg.StlMesh(sg.sphereSTLData(1.0, segments, rings))
+    off = np.array([128.0, ny / 2.0, nz / 2.0], np.float32)
+    scale = D / 2.0
+    dev, wall = [], []
+    eps = None
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        eps, sec = sg.meshSolidFractions(gpu, mesh, nx, ny, nz, scale, off, timing=True)
+        wall.append(time.perf_counter() - t0)
+        dev.append(sec)
+    ana = sg.sphereSolidFractions(nx, ny, nz, 128.0, ny / 2.0, nz / 2.0, D / 2.0)
+    vol, vol_a = float(eps.astype(np.float64).sum()), float(ana.astype(np.float64).sum())
+    return {"lattice": [nx, ny, nz], "triangles": int(len(mesh.triangles)),
+            "kernel_seconds": min(dev), "call_seconds": min(wall),
+            "volume": vol, "volume_analytic": vol_a, "volume_rel_err": abs(vol - vol_a) / vol_a,
+            "digest": hashlib.sha256(eps.tobytes()).hexdigest()}
+
+
 # ------------------------------------------------------------ adjoints
 def _dfg2_sim(gpu, D, uin_max, nz, precision, ramp, sponge_d=3, sponge_tau=1.0):
     nx = 22 * D + 2
@@ -472,7 +498,7 @@ def sphere_adjoint(gpu, nx=512, ny=256, nz=256, D=48, u=0.05, re=300.0, cs=0.1, 
 
 CASES = {"poiseuille": poiseuille, "tg_order": tg_order, "cavity": cavity, "dfg2": dfg2,
          "dfg2_adjoint": dfg2_adjoint, "tgv": tgv, "sphere": sphere,
-         "sphere_adjoint": sphere_adjoint, "ladder": ladder}
+         "sphere_adjoint": sphere_adjoint, "ladder": ladder, "stl_voxelize": stl_voxelize}
 
 
 def main(argv=None):

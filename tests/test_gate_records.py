@@ -133,6 +133,25 @@ def test_batched_small_rungs_beat_sequential():
                r["rounds"]["speedup_vs_sequential"]) >= 3.0
 
 
+def test_voxelizer_record_equals_oracle():
+    """The GPU voxelization of the sphere wake's body at full size (512x256x256,
+    65,024 triangles) hashed to the same SHA-256 as the oracle's restatement,
+    recomputed here on the CPU."""
+    import hashlib
+
+    import numpy as np
+
+    import strouhal_gb300 as sg
+    from oracle import pyoracle as po
+
+    r = rec("stl_voxelize")
+    mesh = sg.StlMesh(sg.sphereSTLData(1.0, 256, 128))
+    eps = po.mesh_solid_fractions(mesh.triangles, 512, 256, 256, 24.0,
+                                  np.array([128.0, 128.0, 128.0], np.float32))
+    assert hashlib.sha256(eps.tobytes()).hexdigest() == r["digest"]
+    assert r["volume_rel_err"] < 0.01
+
+
 def test_adjoint_cost_and_gradients():
     r = rec("sphere_adjoint")
     assert r["grad_finite"]
