@@ -133,6 +133,13 @@ int stro_sim_dissipation(stro_sim* sim, double* sum_eps);
 /* Simulation.stateDigest (Sim.swift:441-444): SHA-256 of the raw state bytes,
  * 64 lowercase hex chars + NUL. */
 int stro_sim_digest(stro_sim* sim, char hex[65]);
+/* The |u| colormap of slice z (colorize, Kernels.metal:465-500) into a
+ * caller array of nx*ny RGBA binary16 texels (uint16 bit patterns), row y
+ * written at ny-1-y as the reference's texture write. The velocity is formed
+ * from the slice's DDFs as Simulation.probeMoments forms it (even step counts
+ * only). Headless: no window, swapchain or graphics API. seconds (optional):
+ * device time of the render kernel. */
+int stro_sim_render_slice(stro_sim* sim, int32_t z, float uref, uint16_t* rgba, double* seconds);
 /* Simulation.massSum (Sim.swift:447-458): sum of all 19*N slots in FP64. */
 int stro_sim_mass(stro_sim* sim, double* total);
 /* 1 if every DDF is finite, else 0 (failure detection, Cases.swift:1250-1252). */

@@ -924,6 +924,52 @@ int orc_mesh_solid_fractions(const float* tris, int ntri, int nx, int ny, int nz
     return 0;
 }
 
+// The |u| colormap of one z slice, colorize + speedColor (Kernels.metal:465-500):
+// moments4 = N float4 (momentsEven output), out = nx*ny*4 binary16 values
+// (RGBA, row y written at ny-1-y). Walls and cells with eps >= 0.5 are slate;
+// other cells take the four-stop map of clamp(|u| / uref, 0, 1), blended toward
+// slate by eps when 0 < eps < 0.5. Vector mixes are a + (b - a) t in float; the
+// half blend is evaluated in float and rounded once. Returns 0.
+int orc_colorize(const float* moments4, const uint8_t* flags, const float* eps, int nx, int ny,
+                 int z_slice, float uref, int use_eps, uint16_t* out) {
+    typedef _Float16 h16;
+    auto mix3 = [](const float* a, const float* b, float t, float* o) {
+        for (int k = 0; k < 3; ++k) o[k] = a[k] + (b[k] - a[k]) * t;
+    };
+    const float c0[3] = {float(0.055), float(0.045), float(0.040)};
+    const float c1[3] = {float(0.420), float(0.100), float(0.050)};
+    const float c2[3] = {float(0.900), float(0.450), float(0.100)};
+    const float c3[3] = {float(1.000), float(0.930), float(0.780)};
+    const h16 slate[3] = {h16(float(0.30L)), h16(float(0.28L)), h16(float(0.25L))};
+    for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x) {
+            const size_t n = (size_t(z_slice) * ny + y) * nx + x;
+            const float e = use_eps ? eps[n] : 0.0f;
+            h16 rgb[3];
+            if (flags[n] != FLUID || e >= 0.5f) {
+                rgb[0] = slate[0]; rgb[1] = slate[1]; rgb[2] = slate[2];
+            } else {
+                const float* u = moments4 + 4 * n;
+                const float len = std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+                const float s = std::fmin(std::fmax(len / uref, 0.0f), 1.0f);
+                float c[3];
+                if (s < 0.35f) mix3(c0, c1, s / 0.35f, c);
+                else if (s < 0.70f) mix3(c1, c2, (s - 0.35f) / 0.35f, c);
+                else mix3(c2, c3, (s - 0.70f) / 0.30f, c);
+                for (int k = 0; k < 3; ++k) rgb[k] = h16(c[k]);
+                if (e > 0.0f) {
+                    const float t = float(h16(e));
+                    for (int k = 0; k < 3; ++k)
+                        rgb[k] = h16(float(rgb[k]) + (float(slate[k]) - float(rgb[k])) * t);
+                }
+            }
+            const size_t o = 4 * (size_t(ny - 1 - y) * nx + x);
+            const h16 px[4] = {rgb[0], rgb[1], rgb[2], h16(1.0f)};
+            std::memcpy(out + o, px, sizeof px);
+        }
+    return 0;
+}
+
 // Sum of all 19*N shifted DDFs in index order, in double (Sim.swift:447-458).
 double orc_mass(int kind, const void* f, size_t count) {
     double total = 0.0;

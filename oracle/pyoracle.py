@@ -62,6 +62,8 @@ def lib():
         L.orc_mass.argtypes = [ctypes.c_int, _P, ctypes.c_size_t]
         L.orc_mesh_solid_fractions.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                ctypes.c_int, ctypes.c_float, _P, _P]
+        L.orc_colorize.argtypes = [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_float, ctypes.c_int, _P]
         L.orc_mass.restype = ctypes.c_double
         _lib = L
     return _lib
@@ -79,6 +81,7 @@ def ref_lib():
         L.ref_step.argtypes = [ctypes.c_int, _P, _P, _P, _P, _P, _P, _P]
         L.ref_moments.argtypes = [ctypes.c_int, _P, _P, _P, _P]
         L.ref_init_field.argtypes = [ctypes.c_int, _P, _P]
+        L.ref_colorize.argtypes = [_P, _P, _P, _P, _P]
         _ref = L
     return _ref
 
@@ -296,4 +299,25 @@ def mesh_solid_fractions(tris, nx, ny, nz, scale, offset):
     out = np.zeros(int(nx) * int(ny) * int(nz), np.float32)
     lib().orc_mesh_solid_fractions(_ptr(t) if t.size else None, t.shape[0], nx, ny, nz,
                                    float(np.float32(scale)), _ptr(off), _ptr(out))
+    return out
+
+
+def colorize(moments4, flags, eps, nx, ny, z_slice, uref, backend="oracle"):
+    """The |u| colormap of slice z (Kernels.metal:465-500) as an (ny, nx, 4)
+    float16 RGBA image, rows as the kernel writes them (y flipped). moments4:
+    (N, 4) float32 momentsEven output; flags: N uint8; eps: N float32 or None.
+    backend "ref" runs the reference's own kernel source."""
+    m = np.ascontiguousarray(moments4, dtype=np.float32).reshape(-1, 4)
+    fl = np.ascontiguousarray(flags, dtype=np.uint8).reshape(-1)
+    e = None if eps is None else np.ascontiguousarray(eps, dtype=np.float32).reshape(-1)
+    out = np.zeros((int(ny), int(nx), 4), np.float16)
+    if backend == "ref":
+        import struct as _st
+        # VizParams {nx, ny, nz, zSlice, uref, useEps, pad0, pad1}, Kernels.metal:458-463
+        vp = _st.pack("<4IfI2f", nx, ny, fl.size // (nx * ny), z_slice, float(uref),
+                      0 if e is None else 1, 0.0, 0.0)
+        ref_lib().ref_colorize(_ptr(m), _ptr(fl), _ptr(e), vp, _ptr(out))
+    else:
+        lib().orc_colorize(_ptr(m), _ptr(fl), _ptr(e), nx, ny, z_slice, float(uref),
+                           0 if e is None else 1, _ptr(out))
     return out

@@ -25,6 +25,8 @@ namespace ref_f16 {
 
 static_assert(sizeof(ref_f32::Params) == 80, "Params is 20 x 4 B (Kernels.metal:49-63)");
 static_assert(sizeof(ref_f32::InitParams) == 32, "InitParams is 8 x 4 B (Kernels.metal:386-391)");
+static_assert(sizeof(ref_f32::VizParams) == 32, "VizParams is 8 x 4 B (Kernels.metal:458-463)");
+static_assert(sizeof(metal::half4) == 8, "half4 is four binary16 values");
 
 extern "C" {
 
@@ -79,6 +81,23 @@ int ref_init_field(int half_storage, void* f, const void* init_params) {
         const uint32_t N = p.nx * p.ny * p.nz;
         for (uint32_t n = 0; n < N; ++n) ref_f32::initField(static_cast<float*>(f), p, n);
     }
+    return 0;
+}
+
+// One `colorize` dispatch (Kernels.metal:476-500) over gid in [0,nx) x [0,ny):
+// moments4 holds N float4 (momentsEven output), viz_params is the 32-byte
+// VizParams {nx, ny, nz, zSlice, uref, useEps, pad, pad}, out receives the
+// nx*ny half4 image (y flipped as the kernel writes it).
+int ref_colorize(const float* moments4, const uint8_t* flags, const float* eps,
+                 const void* viz_params, uint16_t* out_half4) {
+    const auto& v = *static_cast<const ref_f32::VizParams*>(viz_params);
+    metal::texture2d<metal::half, metal::access::write> tex;
+    tex.data = reinterpret_cast<metal::half4*>(out_half4);
+    tex.width = v.nx;
+    for (uint32_t y = 0; y < v.ny; ++y)
+        for (uint32_t x = 0; x < v.nx; ++x)
+            ref_f32::colorize(reinterpret_cast<const metal::float4*>(moments4), flags, eps, v, tex,
+                              metal::uint2(x, y));
     return 0;
 }
 

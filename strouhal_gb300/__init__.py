@@ -106,6 +106,7 @@ def lib():
         "stro_sim_set_variant": ([_P, ctypes.c_int32], c_int),
         "stro_sim_set_rows_tile": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
         "stro_sim_set_arithmetic": ([_P, ctypes.c_int32], c_int),
+        "stro_sim_render_slice": ([_P, ctypes.c_int32, c_float, _P, ctypes.POINTER(c_double)], c_int),
         "stro_sim_set_pair_block": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
         "stro_sim_get_pair_block": ([_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_last_path": ([_P, ctypes.c_char_p, ctypes.c_size_t], c_int),
@@ -447,6 +448,15 @@ class Simulation:
         v = ctypes.c_double()
         _check(lib().stro_sim_mass(self._h, ctypes.byref(v)))
         return v.value
+
+    def renderSlice(self, z, uref, timing=False):
+        """The |u| colormap of slice z (Kernels.metal:465-500) as an (ny, nx, 4)
+        float16 RGBA image, rows as the reference's texture write (y flipped)."""
+        out = np.zeros((self.ny, self.nx, 4), np.float16)
+        sec = ctypes.c_double()
+        _check(lib().stro_sim_render_slice(self._h, int(z), float(uref), out.ctypes.data,
+                                           ctypes.byref(sec)))
+        return (out, sec.value) if timing else out
 
     def checkFinite(self):
         v = ctypes.c_int()

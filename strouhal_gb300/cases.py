@@ -367,6 +367,54 @@ def ladder(gpu, count=32, seed=1234, precision="fp32",
     return results
 
 
+# ------------------------------------------------------ colormap buffer
+def render(gpu, nx=512, ny=256, nz=256, D=48, steps=200, repeats=5, out_png=None):
+    """Headless |u| colormap (colorize, Kernels.metal:465-500) of the sphere
+    wake's mid slice after `steps` steps: device time of the render kernel,
+    whole-call time (with the image read back), and the image's SHA-256.
+    With out_png the image is written as an 8-bit PNG (no graphics API)."""
+    flags = np.zeros((nz, ny, nx), np.uint8)
+    flags[:, :, 0] = flags[:, :, -1] = sg.Cell.inflow
+    nu = 0.05 * D / 300.0
+    wp, _ = sg.trtOmegas(3.0 * nu + 0.5, None)
+    s = sg.Simulation(gpu, precision="fp16s", nx=nx, ny=ny, nz=nz, omega=wp, uin=0.05,
+                      rampSteps=100, cSmago=0.01, flags=flags.reshape(-1))
+    s.inflowUniform = True
+    s.setSolidFractions(sg.sphereSolidFractions(nx, ny, nz, 128.0, ny / 2.0, nz / 2.0, D / 2.0, 8))
+    s.run(steps)
+    dev, wall = [], []
+    img = None
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        img, sec = s.renderSlice(nz // 2, 0.08, timing=True)
+        wall.append(time.perf_counter() - t0)
+        dev.append(sec)
+    s.close()
+    if out_png:
+        _write_png(out_png, img)
+    return {"lattice": [nx, ny, nz], "slice": nz // 2, "pixels": nx * ny,
+            "kernel_seconds": min(dev), "call_seconds": min(wall),
+            "digest": hashlib.sha256(img.tobytes()).hexdigest()}
+
+
+def _write_png(path, img):
+    """8-bit RGB PNG of an (h, w, 4) float image in [0, 1] (zlib, no imaging library)."""
+    import struct
+    import zlib
+
+    rgb = np.clip(np.rint(img[..., :3].astype(np.float32) * 255.0), 0, 255).astype(np.uint8)
+    h, w = rgb.shape[:2]
+    raw = b"".join(b"\x00" + rgb[y].tobytes() for y in range(h))
+
+    def chunk(tag, data):
+        c = struct.pack(">I", len(data)) + tag + data
+        return c + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
+
+    with open(path, "wb") as fh:
+        fh.write(b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0))
+                 + chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b""))
+
+
 # ------------------------------------------------------ STL voxelizer
 def stl_voxelize(gpu, nx=512, ny=256, nz=256, D=48, segments=256, rings=128, repeats=3):
     """meshSolidFractions (StlVoxels.swift:52-117) on the GPU for the sphere
@@ -498,7 +546,8 @@ def sphere_adjoint(gpu, nx=512, ny=256, nz=256, D=48, u=0.05, re=300.0, cs=0.1, 
 
 CASES = {"poiseuille": poiseuille, "tg_order": tg_order, "cavity": cavity, "dfg2": dfg2,
          "dfg2_adjoint": dfg2_adjoint, "tgv": tgv, "sphere": sphere,
-         "sphere_adjoint": sphere_adjoint, "ladder": ladder, "stl_voxelize": stl_voxelize}
+         "sphere_adjoint": sphere_adjoint, "ladder": ladder, "stl_voxelize": stl_voxelize,
+         "render": render}
 
 
 def main(argv=None):

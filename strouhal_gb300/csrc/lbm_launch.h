@@ -83,6 +83,9 @@ int reduction_blocks(uint64_t count);
 cudaError_t launch_init_field(const FieldView& v, int half_storage, uint32_t mode,
                               float amplitude, float tau, cudaStream_t st);
 cudaError_t launch_moments(const FieldView& v, int half_storage, float4* out, cudaStream_t st);
+// |u| colormap of slice z into nx*ny RGBA binary16 texels (colorize, Kernels.metal:476-500).
+cudaError_t launch_render(const FieldView& v, int half_storage, const float* eps, uint32_t z,
+                          float uref, __half* out, cudaStream_t st);
 // out[0] = sum |u|^2, out[1] = sum 2 nu S:S (lattice units)
 cudaError_t launch_observables(const FieldView& v, int half_storage, float omega,
                                double* partials, double* out, cudaStream_t st);

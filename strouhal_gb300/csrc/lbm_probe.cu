@@ -116,6 +116,60 @@ __global__ void __launch_bounds__(kThreads) k_moments(FieldView v, float4* out) 
     out[n] = make_float4(ux, uy, uz, rho);
 }
 
+// The |u| colormap of one z slice (colorize + speedColor, Kernels.metal:465-500)
+// fused with momentsEven: the velocity is formed from the slice's own DDFs
+// exactly as k_moments forms it, so the image equals colorize applied to the
+// moments probe. Walls and cells with eps >= 0.5 are slate; other cells take
+// the four-stop map of clamp(|u| / uref, 0, 1) and, for 0 < eps < 0.5, a blend
+// toward slate by eps (the half-vector mix evaluated in float and rounded
+// once). out: nx*ny RGBA binary16 texels, row y at ny-1-y as the reference's
+// texture write.
+template <typename S>
+__global__ void k_render(FieldView v, const float* eps, uint32_t z, float uref, __half* out) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= v.nx || y >= v.ny) return;
+    const uint32_t n = (z * v.ny + y) * v.nx + x;
+    const uint8_t flag = v.cell != nullptr ? (v.cell[n] & CELL_TYPE_MASK) : CELL_FLUID;
+    const float e = eps != nullptr ? eps[n] : 0.0f;
+    const __half slate[3] = {__float2half_rn(0.30f), __float2half_rn(0.28f), __float2half_rn(0.25f)};
+    __half rgb[3];
+    if (flag != CELL_FLUID || e >= 0.5f) {
+        rgb[0] = slate[0]; rgb[1] = slate[1]; rgb[2] = slate[2];
+    } else {
+        float fh[19];
+        load_cell<S>(v, n, fh);
+        float rhom1, rho, ux, uy, uz;
+        cell_moments(v, n, fh, rhom1, rho, ux, uy, uz);
+        const float len = sqrtf(ux * ux + uy * uy + uz * uz);
+        const float s = fminf(fmaxf(len / uref, 0.0f), 1.0f);
+        // ember map: charcoal -> deep red -> orange -> pale amber
+        const float c0[3] = {(float)0.055, (float)0.045, (float)0.040};
+        const float c1[3] = {(float)0.420, (float)0.100, (float)0.050};
+        const float c2[3] = {(float)0.900, (float)0.450, (float)0.100};
+        const float c3[3] = {(float)1.000, (float)0.930, (float)0.780};
+        const float* a;
+        const float* b;
+        float t;
+        if (s < 0.35f) { a = c0; b = c1; t = s / 0.35f; }
+        else if (s < 0.70f) { a = c1; b = c2; t = (s - 0.35f) / 0.35f; }
+        else { a = c2; b = c3; t = (s - 0.70f) / 0.30f; }
+        for (int k = 0; k < 3; ++k) rgb[k] = __float2half_rn(a[k] + (b[k] - a[k]) * t);
+        if (e > 0.0f) {
+            const float te = __half2float(__float2half_rn(e));
+            for (int k = 0; k < 3; ++k) {
+                const float c = __half2float(rgb[k]);
+                rgb[k] = __float2half_rn(c + (__half2float(slate[k]) - c) * te);
+            }
+        }
+    }
+    __half* px = out + 4 * (size_t(v.ny - 1 - y) * v.nx + x);
+    px[0] = rgb[0];
+    px[1] = rgb[1];
+    px[2] = rgb[2];
+    px[3] = __float2half_rn(1.0f);
+}
+
 // Per cell: |u|^2 (FP32, as the host energy loop forms it) and the viscous
 // dissipation 2 nu S:S with S = -(3 omega / (2 rho)) Pi_neq.
 template <typename S>
@@ -220,6 +274,15 @@ cudaError_t launch_moments(const FieldView& v, int half_storage, float4* out, cu
     const unsigned grid = (v.N + kThreads - 1) / kThreads;
     if (half_storage) k_moments<__half><<<grid, kThreads, 0, st>>>(v, out);
     else k_moments<float><<<grid, kThreads, 0, st>>>(v, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_render(const FieldView& v, int half_storage, const float* eps, uint32_t z,
+                          float uref, __half* out, cudaStream_t st) {
+    const dim3 block(32, 8);
+    const dim3 grid((v.nx + 31) / 32, (v.ny + 7) / 8);
+    if (half_storage) k_render<__half><<<grid, block, 0, st>>>(v, eps, z, uref, out);
+    else k_render<float><<<grid, block, 0, st>>>(v, eps, z, uref, out);
     return cudaGetLastError();
 }
 

@@ -187,6 +187,7 @@ void free_sim(stro_sim* s) {
     cudaFree(s->d_geo);
     cudaFree(s->d_lmask);
     cudaFree(s->d_eps);
+    cudaFree(s->d_render);
     cudaFree(s->d_ffield);
     cudaFree(s->d_moments);
     cudaFree(s->d_partials);
@@ -643,6 +644,37 @@ int stro_sim_moments(stro_sim* s, float* out4) {
     STRO_CUDA(cudaMemcpyAsync(out4, s->d_moments, s->N * sizeof(float4), cudaMemcpyDeviceToHost,
                               s->ctx->stream));
     STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    return STRO_OK;
+}
+
+int stro_sim_render_slice(stro_sim* s, int32_t z, float uref, uint16_t* rgba, double* seconds) {
+    CHECK_SIM(s);
+    if (!rgba) return fail(STRO_ERR_INVALID, "null output");
+    if (z < 0 || z >= s->nz) return fail(STRO_ERR_INVALID, "slice outside the lattice");
+    if (!(uref > 0.0f)) return fail(STRO_ERR_INVALID, "uref must be positive");
+    if (s->steps_done % 2 != 0)
+        return fail(STRO_ERR_STATE, "rendering requires an even step count");
+    cudaSetDevice(s->ctx->device);
+    cudaStream_t st = s->ctx->stream;
+    const size_t bytes = size_t(s->nx) * size_t(s->ny) * 4 * sizeof(__half);
+    if (s->render_bytes < bytes) {
+        cudaFree(s->d_render);
+        s->d_render = nullptr;
+        s->render_bytes = 0;
+        STRO_CUDA(cudaMalloc(&s->d_render, bytes));
+        s->render_bytes = bytes;
+    }
+    STRO_CUDA(cudaEventRecord(s->ev0, st));
+    STRO_CUDA(launch_render(field_view(s), s->precision == STRO_FP16S, s->d_eps, uint32_t(z), uref,
+                            static_cast<__half*>(s->d_render), st));
+    STRO_CUDA(cudaEventRecord(s->ev1, st));
+    STRO_CUDA(cudaMemcpyAsync(rgba, s->d_render, bytes, cudaMemcpyDeviceToHost, st));
+    STRO_CUDA(cudaStreamSynchronize(st));
+    if (seconds) {
+        float ms = 0.0f;
+        STRO_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+        *seconds = double(ms) * 1e-3;
+    }
     return STRO_OK;
 }
 

@@ -54,6 +54,8 @@ struct stro_sim {
     uint32_t* d_geo = nullptr;
     uint32_t* d_lmask = nullptr;
     float* d_eps = nullptr;
+    void* d_render = nullptr;     // RGBA binary16 image of the latest rendered slice
+    size_t render_bytes = 0;
     float* d_ffield = nullptr;
     float4* d_moments = nullptr;
     double* d_partials = nullptr;
