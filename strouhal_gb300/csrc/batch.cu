@@ -149,9 +149,9 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
             ramp_off[k] = ramp.size();
             for (int64_t r = 0; r < I.steps; ++r) ramp.push_back(ramp_factor(s, I.t0 + r));
         }
-        I.tiles_x = (uint32_t(s->nx) + b->block.x - 1) / b->block.x;
-        I.tiles_y = (uint32_t(s->ny) + b->block.y - 1) / b->block.y;
-        I.ntiles = I.tiles_x * I.tiles_y * uint32_t(s->nz);
+        const uint32_t threads = b->block.x * b->block.y;
+        I.cells = uint32_t(s->N);
+        I.ntiles = (I.cells + threads - 1) / threads;
         I.tile_begin = uint32_t(tiles);
         tiles += I.ntiles;
         if (I.log_every > 0) {

@@ -5,7 +5,10 @@
 // advance together: every lattice is cut into tiles of one block each, the
 // instances are sorted by step count (longest first) so that the instances
 // still running in round r are a prefix of the list and so are their tiles,
-// and each round processes the active prefix.
+// and each round processes the active prefix. A tile is a run of consecutive
+// cells in the instance's linear index (x fastest), so one block size fits
+// every instance without idle threads, whatever its edge length; the only
+// partial tile is an instance's last one.
 //
 // Two launch forms, both captured in a CUDA graph by the host:
 //   k_batch_persistent  one cooperative launch; blocks loop over rounds and
@@ -30,10 +33,15 @@ namespace stro {
 
 namespace {
 
+// Instance owning `tile`: binary search over the ascending tile_begin.
 __device__ __forceinline__ int find_instance(const BatchArgs& b, uint32_t tile) {
-    int k = 0;
-    while (k + 1 < b.count && b.inst[k + 1].tile_begin <= tile) ++k;
-    return k;
+    int lo = 0, hi = b.count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (b.inst[mid].tile_begin <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 __device__ __forceinline__ uint32_t active_tiles(const BatchArgs& b, int64_t r) {
@@ -52,14 +60,13 @@ __device__ __forceinline__ bool logs_at(const BatchInstance& I, int64_t r) {
 template <typename S, int GEO, int FEAT, bool CG>
 __device__ __forceinline__ void process_tile(const BatchArgs& b, const BatchInstance& I,
                                              uint32_t tile, int64_t r) {
-    const uint32_t rem = tile - I.tile_begin;
-    const uint32_t bxi = rem % I.tiles_x;
-    const uint32_t t2 = rem / I.tiles_x;
-    const uint32_t byi = t2 % I.tiles_y;
-    const int z = int(t2 / I.tiles_y);
-    const int x = int(bxi * blockDim.x + threadIdx.x);
-    const int y = int(byi * blockDim.y + threadIdx.y);
-    const bool in = x < I.a.nx && y < I.a.ny;
+    const uint32_t threads = blockDim.x * blockDim.y;
+    const uint32_t lin = (tile - I.tile_begin) * threads + threadIdx.y * blockDim.x + threadIdx.x;
+    const bool in = lin < I.cells;
+    const uint32_t nx = uint32_t(I.a.nx), t = lin / nx;
+    const int x = int(lin - t * nx);
+    const int y = int(t % uint32_t(I.a.ny));
+    const int z = int(t / uint32_t(I.a.ny));
     if (((I.t0 + r) & 1) == 0) {
         if (logs_at(I, r)) {
             float u2 = 0.0f;

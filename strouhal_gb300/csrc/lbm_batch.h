@@ -20,8 +20,8 @@ struct BatchInstance {
     int32_t trace_cap;        // capacity of `trace`
     double* trace;            // kinetic-energy samples: trace[s] at round s * log_every
     uint32_t tile_begin;      // first tile of this instance in the batch tile list
-    uint32_t ntiles;          // tiles_x * tiles_y * nz
-    uint32_t tiles_x, tiles_y;
+    uint32_t ntiles;          // ceil(cells / threads per block)
+    uint32_t cells;           // nx * ny * nz
 };
 
 // Grid-barrier and error state of the persistent launch (zeroed before each launch).
