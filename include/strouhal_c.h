@@ -133,6 +133,17 @@ int stro_sim_dissipation(stro_sim* sim, double* sum_eps);
 /* Simulation.stateDigest (Sim.swift:441-444): SHA-256 of the raw state bytes,
  * 64 lowercase hex chars + NUL. */
 int stro_sim_digest(stro_sim* sim, char hex[65]);
+/* Ladder.measure (Ladder.swift:54-72) in one submission: `transient` steps
+ * (rounded down to even), then chunks of max(2, stride - 2) (rounded down to
+ * even) steps each followed by the two-step force probe over the box, until
+ * sample_steps steps are taken. Each probe's FP64 box force is reduced into
+ * a device buffer; the samples come back once, at the end: forces[3 k + d]
+ * for sample k, steps_at[k] (optional) the step count after its probe. The
+ * number of samples is returned in *samples; a capacity below it fails with
+ * *samples set. Requires wants_forces and an even step count. */
+int stro_sim_run_sampled(stro_sim* sim, int64_t transient, int64_t sample_steps, int64_t stride,
+                         int32_t x0, int32_t x1, int32_t y0, int32_t y1, double* forces,
+                         int64_t capacity, int64_t* samples, int64_t* steps_at);
 /* The |u| colormap of slice z (colorize, Kernels.metal:465-500) into a
  * caller array of nx*ny RGBA binary16 texels (uint16 bit patterns), row y
  * written at ny-1-y as the reference's texture write. The velocity is formed
@@ -307,6 +318,62 @@ int stro_sphere_stl(float radius, int32_t segments, int32_t rings, uint8_t* out,
 int stro_mesh_solid_fractions(stro_ctx* ctx, const float* tris, uint32_t ntri, int32_t nx,
                               int32_t ny, int32_t nz, float scale, const float offset[3],
                               float* eps, double* seconds);
+
+/* ---- uncertainty budget (Uncertainty.swift) ----------------------------------
+ * U(phi) = k sqrt(u_num^2 + u_stat^2 + u_Ma^2), k = 2, published only inside
+ * or near the edge of the validated domain. Host-only double arithmetic in
+ * the reference's operation order. */
+typedef struct {
+    double mean;          /* mean of the batch means (series mean when too short) */
+    double half_width95;  /* u_stat = 1.96 sd / sqrt(batches); NaN when too short */
+    double lag1;          /* lag-1 autocorrelation of the batch means */
+    int32_t batches;      /* 0 when the series is shorter than 4 * min_batches */
+    int32_t trustworthy;  /* batches >= 6 and |lag1| <= 0.3 */
+} stro_stat_uq;
+/* StatUncertainty(series:maxBatches:minBatches:) (Uncertainty.swift:47-101):
+ * non-overlapping batch means, the largest batch count (searching down from
+ * max_batches in steps of 2) whose means are uncorrelated (|lag1| <= 0.3). */
+int stro_uq_stat(const double* values, int64_t n, int32_t max_batches, int32_t min_batches,
+                 stro_stat_uq* out);
+typedef struct {
+    int32_t cells_per_feature;
+    double value; /* time-averaged QoI of the rung */
+    double stat;  /* its u_stat (NaN if unknown) */
+} stro_ladder_rung;
+typedef struct {
+    double u_num;          /* max(|finest - next|, finest u_stat); NaN for one rung */
+    double observed_order; /* diagnostic only; NaN unless 3 rungs converge monotonically */
+    int32_t has_order;
+    int32_t note;          /* 0 single resolution, 1 finest two agree within noise, 2 otherwise */
+} stro_num_uq;
+/* NumUncertainty(rungs:) (Uncertainty.swift:123-163). */
+int stro_uq_num(const stro_ladder_rung* rungs, int32_t count, stro_num_uq* out);
+/* MachUncertainty (Uncertainty.swift:168-179): u_Ma = 4/3 |baseline - half-Mach|. */
+int stro_uq_mach(double baseline, double half_mach, double* u_ma);
+enum { STRO_DOMAIN_INSIDE = 0, STRO_DOMAIN_NEAR_EDGE = 1, STRO_DOMAIN_OUTSIDE = 2 };
+enum {
+    STRO_OUTSIDE_RE = 1, STRO_OUTSIDE_MACH = 2, STRO_OUTSIDE_RESOLUTION = 4,
+    STRO_OUTSIDE_GEOMETRY = 8 /* no validated case of that geometry class */
+};
+typedef struct {
+    int32_t verdict;  /* STRO_DOMAIN_* */
+    int32_t anchor;   /* nearest anchor of the geometry class, -1 if none */
+    double distance;  /* fractional extrapolation distance to it */
+    double factor;    /* bar inflation near the edge (1 inside, NaN outside) */
+    int32_t reasons;  /* STRO_OUTSIDE_* bits when outside */
+} stro_domain_verdict;
+/* ValidationDomain.classify (Uncertainty.swift:221-259) over the reference's
+ * anchors (Uncertainty.swift:200-213). */
+int stro_uq_classify(double re, double mach, int32_t cells_per_feature, const char* geometry,
+                     stro_domain_verdict* out);
+/* Anchor `index` (0..3): name, ranges {Re lo, Re hi, Ma lo, Ma hi}, cells per
+ * feature {lo, hi} and geometry class (UTF-8). */
+int stro_uq_anchor(int32_t index, char* name, size_t name_len, double ranges[4],
+                   int32_t cells[2], char* geometry, size_t geometry_len);
+/* UncertaintyBudget.combined (Uncertainty.swift:272-280): 2 * RSS of the
+ * non-NaN components, times the edge factor near the edge, NaN outside. */
+int stro_uq_combined(double u_num, double u_stat, double u_ma, const stro_domain_verdict* verdict,
+                     double* combined);
 
 #ifdef __cplusplus
 }

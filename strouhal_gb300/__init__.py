@@ -59,6 +59,32 @@ class _Desc(ctypes.Structure):
                 ("c_smago", ctypes.c_float), ("wants_forces", ctypes.c_int32)]
 
 
+class StatUQ(ctypes.Structure):
+    """stro_stat_uq"""
+    _fields_ = [("mean", ctypes.c_double), ("half_width95", ctypes.c_double),
+                ("lag1", ctypes.c_double), ("batches", ctypes.c_int32),
+                ("trustworthy", ctypes.c_int32)]
+
+
+class LadderRungC(ctypes.Structure):
+    """stro_ladder_rung"""
+    _fields_ = [("cells_per_feature", ctypes.c_int32), ("value", ctypes.c_double),
+                ("stat", ctypes.c_double)]
+
+
+class NumUQ(ctypes.Structure):
+    """stro_num_uq"""
+    _fields_ = [("u_num", ctypes.c_double), ("observed_order", ctypes.c_double),
+                ("has_order", ctypes.c_int32), ("note", ctypes.c_int32)]
+
+
+class DomainVerdict(ctypes.Structure):
+    """stro_domain_verdict"""
+    _fields_ = [("verdict", ctypes.c_int32), ("anchor", ctypes.c_int32),
+                ("distance", ctypes.c_double), ("factor", ctypes.c_double),
+                ("reasons", ctypes.c_int32)]
+
+
 def lib():
     """Load the C-ABI library (built by __graft_entry__.build() / build.py)."""
     global _lib
@@ -146,6 +172,18 @@ def lib():
         "stro_mesh_solid_fractions": ([_P, _P, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int32,
                                        ctypes.c_int32, c_float, _P, _P,
                                        ctypes.POINTER(c_double)], c_int),
+        "stro_sim_run_sampled": ([_P, c_i64, c_i64, c_i64, ctypes.c_int32, ctypes.c_int32,
+                                  ctypes.c_int32, ctypes.c_int32, _P, c_i64,
+                                  ctypes.POINTER(c_i64), _P], c_int),
+        "stro_uq_stat": ([_P, c_i64, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(StatUQ)], c_int),
+        "stro_uq_num": ([_P, ctypes.c_int32, ctypes.POINTER(NumUQ)], c_int),
+        "stro_uq_mach": ([c_double, c_double, ctypes.POINTER(c_double)], c_int),
+        "stro_uq_classify": ([c_double, c_double, ctypes.c_int32, ctypes.c_char_p,
+                              ctypes.POINTER(DomainVerdict)], c_int),
+        "stro_uq_anchor": ([ctypes.c_int32, ctypes.c_char_p, ctypes.c_size_t, _P, _P,
+                            ctypes.c_char_p, ctypes.c_size_t], c_int),
+        "stro_uq_combined": ([c_double, c_double, c_double, ctypes.POINTER(DomainVerdict),
+                              ctypes.POINTER(c_double)], c_int),
         "stro_sphere_solid_fractions": ([ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                          c_double, c_double, c_double, c_double, ctypes.c_int32,
                                          _P], c_int),
@@ -183,6 +221,7 @@ class GPU:
 
     def __init__(self, device=0):
         self._h = _P()
+        self.device = int(device)
         _check(lib().stro_ctx_create(int(device), ctypes.byref(self._h)))
         name = ctypes.create_string_buffer(256)
         sms = ctypes.c_int()
@@ -427,6 +466,22 @@ class Simulation:
         _check(lib().stro_sim_probe_force(self._h, int(xRange[0]), int(xRange[1]),
                                           int(yRange[0]), int(yRange[1]), out.ctypes.data))
         return out
+
+    def runSampled(self, transientSteps, sampleSteps, stride, xRange, yRange):
+        """Ladder.measure's stepping (Ladder.swift:54-66) in one submission: the
+        transient, then chunk + two-step force probe pairs until sampleSteps
+        steps are taken. Returns (forces (n, 3) float64, step count after each
+        probe (n,) int64); the samples are read back once."""
+        chunk = max(2, int(stride) - 2) & ~1
+        n = (int(sampleSteps) + chunk + 1) // (chunk + 2) if sampleSteps > 0 else 0
+        forces = np.zeros((max(n, 1), 3), np.float64)
+        at = np.zeros(max(n, 1), np.int64)
+        got = ctypes.c_int64()
+        _check(lib().stro_sim_run_sampled(self._h, int(transientSteps), int(sampleSteps),
+                                          int(stride), int(xRange[0]), int(xRange[1]),
+                                          int(yRange[0]), int(yRange[1]), forces.ctypes.data,
+                                          forces.shape[0], ctypes.byref(got), at.ctypes.data))
+        return forces[:got.value], at[:got.value]
 
     def kineticEnergySum(self):
         v = ctypes.c_double()

@@ -38,6 +38,7 @@ SOURCES = [
     ("adjoint.cu", "adjoint.o", []),
     ("voxel.cu", "voxel.o", []),
     ("sha256.cpp", "sha256.o", []),
+    ("uq.cpp", "uq.o", []),
 ]
 
 
@@ -53,8 +54,10 @@ def lib_path():
 
 
 def _flags(verbose_ptxas=False):
+    # -ffp-contract=off for the host compiler as well: host-side arithmetic
+    # (statistics, mesh generation) must not depend on the host's FMA choices
     f = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--expt-relaxed-constexpr",
-                "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
+                "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
     if verbose_ptxas:
         f += ["-Xptxas", "-v"]
     return f

@@ -15,6 +15,7 @@ import argparse
 import hashlib
 import json
 import math
+import os
 import time
 
 import numpy as np
@@ -544,10 +545,67 @@ def sphere_adjoint(gpu, nx=512, ny=256, nz=256, D=48, u=0.05, re=300.0, cs=0.1, 
     return out
 
 
+# ------------------------------------------------------------ credibility ladder
+def credibility(gpu, resolutions=(32, 48, 64), base_mach=0.075, steps_factor=1.0,
+                precision="fp32", report=None, modes=("sequential", "concurrent")):
+    """The DFG 2D-2 credibility run (mean C_D; three resolutions and a half-Mach
+    anchor at the finest) with the four checks the reference's credibility gate
+    makes (Sources/strouhal/Cases.swift:1103-1160): a finite calibrated bar in
+    the validated domain, a bar that reaches the published mean C_D 3.18 (within
+    0.05), a ladder of every resolution, and a refusal out of the domain
+    (Re 250000). Each mode in `modes` runs the whole ladder; the modes must
+    agree bit for bit."""
+    from . import credibility as cr
+    case = cr.StreetLadder(baseMach=base_mach, precision=precision, stepsFactor=steps_factor)
+    runs = {}
+    for mode in modes:
+        runs[mode] = cr.Ladder.credibility(gpu, case, "mean C_D", list(resolutions),
+                                           concurrent=(mode == "concurrent"))
+    first = runs[modes[0]]
+    b = first.budget
+    far = cr.ValidationDomain.classify(250000.0, 0.09, 48, "bluff body in channel")
+    far_budget = cr.UncertaintyBudget("C_D", 1.0, 0.01, 0.01, 0.01, far)
+    gates = {
+        "calibrated_bar_in_domain": bool(math.isfinite(b.combined) and b.combined > 0),
+        "bar_covers_published_mean_cd": bool(abs(b.value - 3.18) <= b.combined + 0.05),
+        "ladder_recorded": len(first.rungs) == len(resolutions),
+        "out_of_domain_refuses": bool(far.isOutside and math.isnan(far_budget.combined)),
+    }
+    md = cr.report_markdown(first, [
+        "cavity, Poiseuille, Taylor-Green order, DFG 2D-1/2D-2 and sphere gates: "
+        "tests/test_gate_records.py over tests/records/",
+        "every step kernel against the oracle: tests/test_gpu_parity.py"])
+    if report:
+        with open(report, "w") as fh:
+            fh.write(md)
+    gates["report_written"] = bool(report is None or os.path.exists(report))
+    out = {"resolutions": list(resolutions), "base_mach": base_mach,
+           "steps_factor": steps_factor, "precision": precision,
+           "value": b.value, "u_num": b.uNum, "u_stat": b.uStat, "u_ma": b.uMa,
+           "combined": b.combined, "headline": b.headline,
+           "verdict": b.verdict.kind, "anchor": b.verdict.anchor,
+           "observed_order": first.num.observedOrder,
+           "stat_batches": first.stat.batches, "stat_lag1": first.stat.lag1,
+           "mach_baseline": first.mach.baseline, "mach_half": first.mach.halfMach,
+           "rungs": [[r.cellsPerFeature, r.value, r.stat] for r in first.rungs],
+           "digest": first.digest, "cell_updates": first.cellUpdates, "gates": gates,
+           "report_chars": len(md)}
+    for mode, r in runs.items():
+        out[mode + "_wall_seconds"] = r.wallSeconds
+        out[mode + "_gpu_seconds"] = r.gpuSeconds
+        out[mode + "_equal"] = (r.digest == first.digest and
+                                [(x.value, x.stat) for x in r.rungs] ==
+                                [(x.value, x.stat) for x in first.rungs] and
+                                r.mach.halfMach == first.mach.halfMach)
+    # every variant's sampled tail, for re-deriving the budget with the oracle's statistics
+    out["series"] = first.series
+    return out
+
+
 CASES = {"poiseuille": poiseuille, "tg_order": tg_order, "cavity": cavity, "dfg2": dfg2,
          "dfg2_adjoint": dfg2_adjoint, "tgv": tgv, "sphere": sphere,
          "sphere_adjoint": sphere_adjoint, "ladder": ladder, "stl_voxelize": stl_voxelize,
-         "render": render}
+         "render": render, "credibility": credibility}
 
 
 def main(argv=None):

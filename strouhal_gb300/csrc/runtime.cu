@@ -647,6 +647,76 @@ int stro_sim_moments(stro_sim* s, float* out4) {
     return STRO_OK;
 }
 
+int stro_sim_run_sampled(stro_sim* s, int64_t transient, int64_t sample_steps, int64_t stride,
+                         int32_t x0, int32_t x1, int32_t y0, int32_t y1, double* forces,
+                         int64_t capacity, int64_t* samples, int64_t* steps_at) {
+    CHECK_SIM(s);
+    if (!samples) return fail(STRO_ERR_INVALID, "null sample count");
+    if (!s->wants_forces) return fail(STRO_ERR_STATE, "force samples require wants_forces");
+    if (s->steps_done % 2 != 0)
+        return fail(STRO_ERR_STATE, "a sampled run must start at an even step count");
+    if (transient < 0 || sample_steps < 0 || stride < 1)
+        return fail(STRO_ERR_INVALID, "negative step counts or stride < 1");
+    if (x0 < 0 || x1 >= s->nx || y0 < 0 || y1 >= s->ny || x0 > x1 || y0 > y1)
+        return fail(STRO_ERR_INVALID, "force box outside the lattice");
+    // Ladder.measure (Ladder.swift:55-66): even transient, then chunks of
+    // max(2, stride - 2) rounded down to even steps, each followed by the
+    // two-step force probe, until sample_steps steps are taken
+    transient &= ~int64_t(1);
+    const int64_t chunk = std::max<int64_t>(2, stride - 2) & ~int64_t(1);
+    const int64_t n = (sample_steps + chunk + 1) / (chunk + 2);
+    *samples = n;
+    if (n > capacity || (n > 0 && !forces)) {
+        return fail(STRO_ERR_INVALID, "sample buffer holds " + std::to_string(capacity) +
+                                          " samples, the run takes " + std::to_string(n));
+    }
+    cudaSetDevice(s->ctx->device);
+    cudaStream_t st = s->ctx->stream;
+    const bool geo = geo_on(s);
+    double* d_samples = nullptr;
+    if (n > 0) STRO_CUDA(cudaMalloc(&d_samples, size_t(n) * 3 * sizeof(double)));
+    if (n > 0) STRO_CUDA(cudaMemsetAsync(d_samples, 0, size_t(n) * 3 * sizeof(double), st));
+    const int box[4] = {x0, x1, y0, y1};
+    const dim3 pgrid = step_grid(step_args(s, 0), s->probe_block);
+    const int nblocks = int(pgrid.x * pgrid.y * pgrid.z);
+    int rc = STRO_OK;
+    cudaError_t e = cudaEventRecord(s->ev0, st);
+    int64_t t = s->steps_done;
+    auto steps = [&](int64_t count, int64_t probe_at) {
+        for (int64_t k = 0; k < count && rc == STRO_OK; ++k, ++t)
+            rc = launch_one_step(s, t, geo && t == probe_at, box);
+    };
+    if (e == cudaSuccess) steps(transient, -1);
+    for (int64_t k = 0; k < n && rc == STRO_OK && e == cudaSuccess; ++k) {
+        steps(chunk, -1);
+        steps(2, t + 1);  // probe pair: the force is taken on its odd step
+        if (rc == STRO_OK && geo)
+            e = launch_fold(s->d_partials, nblocks, 3, d_samples + 3 * k, st);
+        if (steps_at) steps_at[k] = t;
+    }
+    if (rc == STRO_OK && e == cudaSuccess) e = cudaEventRecord(s->ev1, st);
+    if (rc == STRO_OK && e == cudaSuccess && n > 0)
+        e = cudaMemcpyAsync(forces, d_samples, size_t(n) * 3 * sizeof(double),
+                            cudaMemcpyDeviceToHost, st);
+    if (rc == STRO_OK && e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_samples);
+    if (rc != STRO_OK) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "sampled run");
+    float ms = 0.0f;
+    STRO_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    s->gpu_seconds += double(ms) * 1e-3;
+    s->steps_done = t;
+    if (s->variant == 2) {
+        int err = 0;
+        STRO_CUDA(cudaMemcpy(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost));
+        if (err != 0) {
+            cudaMemset(s->d_error, 0, sizeof(int));
+            return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-staged step timed out");
+        }
+    }
+    return STRO_OK;
+}
+
 int stro_sim_render_slice(stro_sim* s, int32_t z, float uref, uint16_t* rgba, double* seconds) {
     CHECK_SIM(s);
     if (!rgba) return fail(STRO_ERR_INVALID, "null output");

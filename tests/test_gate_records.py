@@ -169,3 +169,38 @@ def test_precision_record():
     by = {run["precision"]: run["rows"] for run in r["runs"]}
     assert max(x["ke_rel"] for x in by["fp32"]) < 1e-5
     assert max(x["ke_rel"] for x in by["fp16s"]) < 5e-3
+
+
+def test_credibility_gates_and_budget_from_the_oracle():
+    """The reference's credibility gate (Cases.swift:1103-1160) on the recorded
+    DFG 2D-2 ladder ([32, 48, 64] cells and a half-Mach anchor at 64): a finite
+    calibrated bar inside the validated domain, a bar within 0.05 of covering
+    the published mean C_D 3.18, every rung recorded, and a refusal out of the
+    domain. The budget is re-derived from the recorded sample tails with the
+    oracle's statistics and must be the same doubles."""
+    from oracle import uq_oracle as uo
+
+    r = rec("credibility")
+    assert r["resolutions"] == [32, 48, 64] and r["steps_factor"] == 1.0
+    assert r["sequential_equal"] and r["concurrent_equal"]
+    rungs = []
+    for n, value, stat in r["rungs"]:
+        tail = r["series"][str(n)]
+        st = uo.stat_uncertainty(tail)
+        assert value == uo.qoi_mean(tail) and stat == st.half_width95
+        rungs.append((n, value, stat))
+    num = uo.num_uncertainty(rungs)
+    fine = uo.stat_uncertainty(r["series"]["64"])
+    u_ma = uo.mach_uncertainty(rungs[-1][1], uo.qoi_mean(r["series"]["64 half-Mach"]))
+    verdict = uo.classify(100.0, uo.street_variant(64, 1.0)["mach"], 64, "bluff body in channel")
+    combined = uo.combined(num.u_num, fine.half_width95, u_ma, verdict)
+    assert (r["u_num"], r["u_stat"], r["u_ma"], r["combined"]) == (
+        num.u_num, fine.half_width95, u_ma, combined)
+    assert (r["stat_batches"], r["stat_lag1"]) == (fine.batches, fine.lag1)
+    # the four gates
+    assert verdict.verdict == uo.INSIDE and math.isfinite(combined) and combined > 0
+    assert abs(r["value"] - 3.18) <= combined + 0.05
+    assert len(r["rungs"]) == 3
+    far = uo.classify(250000.0, 0.09, 48, "bluff body in channel")
+    assert far.verdict == uo.OUTSIDE and math.isnan(uo.combined(0.01, 0.01, 0.01, far))
+    assert all(r["gates"].values())

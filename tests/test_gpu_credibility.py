@@ -1,0 +1,132 @@
+"""The credibility ladder on the GPU: stro_sim_run_sampled against the host
+loop of Ladder.measure (Ladder.swift:54-66) and against the oracle, and a
+short DFG 2D-2 ladder whose budget is re-derived with the oracle's
+statistics (oracle/uq_oracle.py)."""
+import math
+
+import numpy as np
+import pytest
+
+import strouhal_gb300 as sg
+from strouhal_gb300 import credibility as cr
+from oracle import uq_oracle as uo
+
+pytestmark = pytest.mark.gpu
+
+
+def same(a, b):
+    return (math.isnan(a) and math.isnan(b)) or a == b
+
+
+def host_loop(sim, transient, sample, stride, box):
+    """Ladder.measure's own loop: run(chunk), then the two-step probe."""
+    sim.run(transient & ~1)
+    chunk = max(2, stride - 2) & ~1
+    forces, at, taken = [], [], 0
+    while taken < sample:
+        sim.run(chunk)
+        forces.append(sim.probeForce(*box))
+        taken += chunk + 2
+        at.append(sim.stepsDone)
+    return np.array(forces).reshape(-1, 3), np.array(at, np.int64)
+
+
+@pytest.mark.parametrize("D,transient,sample,stride", [(10, 301, 600, 26), (12, 0, 97, 8),
+                                                       (8, 40, 40, 3), (10, 20, 0, 26)])
+def test_run_sampled_equals_host_loop(gpu, D, transient, sample, stride):
+    case = cr.StreetLadder()
+    a = case.variant(gpu, D, 1.0)
+    b = case.variant(gpu, D, 1.0)
+    fa, ata = a.sim.runSampled(transient, sample, stride, *a.box)
+    fb, atb = host_loop(b.sim, transient, sample, stride, b.box)
+    assert np.array_equal(fa, fb) and np.array_equal(ata, atb)
+    assert list(ata) == uo.sample_schedule(0, transient, sample, stride)
+    assert a.sim.stepsDone == b.sim.stepsDone and a.sim.stateDigest == b.sim.stateDigest
+    if sample:
+        assert np.all(np.isfinite(fa)) and np.any(fa[:, 0] != 0.0)
+    a.sim.close()
+    b.sim.close()
+
+
+def test_run_sampled_matches_oracle(gpu, oracle):
+    """Forces within 1e-12 of the oracle (FP64 box sums in different orders),
+    final DDFs bitwise equal."""
+    po = oracle
+    D = 8
+    v = cr.StreetLadder().variant(gpu, D, 1.0)
+    s = v.sim
+    o = po.OracleSim(s.nx, s.ny, 1, s.omega, s.omegaMinus, uin=s.uinTarget,
+                     rampSteps=s.rampSteps, wantsForces=True, flags=s._flags, kind=po.KIND_F32)
+    o.setSolidFractions(sg.diskSolidFractions(s.nx, s.ny, 0.5 + 2.0 * D, 0.5 + 2.0 * D, D / 2.0))
+    o.sponge = s.sponge
+    fg, at = s.runSampled(60, 120, 10, *v.box)
+    fo, ato = host_loop(o, 60, 120, 10, v.box)
+    assert np.array_equal(at, ato)
+    assert np.allclose(fg, fo, rtol=1e-12, atol=1e-15), np.abs(fg - fo).max()
+    assert np.array_equal(s.downloadState(), o.f)
+    s.close()
+
+
+def test_run_sampled_errors(gpu):
+    v = cr.StreetLadder().variant(gpu, 8, 1.0)
+    s = v.sim
+    L = sg.lib()
+    f = np.zeros((2, 3))
+    n = sg.ctypes.c_int64()
+    # the capacity is checked before any step: state and step count unchanged
+    rc = L.stro_sim_run_sampled(s._h, 10, 100, 10, *v.box[0], *v.box[1], f.ctypes.data, 2,
+                                sg.ctypes.byref(n), None)
+    assert rc != 0
+    assert n.value == 10 and s.stepsDone == 0
+    with pytest.raises(sg.StrouhalError):
+        s.runSampled(10, 10, 10, (0, s.nx), (0, 3))    # box outside the lattice
+    with pytest.raises(sg.StrouhalError):
+        s.runSampled(10, 10, 0, *v.box)               # stride < 1
+    s.run(1)
+    with pytest.raises(sg.StrouhalError):
+        s.runSampled(10, 10, 10, *v.box)              # odd step count
+    s.close()
+    plain = sg.Simulation(gpu, nx=16, ny=8, nz=1, omega=1.2)
+    with pytest.raises(sg.StrouhalError):
+        plain.runSampled(2, 10, 10, (1, 4), (1, 4))   # wantsForces off
+    plain.close()
+
+
+def _budget_from_oracle(run, finest):
+    """The budget re-derived from the run's sampled tails with the oracle."""
+    rungs = []
+    for r in run.rungs:
+        tail = run.series["%d" % r.cellsPerFeature]
+        st = uo.stat_uncertainty(tail)
+        assert same(r.value, uo.qoi_mean(tail)) and same(r.stat, st.half_width95)
+        rungs.append((r.cellsPerFeature, r.value, r.stat))
+    num = uo.num_uncertainty(rungs)
+    half = uo.qoi_mean(run.series["%d half-Mach" % finest])
+    u_ma = uo.mach_uncertainty(rungs[-1][1], half)
+    fine = uo.stat_uncertainty(run.series["%d" % finest])
+    v = uo.street_variant(finest, 1.0)
+    verdict = uo.classify(100.0, v["mach"], finest, "bluff body in channel")
+    return num, fine, u_ma, verdict, uo.combined(num.u_num, fine.half_width95, u_ma, verdict)
+
+
+def test_short_ladder_budget_matches_oracle_and_modes_agree(gpu):
+    case = cr.StreetLadder(stepsFactor=0.01)
+    res = [24, 32, 40]
+    seq = cr.Ladder.credibility(gpu, case, "mean C_D", res)
+    con = cr.Ladder.credibility(gpu, case, "mean C_D", res, concurrent=True)
+    for r in (seq, con):
+        assert [x.cellsPerFeature for x in r.rungs] == res
+    # concurrent streams give the same bits as one variant after another
+    assert seq.digest == con.digest
+    assert [(x.value, x.stat) for x in seq.rungs] == [(x.value, x.stat) for x in con.rungs]
+    assert seq.series == con.series
+    num, fine, u_ma, verdict, comb = _budget_from_oracle(seq, 40)
+    b = seq.budget
+    assert same(b.uNum, num.u_num) and same(b.uStat, fine.half_width95) and b.uMa == u_ma
+    assert b.verdict.kind == verdict.verdict == uo.INSIDE
+    assert same(b.combined, comb) and math.isfinite(b.combined)
+    # the finest rung keeps the second half of its samples (transient 600, sample 1200)
+    n = len(uo.sample_schedule(0, 600, 1200, uo.street_variant(40, 1.0)["stride"]))
+    assert len(seq.series["40"]) == n - int(n * 0.5)
+    md = cr.report_markdown(seq)
+    assert "Inside" in md and "| 40 |" in md
