@@ -229,6 +229,18 @@ int stro_batch_set_spin_limit(stro_batch* batch, int64_t polls);
  * the number of samples. */
 int stro_batch_run(stro_batch* batch, const int64_t* steps, const int32_t* log_every,
                    double* traces, int32_t trace_stride, int32_t* trace_counts);
+/* stro_sim_run_sampled for every simulation of the batch in one submission:
+ * instance i takes transient[i] steps, then probes the force over the box
+ * boxes[4 i .. 4 i + 3] = {x0, x1, y0, y1} every max(2, stride[i] - 2) + 2
+ * steps (rounded as stro_sim_run_sampled does) until sample_steps[i] steps are
+ * taken; its samples go to forces[i][3 k + d], at most capacity[i] of them, and
+ * their number to samples[i]. DDFs and step counts are bitwise those of
+ * stro_sim_run_sampled; the box sums are folded per tile, so forces agree with
+ * it to rounding (FP64). In STRO_BATCH_SEQUENTIAL mode the simulations run one
+ * after another through stro_sim_run_sampled (the reference's order). */
+int stro_batch_run_sampled(stro_batch* batch, const int64_t* transient, const int64_t* sample_steps,
+                           const int64_t* stride, const int32_t* boxes, double* const* forces,
+                           const int64_t* capacity, int64_t* samples);
 int stro_batch_gpu_seconds(stro_batch* batch, double* seconds);
 /* "persistent-graph", "rounds-graph" or "sequential": the path the last run took. */
 int stro_batch_last_path(stro_batch* batch, char* buf, size_t len);

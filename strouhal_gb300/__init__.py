@@ -151,6 +151,7 @@ def lib():
         "stro_batch_set_spin_limit": ([_P, c_i64], c_int),
         "stro_batch_run": ([_P, _P, _P, _P, ctypes.c_int32, _P], c_int),
         "stro_batch_gpu_seconds": ([_P, ctypes.POINTER(c_double)], c_int),
+        "stro_batch_run_sampled": ([_P, _P, _P, _P, _P, _P, _P, _P], c_int),
         "stro_batch_last_path": ([_P, ctypes.c_char_p, ctypes.c_size_t], c_int),
         "stro_batch_autotune": ([_P, c_i64, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
                                  ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(c_double)], c_int),
@@ -639,6 +640,33 @@ class Batch:
         _check(lib().stro_batch_run(self._h, st.ctypes.data, le.ctypes.data, tr.ctypes.data,
                                     stride, cnt.ctypes.data))
         return [tr[i, :cnt[i]].copy() for i in range(n)]
+
+    def runSampled(self, transientSteps, sampleSteps, strides, boxes):
+        """Simulation.runSampled for every member in one submission; boxes[i] =
+        (xRange, yRange). Returns a list of (forces (n_i, 3), step counts (n_i,))."""
+        n = len(self.sims)
+        tr = np.ascontiguousarray(transientSteps, np.int64).reshape(n)
+        sa = np.ascontiguousarray(sampleSteps, np.int64).reshape(n)
+        sd = np.ascontiguousarray(strides, np.int64).reshape(n)
+        bx = np.ascontiguousarray([[b[0][0], b[0][1], b[1][0], b[1][1]] for b in boxes],
+                                  np.int32).reshape(n, 4)
+        t0 = [s.stepsDone for s in self.sims]
+        chunks = [max(2, int(s) - 2) & ~1 for s in sd]
+        counts = [(int(a) + c + 1) // (c + 2) if a > 0 else 0 for a, c in zip(sa, chunks)]
+        bufs = [np.zeros((max(c, 1), 3), np.float64) for c in counts]
+        ptrs = (_P * n)(*[b.ctypes.data for b in bufs])
+        cap = np.ascontiguousarray([b.shape[0] for b in bufs], np.int64)
+        got = np.zeros(n, np.int64)
+        _check(lib().stro_batch_run_sampled(self._h, tr.ctypes.data, sa.ctypes.data, sd.ctypes.data,
+                                            bx.ctypes.data, ptrs, cap.ctypes.data,
+                                            got.ctypes.data))
+        out = []
+        for i in range(n):
+            k = int(got[i])
+            T = int(tr[i]) & ~1
+            at = t0[i] + T + (np.arange(1, k + 1, dtype=np.int64) * (chunks[i] + 2))
+            out.append((bufs[i][:k], at))
+        return out
 
     @property
     def gpuSeconds(self):

@@ -547,20 +547,22 @@ def sphere_adjoint(gpu, nx=512, ny=256, nz=256, D=48, u=0.05, re=300.0, cs=0.1, 
 
 # ------------------------------------------------------------ credibility ladder
 def credibility(gpu, resolutions=(32, 48, 64), base_mach=0.075, steps_factor=1.0,
-                precision="fp32", report=None, modes=("sequential", "concurrent")):
+                precision="fp32", report=None, modes=("sequential", "concurrent", "batched"),
+                autotune=True):
     """The DFG 2D-2 credibility run (mean C_D; three resolutions and a half-Mach
     anchor at the finest) with the four checks the reference's credibility gate
     makes (Sources/strouhal/Cases.swift:1103-1160): a finite calibrated bar in
     the validated domain, a bar that reaches the published mean C_D 3.18 (within
     0.05), a ladder of every resolution, and a refusal out of the domain
-    (Re 250000). Each mode in `modes` runs the whole ladder; the modes must
-    agree bit for bit."""
+    (Re 250000). Each mode in `modes` runs the whole ladder: the final lattices
+    must be bitwise equal across modes, the QoIs equal (sequential, concurrent)
+    or equal to FP64 rounding (batched: box sums folded per tile)."""
     from . import credibility as cr
     case = cr.StreetLadder(baseMach=base_mach, precision=precision, stepsFactor=steps_factor)
     runs = {}
     for mode in modes:
-        runs[mode] = cr.Ladder.credibility(gpu, case, "mean C_D", list(resolutions),
-                                           concurrent=(mode == "concurrent"))
+        runs[mode] = cr.Ladder.credibility(gpu, case, "mean C_D", list(resolutions), mode=mode,
+                                           autotune=autotune)
     first = runs[modes[0]]
     b = first.budget
     far = cr.ValidationDomain.classify(250000.0, 0.09, 48, "bluff body in channel")
@@ -593,10 +595,12 @@ def credibility(gpu, resolutions=(32, 48, 64), base_mach=0.075, steps_factor=1.0
     for mode, r in runs.items():
         out[mode + "_wall_seconds"] = r.wallSeconds
         out[mode + "_gpu_seconds"] = r.gpuSeconds
-        out[mode + "_equal"] = (r.digest == first.digest and
-                                [(x.value, x.stat) for x in r.rungs] ==
-                                [(x.value, x.stat) for x in first.rungs] and
-                                r.mach.halfMach == first.mach.halfMach)
+        out[mode + "_path"] = r.path
+        # the final lattices bitwise equal; the QoIs equal (batched: to FP64 rounding)
+        out[mode + "_digest_equal"] = r.digest == first.digest
+        out[mode + "_max_rel_diff"] = max(
+            [abs(a.value - b.value) / abs(b.value) for a, b in zip(r.rungs, first.rungs)] +
+            [abs(r.mach.halfMach - first.mach.halfMach) / abs(first.mach.halfMach)])
     # every variant's sampled tail, for re-deriving the budget with the oracle's statistics
     out["series"] = first.series
     return out

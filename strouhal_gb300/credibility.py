@@ -11,9 +11,16 @@ doubles, the reference's operation order). Each variant's stepping is one
 `stro_sim_run_sampled` submission: the transient, then chunk + force-probe
 pairs whose FP64 box forces are reduced on the GPU into a device buffer and
 read back once, instead of one host round trip per sample. The variants are
-independent lattices, so `Ladder.credibility(concurrent=True)` runs each on
-its own context (its own CUDA stream) from its own host thread; their results
-are bitwise the same as one after another.
+independent lattices, and `Ladder.credibility(mode=...)` runs them
+  "sequential"  one after another (the reference's order),
+  "concurrent"  each on its own context (its own CUDA stream) from its own
+                host thread,
+  "batched"     all in one batched submission (`stro_batch_run_sampled`: one
+                persistent kernel or one launch per round over every
+                variant's tiles, force probes fused into the odd pass).
+The lattices end bitwise the same in every mode; the batched box-force sums
+are folded per tile instead of per block, so its samples agree to FP64
+rounding.
 """
 from __future__ import annotations
 
@@ -25,8 +32,10 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import (Cell, DomainVerdict, GPU, LadderRungC, NumUQ, Simulation, StatUQ,
+from . import (Batch, Cell, DomainVerdict, GPU, LadderRungC, NumUQ, Simulation, StatUQ,
                _check, diskSolidFractions, lib, trtOmegas)
+
+MODES = ("sequential", "concurrent", "batched")
 
 NAN = float("nan")
 
@@ -319,11 +328,21 @@ class CredibilityRun:
     cellUpdates: int
     digest: str
     setup: str
-    concurrent: bool
+    mode: str
     series: dict = field(default_factory=dict)  # label -> sampled tail values
+    path: str = ""                               # kernel path (batched: the batch's)
 
 
 class Ladder:
+    @staticmethod
+    def _measurement(v, qoi, forces, at, gpu_seconds, steps):
+        series = QoISeries(qoi)
+        for step, value in zip(at, v.qoi(forces)):
+            series.append(step, value)
+        tail = series.stationaryTail(0.5)
+        return Measurement(tail, StatUncertainty.of(tail), v.sim.stateDigest, gpu_seconds, steps,
+                           v.sim.cells)
+
     @staticmethod
     def measure(v, qoi):
         """One variant's time-averaged QoI (Ladder.swift:54-72): the second
@@ -331,22 +350,24 @@ class Ladder:
         sim = v.sim
         g0, s0 = sim.gpuSeconds, sim.stepsDone
         forces, at = sim.runSampled(v.transientSteps, v.sampleSteps, v.stride, *v.box)
-        series = QoISeries(qoi)
-        for step, value in zip(at, v.qoi(forces)):
-            series.append(step, value)
-        tail = series.stationaryTail(0.5)
-        return Measurement(tail, StatUncertainty.of(tail), sim.stateDigest,
-                           sim.gpuSeconds - g0, sim.stepsDone - s0, sim.cells)
+        return Ladder._measurement(v, qoi, forces, at, sim.gpuSeconds - g0, sim.stepsDone - s0)
 
     @staticmethod
-    def credibility(gpu, case, qoi, resolutions, progress=None, concurrent=False):
+    def credibility(gpu, case, qoi, resolutions, progress=None, mode="sequential",
+                    autotune=True):
         """Every resolution at the base Mach number plus the finest at half
-        Mach, then the budget (Ladder.swift:74-121)."""
+        Mach, then the budget (Ladder.swift:74-121). `autotune` picks each
+        variant's kernel and launch shape (or the batch's mode and tile) with
+        a short timed trial on a copy of the state; results do not depend on
+        it."""
+        if mode not in MODES:
+            raise ValueError("mode must be one of %s" % (MODES,))
         t0 = time.perf_counter()
         res = sorted(int(n) for n in resolutions)
         finest = res[-1]
         jobs = [(n, 1.0) for n in res] + [(finest, 0.5)]
         results = [None] * len(jobs)
+        paths = []
 
         def one(k, g):
             n, ms = jobs[k]
@@ -354,11 +375,39 @@ class Ladder:
                 progress("%d cells per feature, Mach scale %.1f" % (n, ms))
             v = case.variant(g, n, ms)
             try:
+                if autotune:
+                    v.sim.autotune(200)
                 results[k] = (v.mach, Ladder.measure(v, qoi))
+                paths.append(v.sim.lastPath)
             finally:
                 v.sim.close()
 
-        if concurrent:
+        if mode == "batched":
+            variants = [case.variant(gpu, n, ms) for n, ms in jobs]
+            batch = None
+            try:
+                batch = Batch(gpu, [v.sim for v in variants], mode="persistent")
+                if autotune:
+                    batch.autotune(rounds=200)
+                g0 = batch.gpuSeconds
+                s0 = [v.sim.stepsDone for v in variants]
+                out = batch.runSampled([v.transientSteps for v in variants],
+                                       [v.sampleSteps for v in variants],
+                                       [v.stride for v in variants], [v.box for v in variants])
+                g = batch.gpuSeconds - g0
+                paths.append(batch.lastPath)
+                cells = sum(v.sim.cells * (v.sim.stepsDone - s) for v, s in zip(variants, s0))
+                for k, (v, (forces, at)) in enumerate(zip(variants, out)):
+                    steps = v.sim.stepsDone - s0[k]
+                    # the batch's GPU time, shared out by cell updates
+                    share = g * v.sim.cells * steps / cells if cells else 0.0
+                    results[k] = (v.mach, Ladder._measurement(v, qoi, forces, at, share, steps))
+            finally:
+                if batch is not None:
+                    batch.close()
+                for v in variants:
+                    v.sim.close()
+        elif mode == "concurrent":
             errors = []
             ctxs = [GPU(gpu.device) for _ in jobs]
 
@@ -399,9 +448,10 @@ class Ladder:
             wallSeconds=time.perf_counter() - t0,
             gpuSeconds=sum(m.gpuSeconds for _, m in results),
             cellUpdates=sum(m.steps * m.cells for _, m in results),
-            digest=fine.digest, setup=case.setupDescription, concurrent=concurrent,
+            digest=fine.digest, setup=case.setupDescription, mode=mode,
             series={("%d" % n if ms == 1.0 else "%d half-Mach" % n): m.series.values
-                    for (n, ms), (_, m) in zip(jobs, results)})
+                    for (n, ms), (_, m) in zip(jobs, results)},
+            path=",".join(sorted(set(paths))))
 
 
 def report_markdown(run, buildGates=()):
@@ -454,9 +504,10 @@ def report_markdown(run, buildGates=()):
         out += ["", "## Solver checks of this build", ""] + ["- " + g for g in buildGates]
     out += ["", "## Reproducibility", "",
             "- SHA-256 of the finest rung's final state: `%s`" % run.digest,
-            "- %.1f s wall time, %.1f s on the GPU, %.3g cell updates%s" % (
+            "- %.1f s wall time, %.1f s on the GPU, %.3g cell updates, variants run %s" % (
                 run.wallSeconds, run.gpuSeconds, float(run.cellUpdates),
-                " (variants on concurrent streams)" if run.concurrent else ""),
+                {"sequential": "one after another", "concurrent": "on concurrent streams",
+                 "batched": "in one batched submission"}[run.mode]),
             "", "## Not covered by the bar", "",
             "- Model-form error of the collision closure.",
             "- A grid convergence index: not defined for scale-resolving runs.",

@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <numeric>
@@ -42,6 +43,10 @@ struct stro_batch {
     size_t inst_cap = 0;
     double* d_kepart = nullptr;
     size_t kepart_cap = 0;
+    double* d_fpart = nullptr;
+    size_t fpart_cap = 0;
+    double* d_samples = nullptr;
+    size_t samples_cap = 0;
     BatchCtl* d_ctl = nullptr;
     float* d_ramp = nullptr;
     size_t ramp_cap = 0;
@@ -55,6 +60,20 @@ struct stro_batch {
 };
 
 namespace {
+
+// Rounds-mode runs longer than this are launched round by round on the
+// stream instead of being captured into one graph (a graph node per round).
+constexpr int64_t kMaxGraphRounds = 32768;
+
+// One instance's force-probe schedule in a sampled run (Ladder.measure): the
+// first probe at round `first` (an odd step), then every `period` rounds,
+// `count` probes, each over the box {x0, x1, y0, y1}.
+struct SamplePlan {
+    int64_t first = -1;
+    int32_t period = 0;
+    int32_t count = 0;
+    int box[4] = {0, 0, 0, 0};
+};
 
 template <typename T>
 int grow(T** p, size_t* cap, size_t n) {
@@ -116,11 +135,15 @@ int run_sequential(stro_batch* b, const int64_t* steps, const int32_t* log_every
 }
 
 int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
-              std::vector<std::vector<double>>& traces) {
+              std::vector<std::vector<double>>& traces, const SamplePlan* plans = nullptr,
+              std::vector<std::vector<double>>* samples = nullptr) {
     const size_t n = b->sims.size();
     cudaStream_t st = b->ctx->stream;
     const int geo = batch_geo(b) ? 1 : 0;
     const int feat = batch_feat(b);
+    int probes = 0;
+    if (plans && geo)
+        for (size_t i = 0; i < n; ++i) probes |= plans[i].count > 0 ? 1 : 0;
     if (geo)
         for (auto* s : b->sims) {
             const int rc = ensure_geometry(s);
@@ -132,8 +155,8 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
                      [&](size_t p, size_t q) { return steps[p] > steps[q]; });
     std::vector<BatchInstance> inst(n);
     std::vector<float> ramp;
-    std::vector<size_t> ramp_off(n, size_t(-1)), trace_off(n, 0);
-    size_t tiles = 0, trace_total = 0;
+    std::vector<size_t> ramp_off(n, size_t(-1)), trace_off(n, 0), sample_off(n, 0);
+    size_t tiles = 0, trace_total = 0, sample_total = 0;
     int64_t max_steps = 0;
     for (size_t k = 0; k < n; ++k) {
         stro_sim* s = b->sims[order[k]];
@@ -159,6 +182,19 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
             trace_off[k] = trace_total;
             trace_total += size_t(I.trace_cap);
         }
+        I.probe_first = -1;
+        if (probes && plans[order[k]].count > 0) {
+            const SamplePlan& pl = plans[order[k]];
+            I.probe_first = pl.first;
+            I.probe_period = pl.period;
+            I.probe_count = pl.count;
+            I.a.box_x0 = pl.box[0];
+            I.a.box_x1 = pl.box[1];
+            I.a.box_y0 = pl.box[2];
+            I.a.box_y1 = pl.box[3];
+            sample_off[k] = sample_total;
+            sample_total += 3 * size_t(pl.count);
+        }
         max_steps = std::max(max_steps, I.steps);
     }
     if (tiles >= (1ull << 31)) return fail(STRO_ERR_INVALID, "batch too large");
@@ -166,11 +202,14 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
     if (rc == STRO_OK) rc = grow(&b->d_kepart, &b->kepart_cap, tiles);
     if (rc == STRO_OK) rc = grow(&b->d_ramp, &b->ramp_cap, ramp.size());
     if (rc == STRO_OK) rc = grow(&b->d_traces, &b->traces_cap, trace_total);
+    if (rc == STRO_OK && probes) rc = grow(&b->d_fpart, &b->fpart_cap, 3 * tiles);
+    if (rc == STRO_OK && probes) rc = grow(&b->d_samples, &b->samples_cap, sample_total);
     if (rc == STRO_OK && !b->d_ctl) STRO_CUDA(cudaMalloc(&b->d_ctl, sizeof(BatchCtl)));
     if (rc != STRO_OK) return rc;
     for (size_t k = 0; k < n; ++k) {
         inst[k].ramp = ramp_off[k] == size_t(-1) ? nullptr : b->d_ramp + ramp_off[k];
         inst[k].trace = inst[k].log_every > 0 ? b->d_traces + trace_off[k] : nullptr;
+        inst[k].samples = inst[k].probe_first >= 0 ? b->d_samples + sample_off[k] : nullptr;
     }
     STRO_CUDA(cudaMemcpyAsync(b->d_inst, inst.data(), n * sizeof(BatchInstance),
                               cudaMemcpyHostToDevice, st));
@@ -182,6 +221,7 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
     args.count = int32_t(n);
     args.max_steps = max_steps;
     args.kepart = b->d_kepart;
+    args.fpart = probes ? b->d_fpart : nullptr;
     args.ctl = b->d_ctl;
     args.spin_limit = b->spin_limit;
 
@@ -190,22 +230,59 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
                                 b->half, int64_t(n), max_steps, int64_t(tiles),
                                 int64_t(reinterpret_cast<uintptr_t>(b->d_inst)),
                                 int64_t(reinterpret_cast<uintptr_t>(b->d_kepart)),
-                                int64_t(reinterpret_cast<uintptr_t>(b->d_ctl))};
+                                int64_t(reinterpret_cast<uintptr_t>(b->d_ctl)), probes,
+                                int64_t(reinterpret_cast<uintptr_t>(args.fpart))};
     for (size_t k = 0; k < n; ++k) {
         key.push_back(inst[k].steps);
         key.push_back(inst[k].log_every);
         key.push_back(inst[k].ntiles);
         key.push_back(inst[k].t0 & 1);
+        key.push_back(inst[k].probe_first);
+        key.push_back(inst[k].probe_period);
+        key.push_back(inst[k].probe_count);
     }
+    // what round r launches in rounds mode: the active tile prefix, and whether
+    // some instance logs or probes in it
+    auto round_plan = [&](int64_t r, uint32_t* active, bool* logs, bool* probing) {
+        *active = 0;
+        *logs = *probing = false;
+        for (size_t k = 0; k < n; ++k) {
+            if (inst[k].steps <= r) break;
+            *active = inst[k].tile_begin + inst[k].ntiles;
+            if (inst[k].log_every > 0 && r % inst[k].log_every == 0 && ((inst[k].t0 + r) & 1) == 0)
+                *logs = true;
+            if (inst[k].probe_first >= 0 && r >= inst[k].probe_first &&
+                (r - inst[k].probe_first) % inst[k].probe_period == 0 &&
+                (r - inst[k].probe_first) / inst[k].probe_period < inst[k].probe_count)
+                *probing = true;
+        }
+    };
+    auto launch_rounds = [&]() {
+        cudaError_t le = cudaSuccess;
+        for (int64_t r = 0; r < max_steps && le == cudaSuccess; ++r) {
+            uint32_t active;
+            bool logs, probing;
+            round_plan(r, &active, &logs, &probing);
+            le = launch_batch_round(args, b->half, geo, feat, probing ? 1 : 0, r, active, b->block,
+                                    st);
+            if (le == cudaSuccess && (logs || probing)) le = launch_batch_fold(args, r, st);
+        }
+        return le;
+    };
+    const bool stream_rounds = b->mode == STRO_BATCH_ROUNDS && max_steps > kMaxGraphRounds;
     unsigned grid = 0;
     if (b->mode == STRO_BATCH_PERSISTENT) {
-        const int per_sm = batch_persistent_blocks_per_sm(b->half, geo, feat, b->block);
+        const int per_sm = batch_persistent_blocks_per_sm(b->half, geo, feat, probes, b->block);
         if (per_sm <= 0) return fail(STRO_ERR_CUDA, "persistent kernel cannot be resident");
         grid = unsigned(std::min<size_t>(tiles, size_t(per_sm) * b->ctx->sm_count));
         if (grid == 0) grid = 1;
         key.push_back(grid);
     }
-    if (key != b->exec_key) {
+    if (stream_rounds) {
+        drop_graph(b);
+        STRO_CUDA(launch_rounds());
+        b->last_path = "rounds-stream";
+    } else if (key != b->exec_key) {
         drop_graph(b);
         cudaGraph_t graph = nullptr;
         cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
@@ -214,21 +291,9 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
         if (b->mode == STRO_BATCH_PERSISTENT) {
             le = cudaMemsetAsync(b->d_ctl, 0, sizeof(BatchCtl), st);
             if (le == cudaSuccess)
-                le = launch_batch_persistent(args, b->half, geo, feat, grid, b->block, st);
+                le = launch_batch_persistent(args, b->half, geo, feat, probes, grid, b->block, st);
         } else {
-            for (int64_t r = 0; r < max_steps && le == cudaSuccess; ++r) {
-                uint32_t active = 0;
-                bool logs = false;
-                for (size_t k = 0; k < n; ++k) {
-                    if (inst[k].steps <= r) break;
-                    active = inst[k].tile_begin + inst[k].ntiles;
-                    if (inst[k].log_every > 0 && r % inst[k].log_every == 0 &&
-                        ((inst[k].t0 + r) & 1) == 0)
-                        logs = true;
-                }
-                le = launch_batch_round(args, b->half, geo, feat, r, active, b->block, st);
-                if (le == cudaSuccess && logs) le = launch_batch_fold(args, r, st);
-            }
+            le = launch_rounds();
         }
         e = cudaStreamEndCapture(st, &graph);
         if (le != cudaSuccess) {
@@ -244,9 +309,11 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
         }
         b->exec_key = key;
     }
-    b->last_path = b->mode == STRO_BATCH_PERSISTENT ? "persistent-graph" : "rounds-graph";
+    if (!stream_rounds) {
+        b->last_path = b->mode == STRO_BATCH_PERSISTENT ? "persistent-graph" : "rounds-graph";
+        STRO_CUDA(cudaGraphLaunch(b->exec, st));
+    }
     b->last_rounds = max_steps;
-    STRO_CUDA(cudaGraphLaunch(b->exec, st));
     BatchCtl ctl{};
     STRO_CUDA(cudaMemcpyAsync(&ctl, b->d_ctl, sizeof ctl, cudaMemcpyDeviceToHost, st));
     STRO_CUDA(cudaStreamSynchronize(st));
@@ -257,6 +324,20 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
     if (trace_total)
         STRO_CUDA(cudaMemcpy(host.data(), b->d_traces, trace_total * sizeof(double),
                              cudaMemcpyDeviceToHost));
+    if (samples) {
+        std::vector<double> hs(sample_total);
+        if (sample_total)
+            STRO_CUDA(cudaMemcpy(hs.data(), b->d_samples, sample_total * sizeof(double),
+                                 cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < n; ++k) {
+            const size_t i = order[k];
+            const size_t cnt = plans ? 3 * size_t(std::max(plans[i].count, 0)) : 0;
+            if (inst[k].probe_first >= 0)
+                (*samples)[i].assign(hs.begin() + sample_off[k], hs.begin() + sample_off[k] + cnt);
+            else
+                (*samples)[i].assign(cnt, 0.0);  // no geometry: no momentum exchange
+        }
+    }
     for (size_t k = 0; k < n; ++k) {
         const size_t i = order[k];
         stro_sim* s = b->sims[i];
@@ -375,6 +456,8 @@ int stro_batch_destroy(stro_batch* b) {
     drop_graph(b);
     cudaFree(b->d_inst);
     cudaFree(b->d_kepart);
+    cudaFree(b->d_fpart);
+    cudaFree(b->d_samples);
     cudaFree(b->d_ctl);
     cudaFree(b->d_ramp);
     cudaFree(b->d_traces);
@@ -452,6 +535,77 @@ int stro_batch_run(stro_batch* b, const int64_t* steps, const int32_t* log_every
             trace_counts[i] = int32_t(tr[i].size());
         }
     }
+    return STRO_OK;
+}
+
+int stro_batch_run_sampled(stro_batch* b, const int64_t* transient, const int64_t* sample_steps,
+                           const int64_t* stride, const int32_t* boxes, double* const* forces,
+                           const int64_t* capacity, int64_t* samples) {
+    if (!b || !transient || !sample_steps || !stride || !boxes || !forces || !capacity || !samples)
+        return fail(STRO_ERR_INVALID, "null argument");
+    const size_t n = b->sims.size();
+    std::vector<SamplePlan> plans(n);
+    std::vector<int64_t> steps(n);
+    bool short_buffer = false;
+    for (size_t i = 0; i < n; ++i) {
+        stro_sim* s = b->sims[i];
+        const int32_t* bx = boxes + 4 * i;
+        if (s->arith != STRO_ARITH_REFERENCE)
+            return fail(STRO_ERR_INVALID, "batches run the reference arithmetic only");
+        if (!s->wants_forces) return fail(STRO_ERR_STATE, "force samples require wants_forces");
+        if (s->steps_done % 2 != 0)
+            return fail(STRO_ERR_STATE, "a sampled run must start at an even step count");
+        if (transient[i] < 0 || sample_steps[i] < 0 || stride[i] < 1)
+            return fail(STRO_ERR_INVALID, "negative step counts or stride < 1");
+        if (bx[0] < 0 || bx[1] >= s->nx || bx[2] < 0 || bx[3] >= s->ny || bx[0] > bx[1] ||
+            bx[2] > bx[3])
+            return fail(STRO_ERR_INVALID, "force box outside the lattice");
+        // the schedule of stro_sim_run_sampled (Ladder.swift:55-66)
+        const int64_t T = transient[i] & ~int64_t(1);
+        const int64_t chunk = std::max<int64_t>(2, stride[i] - 2) & ~int64_t(1);
+        const int64_t cnt = (sample_steps[i] + chunk + 1) / (chunk + 2);
+        if (chunk + 2 > INT32_MAX || cnt > INT32_MAX)
+            return fail(STRO_ERR_INVALID, "stride or sample count too large");
+        samples[i] = cnt;
+        if (cnt > capacity[i] || (cnt > 0 && !forces[i])) short_buffer = true;
+        plans[i].first = cnt > 0 ? T + chunk + 1 : -1;
+        plans[i].period = int32_t(chunk + 2);
+        plans[i].count = int32_t(cnt);
+        std::copy(bx, bx + 4, plans[i].box);
+        steps[i] = T + cnt * (chunk + 2);
+    }
+    if (short_buffer) return fail(STRO_ERR_INVALID, "a sample buffer is smaller than its run");
+    cudaSetDevice(b->ctx->device);
+    cudaStream_t st = b->ctx->stream;
+    if (b->mode == STRO_BATCH_SEQUENTIAL) {  // the reference's order, variant after variant
+        const double g0 = b->gpu_seconds;
+        double g = 0.0;
+        for (size_t i = 0; i < n; ++i) {
+            stro_sim* s = b->sims[i];
+            const double s0 = s->gpu_seconds;
+            int64_t got = 0;
+            const int rc = stro_sim_run_sampled(s, transient[i], sample_steps[i], stride[i],
+                                                boxes[4 * i], boxes[4 * i + 1], boxes[4 * i + 2],
+                                                boxes[4 * i + 3], forces[i], capacity[i], &got,
+                                                nullptr);
+            if (rc != STRO_OK) return rc;
+            g += s->gpu_seconds - s0;
+        }
+        b->gpu_seconds = g0 + g;
+        b->last_path = "sequential";
+        return STRO_OK;
+    }
+    std::vector<std::vector<double>> tr(n), out(n);
+    STRO_CUDA(cudaEventRecord(b->ev0, st));
+    const int rc = run_fused(b, steps.data(), nullptr, tr, plans.data(), &out);
+    if (rc != STRO_OK) return rc;
+    STRO_CUDA(cudaEventRecord(b->ev1, st));
+    STRO_CUDA(cudaEventSynchronize(b->ev1));
+    float ms = 0.0f;
+    STRO_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    b->gpu_seconds += double(ms) * 1e-3;
+    for (size_t i = 0; i < n; ++i)
+        if (!out[i].empty()) std::copy(out[i].begin(), out[i].end(), forces[i]);
     return STRO_OK;
 }
 

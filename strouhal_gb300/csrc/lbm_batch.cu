@@ -26,6 +26,12 @@
 // on a logging round each tile reduces sum |u|^2 of its cells (FP64, fixed
 // order) into one partial, and the partials of an instance are folded in tile
 // order after the round, so a trace is bitwise reproducible.
+//
+// Force probes (the sampled runs of a credibility ladder, Ladder.swift:54-66)
+// work the same way on the odd pass: on an instance's probe round each tile
+// reduces the momentum-exchange force of its boundary cells inside the
+// instance's box into three FP64 partials, folded in tile order into the
+// instance's sample buffer after the round.
 #include "lbm_batch.h"
 #include "lbm_cell.cuh"
 
@@ -57,7 +63,13 @@ __device__ __forceinline__ bool logs_at(const BatchInstance& I, int64_t r) {
     return I.log_every > 0 && r < I.steps && (r % I.log_every) == 0 && ((I.t0 + r) & 1) == 0;
 }
 
-template <typename S, int GEO, int FEAT, bool CG>
+__device__ __forceinline__ bool probes_at(const BatchInstance& I, int64_t r) {
+    if (I.probe_count <= 0 || r < I.probe_first) return false;
+    const int64_t d = r - I.probe_first;
+    return d % I.probe_period == 0 && d / I.probe_period < I.probe_count;
+}
+
+template <typename S, int GEO, int FEAT, bool PROBES, bool CG>
 __device__ __forceinline__ void process_tile(const BatchArgs& b, const BatchInstance& I,
                                              uint32_t tile, int64_t r) {
     const uint32_t threads = blockDim.x * blockDim.y;
@@ -76,7 +88,25 @@ __device__ __forceinline__ void process_tile(const BatchArgs& b, const BatchInst
         } else if (in) {
             even_cell<S, GEO, FEAT, false, CG>(I.a, x, y, z);
         }
-    } else if (in) {
+    } else {
+        if constexpr (PROBES) {
+            if (probes_at(I, r)) {
+                double c[3] = {0.0, 0.0, 0.0};
+                if (in) {
+                    if (I.ramp != nullptr) {
+                        const float rr = I.ramp[r];
+                        const WallVel wv(I.uin_target * rr, I.lid_target[0] * rr,
+                                         I.lid_target[1] * rr, I.lid_target[2] * rr);
+                        odd_cell<S, GEO, FEAT, true, CG>(I.a, wv, x, y, z, c);
+                    } else {
+                        odd_cell<S, GEO, FEAT, true, CG>(I.a, WallVel(I.a), x, y, z, c);
+                    }
+                }
+                block_reduce_store<3>(c, b.fpart + 3u * tile);
+                return;
+            }
+        }
+        if (!in) return;
         double dummy[3];
         if (I.ramp != nullptr) {
             const float rr = I.ramp[r];
@@ -90,8 +120,9 @@ __device__ __forceinline__ void process_tile(const BatchArgs& b, const BatchInst
 }
 
 // Fold the kinetic-energy partials of every instance that logged in round r,
-// in tile order, into its trace. Called by one whole block.
-__device__ void fold_logs(const BatchArgs& b, int64_t r) {
+// and the force partials of every instance that probed in it, in tile order,
+// into its trace or sample buffer. Called by one whole block.
+__device__ void fold_round(const BatchArgs& b, int64_t r) {
     for (int k = 0; k < b.count; ++k) {
         const BatchInstance& I = b.inst[k];
         if (!logs_at(I, r)) continue;
@@ -103,6 +134,28 @@ __device__ void fold_logs(const BatchArgs& b, int64_t r) {
         __shared__ double folded[1];
         block_reduce_store<1>(acc, folded);
         if (tid == 0 && s < I.trace_cap) I.trace[s] = folded[0];
+        __syncthreads();
+    }
+    for (int k = 0; k < b.count; ++k) {
+        const BatchInstance& I = b.inst[k];
+        if (!probes_at(I, r)) continue;
+        const int64_t s = (r - I.probe_first) / I.probe_period;
+        double acc[3] = {0.0, 0.0, 0.0};
+        const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+        const int nth = blockDim.x * blockDim.y;
+        for (uint32_t t = tid; t < I.ntiles; t += nth) {
+            const double* p = b.fpart + 3u * (I.tile_begin + t);
+            acc[0] += __ldcg(p);
+            acc[1] += __ldcg(p + 1);
+            acc[2] += __ldcg(p + 2);
+        }
+        __shared__ double folded3[3];
+        block_reduce_store<3>(acc, folded3);
+        if (tid == 0) {
+            I.samples[3 * s] = folded3[0];
+            I.samples[3 * s + 1] = folded3[1];
+            I.samples[3 * s + 2] = folded3[2];
+        }
         __syncthreads();
     }
 }
@@ -136,70 +189,80 @@ __device__ bool grid_barrier(BatchCtl* ctl, unsigned& gen, long long spin_limit,
     return *((volatile int*)&ctl->error) == 0;
 }
 
-template <typename S, int GEO, int FEAT>
+template <typename S, int GEO, int FEAT, bool PROBES>
 __global__ void __launch_bounds__(256) k_batch_persistent(const BatchArgs b) {
     unsigned gen = 0;
     for (int64_t r = 0; r < b.max_steps; ++r) {
-        if (blockIdx.x == 0 && r > 0) fold_logs(b, r - 1);
+        if (blockIdx.x == 0 && r > 0) fold_round(b, r - 1);
         const uint32_t tiles = active_tiles(b, r);
         for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
             const BatchInstance& I = b.inst[find_instance(b, tile)];
-            process_tile<S, GEO, FEAT, true>(b, I, tile, r);
+            process_tile<S, GEO, FEAT, PROBES, true>(b, I, tile, r);
         }
         if (!grid_barrier(b.ctl, gen, b.spin_limit, r)) return;
     }
-    if (blockIdx.x == 0 && b.max_steps > 0) fold_logs(b, b.max_steps - 1);
+    if (blockIdx.x == 0 && b.max_steps > 0) fold_round(b, b.max_steps - 1);
 }
 
-template <typename S, int GEO, int FEAT>
+template <typename S, int GEO, int FEAT, bool PROBES>
 __global__ void __launch_bounds__(256) k_batch_round(const BatchArgs b, int64_t r) {
     const uint32_t tile = blockIdx.x;
     const BatchInstance& I = b.inst[find_instance(b, tile)];
-    process_tile<S, GEO, FEAT, false>(b, I, tile, r);
+    process_tile<S, GEO, FEAT, PROBES, false>(b, I, tile, r);
 }
 
 __global__ void __launch_bounds__(256) k_batch_fold(const BatchArgs b, int64_t r) {
-    fold_logs(b, r);
+    fold_round(b, r);
 }
 
-template <typename S, int GEO, int FEAT>
+template <typename S, int GEO, int FEAT, bool PROBES>
 const void* persistent_fn() {
-    return reinterpret_cast<const void*>(&k_batch_persistent<S, GEO, FEAT>);
+    return reinterpret_cast<const void*>(&k_batch_persistent<S, GEO, FEAT, PROBES>);
 }
 
+// Probe-capable kernels exist for geometry batches only: without walls or
+// solid fractions nothing exchanges momentum and the host writes zero forces.
 template <typename S>
-const void* pick_persistent(int geo, int feat) {
+const void* pick_persistent(int geo, int feat, int probes) {
+    if (geo && probes)
+        return feat == 2 ? persistent_fn<S, 1, 2, true>()
+                         : (feat == 1 ? persistent_fn<S, 1, 1, true>()
+                                      : persistent_fn<S, 1, 0, true>());
     if (geo)
-        return feat == 2 ? persistent_fn<S, 1, 2>()
-                         : (feat == 1 ? persistent_fn<S, 1, 1>() : persistent_fn<S, 1, 0>());
-    return feat == 2 ? persistent_fn<S, 0, 2>()
-                     : (feat == 1 ? persistent_fn<S, 0, 1>() : persistent_fn<S, 0, 0>());
+        return feat == 2 ? persistent_fn<S, 1, 2, false>()
+                         : (feat == 1 ? persistent_fn<S, 1, 1, false>()
+                                      : persistent_fn<S, 1, 0, false>());
+    return feat == 2 ? persistent_fn<S, 0, 2, false>()
+                     : (feat == 1 ? persistent_fn<S, 0, 1, false>() : persistent_fn<S, 0, 0, false>());
+}
+
+template <typename S, int GEO, bool PROBES>
+void launch_round_feat(const BatchArgs& b, int feat, int64_t r, uint32_t tiles, dim3 block,
+                       cudaStream_t st) {
+    if (feat == 2) k_batch_round<S, GEO, 2, PROBES><<<tiles, block, 0, st>>>(b, r);
+    else if (feat == 1) k_batch_round<S, GEO, 1, PROBES><<<tiles, block, 0, st>>>(b, r);
+    else k_batch_round<S, GEO, 0, PROBES><<<tiles, block, 0, st>>>(b, r);
 }
 
 template <typename S>
-cudaError_t launch_round_typed(const BatchArgs& b, int geo, int feat, int64_t r, uint32_t tiles,
-                               dim3 block, cudaStream_t st) {
-    if (geo) {
-        if (feat == 2) k_batch_round<S, 1, 2><<<tiles, block, 0, st>>>(b, r);
-        else if (feat == 1) k_batch_round<S, 1, 1><<<tiles, block, 0, st>>>(b, r);
-        else k_batch_round<S, 1, 0><<<tiles, block, 0, st>>>(b, r);
-    } else {
-        if (feat == 2) k_batch_round<S, 0, 2><<<tiles, block, 0, st>>>(b, r);
-        else if (feat == 1) k_batch_round<S, 0, 1><<<tiles, block, 0, st>>>(b, r);
-        else k_batch_round<S, 0, 0><<<tiles, block, 0, st>>>(b, r);
-    }
+cudaError_t launch_round_typed(const BatchArgs& b, int geo, int feat, int probes, int64_t r,
+                               uint32_t tiles, dim3 block, cudaStream_t st) {
+    if (geo && probes) launch_round_feat<S, 1, true>(b, feat, r, tiles, block, st);
+    else if (geo) launch_round_feat<S, 1, false>(b, feat, r, tiles, block, st);
+    else launch_round_feat<S, 0, false>(b, feat, r, tiles, block, st);
     return cudaGetLastError();
 }
 
 }  // namespace
 
-const void* batch_persistent_kernel(int half_storage, int geo, int feat) {
-    return half_storage ? pick_persistent<__half>(geo, feat) : pick_persistent<float>(geo, feat);
+const void* batch_persistent_kernel(int half_storage, int geo, int feat, int probes) {
+    return half_storage ? pick_persistent<__half>(geo, feat, probes)
+                        : pick_persistent<float>(geo, feat, probes);
 }
 
 cudaError_t launch_batch_persistent(const BatchArgs& b, int half_storage, int geo, int feat,
-                                    unsigned grid, dim3 block, cudaStream_t st) {
-    const void* fn = batch_persistent_kernel(half_storage, geo, feat);
+                                    int probes, unsigned grid, dim3 block, cudaStream_t st) {
+    const void* fn = batch_persistent_kernel(half_storage, geo, feat, probes);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid, 1, 1);
     cfg.blockDim = block;
@@ -214,11 +277,11 @@ cudaError_t launch_batch_persistent(const BatchArgs& b, int half_storage, int ge
     return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
-cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, int feat, int64_t r,
-                               uint32_t tiles, dim3 block, cudaStream_t st) {
+cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, int feat, int probes,
+                               int64_t r, uint32_t tiles, dim3 block, cudaStream_t st) {
     if (tiles == 0) return cudaSuccess;
-    return half_storage ? launch_round_typed<__half>(b, geo, feat, r, tiles, block, st)
-                        : launch_round_typed<float>(b, geo, feat, r, tiles, block, st);
+    return half_storage ? launch_round_typed<__half>(b, geo, feat, probes, r, tiles, block, st)
+                        : launch_round_typed<float>(b, geo, feat, probes, r, tiles, block, st);
 }
 
 cudaError_t launch_batch_fold(const BatchArgs& b, int64_t r, cudaStream_t st) {
@@ -226,9 +289,9 @@ cudaError_t launch_batch_fold(const BatchArgs& b, int64_t r, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-int batch_persistent_blocks_per_sm(int half_storage, int geo, int feat, dim3 block) {
+int batch_persistent_blocks_per_sm(int half_storage, int geo, int feat, int probes, dim3 block) {
     int n = 0;
-    const void* fn = batch_persistent_kernel(half_storage, geo, feat);
+    const void* fn = batch_persistent_kernel(half_storage, geo, feat, probes);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, int(block.x * block.y * block.z), 0) !=
         cudaSuccess)
         return 0;

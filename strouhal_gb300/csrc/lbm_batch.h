@@ -19,6 +19,10 @@ struct BatchInstance {
     int32_t log_every;        // log sum |u|^2 every so many rounds (even, 0 = off)
     int32_t trace_cap;        // capacity of `trace`
     double* trace;            // kinetic-energy samples: trace[s] at round s * log_every
+    int64_t probe_first;      // round of the first force probe (an odd step), -1 = none
+    int32_t probe_period;     // rounds from one probe to the next (chunk + 2, even)
+    int32_t probe_count;      // probes in this run
+    double* samples;          // box forces, samples[3 k + d] for probe k
     uint32_t tile_begin;      // first tile of this instance in the batch tile list
     uint32_t ntiles;          // ceil(cells / threads per block)
     uint32_t cells;           // nx * ny * nz
@@ -38,15 +42,18 @@ struct BatchArgs {
     int32_t count;
     int64_t max_steps;
     double* kepart;             // one kinetic-energy partial per tile
+    double* fpart;              // three force partials per tile (probe rounds)
     BatchCtl* ctl;
     long long spin_limit;       // polls before a barrier wait gives up
 };
 
+// `probes`: some instance takes force probes in this run (geometry batches
+// only; the probe-capable kernels are used then).
 cudaError_t launch_batch_persistent(const BatchArgs& b, int half_storage, int geo, int feat,
-                                    unsigned grid, dim3 block, cudaStream_t st);
-cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, int feat, int64_t r,
-                               uint32_t tiles, dim3 block, cudaStream_t st);
+                                    int probes, unsigned grid, dim3 block, cudaStream_t st);
+cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, int feat, int probes,
+                               int64_t r, uint32_t tiles, dim3 block, cudaStream_t st);
 cudaError_t launch_batch_fold(const BatchArgs& b, int64_t r, cudaStream_t st);
-int batch_persistent_blocks_per_sm(int half_storage, int geo, int feat, dim3 block);
+int batch_persistent_blocks_per_sm(int half_storage, int geo, int feat, int probes, dim3 block);
 
 }  // namespace stro

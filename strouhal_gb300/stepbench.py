@@ -1,6 +1,9 @@
-"""Time the D3Q19 step for one kernel variant on a periodic Taylor-Green box.
+"""Time the D3Q19 step for one kernel variant on a periodic Taylor-Green box,
+or (--street D) on the DFG 2D-2 street of the credibility ladder at D cells
+per diameter (FP32 TRT, walls, NT disk, sponge; 22 D + 2 by 4.1 D + 2).
 
     python -m strouhal_gb300.stepbench --n 256 --precision fp16s --variant 2 --steps 20
+    python -m strouhal_gb300.stepbench --street 64 --variant 0 --block 32 4 --split 0
 
 Prints one line: lattice, precision, variant, launch shape, ms per step and
 GLUPS (CUDA-event device time of the step launches). Useful for comparing the
@@ -22,6 +25,10 @@ def main(argv=None):
     ap.add_argument("--trt", action="store_true", help="TRT Lambda=3/16 instead of SRT")
     ap.add_argument("--arith", default="reference", choices=["reference", "fused"],
                     help="step arithmetic (stro_sim_set_arithmetic)")
+    ap.add_argument("--street", type=int, default=0, metavar="D",
+                    help="the DFG 2D-2 street at D cells per diameter instead of the TGV box")
+    ap.add_argument("--split", type=int, default=-1, choices=[-1, 0, 1],
+                    help="bulk / boundary split of walled lattices (-1 = library default)")
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=4)
     a = ap.parse_args(argv)
@@ -30,9 +37,19 @@ def main(argv=None):
     tau = 3 * 0.05 * L / 1600 + 0.5
     wp, wm = sg.trtOmegas(tau, 3.0 / 16.0 if a.trt else None)
     gpu = sg.GPU(0)
-    s = sg.Simulation(gpu, precision=a.precision, nx=n, ny=n, nz=n, omega=wp, omegaMinus=wm,
-                      arithmetic=a.arith)
-    s.initField(2, 0.05)
+    if a.street:
+        from . import credibility as cr
+        s = cr.StreetLadder(precision=a.precision).variant(gpu, a.street, 1.0).sim
+        if a.arith != "reference":
+            s.arithmetic = a.arith
+        what = "street D=%d %dx%d" % (a.street, s.nx, s.ny)
+    else:
+        s = sg.Simulation(gpu, precision=a.precision, nx=n, ny=n, nz=n, omega=wp, omegaMinus=wm,
+                          arithmetic=a.arith)
+        s.initField(2, 0.05)
+        what = "lattice %d^3" % n
+    if a.split >= 0:
+        s.setBlockSplit(bool(a.split))
     if a.variant < 0:
         s.autotune(steps=10)
     else:
@@ -48,9 +65,9 @@ def main(argv=None):
     s.run(a.steps)
     dt = s.gpuSeconds - t0
     bx, by = {1: s.pairBlock, 2: s.rowsTile}.get(s.variant, s.block)
-    print("lattice %d^3 %s %s %s variant %d (%s) block %dx%d: %.4f ms/step, %.2f GLUPS"
-          % (n, a.precision, "TRT" if a.trt else "SRT", a.arith, s.variant, s.lastPath, bx, by,
-             1e3 * dt / a.steps, s.cells * a.steps / dt / 1e9))
+    print("%s %s %s %s variant %d (%s) block %dx%d: %.4f ms/step, %.2f GLUPS"
+          % (what, a.precision, "TRT" if a.trt or a.street else "SRT", a.arith, s.variant,
+             s.lastPath, bx, by, 1e3 * dt / a.steps, s.cells * a.steps / dt / 1e9))
     s.close()
     gpu.close()
 

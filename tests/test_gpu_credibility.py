@@ -67,6 +67,69 @@ def test_run_sampled_matches_oracle(gpu, oracle):
     s.close()
 
 
+@pytest.mark.parametrize("mode", ["persistent", "rounds", "sequential"])
+def test_batch_run_sampled_equals_single_runs(gpu, mode):
+    """Three variants of different sizes and schedules in one batched sampled
+    run: DDFs and step counts bitwise those of Simulation.runSampled, forces
+    within FP64 rounding (box sums folded per tile)."""
+    case = cr.StreetLadder()
+    plan = [(8, 1.0, 101, 300, 10), (10, 1.0, 40, 120, 26), (12, 0.5, 0, 64, 4)]
+    solo, group = [], []
+    for D, ms, tr, sa, sd in plan:
+        a, b = case.variant(gpu, D, ms), case.variant(gpu, D, ms)
+        solo.append((a, a.sim.runSampled(tr, sa, sd, *a.box)))
+        group.append(b)
+    batch = sg.Batch(gpu, [v.sim for v in group], mode=mode)
+    out = batch.runSampled([p[2] for p in plan], [p[3] for p in plan], [p[4] for p in plan],
+                           [v.box for v in group])
+    assert batch.lastPath in ({"persistent": "persistent-graph", "rounds": "rounds-graph",
+                               "sequential": "sequential"}[mode],)
+    for (a, (fa, ata)), b, (fb, atb) in zip(solo, group, out):
+        assert np.array_equal(ata, atb)
+        assert b.sim.stepsDone == a.sim.stepsDone and b.sim.stateDigest == a.sim.stateDigest
+        assert fa.shape == fb.shape and np.allclose(fb, fa, rtol=1e-12, atol=1e-16)
+        if mode == "sequential":
+            assert np.array_equal(fa, fb)
+    batch.close()
+    for (a, _), b in zip(solo, group):
+        a.sim.close()
+        b.sim.close()
+
+
+def test_batch_run_sampled_long_rounds_stream(gpu):
+    """A rounds-mode sampled run longer than one graph holds is launched round
+    by round on the stream, with the same result. (Re 20 keeps the 6-cell
+    cylinder stable over 33000 steps.)"""
+    case = cr.StreetLadder(re=20.0)
+    a, b = case.variant(gpu, 6, 1.0), case.variant(gpu, 6, 1.0)
+    fa, _ = a.sim.runSampled(32000, 1000, 40, *a.box)
+    assert np.all(np.isfinite(fa)) and np.all(fa[:, 0] > 0)
+    batch = sg.Batch(gpu, [b.sim], mode="rounds")
+    (fb, _), = batch.runSampled([32000], [1000], [40], [b.box])
+    assert batch.lastPath == "rounds-stream"
+    assert b.sim.stateDigest == a.sim.stateDigest
+    assert np.allclose(fb, fa, rtol=1e-12, atol=1e-16)
+    batch.close()
+    a.sim.close()
+    b.sim.close()
+
+
+def test_batch_run_sampled_errors(gpu):
+    case = cr.StreetLadder()
+    v = case.variant(gpu, 8, 1.0)
+    batch = sg.Batch(gpu, [v.sim])
+    with pytest.raises(sg.StrouhalError):
+        batch.runSampled([10], [10], [0], [v.box])                 # stride < 1
+    with pytest.raises(sg.StrouhalError):
+        batch.runSampled([10], [10], [10], [((0, v.sim.nx), (0, 2))])  # box outside
+    v.sim.run(1)
+    with pytest.raises(sg.StrouhalError):
+        batch.runSampled([10], [10], [10], [v.box])                # odd step count
+    assert v.sim.stepsDone == 1
+    batch.close()
+    v.sim.close()
+
+
 def test_run_sampled_errors(gpu):
     v = cr.StreetLadder().variant(gpu, 8, 1.0)
     s = v.sim
@@ -113,13 +176,18 @@ def test_short_ladder_budget_matches_oracle_and_modes_agree(gpu):
     case = cr.StreetLadder(stepsFactor=0.01)
     res = [24, 32, 40]
     seq = cr.Ladder.credibility(gpu, case, "mean C_D", res)
-    con = cr.Ladder.credibility(gpu, case, "mean C_D", res, concurrent=True)
-    for r in (seq, con):
+    con = cr.Ladder.credibility(gpu, case, "mean C_D", res, mode="concurrent")
+    bat = cr.Ladder.credibility(gpu, case, "mean C_D", res, mode="batched")
+    for r in (seq, con, bat):
         assert [x.cellsPerFeature for x in r.rungs] == res
+        assert r.digest == seq.digest
     # concurrent streams give the same bits as one variant after another
-    assert seq.digest == con.digest
     assert [(x.value, x.stat) for x in seq.rungs] == [(x.value, x.stat) for x in con.rungs]
     assert seq.series == con.series
+    # the batch folds box sums per tile: same QoIs to FP64 rounding
+    for key, vals in seq.series.items():
+        assert np.allclose(bat.series[key], vals, rtol=1e-12, atol=0), key
+    assert bat.path in ("persistent-graph", "rounds-graph", "rounds-stream", "sequential")
     num, fine, u_ma, verdict, comb = _budget_from_oracle(seq, 40)
     b = seq.budget
     assert same(b.uNum, num.u_num) and same(b.uStat, fine.half_width95) and b.uMa == u_ma

@@ -224,7 +224,7 @@ def test_report_renders_outside_and_inside():
         b = cr.UncertaintyBudget("mean C_D", 3.20, num.uNum, stat.halfWidth95, mach.uMa, verdict,
                                  [num.note])
         run = cr.CredibilityRun("mean C_D", b, rungs, num, stat, mach, 1.0, 0.5, 10, "ab" * 32,
-                                "setup", False)
+                                "setup", "sequential")
         md = cr.report_markdown(run, ["a gate"])
         assert word in md and "| 64 | 3.2000 | 0.0010 |" in md and "a gate" in md
         if verdict is far:
