@@ -259,14 +259,11 @@ def tgv(gpu, n=256, u0=0.05, t_end=20.0, precision="fp16s", lam=None, log_every=
 
 
 # ------------------------------------------------------------- sphere (C5)
-def sphere(gpu, nx=512, ny=256, nz=256, D=48, center=(128.0, 128.0, 128.0), u=0.05, re=300.0,
-           cs=0.1, steps=50000, probe_every=500, ramp=8000, sponge=True, precision="fp16s",
-           sub=8, tune=True):
-    """3-D sphere wake with LES (workload set-up from CaseSetups.swift:95-134):
-    uniform-inflow velocity walls at x = 0 and x = nx-1, periodic y and z,
-    Noble-Torczynski sphere from 8^3 subcell sampling, Smagorinsky
-    cSmago = Cs^2, Guo force field present and zero. Drag coefficient
-    2 F_x / (u^2 pi D^2 / 4) every `probe_every` steps."""
+def sphere_sim(gpu, nx=512, ny=256, nz=256, D=48, center=(128.0, 128.0, 128.0), u=0.05,
+               re=300.0, cs=0.1, ramp=8000, sponge=True, precision="fp16s", sub=8):
+    """The C5 lattice: uniform-inflow velocity walls at x = 0 and x = nx-1,
+    periodic y and z, NT sphere from sub^3 subcell sampling, Smagorinsky
+    cSmago = Cs^2, a zero Guo force field, outlet sponge one diameter wide."""
     nu = u * D / re
     wp, _ = sg.trtOmegas(3.0 * nu + 0.5, None)
     flags = np.zeros((nz, ny, nx), np.uint8)
@@ -279,6 +276,19 @@ def sphere(gpu, nx=512, ny=256, nz=256, D=48, center=(128.0, 128.0, 128.0), u=0.
     s.setForceField(np.zeros((3, nx * ny * nz), np.float32))
     if sponge:
         s.sponge = (float(nx - 1 - D), float(D), 1.0)
+    return s
+
+
+def sphere(gpu, nx=512, ny=256, nz=256, D=48, center=(128.0, 128.0, 128.0), u=0.05, re=300.0,
+           cs=0.1, steps=50000, probe_every=500, ramp=8000, sponge=True, precision="fp16s",
+           sub=8, tune=True):
+    """3-D sphere wake with LES (workload set-up from CaseSetups.swift:95-134):
+    uniform-inflow velocity walls at x = 0 and x = nx-1, periodic y and z,
+    Noble-Torczynski sphere from 8^3 subcell sampling, Smagorinsky
+    cSmago = Cs^2, Guo force field present and zero. Drag coefficient
+    2 F_x / (u^2 pi D^2 / 4) every `probe_every` steps."""
+    s = sphere_sim(gpu, nx, ny, nz, D, center, u, re, cs, ramp, sponge, precision, sub)
+    cx, cy, cz = center
     bx = (int(cx) - D // 2 - 3, int(cx) + D // 2 + 3)
     byr = (int(cy) - D // 2 - 3, int(cy) + D // 2 + 3)
     area = u * u * math.pi * D * D / 4.0

@@ -27,6 +27,8 @@ def main(argv=None):
                     help="step arithmetic (stro_sim_set_arithmetic)")
     ap.add_argument("--street", type=int, default=0, metavar="D",
                     help="the DFG 2D-2 street at D cells per diameter instead of the TGV box")
+    ap.add_argument("--sphere", action="store_true",
+                    help="the 512x256x256 sphere wake (FP16 storage, LES, NT sphere, sponge)")
     ap.add_argument("--split", type=int, default=-1, choices=[-1, 0, 1],
                     help="bulk / boundary split of walled lattices (-1 = library default)")
     ap.add_argument("--steps", type=int, default=20)
@@ -37,7 +39,13 @@ def main(argv=None):
     tau = 3 * 0.05 * L / 1600 + 0.5
     wp, wm = sg.trtOmegas(tau, 3.0 / 16.0 if a.trt else None)
     gpu = sg.GPU(0)
-    if a.street:
+    if a.sphere:
+        from . import cases
+        s = cases.sphere_sim(gpu, precision=a.precision)
+        if a.arith != "reference":
+            s.arithmetic = a.arith
+        what = "sphere 512x256x256 LES"
+    elif a.street:
         from . import credibility as cr
         s = cr.StreetLadder(precision=a.precision).variant(gpu, a.street, 1.0).sim
         if a.arith != "reference":
