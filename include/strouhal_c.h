@@ -183,6 +183,16 @@ int stro_sim_get_variant(stro_sim* sim, int32_t* variant);
 enum { STRO_ARITH_REFERENCE = 0, STRO_ARITH_FUSED = 1 };
 int stro_sim_set_arithmetic(stro_sim* sim, int32_t arith);
 int stro_sim_get_arithmetic(stro_sim* sim, int32_t* arith);
+/* Outflow walls (Cell code 4). STRO_OUTFLOW_DORMANT (default) is the
+ * reference's dormant anti-bounce-back: a link to an outflow cell reflects the
+ * shifted DDF with its sign flipped (Kernels.metal:28-29, 299-300, 328-329).
+ * STRO_OUTFLOW_PRESSURE completes it as a pressure wall at rho_w = 1: the
+ * reflected shifted DDF of link i also gains w_i (9 (c_i . u)^2 - 3 u^2), with
+ * u = p / rho of the wall cell's gathered DDFs. No reference counterpart; the
+ * adjoint requires the dormant wall. */
+enum { STRO_OUTFLOW_DORMANT = 0, STRO_OUTFLOW_PRESSURE = 1 };
+int stro_sim_set_outflow_mode(stro_sim* sim, int32_t mode);
+int stro_sim_get_outflow_mode(stro_sim* sim, int32_t* mode);
 /* Launch shape of variant 1: bx threads (a multiple of 32 dividing nx/2, at
  * most 256) covering 2*bx cells of one row; by must be 1. */
 int stro_sim_set_pair_block(stro_sim* sim, int32_t bx, int32_t by);

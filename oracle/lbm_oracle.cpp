@@ -217,9 +217,13 @@ void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt
             s = true;
         };
         for (int i = 1; i < 19; ++i) {
-            const R cu = R(3) * cdot<R>(i, ux, uy, uz);
-            const R feq = weight<R>(i) * (rhom1 + rho * (cu + R(0.5) * cu * cu - R(1.5) * u2));
-            const R d = fh[i] - feq;
+            R d = fh[i];  // fused: raw second moments, the equilibrium's are subtracted below
+            if (!FUSED) {
+                const R cu = R(3) * cdot<R>(i, ux, uy, uz);
+                const R feq =
+                    weight<R>(i) * (rhom1 + rho * (cu + R(0.5) * cu * cu - R(1.5) * u2));
+                d = fh[i] - feq;
+            }
             acc(pxx, sxx, CX[i] * CX[i], d);
             acc(pyy, syy, CY[i] * CY[i], d);
             acc(pzz, szz, CZ[i] * CZ[i], d);
@@ -227,11 +231,26 @@ void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt
             acc(pxz, sxz, CX[i] * CZ[i], d);
             acc(pyz, syz, CY[i] * CZ[i], d);
         }
-        const R Q = Sqrt(pxx * pxx + pyy * pyy + pzz * pzz +
-                         R(2) * (pxy * pxy + pxz * pxz + pyz * pyz));
+        R Q, tauEff;
         const R tau0 = R(1) / wp;
-        const R tauEff =
-            R(0.5) * (tau0 + Sqrt(tau0 * tau0 + smagConst<R>() * R(p.cSmago) * Q * inv));
+        if (!FUSED) {
+            Q = Sqrt(pxx * pxx + pyy * pyy + pzz * pzz + R(2) * (pxy * pxy + pxz * pxz + pyz * pyz));
+            tauEff = R(0.5) * (tau0 + Sqrt(tau0 * tau0 + smagConst<R>() * R(p.cSmago) * Q * inv));
+        } else {
+            // sum_i c_ia c_ib feq_i = rhom1/3 delta_ab + rho u_a u_b for shifted DDFs
+            const R r3 = rhom1 * (R(1) / R(3));
+            const R rux = rho * ux, ruy = rho * uy, ruz = rho * uz;
+            pxx = Fma(-rux, ux, pxx - r3);
+            pyy = Fma(-ruy, uy, pyy - r3);
+            pzz = Fma(-ruz, uz, pzz - r3);
+            pxy = Fma(-rux, uy, pxy);
+            pxz = Fma(-rux, uz, pxz);
+            pyz = Fma(-ruy, uz, pyz);
+            Q = Sqrt(Fma(pzz, pzz, Fma(pyy, pyy, pxx * pxx)) +
+                     R(2) * Fma(pyz, pyz, Fma(pxz, pxz, pxy * pxy)));
+            tauEff = R(0.5) *
+                     (tau0 + Sqrt(Fma(tau0, tau0, smagConst<R>() * R(p.cSmago) * Q * inv)));
+        }
         if (p.omegaMinus == p.omega) {
             wp = R(1) / tauEff;
             wm = wp;
@@ -416,10 +435,16 @@ inline void cell_slots(const Params& p, uint32_t sMask, size_t N, size_t n, int 
 // rd[i]): out[i] is stored to slot wr[i]; a[] receives the cell's
 // momentum-exchange force and force_out tells whether the reference writes it
 // (Kernels.metal:240-354, same order of operations).
+//
+// With abbp (pressure outflow, an extension of the reference's dormant
+// outflow wall): each link reflected from an outflow wall also gains
+// w_i (9 (c_i . u)^2 - 3 u^2), u = p / rho (no force term) of the gathered
+// DDFs (reflections without the terms) on the load side, before the
+// collision, and of the post-collision DDFs on the store side.
 template <class R, bool FUSED = false>
 void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_t lMask, int x,
                   int y, int z, const R in[19], R eps, const R F[3], R out[19], R a[3],
-                  bool& force_out) {
+                  bool& force_out, bool abbp = false) {
     const int nx = int(p.nx), ny = int(p.ny), nz = int(p.nz);
     R fh[19];
     for (int i = 0; i < 19; ++i) fh[i] = in[i];
@@ -455,6 +480,30 @@ void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_
             if (p.writeForce != 0u) acc_sub(i, fh[i]);
         }
     }
+    uint32_t abb = 0;
+    R wu[3] = {R(0), R(0), R(0)}, wu2 = R(0);
+    auto abb_term = [&](int i) {
+        const R cu = cdot<R>(i, wu[0], wu[1], wu[2]);
+        return weight<R>(i) * (R(9) * cu * cu - R(3) * wu2);
+    };
+    auto estimate = [&]() {  // u = p / rho of fh, the moments' summation order
+        R rhom1 = fh[0];
+        for (int i = 1; i < 19; ++i) rhom1 += fh[i];
+        R pc[3] = {R(0), R(0), R(0)};
+        bool started[3] = {false, false, false};
+        for (int i = 1; i < 19; ++i) {
+            const int c[3] = {CX[i], CY[i], CZ[i]};
+            for (int k = 0; k < 3; ++k) {
+                if (c[k] == 0) continue;
+                const R t = c[k] > 0 ? fh[i] : -fh[i];
+                pc[k] = started[k] ? pc[k] + t : t;
+                started[k] = true;
+            }
+        }
+        const R inv = R(1) / (R(1) + rhom1);
+        for (int k = 0; k < 3; ++k) wu[k] = pc[k] * inv;
+        wu2 = wu[0] * wu[0] + wu[1] * wu[1] + wu[2] * wu[2];
+    };
     if (deferred != 0u) {
         for (int i = 1; i < 19; ++i) {
             if (!((deferred >> i) & 1u)) continue;
@@ -463,6 +512,7 @@ void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_
             const uint8_t wf = flags[s];
             if (wf == OUTFLOW) {
                 fh[i] = -fh[i];
+                abb |= 1u << i;
             } else {
                 const V3<R> uw = wall_velocity<R>(wf, sy, p);
                 const R cu = cdot<R>(i, uw.x, uw.y, uw.z);
@@ -472,10 +522,16 @@ void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_
             }
         }
     }
+    if (abbp && lMask != 0u) {
+        estimate();
+        for (int i = 1; i < 19; ++i)
+            if ((abb >> i) & 1u) fh[i] += abb_term(i);
+    }
     collide<R, FUSED>(fh, p, x, eps, F, rho, nt);
     a[0] += nt[0];
     a[1] += nt[1];
     a[2] += nt[2];
+    if (abbp && lMask != 0u) estimate();
     out[0] = fh[0];
     for (int i = 1; i < 19; ++i) {
         const int dstBit = i - 1;
@@ -497,7 +553,7 @@ void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_
                 }
             }
             const R sv = sign * fh[i];
-            out[i] = has_corr ? sv - corr : sv;
+            out[i] = has_corr ? sv - corr : (abbp && sign < R(0) ? sv + abb_term(i) : sv);
             if (p.writeForce != 0u) acc_add(i, sv + R(2) * weight<R>(i));
         } else {
             out[i] = fh[i];
@@ -511,7 +567,7 @@ void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_
 template <class R, class S, class FOut, bool FUSED>
 void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMaskBuf,
                const uint32_t* lMaskBuf, const Params& p, FOut* force, const float* epsBuf,
-               const float* ffield, size_t n) {
+               const float* ffield, size_t n, bool abbp) {
     const size_t N = A.N;
     if (flags && flags[n] != FLUID) return;
     const R eps = (p.useEps != 0u && epsBuf) ? R(epsBuf[n]) : R(0);
@@ -528,7 +584,7 @@ void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMask
     R in[19], out[19], a[3];
     for (int i = 0; i < 19; ++i) in[i] = R(A.f[c.rd[i]]);
     bool fo = false;
-    cell_compute<R, FUSED>(p, flags, sMask, lMask, x, y, z, in, eps, F, out, a, fo);
+    cell_compute<R, FUSED>(p, flags, sMask, lMask, x, y, z, in, eps, F, out, a, fo, abbp);
     for (int i = 0; i < 19; ++i) A.f[c.wr[i]] = S(out[i]);
     if (fo && force) {
         force[4 * n + 0] = FOut(a[0]);
@@ -540,14 +596,15 @@ void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMask
 
 template <class R, class S, class FOut, bool FUSED = false>
 void step_all(void* f, const uint8_t* flags, const uint32_t* sm, const uint32_t* lm,
-              const Params& p, FOut* force, const float* eps, const float* ffield, int threads) {
+              const Params& p, FOut* force, const float* eps, const float* ffield, int threads,
+              bool abbp = false) {
     const size_t N = size_t(p.nx) * p.ny * p.nz;
     Field<R, S> A{static_cast<S*>(f), N};
     // The AA pattern gives every slot one reader and one writer, and they are the
     // same thread, so cells may be processed in any order or in parallel.
 #pragma omp parallel for schedule(static) num_threads(threads > 0 ? threads : 1) if (threads > 1)
     for (long long n = 0; n < (long long)N; ++n)
-        step_cell<R, S, FOut, FUSED>(A, flags, sm, lm, p, force, eps, ffield, size_t(n));
+        step_cell<R, S, FOut, FUSED>(A, flags, sm, lm, p, force, eps, ffield, size_t(n), abbp);
 }
 
 // momentsEven, Kernels.metal:359-380 (division by rho, not by a reciprocal).
@@ -698,27 +755,34 @@ int orc_params(void* out, uint32_t nx, uint32_t ny, uint32_t nz, long long step,
 
 // One full step over all cells. force: N*4 float (kinds 0/1) or double (kind 2),
 // or null. ffield: optional per-cell force field, 3 planes of N floats.
+// kind | ORC_PRESSURE_OUTFLOW: outflow walls with the pressure terms.
+constexpr int ORC_PRESSURE_OUTFLOW = 0x100;
 int orc_step(int kind, void* f, const uint8_t* flags, const uint32_t* solid_mask,
              const uint32_t* lid_mask, const void* params, void* force, const float* eps,
              const float* ffield, int threads) {
     Params p;
     std::memcpy(&p, params, sizeof p);
-    switch (kind) {
+    const bool abbp = (kind & ORC_PRESSURE_OUTFLOW) != 0;
+    switch (kind & ~ORC_PRESSURE_OUTFLOW) {
         case 0: step_all<float, float, float>(f, flags, solid_mask, lid_mask, p,
-                                              static_cast<float*>(force), eps, ffield, threads);
+                                              static_cast<float*>(force), eps, ffield, threads,
+                                              abbp);
                 return 0;
         case 1: step_all<float, _Float16, float>(f, flags, solid_mask, lid_mask, p,
-                                                 static_cast<float*>(force), eps, ffield, threads);
+                                                 static_cast<float*>(force), eps, ffield, threads,
+                                                 abbp);
                 return 0;
         case 2: step_all<double, double, double>(f, flags, solid_mask, lid_mask, p,
-                                                 static_cast<double*>(force), eps, ffield, threads);
+                                                 static_cast<double*>(force), eps, ffield, threads,
+                                                 abbp);
                 return 0;
         case 3: step_all<float, float, float, true>(f, flags, solid_mask, lid_mask, p,
-                                                    static_cast<float*>(force), eps, ffield, threads);
+                                                    static_cast<float*>(force), eps, ffield, threads,
+                                                    abbp);
                 return 0;
         case 4: step_all<float, _Float16, float, true>(f, flags, solid_mask, lid_mask, p,
                                                        static_cast<float*>(force), eps, ffield,
-                                                       threads);
+                                                       threads, abbp);
                 return 0;
     }
     return 1;

@@ -40,6 +40,7 @@ class Precision(str, enum.Enum):
 
 # Arithmetic of the step, indexed by STRO_ARITH_* (see Simulation.arithmetic).
 ARITHMETICS = ("reference", "fused")
+OUTFLOW_MODES = ("dormant", "pressure")
 
 
 class Cell(enum.IntEnum):
@@ -132,6 +133,8 @@ def lib():
         "stro_sim_set_variant": ([_P, ctypes.c_int32], c_int),
         "stro_sim_set_rows_tile": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
         "stro_sim_set_arithmetic": ([_P, ctypes.c_int32], c_int),
+        "stro_sim_set_outflow_mode": ([_P, ctypes.c_int32], c_int),
+        "stro_sim_get_outflow_mode": ([_P, ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_render_slice": ([_P, ctypes.c_int32, c_float, _P, ctypes.POINTER(c_double)], c_int),
         "stro_sim_set_pair_block": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
         "stro_sim_get_pair_block": ([_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)], c_int),
@@ -553,6 +556,21 @@ class Simulation:
         if v not in ARITHMETICS:
             raise ValueError("arithmetic must be one of %s" % (ARITHMETICS,))
         _check(lib().stro_sim_set_arithmetic(self._h, ARITHMETICS.index(v)))
+
+    @property
+    def outflowMode(self):
+        """Outflow walls: 'dormant' (the reference's sign-flip reflection) or
+        'pressure' (anti-bounce-back at rho = 1 with its velocity terms;
+        stro_sim_set_outflow_mode)."""
+        v = ctypes.c_int32()
+        _check(lib().stro_sim_get_outflow_mode(self._h, ctypes.byref(v)))
+        return OUTFLOW_MODES[v.value]
+
+    @outflowMode.setter
+    def outflowMode(self, v):
+        if v not in OUTFLOW_MODES:
+            raise ValueError("outflowMode must be one of %s" % (OUTFLOW_MODES,))
+        _check(lib().stro_sim_set_outflow_mode(self._h, OUTFLOW_MODES.index(v)))
 
     @property
     def pairBlock(self):

@@ -260,7 +260,8 @@ def tgv(gpu, n=256, u0=0.05, t_end=20.0, precision="fp16s", lam=None, log_every=
 
 # ------------------------------------------------------------- sphere (C5)
 def sphere_sim(gpu, nx=512, ny=256, nz=256, D=48, center=(128.0, 128.0, 128.0), u=0.05,
-               re=300.0, cs=0.1, ramp=8000, sponge=True, precision="fp16s", sub=8):
+               re=300.0, cs=0.1, ramp=8000, sponge=True, precision="fp16s", sub=8,
+               arithmetic="reference"):
     """The C5 lattice: uniform-inflow velocity walls at x = 0 and x = nx-1,
     periodic y and z, NT sphere from sub^3 subcell sampling, Smagorinsky
     cSmago = Cs^2, a zero Guo force field, outlet sponge one diameter wide."""
@@ -269,7 +270,8 @@ def sphere_sim(gpu, nx=512, ny=256, nz=256, D=48, center=(128.0, 128.0, 128.0), 
     flags = np.zeros((nz, ny, nx), np.uint8)
     flags[:, :, 0] = flags[:, :, -1] = sg.Cell.inflow
     s = sg.Simulation(gpu, precision=precision, nx=nx, ny=ny, nz=nz, omega=wp, uin=u,
-                      rampSteps=ramp, cSmago=cs * cs, wantsForces=True, flags=flags.reshape(-1))
+                      rampSteps=ramp, cSmago=cs * cs, wantsForces=True, flags=flags.reshape(-1),
+                      arithmetic=arithmetic)
     s.inflowUniform = True
     cx, cy, cz = center
     s.setSolidFractions(sg.sphereSolidFractions(nx, ny, nz, cx, cy, cz, D / 2.0, sub))
@@ -281,13 +283,14 @@ def sphere_sim(gpu, nx=512, ny=256, nz=256, D=48, center=(128.0, 128.0, 128.0), 
 
 def sphere(gpu, nx=512, ny=256, nz=256, D=48, center=(128.0, 128.0, 128.0), u=0.05, re=300.0,
            cs=0.1, steps=50000, probe_every=500, ramp=8000, sponge=True, precision="fp16s",
-           sub=8, tune=True):
+           sub=8, tune=True, arithmetic="reference"):
     """3-D sphere wake with LES (workload set-up from CaseSetups.swift:95-134):
     uniform-inflow velocity walls at x = 0 and x = nx-1, periodic y and z,
     Noble-Torczynski sphere from 8^3 subcell sampling, Smagorinsky
     cSmago = Cs^2, Guo force field present and zero. Drag coefficient
     2 F_x / (u^2 pi D^2 / 4) every `probe_every` steps."""
-    s = sphere_sim(gpu, nx, ny, nz, D, center, u, re, cs, ramp, sponge, precision, sub)
+    s = sphere_sim(gpu, nx, ny, nz, D, center, u, re, cs, ramp, sponge, precision, sub,
+                   arithmetic)
     cx, cy, cz = center
     bx = (int(cx) - D // 2 - 3, int(cx) + D // 2 + 3)
     byr = (int(cy) - D // 2 - 3, int(cy) + D // 2 + 3)
@@ -305,7 +308,7 @@ def sphere(gpu, nx=512, ny=256, nz=256, D=48, center=(128.0, 128.0, 128.0), u=0.
     out = {"nx": nx, "ny": ny, "nz": nz, "D": D, "re": re, "steps": s.stepsDone, "t": t,
            "cd": cd, "finite": s.checkFinite(), "gpu_seconds": s.gpuSeconds,
            "wall_seconds": wall, "glups": s.cells * s.stepsDone / max(s.gpuSeconds, 1e-30) / 1e9,
-           "variant": s.variant, "block": list(s.block)}
+           "variant": s.variant, "block": list(s.block), "arithmetic": s.arithmetic}
     s.close()
     return out
 

@@ -677,6 +677,20 @@ int stro_sim_get_arithmetic(stro_sim* s, int32_t* arith) {
     return STRO_OK;
 }
 
+int stro_sim_set_outflow_mode(stro_sim* s, int32_t mode) {
+    if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
+    if (mode != STRO_OUTFLOW_DORMANT && mode != STRO_OUTFLOW_PRESSURE)
+        return fail(STRO_ERR_INVALID, "outflow mode must be STRO_OUTFLOW_DORMANT or STRO_OUTFLOW_PRESSURE");
+    s->outflow = mode;
+    return STRO_OK;
+}
+
+int stro_sim_get_outflow_mode(stro_sim* s, int32_t* mode) {
+    if (!s || !mode) return fail(STRO_ERR_INVALID, "null argument");
+    *mode = s->outflow;
+    return STRO_OK;
+}
+
 int stro_sim_set_rows_tile(stro_sim* s, int32_t threads, int32_t rows) {
     if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
     if (threads < 32 || threads > 256 || threads % 32 != 0 || rows < 1 || rows > 8)

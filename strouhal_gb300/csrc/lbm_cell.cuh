@@ -269,28 +269,54 @@ __device__ __forceinline__ void collide(float (&fh)[19], const StepArgs& a, int 
     if constexpr (FEAT == 2) {
         if (a.c_smago > 0.0f) {  // Smagorinsky LES, Kernels.metal:140-167
             float pxx = 0.f, pyy = 0.f, pzz = 0.f, pxy = 0.f, pxz = 0.f, pyz = 0.f;
-            sfor<1, 19>([&](auto I) {
-                constexpr int i = I;
-                constexpr float w = wgt(i);
-                const float cu = 3.0f * cdot<i>(ux, uy, uz);
-                const float feq = w * (rhom1 + rho * (cu + 0.5f * cu * cu - 1.5f * u2));
-                const float d = fh[i] - feq;
-                // first nonzero term of each sum starts it (index 1, 3, 5, 7, 11, 15)
-                if constexpr (dcx(i) != 0) pxx = (i == 1) ? d : pxx + d;
-                if constexpr (dcy(i) != 0) pyy = (i == 3) ? d : pyy + d;
-                if constexpr (dcz(i) != 0) pzz = (i == 5) ? d : pzz + d;
-                if constexpr (dcx(i) * dcy(i) > 0) pxy = (i == 7) ? d : pxy + d;
-                if constexpr (dcx(i) * dcy(i) < 0) pxy -= d;
-                if constexpr (dcx(i) * dcz(i) > 0) pxz = (i == 11) ? d : pxz + d;
-                if constexpr (dcx(i) * dcz(i) < 0) pxz -= d;
-                if constexpr (dcy(i) * dcz(i) > 0) pyz = (i == 15) ? d : pyz + d;
-                if constexpr (dcy(i) * dcz(i) < 0) pyz -= d;
-            });
-            const float Q = sqrtf(pxx * pxx + pyy * pyy + pzz * pzz +
-                                  2.0f * (pxy * pxy + pxz * pxz + pyz * pyz));
+            // second moments of d_i: d = f - feq (reference), or the raw f (fused)
+            auto second_moments = [&](auto dof) {
+                sfor<1, 19>([&](auto I) {
+                    constexpr int i = I;
+                    const float d = dof(I);
+                    // first nonzero term of each sum starts it (index 1, 3, 5, 7, 11, 15)
+                    if constexpr (dcx(i) != 0) pxx = (i == 1) ? d : pxx + d;
+                    if constexpr (dcy(i) != 0) pyy = (i == 3) ? d : pyy + d;
+                    if constexpr (dcz(i) != 0) pzz = (i == 5) ? d : pzz + d;
+                    if constexpr (dcx(i) * dcy(i) > 0) pxy = (i == 7) ? d : pxy + d;
+                    if constexpr (dcx(i) * dcy(i) < 0) pxy -= d;
+                    if constexpr (dcx(i) * dcz(i) > 0) pxz = (i == 11) ? d : pxz + d;
+                    if constexpr (dcx(i) * dcz(i) < 0) pxz -= d;
+                    if constexpr (dcy(i) * dcz(i) > 0) pyz = (i == 15) ? d : pyz + d;
+                    if constexpr (dcy(i) * dcz(i) < 0) pyz -= d;
+                });
+            };
+            float Q, tauEff;
             const float tau0 = 1.0f / wp;
-            const float tauEff =
-                0.5f * (tau0 + sqrtf(tau0 * tau0 + 25.455844f * a.c_smago * Q * inv));
+            if constexpr (ARITH == ARITH_REFERENCE) {
+                second_moments([&](auto I) {
+                    constexpr int i = I;
+                    constexpr float w = wgt(i);
+                    const float cu = 3.0f * cdot<i>(ux, uy, uz);
+                    const float feq = w * (rhom1 + rho * (cu + 0.5f * cu * cu - 1.5f * u2));
+                    return fh[i] - feq;
+                });
+                Q = sqrtf(pxx * pxx + pyy * pyy + pzz * pzz +
+                          2.0f * (pxy * pxy + pxz * pxz + pyz * pyz));
+                tauEff = 0.5f * (tau0 + sqrtf(tau0 * tau0 + 25.455844f * a.c_smago * Q * inv));
+            } else {
+                // The equilibrium's second moments are known in closed form,
+                // sum_i c_ia c_ib feq_i = rhom1/3 delta_ab + rho u_a u_b (shifted
+                // DDFs), so Pi_neq = sum_i c_ia c_ib f_i minus them: no per-direction
+                // equilibria.
+                second_moments([&](auto I) { return fh[I]; });
+                const float r3 = rhom1 * (1.0f / 3.0f);
+                const float rux = rho * ux, ruy = rho * uy, ruz = rho * uz;
+                pxx = fmaf(-rux, ux, pxx - r3);
+                pyy = fmaf(-ruy, uy, pyy - r3);
+                pzz = fmaf(-ruz, uz, pzz - r3);
+                pxy = fmaf(-rux, uy, pxy);
+                pxz = fmaf(-rux, uz, pxz);
+                pyz = fmaf(-ruy, uz, pyz);
+                Q = sqrtf(fmaf(pzz, pzz, fmaf(pyy, pyy, pxx * pxx)) +
+                          2.0f * fmaf(pyz, pyz, fmaf(pxz, pxz, pxy * pxy)));
+                tauEff = 0.5f * (tau0 + sqrtf(fmaf(tau0, tau0, 25.455844f * a.c_smago * Q * inv)));
+            }
             if (a.omega_minus == a.omega) {
                 wp = 1.0f / tauEff;
                 wm = wp;
@@ -378,11 +404,12 @@ struct NbrOffsets {
 };
 
 // Deferred moving-wall corrections of the gathered DDFs, Kernels.metal:292-314.
+// Bit i of `abb` is set for each link reflected from an outflow wall.
 template <bool PROBE>
 __device__ __forceinline__ void moving_wall_loads(float (&fh)[19], const StepArgs& a,
                                                   const WallVel& wv, uint32_t wb, uint32_t lm,
                                                   int x, int y, int z, float& ax, float& ay,
-                                                  float& az) {
+                                                  float& az, uint32_t& abb) {
     sfor<1, 19>([&](auto I) {
         constexpr int i = I;
         constexpr int bit = opp(i) - 1;
@@ -394,6 +421,7 @@ __device__ __forceinline__ void moving_wall_loads(float (&fh)[19], const StepArg
             const uint8_t wf = a.cell[s] & CELL_TYPE_MASK;
             if (wf == CELL_OUTFLOW) {
                 fh[i] = -fh[i];
+                abb |= 1u << i;
             } else {
                 float uwx, uwy, uwz;
                 wall_velocity(wf, sy, a, wv, uwx, uwy, uwz);
@@ -405,13 +433,53 @@ __device__ __forceinline__ void moving_wall_loads(float (&fh)[19], const StepArg
     });
 }
 
+// Pressure outflow (anti-bounce-back at rho_w = 1 with its velocity terms):
+// the reflected shifted DDF of link i gains w_i (9 (c_i . u)^2 - 3 u^2), the
+// equilibrium part 2 w_i rho_w (1 + 4.5 (c_i . u)^2 - 1.5 u^2) of raw DDFs
+// minus the 2 w_i of the shift. u = p / rho of the wall cell's DDFs, no
+// force term: the gathered ones (reflections without the terms) for the
+// incoming links, the post-collision ones for the outgoing links.
+struct OutflowVel {
+    float ux = 0.f, uy = 0.f, uz = 0.f, u2 = 0.f;
+    __device__ __forceinline__ void estimate(const float (&fh)[19]) {
+        float rhom1 = fh[0];
+        sfor<1, 19>([&](auto I) { rhom1 += fh[I]; });
+        float px = fh[1], py = fh[3], pz = fh[5];
+        sfor<2, 19>([&](auto I) {
+            constexpr int i = I;
+            if constexpr (dcx(i) > 0) px += fh[i];
+            if constexpr (dcx(i) < 0) px -= fh[i];
+        });
+        sfor<4, 19>([&](auto I) {
+            constexpr int i = I;
+            if constexpr (dcy(i) > 0) py += fh[i];
+            if constexpr (dcy(i) < 0) py -= fh[i];
+        });
+        sfor<6, 19>([&](auto I) {
+            constexpr int i = I;
+            if constexpr (dcz(i) > 0) pz += fh[i];
+            if constexpr (dcz(i) < 0) pz -= fh[i];
+        });
+        const float inv = 1.0f / (1.0f + rhom1);
+        ux = px * inv;
+        uy = py * inv;
+        uz = pz * inv;
+        u2 = ux * ux + uy * uy + uz * uz;
+    }
+    template <int I>
+    __device__ __forceinline__ float term() const {
+        const float cu = cdot<I>(ux, uy, uz);
+        return wgt(I) * (9.0f * cu * cu - 3.0f * u2);
+    }
+};
+
 // Scatter with moving-wall corrections, Kernels.metal:317-350.
 template <typename S, bool PROBE>
 __device__ __forceinline__ void moving_wall_stores(const float (&fh)[19], const StepArgs& a,
                                                    const WallVel& wv, uint32_t n, uint32_t wb,
                                                    uint32_t lm, int x, int y, int z,
                                                    const NbrOffsets& nb, float& ax, float& ay,
-                                                   float& az) {
+                                                   float& az, const OutflowVel& ov) {
     S* __restrict__ f = static_cast<S*>(a.f);
     const uint64_t P = a.plane;
     sfor<1, 19>([&](auto I) {
@@ -429,7 +497,7 @@ __device__ __forceinline__ void moving_wall_stores(const float (&fh)[19], const 
                 const uint8_t wf = a.cell[d] & CELL_TYPE_MASK;
                 if (wf == CELL_OUTFLOW) {
                     sv = -fh[i];
-                    out = sv;
+                    out = a.outflow_pressure ? sv + ov.template term<i>() : sv;
                 } else {
                     float uwx, uwy, uwz;
                     wall_velocity(wf, dy, a, wv, uwx, uwy, uwz);
@@ -555,7 +623,15 @@ __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, i
     if constexpr (GEO) {
         if (g & GEO_MOVING) {
             lm = a.lmask[n];
-            moving_wall_loads<PROBE>(fh, a, wv, wb, lm, x, y, z, ax, ay, az);
+            uint32_t abb = 0;
+            moving_wall_loads<PROBE>(fh, a, wv, wb, lm, x, y, z, ax, ay, az, abb);
+            if (a.outflow_pressure) {
+                OutflowVel ov;
+                ov.estimate(fh);
+                sfor<1, 19>([&](auto I) {
+                    if ((abb >> int(I)) & 1u) fh[I] += ov.template term<I>();
+                });
+            }
         }
     }
     float Fx = 0.f, Fy = 0.f, Fz = 0.f;
@@ -570,7 +646,10 @@ __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, i
     forget_ptr(f);
     store_ddf<S>(f + n, fh[0]);
     if constexpr (GEO) {
-        if (!(g & GEO_MOVING)) {
+        // A warp that holds a moving-wall cell runs the moving-wall scatter for
+        // all its lanes (it covers plain and bounce-back links too) instead of
+        // running both scatters one after the other; the stored values are the same.
+        if (!__any_sync(__activemask(), (g & GEO_MOVING) != 0u)) {
             sfor<1, 19>([&](auto I) {
                 constexpr int i = I;
                 constexpr int o = opp(i);
@@ -583,7 +662,9 @@ __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, i
                 }
             });
         } else {
-            moving_wall_stores<S, PROBE>(fh, a, wv, n, wb, lm, x, y, z, nb, ax, ay, az);
+            OutflowVel ov;
+            if (a.outflow_pressure && (g & GEO_MOVING)) ov.estimate(fh);
+            moving_wall_stores<S, PROBE>(fh, a, wv, n, wb, lm, x, y, z, nb, ax, ay, az, ov);
         }
     } else {
         sfor<1, 19>([&](auto I) {

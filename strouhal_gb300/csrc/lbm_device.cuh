@@ -121,6 +121,7 @@ struct StepArgs {
     int32_t inflow_uniform;
     float sponge_x0, sponge_inv_w, sponge_tau;
     int32_t force_on;         // any nonzero uniform force or a force field
+    int32_t outflow_pressure; // outflow walls: 0 the reference's sign flip, 1 with the u-terms
     // force probe (odd pass only)
     int32_t box_x0, box_x1, box_y0, box_y1;
     double* partials;         // 3 doubles per block

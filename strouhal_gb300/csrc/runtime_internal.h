@@ -75,6 +75,7 @@ struct stro_sim {
     int rows_threads = 256;       // threads per block of the row-staged variant
     int rows_per_tile = 1;        // lattice rows per tile of the row-staged variant
     int arith = 0;                // STRO_ARITH_REFERENCE or STRO_ARITH_FUSED
+    int outflow = 0;              // STRO_OUTFLOW_DORMANT or STRO_OUTFLOW_PRESSURE
     int* d_error = nullptr;       // device error word of the row-streaming variant
     // bulk / boundary block lists of a walled lattice for the current block shape
     bool split = true;

@@ -41,9 +41,7 @@ def main(argv=None):
     gpu = sg.GPU(0)
     if a.sphere:
         from . import cases
-        s = cases.sphere_sim(gpu, precision=a.precision)
-        if a.arith != "reference":
-            s.arithmetic = a.arith
+        s = cases.sphere_sim(gpu, precision=a.precision, arithmetic=a.arith)
         what = "sphere 512x256x256 LES"
     elif a.street:
         from . import credibility as cr

@@ -102,11 +102,12 @@ def test_tgv_fp32_trt_is_reported():
     assert r["nonfinite_at"] is None or r["nonfinite_at"] > 1.0
 
 
-def test_sphere_drag_against_the_reference_correlation():
+@pytest.mark.parametrize("record", ["sphere", "sphere_fused"])
+def test_sphere_drag_against_the_reference_correlation(record):
     src = ref_source(SETUPS_SWIFT)
     m = re.search(r"cdRef = ([\d.]+) / re \* \(1\.0 \+ ([\d.]+) \* pow\(re, ([\d.]+)\)\)", src)
     a, b, c = (float(m.group(k)) for k in (1, 2, 3))
-    r = rec("sphere")
+    r = rec(record)
     assert r["finite"]
     cd = sum(r["cd"][-20:]) / 20
     ref = a / r["re"] * (1.0 + b * r["re"] ** c)

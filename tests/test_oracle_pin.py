@@ -80,7 +80,7 @@ FEATURES = [(0, 0, 0, 0, 0), (1, 0, 0, 0, 0), (0, 1, 0, 0, 0), (0, 0, 1, 0, 0),
 
 
 @pytest.mark.parametrize("kind", [0, 1])
-@pytest.mark.parametrize("walls", [0, 1])
+@pytest.mark.parametrize("walls", [0, 1, 2])  # 2: the x = nx-1 wall is a (dormant) outflow
 @pytest.mark.parametrize("feat", FEATURES)
 def test_oracle_matches_reference_source(oracle, kind, walls, feat):
     po = oracle
@@ -95,6 +95,8 @@ def test_oracle_matches_reference_source(oracle, kind, walls, feat):
             return po.LID
         if y == 0:
             return po.SOLID
+        if x == nx - 1 and walls == 2:
+            return po.OUTFLOW
         if x == 0 or x == nx - 1:
             return po.INFLOW
         if (x, y) == (5, 4):
