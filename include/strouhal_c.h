@@ -191,6 +191,16 @@ int stro_sim_get_arithmetic(stro_sim* sim, int32_t* arith);
  * u = p / rho of the wall cell's gathered DDFs. No reference counterpart; the
  * adjoint requires the dormant wall. */
 enum { STRO_OUTFLOW_DORMANT = 0, STRO_OUTFLOW_PRESSURE = 1 };
+/* Collision operator. STRO_COLLISION_REFERENCE (default): the reference's
+ * SRT / TRT with its sponge, Guo force, Smagorinsky LES and Noble-Torczynski
+ * cells. STRO_COLLISION_KBC: the KBC entropic collision (shear part of the
+ * non-equilibrium at omega, the rest with the entropic stabiliser), with the
+ * sponge and the Guo force; it refuses LES (c_smago > 0) and partially solid
+ * cells. No reference counterpart (its roadmap names a cumulant or KBC
+ * operator); one-cell kernels only; batches and the adjoint refuse it. */
+enum { STRO_COLLISION_REFERENCE = 0, STRO_COLLISION_KBC = 1 };
+int stro_sim_set_collision(stro_sim* sim, int32_t collision);
+int stro_sim_get_collision(stro_sim* sim, int32_t* collision);
 int stro_sim_set_outflow_mode(stro_sim* sim, int32_t mode);
 int stro_sim_get_outflow_mode(stro_sim* sim, int32_t* mode);
 /* Launch shape of variant 1: bx threads (a multiple of 32 dividing nx/2, at

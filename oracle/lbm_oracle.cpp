@@ -48,6 +48,10 @@ struct Params {
 };
 static_assert(sizeof(Params) == 80, "Params layout");
 
+// Options of the library's extensions, outside the reference's Params.
+constexpr int OPT_PRESSURE_OUTFLOW = 1;
+constexpr int OPT_KBC = 2;
+
 // Math through unqualified calls, so a dual-number type can supply its own.
 using std::fma;
 using std::fmax;
@@ -161,8 +165,12 @@ template <class R>
 void relax_fused(R* fh, R wp, R wm, R rho, R rhom1, R ux, R uy, R uz, R u2, const R F[3], R eps,
                  R nt[3]);
 
+template <class R>
+void relax_kbc(R* fh, R w, R rho, R rhom1, R ux, R uy, R uz, R u2, const R F[3], bool force);
+
 template <class R, bool FUSED = false>
-void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt[3]) {
+void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt[3],
+             bool kbc = false) {
     R wp = R(p.omega), wm = R(p.omegaMinus);
     if (R(x) > R(p.spongeX0)) {  // sponge, Kernels.metal:112-123
         const R frac = Fmin((R(x) - R(p.spongeX0)) * R(p.spongeInvW), R(1));
@@ -205,6 +213,12 @@ void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt
         uy = Fma(R(0.5), F[1], pc[1]) * inv;
         uz = Fma(R(0.5), F[2], pc[2]) * inv;
         u2 = Fma(uz, uz, Fma(uy, uy, ux * ux));
+    }
+    if (kbc) {  // the KBC collision: sponge and force only (the library refuses LES and NT)
+        const R u2k = ux * ux + uy * uy + uz * uz;
+        const bool force = !(F[0] == R(0)) || !(F[1] == R(0)) || !(F[2] == R(0));
+        relax_kbc<R>(fh, wp, rho, rhom1, ux, uy, uz, u2k, F, force);
+        return;
     }
 
     if (R(p.cSmago) > R(0)) {  // Smagorinsky, Kernels.metal:140-167
@@ -325,6 +339,90 @@ void collide(R* fh, const Params& p, int x, R eps, const R F[3], R& rhoOut, R nt
 // with cd = c_i . u, j = opp(i), s+/s- the split Guo source terms; partially
 // saturated cells blend with the Noble-Torczynski bounce operator as in
 // Kernels.metal:201-227. Same steps as relax_fused in lbm_cell.cuh.
+// KBC collision (an extension of the library, no reference counterpart):
+// f - feq = ds + dh, ds_i = 4.5 w_i (c_i . D . c_i) with D the deviatoric
+// non-equilibrium stress, ds relaxed at omega and dh at gamma omega / 2,
+// gamma = 1/beta - (2 - 1/beta) <ds|dh>/<dh|dh> (beta = omega/2, <x|y> =
+// sum x_i y_i / feq_i, raw feq; 2 when <dh|dh> = 0; kept in [0, 2/beta]).
+// Where F != 0 the part
+// dk_i = -1.5 w_i (c_i . F) of f - feq relaxes at omega, outside dh, and the
+// Guo source (1 - omega/2) w_i (3 c.F + 9 (c.u)(c.F) - 3 u.F) is added. Same
+// operation order as relax_kbc in lbm_cell.cuh.
+template <class R>
+void relax_kbc(R* fh, R w, R rho, R rhom1, R ux, R uy, R uz, R u2, const R F[3], bool force) {
+    auto geq = [&](int i) {
+        const R cu = i == 0 ? R(0) : R(3) * cdot<R>(i, ux, uy, uz);
+        return weight<R>(i) * (rhom1 + rho * (cu + R(0.5) * cu * cu - R(1.5) * u2));
+    };
+    R P[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};  // xx, yy, zz, xy, xz, yz
+    bool st[6] = {false, false, false, false, false, false};
+    auto acc = [&](int k, int coef, R d) {
+        if (coef == 0) return;
+        const R t = coef > 0 ? d : -d;
+        P[k] = st[k] ? P[k] + t : t;
+        st[k] = true;
+    };
+    for (int i = 1; i < 19; ++i) {
+        const R d = fh[i] - geq(i);
+        acc(0, CX[i] * CX[i], d);
+        acc(1, CY[i] * CY[i], d);
+        acc(2, CZ[i] * CZ[i], d);
+        acc(3, CX[i] * CY[i], d);
+        acc(4, CX[i] * CZ[i], d);
+        acc(5, CY[i] * CZ[i], d);
+    }
+    const R tr = (P[0] + P[1] + P[2]) * (R(1) / R(3));
+    const R dxx = P[0] - tr, dyy = P[1] - tr, dzz = P[2] - tr;
+    auto cdc = [&](int i) {  // c_i . D . c_i
+        const int a = CX[i], b = CY[i], c = CZ[i];
+        if (i == 0) return R(0);
+        if (a != 0 && b != 0) return (dxx + dyy) + R(2) * (a * b > 0 ? P[3] : -P[3]);
+        if (a != 0 && c != 0) return (dxx + dzz) + R(2) * (a * c > 0 ? P[4] : -P[4]);
+        if (b != 0 && c != 0) return (dyy + dzz) + R(2) * (b * c > 0 ? P[5] : -P[5]);
+        return a != 0 ? dxx : (b != 0 ? dyy : dzz);
+    };
+    auto dk_of = [&](int i) {
+        return i == 0 ? R(0) : (R(-1.5) * weight<R>(i)) * cdot<R>(i, F[0], F[1], F[2]);
+    };
+    auto dh_of = [&](int i, R g, R ds) {
+        R dh = (fh[i] - g) - ds;
+        if (force) dh = dh - dk_of(i);
+        return dh;
+    };
+    R sh = R(0), hh = R(0);
+    for (int i = 0; i < 19; ++i) {
+        const R g = geq(i);
+        const R ds = (R(4.5) * weight<R>(i)) * cdc(i);
+        const R dh = dh_of(i, g, ds);
+        const R r = dh / (g + weight<R>(i));
+        sh = sh + ds * r;
+        hh = hh + dh * r;
+    }
+    const R beta = R(0.5) * w;
+    const R ib = R(1) / beta;
+    const R gamma = Fmin(Fmax(hh > R(0) ? ib - (R(2) - ib) * sh / hh : R(2), R(0)), R(2) * ib);
+    const R a = R(1) - R(0.5) * w;
+    const R uF = ux * F[0] + uy * F[1] + uz * F[2];
+    R out[19];
+    for (int i = 0; i < 19; ++i) {
+        const R g = geq(i);
+        const R ds = (R(4.5) * weight<R>(i)) * cdc(i);
+        const R dh = dh_of(i, g, ds);
+        R v;
+        if (force) {
+            const R cF = i == 0 ? R(0) : cdot<R>(i, F[0], F[1], F[2]);
+            const R cu = i == 0 ? R(0) : cdot<R>(i, ux, uy, uz);
+            const R dk = (R(-1.5) * weight<R>(i)) * cF;
+            v = fh[i] - beta * (R(2) * (ds + dk) + gamma * dh);
+            v = v + a * weight<R>(i) * (R(3) * cF + R(9) * cu * cF - R(3) * uF);
+        } else {
+            v = fh[i] - beta * (R(2) * ds + gamma * dh);
+        }
+        out[i] = v;
+    }
+    for (int i = 0; i < 19; ++i) fh[i] = out[i];
+}
+
 template <class R>
 void relax_fused(R* fh, R wp, R wm, R rho, R rhom1, R ux, R uy, R uz, R u2, const R F[3], R eps,
                  R nt[3]) {
@@ -436,7 +534,8 @@ inline void cell_slots(const Params& p, uint32_t sMask, size_t N, size_t n, int 
 // momentum-exchange force and force_out tells whether the reference writes it
 // (Kernels.metal:240-354, same order of operations).
 //
-// With abbp (pressure outflow, an extension of the reference's dormant
+// opts: OPT_PRESSURE_OUTFLOW, OPT_KBC (library extensions, below).
+// With OPT_PRESSURE_OUTFLOW (pressure outflow, an extension of the reference's dormant
 // outflow wall): each link reflected from an outflow wall also gains
 // w_i (9 (c_i . u)^2 - 3 u^2), u = p / rho (no force term) of the gathered
 // DDFs (reflections without the terms) on the load side, before the
@@ -444,7 +543,9 @@ inline void cell_slots(const Params& p, uint32_t sMask, size_t N, size_t n, int 
 template <class R, bool FUSED = false>
 void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_t lMask, int x,
                   int y, int z, const R in[19], R eps, const R F[3], R out[19], R a[3],
-                  bool& force_out, bool abbp = false) {
+                  bool& force_out, int opts = 0) {
+    const bool abbp = (opts & OPT_PRESSURE_OUTFLOW) != 0;
+    const bool kbc = (opts & OPT_KBC) != 0;
     const int nx = int(p.nx), ny = int(p.ny), nz = int(p.nz);
     R fh[19];
     for (int i = 0; i < 19; ++i) fh[i] = in[i];
@@ -453,7 +554,7 @@ void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_
     a[0] = a[1] = a[2] = R(0);
     force_out = false;
     if (p.parity == 0u) {  // even: in-cell pass
-        collide<R, FUSED>(fh, p, x, eps, F, rho, nt);
+        collide<R, FUSED>(fh, p, x, eps, F, rho, nt, kbc);
         for (int i = 0; i < 19; ++i) out[i] = fh[i];
         if (p.writeForce != 0u && eps > R(0)) {
             a[0] = nt[0]; a[1] = nt[1]; a[2] = nt[2];
@@ -527,7 +628,7 @@ void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_
         for (int i = 1; i < 19; ++i)
             if ((abb >> i) & 1u) fh[i] += abb_term(i);
     }
-    collide<R, FUSED>(fh, p, x, eps, F, rho, nt);
+    collide<R, FUSED>(fh, p, x, eps, F, rho, nt, kbc);
     a[0] += nt[0];
     a[1] += nt[1];
     a[2] += nt[2];
@@ -567,7 +668,7 @@ void cell_compute(const Params& p, const uint8_t* flags, uint32_t sMask, uint32_
 template <class R, class S, class FOut, bool FUSED>
 void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMaskBuf,
                const uint32_t* lMaskBuf, const Params& p, FOut* force, const float* epsBuf,
-               const float* ffield, size_t n, bool abbp) {
+               const float* ffield, size_t n, int opts) {
     const size_t N = A.N;
     if (flags && flags[n] != FLUID) return;
     const R eps = (p.useEps != 0u && epsBuf) ? R(epsBuf[n]) : R(0);
@@ -584,7 +685,7 @@ void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMask
     R in[19], out[19], a[3];
     for (int i = 0; i < 19; ++i) in[i] = R(A.f[c.rd[i]]);
     bool fo = false;
-    cell_compute<R, FUSED>(p, flags, sMask, lMask, x, y, z, in, eps, F, out, a, fo, abbp);
+    cell_compute<R, FUSED>(p, flags, sMask, lMask, x, y, z, in, eps, F, out, a, fo, opts);
     for (int i = 0; i < 19; ++i) A.f[c.wr[i]] = S(out[i]);
     if (fo && force) {
         force[4 * n + 0] = FOut(a[0]);
@@ -597,14 +698,14 @@ void step_cell(const Field<R, S>& A, const uint8_t* flags, const uint32_t* sMask
 template <class R, class S, class FOut, bool FUSED = false>
 void step_all(void* f, const uint8_t* flags, const uint32_t* sm, const uint32_t* lm,
               const Params& p, FOut* force, const float* eps, const float* ffield, int threads,
-              bool abbp = false) {
+              int opts = 0) {
     const size_t N = size_t(p.nx) * p.ny * p.nz;
     Field<R, S> A{static_cast<S*>(f), N};
     // The AA pattern gives every slot one reader and one writer, and they are the
     // same thread, so cells may be processed in any order or in parallel.
 #pragma omp parallel for schedule(static) num_threads(threads > 0 ? threads : 1) if (threads > 1)
     for (long long n = 0; n < (long long)N; ++n)
-        step_cell<R, S, FOut, FUSED>(A, flags, sm, lm, p, force, eps, ffield, size_t(n), abbp);
+        step_cell<R, S, FOut, FUSED>(A, flags, sm, lm, p, force, eps, ffield, size_t(n), opts);
 }
 
 // momentsEven, Kernels.metal:359-380 (division by rho, not by a reciprocal).
@@ -755,15 +856,18 @@ int orc_params(void* out, uint32_t nx, uint32_t ny, uint32_t nz, long long step,
 
 // One full step over all cells. force: N*4 float (kinds 0/1) or double (kind 2),
 // or null. ffield: optional per-cell force field, 3 planes of N floats.
-// kind | ORC_PRESSURE_OUTFLOW: outflow walls with the pressure terms.
+// kind | ORC_PRESSURE_OUTFLOW: outflow walls with the pressure terms;
+// kind | ORC_KBC: the KBC collision.
 constexpr int ORC_PRESSURE_OUTFLOW = 0x100;
+constexpr int ORC_KBC = 0x200;
 int orc_step(int kind, void* f, const uint8_t* flags, const uint32_t* solid_mask,
              const uint32_t* lid_mask, const void* params, void* force, const float* eps,
              const float* ffield, int threads) {
     Params p;
     std::memcpy(&p, params, sizeof p);
-    const bool abbp = (kind & ORC_PRESSURE_OUTFLOW) != 0;
-    switch (kind & ~ORC_PRESSURE_OUTFLOW) {
+    const int abbp = ((kind & ORC_PRESSURE_OUTFLOW) ? OPT_PRESSURE_OUTFLOW : 0) |
+                     ((kind & ORC_KBC) ? OPT_KBC : 0);
+    switch (kind & ~(ORC_PRESSURE_OUTFLOW | ORC_KBC)) {
         case 0: step_all<float, float, float>(f, flags, solid_mask, lid_mask, p,
                                               static_cast<float*>(force), eps, ffield, threads,
                                               abbp);

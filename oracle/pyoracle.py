@@ -25,6 +25,7 @@ _DTYPES = {KIND_F32: np.float32, KIND_F16: np.float16, KIND_F64: np.float64}
 # step kinds of the fused-multiply-add arithmetic over FP32 / FP16 storage
 _FUSED_STEP_KIND = {KIND_F32: 3, KIND_F16: 4}
 ORC_PRESSURE_OUTFLOW = 0x100  # orc_step kind flag: outflow walls with the pressure terms
+ORC_KBC = 0x200               # orc_step kind flag: the KBC collision
 
 CX = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0])
 CY = np.array([0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1])
@@ -149,6 +150,8 @@ class OracleSim:
         # outflow walls: "dormant" (the reference's sign flip) or "pressure"
         # (anti-bounce-back with its velocity terms, the library's extension)
         self.outflowMode = "dormant"
+        # "reference" (SRT / TRT) or "kbc" (the library's KBC collision)
+        self.collision = "reference"
         self.stepsDone = 0
         self.f = np.zeros((19, self.N), _DTYPES[kind])
         if flags is None:
@@ -210,8 +213,9 @@ class OracleSim:
             p = self.params(t, writeForce=(t in self._force_steps))
             eps = self.eps if self.eps is not None else dummy_eps
             if self.backend == "ref":
-                if self.outflowMode != "dormant":
-                    raise ValueError("the reference source has the dormant outflow wall only")
+                if self.outflowMode != "dormant" or self.collision != "reference":
+                    raise ValueError("the reference source has the dormant outflow wall and "
+                                     "the SRT / TRT collision only")
                 force = self.forceBuf if self.forceBuf is not None else np.zeros((1, 4), np.float32)
                 ref_lib().ref_step(int(self.kind == KIND_F16), _ptr(self.f), _ptr(self.flags),
                                    _ptr(self.solidMask), _ptr(self.lidMask), p, _ptr(force),
@@ -219,8 +223,10 @@ class OracleSim:
             else:
                 if self.outflowMode not in ("dormant", "pressure"):
                     raise ValueError("outflowMode must be 'dormant' or 'pressure'")
+                if self.collision not in ("reference", "kbc"):
+                    raise ValueError("collision must be 'reference' or 'kbc'")
                 kind = self.step_kind | (ORC_PRESSURE_OUTFLOW if self.outflowMode == "pressure"
-                                         else 0)
+                                         else 0) | (ORC_KBC if self.collision == "kbc" else 0)
                 rc = lib().orc_step(kind, _ptr(self.f), _ptr(self.flags),
                                     _ptr(self.solidMask), _ptr(self.lidMask), p,
                                     _ptr(self.forceBuf), _ptr(eps), _ptr(self.forceField),
@@ -279,8 +285,9 @@ class OracleSim:
         FP64 (the state itself is not advanced). Returns (J, dJ/deps, dJ/dF) with
         dJ/dF of shape (3, N); the gradients are None when grads=False."""
         f0 = np.ascontiguousarray(self.f, dtype=np.float64)
-        if self.outflowMode != "dormant":
-            raise ValueError("the oracle adjoint covers the dormant outflow wall only")
+        if self.outflowMode != "dormant" or self.collision != "reference":
+            raise ValueError("the oracle adjoint covers the dormant outflow wall and the "
+                             "reference collision only")
         P = b"".join(self.params(self.stepsDone + t) for t in range(int(steps)))
         box = (ctypes.c_int * 4)(int(box[0][0]), int(box[0][1]), int(box[1][0]), int(box[1][1]))
         d3 = (ctypes.c_double * 3)(*[float(v) for v in direction])

@@ -41,6 +41,7 @@ class Precision(str, enum.Enum):
 # Arithmetic of the step, indexed by STRO_ARITH_* (see Simulation.arithmetic).
 ARITHMETICS = ("reference", "fused")
 OUTFLOW_MODES = ("dormant", "pressure")
+COLLISIONS = ("reference", "kbc")
 
 
 class Cell(enum.IntEnum):
@@ -134,6 +135,8 @@ def lib():
         "stro_sim_set_rows_tile": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
         "stro_sim_set_arithmetic": ([_P, ctypes.c_int32], c_int),
         "stro_sim_set_outflow_mode": ([_P, ctypes.c_int32], c_int),
+        "stro_sim_set_collision": ([_P, ctypes.c_int32], c_int),
+        "stro_sim_get_collision": ([_P, ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_get_outflow_mode": ([_P, ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_render_slice": ([_P, ctypes.c_int32, c_float, _P, ctypes.POINTER(c_double)], c_int),
         "stro_sim_set_pair_block": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
@@ -556,6 +559,20 @@ class Simulation:
         if v not in ARITHMETICS:
             raise ValueError("arithmetic must be one of %s" % (ARITHMETICS,))
         _check(lib().stro_sim_set_arithmetic(self._h, ARITHMETICS.index(v)))
+
+    @property
+    def collision(self):
+        """'reference' (the reference's SRT / TRT) or 'kbc' (the KBC entropic
+        collision; stro_sim_set_collision)."""
+        v = ctypes.c_int32()
+        _check(lib().stro_sim_get_collision(self._h, ctypes.byref(v)))
+        return COLLISIONS[v.value]
+
+    @collision.setter
+    def collision(self, v):
+        if v not in COLLISIONS:
+            raise ValueError("collision must be one of %s" % (COLLISIONS,))
+        _check(lib().stro_sim_set_collision(self._h, COLLISIONS.index(v)))
 
     @property
     def outflowMode(self):

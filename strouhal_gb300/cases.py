@@ -202,17 +202,19 @@ def cycle_stats(t, cd, cl, D, umean):
 
 # --------------------------------------------------------------- TGV (C2)
 def tgv(gpu, n=256, u0=0.05, t_end=20.0, precision="fp16s", lam=None, log_every=100,
-        re=1600.0):
+        re=1600.0, collision="reference"):
     """3-D Taylor-Green vortex at Re=1600 (Cases.swift:1217-1282, with the
     logging cadence of the workload): kinetic energy E = sum|u|^2/(2 N u0^2)
     and the strain-rate dissipation every `log_every` steps, dissipation also
     as -dE/dt* by central differences, peak refined by a parabola. A run that
-    goes non-finite stops and reports the time."""
+    goes non-finite stops and reports the time. collision="kbc" runs the KBC
+    collision instead of SRT / TRT."""
     L = n / (2.0 * math.pi)
     nu = u0 * L / re
     tau = 3.0 * nu + 0.5
     wp, wm = sg.trtOmegas(tau, lam)
     s = sg.Simulation(gpu, precision=precision, nx=n, ny=n, nz=n, omega=wp, omegaMinus=wm)
+    s.collision = collision
     s.initField(2, u0)
     s.autotune(steps=10)
     tc = L / u0
@@ -249,7 +251,8 @@ def tgv(gpu, n=256, u0=0.05, t_end=20.0, precision="fp16s", lam=None, log_every=
                 peak_t = t_fd[k] + dd * (t_fd[1] - t_fd[0])
                 peak_e = y1 - 0.25 * (y0 - y2) * dd
     out = {"n": n, "u0": u0, "tau": tau, "precision": precision,
-           "collision": "SRT" if lam is None else "TRT Lambda=%g" % lam, "steps": s.stepsDone,
+           "collision": ("KBC" if collision == "kbc" else
+                         "SRT" if lam is None else "TRT Lambda=%g" % lam), "steps": s.stepsDone,
            "steps_per_tstar": tc, "t": times, "E": E, "eps_strain": eps_s, "t_fd": t_fd,
            "eps_fd": eps_fd, "peak_t": peak_t, "peak_eps": peak_e, "nonfinite_at": nonfinite,
            "gpu_seconds": s.gpuSeconds, "wall_seconds": wall,

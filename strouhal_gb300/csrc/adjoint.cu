@@ -80,6 +80,8 @@ int stro_adj_create(stro_sim* s, const double dir[3], const int32_t box[4], int6
         return fail(STRO_ERR_INVALID, "the adjoint differentiates the reference arithmetic only");
     if (s->outflow != STRO_OUTFLOW_DORMANT)
         return fail(STRO_ERR_INVALID, "the adjoint covers the dormant outflow wall only");
+    if (s->collision != STRO_COLLISION_REFERENCE)
+        return fail(STRO_ERR_INVALID, "the adjoint differentiates the reference collision only");
     if (checkpoints < 1) checkpoints = 1;
     if (checkpoints > steps) checkpoints = int32_t(steps);
     if (box[0] < 0 || box[1] >= s->nx || box[2] < 0 || box[3] >= s->ny || box[0] > box[1] ||
@@ -128,6 +130,8 @@ int stro_adj_forward(stro_adjoint* a, double* J) {
         return fail(STRO_ERR_INVALID, "the adjoint differentiates the reference arithmetic only");
     if (s->outflow != STRO_OUTFLOW_DORMANT)
         return fail(STRO_ERR_INVALID, "the adjoint covers the dormant outflow wall only");
+    if (s->collision != STRO_COLLISION_REFERENCE)
+        return fail(STRO_ERR_INVALID, "the adjoint differentiates the reference collision only");
     cudaSetDevice(s->ctx->device);
     cudaStream_t st = s->ctx->stream;
     a->t0 = s->steps_done;
@@ -194,6 +198,8 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
         return fail(STRO_ERR_INVALID, "the adjoint differentiates the reference arithmetic only");
     if (s->outflow != STRO_OUTFLOW_DORMANT)
         return fail(STRO_ERR_INVALID, "the adjoint covers the dormant outflow wall only");
+    if (s->collision != STRO_COLLISION_REFERENCE)
+        return fail(STRO_ERR_INVALID, "the adjoint differentiates the reference collision only");
     cudaSetDevice(s->ctx->device);
     cudaStream_t st = s->ctx->stream;
     const uint64_t N = s->N;

@@ -424,6 +424,8 @@ int stro_batch_create(stro_ctx* ctx, int32_t count, stro_sim* const* sims, stro_
             return fail(STRO_ERR_INVALID, "batch mixes precisions");
         if (sims[i]->arith != STRO_ARITH_REFERENCE)
             return fail(STRO_ERR_INVALID, "batches run the reference arithmetic only");
+        if (sims[i]->collision != STRO_COLLISION_REFERENCE)
+            return fail(STRO_ERR_INVALID, "batches run the reference collision only");
         for (int32_t j = 0; j < i; ++j)
             if (sims[j] == sims[i]) return fail(STRO_ERR_INVALID, "simulation listed twice");
     }
@@ -499,6 +501,8 @@ int stro_batch_run(stro_batch* b, const int64_t* steps, const int32_t* log_every
         if (steps[i] < 0) return fail(STRO_ERR_INVALID, "negative step count");
         if (b->sims[i]->arith != STRO_ARITH_REFERENCE)
             return fail(STRO_ERR_INVALID, "batches run the reference arithmetic only");
+        if (b->sims[i]->collision != STRO_COLLISION_REFERENCE)
+            return fail(STRO_ERR_INVALID, "batches run the reference collision only");
         if (log_every && log_every[i] != 0) {
             if (log_every[i] < 0 || log_every[i] % 2 != 0)
                 return fail(STRO_ERR_INVALID, "log_every must be even");
@@ -552,6 +556,8 @@ int stro_batch_run_sampled(stro_batch* b, const int64_t* transient, const int64_
         const int32_t* bx = boxes + 4 * i;
         if (s->arith != STRO_ARITH_REFERENCE)
             return fail(STRO_ERR_INVALID, "batches run the reference arithmetic only");
+        if (s->collision != STRO_COLLISION_REFERENCE)
+            return fail(STRO_ERR_INVALID, "batches run the reference collision only");
         if (!s->wants_forces) return fail(STRO_ERR_STATE, "force samples require wants_forces");
         if (s->steps_done % 2 != 0)
             return fail(STRO_ERR_STATE, "a sampled run must start at an even step count");
@@ -677,6 +683,27 @@ int stro_sim_get_arithmetic(stro_sim* s, int32_t* arith) {
     return STRO_OK;
 }
 
+int stro_sim_set_collision(stro_sim* s, int32_t collision) {
+    if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
+    if (collision != STRO_COLLISION_REFERENCE && collision != STRO_COLLISION_KBC)
+        return fail(STRO_ERR_INVALID, "collision must be STRO_COLLISION_REFERENCE or STRO_COLLISION_KBC");
+    if (collision == STRO_COLLISION_KBC) {
+        if (s->c_smago > 0.0f)
+            return fail(STRO_ERR_INVALID, "the KBC collision has no Smagorinsky model");
+        for (float e : s->eps)
+            if (e > 0.0f)
+                return fail(STRO_ERR_INVALID, "the KBC collision has no partially solid cells");
+    }
+    s->collision = collision;
+    return STRO_OK;
+}
+
+int stro_sim_get_collision(stro_sim* s, int32_t* collision) {
+    if (!s || !collision) return fail(STRO_ERR_INVALID, "null argument");
+    *collision = s->collision;
+    return STRO_OK;
+}
+
 int stro_sim_set_outflow_mode(stro_sim* s, int32_t mode) {
     if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
     if (mode != STRO_OUTFLOW_DORMANT && mode != STRO_OUTFLOW_PRESSURE)
@@ -757,6 +784,7 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
                                                             int(c.x), int(c.y)))
                     continue;
                 if (variant != 0 && split == 0) continue;  // the split only changes variant 0
+                if (variant != 0 && s->collision != STRO_COLLISION_REFERENCE) continue;
                 double sec = 0.0;
                 rc = tune_sim_shape(s, steps, variant, c, &sec);
                 if (rc == STRO_OK && sec < best) {

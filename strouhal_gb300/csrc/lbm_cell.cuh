@@ -206,7 +206,120 @@ __device__ __forceinline__ void relax_fused(float (&fh)[19], float wp, float wm,
 constexpr int ARITH_REFERENCE = 0;
 constexpr int ARITH_FUSED = 1;
 
-// Collision, Kernels.metal:105-228.
+// KBC collision (Karlin, Boesch, Chikatamarla, PRE 90, 031302, 2014), an
+// extension with no reference counterpart (the reference names a cumulant or
+// KBC operator as its roadmap for the transitional Taylor-Green vortex). The
+// non-equilibrium part f - feq = ds + dh splits into a shear part ds, the
+// Hermite projection of the deviatoric non-equilibrium stress D,
+//     ds_i = 4.5 w_i (c_i . D . c_i),
+// and the rest dh. ds relaxes at omega, dh at gamma * omega / 2 with the
+// entropic stabiliser
+//     gamma = 1/beta - (2 - 1/beta) <ds|dh> / <dh|dh>,  beta = omega / 2,
+// <x|y> = sum_i x_i y_i / feq_i (raw feq); gamma = 2 is BGK. gamma is kept in
+// [0, 2/beta] (the rest relaxes at a rate between 0 and 2): where dh is at the
+// rounding level the ratio is noise, and the bound keeps gamma * dh there too.
+// With a force,
+// u = (p + F/2) / rho leaves f - feq a first moment -F/2; its part
+// dk_i = -1.5 w_i (c_i . F) relaxes at omega (as in BGK) and is kept out of
+// dh, and the Guo source (1 - omega/2) w_i (3 c.F + 9 (c.u)(c.F) - 3 u.F) is
+// added, so the momentum changes by F exactly as with BGK + Guo. The per-
+// direction values are recomputed in each pass instead of held in registers.
+template <int I>
+__device__ __forceinline__ float kbc_geq(float rho, float rhom1, float ux, float uy, float uz,
+                                         float u2) {
+    const float cu = I == 0 ? 0.0f : 3.0f * cdot<I>(ux, uy, uz);
+    return wgt(I) * (rhom1 + rho * (cu + 0.5f * cu * cu - 1.5f * u2));
+}
+
+// c_i . D . c_i: the diagonal terms in x, y, z order, then twice the one
+// off-diagonal term of a two-component direction.
+template <int I>
+__device__ __forceinline__ float kbc_cdc(float dxx, float dyy, float dzz, float dxy, float dxz,
+                                         float dyz) {
+    constexpr int a = dcx(I), b = dcy(I), c = dcz(I);
+    if constexpr (I == 0) {
+        return 0.0f;
+    } else if constexpr (a != 0 && b != 0) {
+        return (dxx + dyy) + 2.0f * (a * b > 0 ? dxy : -dxy);
+    } else if constexpr (a != 0 && c != 0) {
+        return (dxx + dzz) + 2.0f * (a * c > 0 ? dxz : -dxz);
+    } else if constexpr (b != 0 && c != 0) {
+        return (dyy + dzz) + 2.0f * (b * c > 0 ? dyz : -dyz);
+    } else {
+        return a != 0 ? dxx : (b != 0 ? dyy : dzz);
+    }
+}
+
+template <bool FORCE>
+__device__ __forceinline__ void relax_kbc(float (&fh)[19], float w, float rho, float rhom1,
+                                          float ux, float uy, float uz, float u2, float Fx,
+                                          float Fy, float Fz) {
+    float pxx = 0.f, pyy = 0.f, pzz = 0.f, pxy = 0.f, pxz = 0.f, pyz = 0.f;
+    sfor<1, 19>([&](auto I) {
+        constexpr int i = I;
+        const float d = fh[i] - kbc_geq<i>(rho, rhom1, ux, uy, uz, u2);
+        if constexpr (dcx(i) != 0) pxx = (i == 1) ? d : pxx + d;
+        if constexpr (dcy(i) != 0) pyy = (i == 3) ? d : pyy + d;
+        if constexpr (dcz(i) != 0) pzz = (i == 5) ? d : pzz + d;
+        if constexpr (dcx(i) * dcy(i) > 0) pxy = (i == 7) ? d : pxy + d;
+        if constexpr (dcx(i) * dcy(i) < 0) pxy -= d;
+        if constexpr (dcx(i) * dcz(i) > 0) pxz = (i == 11) ? d : pxz + d;
+        if constexpr (dcx(i) * dcz(i) < 0) pxz -= d;
+        if constexpr (dcy(i) * dcz(i) > 0) pyz = (i == 15) ? d : pyz + d;
+        if constexpr (dcy(i) * dcz(i) < 0) pyz -= d;
+    });
+    const float tr = (pxx + pyy + pzz) * (1.0f / 3.0f);
+    const float dxx = pxx - tr, dyy = pyy - tr, dzz = pzz - tr;
+    // dh of direction i (ds and, with a force, dk taken out)
+    auto kbc_dh = [&](auto I, float geq, float ds) {
+        constexpr int i = I;
+        float dh = (fh[i] - geq) - ds;
+        if constexpr (FORCE) {
+            const float dk = i == 0 ? 0.0f : (-1.5f * wgt(i)) * cdot<i>(Fx, Fy, Fz);
+            dh = dh - dk;
+        }
+        return dh;
+    };
+    float sh = 0.0f, hh = 0.0f;
+    sfor<0, 19>([&](auto I) {
+        constexpr int i = I;
+        const float geq = kbc_geq<i>(rho, rhom1, ux, uy, uz, u2);
+        const float ds = (4.5f * wgt(i)) * kbc_cdc<i>(dxx, dyy, dzz, pxy, pxz, pyz);
+        const float dh = kbc_dh(I, geq, ds);
+        const float r = dh / (geq + wgt(i));
+        sh = sh + ds * r;
+        hh = hh + dh * r;
+    });
+    const float beta = 0.5f * w;
+    const float ib = 1.0f / beta;
+    const float gamma =
+        fminf(fmaxf(hh > 0.0f ? ib - (2.0f - ib) * sh / hh : 2.0f, 0.0f), 2.0f * ib);
+    float a = 0.0f, uF = 0.0f;
+    if constexpr (FORCE) {
+        a = 1.0f - 0.5f * w;
+        uF = ux * Fx + uy * Fy + uz * Fz;
+    }
+    sfor<0, 19>([&](auto I) {
+        constexpr int i = I;
+        const float geq = kbc_geq<i>(rho, rhom1, ux, uy, uz, u2);
+        const float ds = (4.5f * wgt(i)) * kbc_cdc<i>(dxx, dyy, dzz, pxy, pxz, pyz);
+        const float dh = kbc_dh(I, geq, ds);
+        float v;
+        if constexpr (FORCE) {
+            const float cF = i == 0 ? 0.0f : cdot<i>(Fx, Fy, Fz);
+            const float cu = i == 0 ? 0.0f : cdot<i>(ux, uy, uz);
+            const float dk = (-1.5f * wgt(i)) * cF;
+            v = fh[i] - beta * (2.0f * (ds + dk) + gamma * dh);
+            v = v + a * wgt(i) * (3.0f * cF + 9.0f * cu * cF - 3.0f * uF);
+        } else {
+            v = fh[i] - beta * (2.0f * ds + gamma * dh);
+        }
+        fh[i] = v;
+    });
+}
+
+// Collision, Kernels.metal:105-228. FEAT 3 is the KBC collision (sponge and
+// force as FEAT 1; no LES, no Noble-Torczynski cells).
 template <int FEAT, int ARITH = ARITH_REFERENCE>
 __device__ __forceinline__ void collide(float (&fh)[19], const StepArgs& a, int x, float eps,
                                         float Fx, float Fy, float Fz, float& ntx, float& nty,
@@ -262,6 +375,14 @@ __device__ __forceinline__ void collide(float (&fh)[19], const StepArgs& a, int 
         ux = px * inv;
         uy = py * inv;
         uz = pz * inv;
+    }
+    if constexpr (FEAT == 3) {  // KBC (the arithmetic only changes u); no LES, no NT cells
+        const float u2k = ux * ux + uy * uy + uz * uz;
+        // the Guo source where the cell's force is nonzero
+        if (a.force_on && (Fx != 0.0f || Fy != 0.0f || Fz != 0.0f))
+            relax_kbc<true>(fh, wp, rho, rhom1, ux, uy, uz, u2k, Fx, Fy, Fz);
+        else relax_kbc<false>(fh, wp, rho, rhom1, ux, uy, uz, u2k, Fx, Fy, Fz);
+        return;
     }
     const float u2 = ARITH == ARITH_REFERENCE ? ux * ux + uy * uy + uz * uz
                                               : fmaf(uz, uz, fmaf(uy, uy, ux * ux));

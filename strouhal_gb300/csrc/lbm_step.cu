@@ -18,7 +18,9 @@
 //   GEO  = 0 periodic all-fluid box: no cell bytes, masks or wall logic;
 //          1 walls and/or partially saturated cells.
 //   FEAT = 0 lean collide: no sponge, LES, body force or NT cells;
-//          1 all features, each behind a uniform or per-cell branch.
+//          1 sponge, body force, NT cells, each behind a uniform or per-cell branch;
+//          2 also the Smagorinsky LES block;
+//          3 the KBC collision instead of SRT / TRT (sponge and body force).
 //   PROBE  odd pass with momentum-exchange force accumulation, reduced per
 //          block in FP64 in a fixed order (no per-cell force buffer).
 //
@@ -153,7 +155,8 @@ static void launch_list(const StepArgs& a, int parity, const uint32_t* list, uin
 template <typename S, int GEO>
 static void launch_list_level(const StepArgs& a, int parity, int feat, const uint32_t* list,
                               uint32_t count, dim3 block, cudaStream_t st) {
-    if (feat == 2) launch_list<S, GEO, 2>(a, parity, list, count, block, st);
+    if (feat == 3) launch_list<S, GEO, 3>(a, parity, list, count, block, st);
+    else if (feat == 2) launch_list<S, GEO, 2>(a, parity, list, count, block, st);
     else if (feat == 1) launch_list<S, GEO, 1>(a, parity, list, count, block, st);
     else launch_list<S, GEO, 0>(a, parity, list, count, block, st);
 }
@@ -191,7 +194,8 @@ template <typename S>
 static cudaError_t launch_typed(const StepArgs& a, int parity, int geo, int feat, bool probe,
                                 dim3 grid, dim3 block, cudaStream_t st) {
     if (probe && (parity == 0 || !geo)) return cudaErrorInvalidValue;
-    if (feat == 2) launch_level<S, 2>(a, parity, geo, probe, grid, block, st);
+    if (feat == 3) launch_level<S, 3>(a, parity, geo, probe, grid, block, st);
+    else if (feat == 2) launch_level<S, 2>(a, parity, geo, probe, grid, block, st);
     else if (feat == 1) launch_level<S, 1>(a, parity, geo, probe, grid, block, st);
     else launch_level<S, 0>(a, parity, geo, probe, grid, block, st);
     return cudaGetLastError();

@@ -63,6 +63,7 @@ bool force_on(const stro_sim* s) {
            s->force[2] != 0.0f;
 }
 int feat_on(const stro_sim* s) {
+    if (s->collision == STRO_COLLISION_KBC) return 3;
     if (s->c_smago > 0.0f) return 2;  // features with the Smagorinsky block compiled in
     return (s->has_eps || sponge_active(s) || force_on(s)) ? 1 : 0;
 }
@@ -284,6 +285,7 @@ static int ensure_block_lists(stro_sim* s) {
 
 // Feature level of wall-free cells (no solid fraction among them).
 static int bulk_feat(const stro_sim* s) {
+    if (s->collision == STRO_COLLISION_KBC) return 3;
     if (s->c_smago > 0.0f) return 2;
     return (sponge_active(s) || force_on(s)) ? 1 : 0;
 }
@@ -301,15 +303,16 @@ cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool prob
                        s->nbulk, s->d_blocks + s->nbulk, s->nedge, s->ctx->stream);
     }
     const PairLaunchers& PL = fused ? fused::kPair : exact::kPair;
-    if (s->variant == 1 && PL.supported(half, geo, probe, s->nx, s->plane, s->pair_block)) {
+    const bool kbc = s->collision == STRO_COLLISION_KBC;  // one-cell kernels only
+    if (!kbc && s->variant == 1 && PL.supported(half, geo, probe, s->nx, s->plane, s->pair_block)) {
         s->last_path = "pair";
         return PL.launch(a, int(t & 1), feat_on(s), s->pair_block, s->ctx->stream);
     }
-    if (s->variant == 3 && !geo && !probe && s->block.x * s->block.y <= 128) {
+    if (!kbc && s->variant == 3 && !geo && !probe && s->block.x * s->block.y <= 128) {
         s->last_path = "capped";
         return L.capped(a, half, int(t & 1), feat_on(s), s->block, s->ctx->stream);
     }
-    if (s->variant == 2 &&
+    if (!kbc && s->variant == 2 &&
         R.supported(half, geo, probe, s->nx, s->ny, s->rows_threads, s->rows_per_tile)) {
         s->last_path = "rows";
         return R.launch(a, half, int(t & 1), feat_on(s), s->rows_threads, s->rows_per_tile,
@@ -516,6 +519,8 @@ int stro_sim_set_force(stro_sim* s, const float f[3]) {
 }
 int stro_sim_set_c_smago(stro_sim* s, float c) {
     CHECK_SIM(s);
+    if (c > 0.0f && s->collision == STRO_COLLISION_KBC)
+        return fail(STRO_ERR_INVALID, "the KBC collision has no Smagorinsky model");
     s->c_smago = c;
     return STRO_OK;
 }
@@ -537,6 +542,10 @@ int stro_sim_set_sponge(stro_sim* s, int enabled, float x0, float width, float t
 int stro_sim_set_solid_fractions(stro_sim* s, const float* eps) {
     CHECK_SIM(s);
     if (!eps) return fail(STRO_ERR_INVALID, "null eps");
+    if (s->collision == STRO_COLLISION_KBC)
+        for (uint64_t n = 0; n < s->N; ++n)
+            if (eps[n] > 0.0f)
+                return fail(STRO_ERR_INVALID, "the KBC collision has no partially solid cells");
     cudaSetDevice(s->ctx->device);
     s->eps.assign(eps, eps + s->N);
     s->has_eps = true;

@@ -76,6 +76,7 @@ struct stro_sim {
     int rows_per_tile = 1;        // lattice rows per tile of the row-staged variant
     int arith = 0;                // STRO_ARITH_REFERENCE or STRO_ARITH_FUSED
     int outflow = 0;              // STRO_OUTFLOW_DORMANT or STRO_OUTFLOW_PRESSURE
+    int collision = 0;            // STRO_COLLISION_REFERENCE or STRO_COLLISION_KBC
     int* d_error = nullptr;       // device error word of the row-streaming variant
     // bulk / boundary block lists of a walled lattice for the current block shape
     bool split = true;
@@ -92,7 +93,8 @@ namespace rt {
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
 bool geo_on(const stro_sim* s);
-// Feature level of the step kernels: 0 lean, 1 sponge / force / NT, 2 also LES.
+// Feature level of the step kernels: 0 lean, 1 sponge / force / NT, 2 also LES,
+// 3 the KBC collision.
 int feat_on(const stro_sim* s);
 float ramp_factor(const stro_sim* s, int64_t t);
 StepArgs step_args(const stro_sim* s, int64_t t);

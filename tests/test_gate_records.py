@@ -208,3 +208,36 @@ def test_credibility_gates_and_budget_from_the_oracle():
     far = uo.classify(250000.0, 0.09, 48, "bluff body in channel")
     assert far.verdict == uo.OUTSIDE and math.isnan(uo.combined(0.01, 0.01, 0.01, far))
     assert all(r["gates"].values())
+
+
+def test_tgv_kbc_dissipation_peak_and_curve():
+    """The KBC collision on the 256^3 FP16 TGV: the reference's peak gates
+    (Cases.swift:1311-1327) and a dissipation curve at least as close to the
+    DNS table as the SRT run's."""
+    src = ref_source(CASES_SWIFT)
+    m = re.search(r"let tgvRefPeak = \(t: ([\d.]+), eps: ([\d.]+)\)", src)
+    t_ref, e_ref = float(m.group(1)), float(m.group(2))
+    table = ref_table(src, "tgvReference")
+    r, srt = rec("tgv_kbc"), rec("tgv")
+    assert r["collision"] == "KBC" and r["nonfinite_at"] is None
+    assert abs(r["peak_t"] - t_ref) <= 0.5
+    assert abs(r["peak_eps"] - e_ref) / e_ref <= 0.10
+
+    def rms(rr):
+        t, e = rr["t_fd"], rr["eps_fd"]
+        d = [min(range(len(t)), key=lambda k: abs(t[k] - tr)) for tr, _ in table
+             if 1.0 <= tr <= 10.5]
+        ref = [er for tr, er in table if 1.0 <= tr <= 10.5]
+        return math.sqrt(sum((e[j] - v) ** 2 for j, v in zip(d, ref)) / len(ref))
+
+    assert rms(r) <= rms(srt)
+
+
+def test_kbc_carries_the_transitional_tgv_through_the_decay():
+    """128^3, u0 = 0.1 (tau 0.5038): TRT Lambda = 1/4 goes non-finite in the
+    transition (the reference measured t* = 5.4, Cases.swift:1290-1293); KBC
+    runs the whole decay to t* = 14."""
+    trt, kbc = rec("tgv_trt128_u01"), rec("tgv_kbc128_u01")
+    assert trt["nonfinite_at"] is not None and trt["nonfinite_at"] < 6.0
+    assert kbc["nonfinite_at"] is None and kbc["t"][-1] >= 13.9  # last sample before t* = 14
+    assert all(b <= a for a, b in zip(kbc["E"], kbc["E"][1:]))
