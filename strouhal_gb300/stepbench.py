@@ -31,6 +31,8 @@ def main(argv=None):
                     help="the 512x256x256 sphere wake (FP16 storage, LES, NT sphere, sponge)")
     ap.add_argument("--split", type=int, default=-1, choices=[-1, 0, 1],
                     help="bulk / boundary split of walled lattices (-1 = library default)")
+    ap.add_argument("--collision", default="reference", choices=["reference", "kbc"],
+                    help="collision operator (stro_sim_set_collision)")
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=4)
     a = ap.parse_args(argv)
@@ -54,6 +56,8 @@ def main(argv=None):
                           arithmetic=a.arith)
         s.initField(2, 0.05)
         what = "lattice %d^3" % n
+    if a.collision != "reference":
+        s.collision = a.collision
     if a.split >= 0:
         s.setBlockSplit(bool(a.split))
     if a.variant < 0:
@@ -72,7 +76,8 @@ def main(argv=None):
     dt = s.gpuSeconds - t0
     bx, by = {1: s.pairBlock, 2: s.rowsTile}.get(s.variant, s.block)
     print("%s %s %s %s variant %d (%s) block %dx%d: %.4f ms/step, %.2f GLUPS"
-          % (what, a.precision, "TRT" if a.trt or a.street else "SRT", a.arith, s.variant,
+          % (what, a.precision, "KBC" if a.collision == "kbc" else
+             ("TRT" if a.trt or a.street else "SRT"), a.arith, s.variant,
              s.lastPath, bx, by, 1e3 * dt / a.steps, s.cells * a.steps / dt / 1e9))
     s.close()
     gpu.close()
