@@ -17,7 +17,8 @@ PREC = {0: "fp32", 1: "fp16s"}
 @pytest.mark.parametrize("kind", [0, 1])
 @pytest.mark.parametrize("geometry", ["periodic", "channel"])
 @pytest.mark.parametrize("split", [True, False])
-def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split):
+@pytest.mark.parametrize("collision", ["trt", "srt"])
+def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split, collision):
     import strouhal_gb300 as sg
 
     po = oracle
@@ -25,8 +26,8 @@ def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split):
     rng = np.random.default_rng(17 + kind + 2 * (geometry == "channel") + 4 * split)
     flags = None
     eps = None
-    kw = dict(omega=1.55, omegaMinus=1.2, uin=0.05, rampSteps=7, force=(3e-5, -1e-5, 2e-5),
-              cSmago=0.01, wantsForces=True)
+    kw = dict(omega=1.55, omegaMinus=1.2 if collision == "trt" else 1.55, uin=0.05, rampSteps=7,
+              force=(3e-5, -1e-5, 2e-5), cSmago=0.01, wantsForces=True)
     if geometry == "channel":
         fl = np.zeros((nz, ny, nx), np.uint8)
         fl[:, 0, :] = fl[:, -1, :] = po.SOLID
@@ -65,14 +66,15 @@ def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split):
                                            (3, (32, 4)), (1, None)])
 @pytest.mark.parametrize("kind", [0, 1])
 @pytest.mark.parametrize("feature", ["plain", "force_les_sponge"])
-def test_fused_variants_match_fused_oracle(gpu, oracle, variant, shape, kind, feature):
+@pytest.mark.parametrize("srt", [False, True])
+def test_fused_variants_match_fused_oracle(gpu, oracle, variant, shape, kind, feature, srt):
     """Periodic lattice: every variant in the fused arithmetic (variant 1, the
     FP16 pair kernel, has no fused build and runs variant 0)."""
     import strouhal_gb300 as sg
 
     po = oracle
     nx, ny, nz = 64, 6, 5
-    kw = dict(omega=1.7, omegaMinus=1.3)
+    kw = dict(omega=1.7, omegaMinus=1.7 if srt else 1.3)
     if feature != "plain":
         kw.update(force=(2e-5, -3e-5, 1e-5), cSmago=0.01)
     g = sg.Simulation(gpu, precision=PREC[kind], nx=nx, ny=ny, nz=nz, arithmetic="fused", **kw)
