@@ -171,12 +171,15 @@ __global__ void k_render(FieldView v, const float* eps, uint32_t z, float uref, 
 }
 
 // Per cell: |u|^2 (FP32, as the host energy loop forms it) and the viscous
-// dissipation 2 nu S:S with S = -(3 omega / (2 rho)) Pi_neq.
+// dissipation 2 nu S:S with S = -(3 omega / (2 rho)) Pi_neq, both formed in
+// FP32 and summed in FP64 (one FP64 add per cell and quantity: the FP64 rate
+// of this part is a small fraction of its FP32 rate, so per-cell FP64
+// arithmetic would make the reduction compute-bound). nu comes from the host,
+// formed in FP64 from omega.
 template <typename S>
-__global__ void __launch_bounds__(kThreads) k_observables(FieldView v, float omega,
+__global__ void __launch_bounds__(kThreads) k_observables(FieldView v, float omega, float nu,
                                                           double* partials) {
     double acc[2] = {0.0, 0.0};
-    const double nu = (1.0 / (double)omega - 0.5) / 3.0;
     for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < v.N; n += gridDim.x * blockDim.x) {
         if (v.cell != nullptr && (v.cell[n] & CELL_TYPE_MASK) != CELL_FLUID) continue;
         float fh[19];
@@ -201,10 +204,10 @@ __global__ void __launch_bounds__(kThreads) k_observables(FieldView v, float ome
             if constexpr (dcy(i) * dcz(i) > 0) pyz += d;
             if constexpr (dcy(i) * dcz(i) < 0) pyz -= d;
         });
-        const double pipi = (double)pxx * pxx + (double)pyy * pyy + (double)pzz * pzz +
-                            2.0 * ((double)pxy * pxy + (double)pxz * pxz + (double)pyz * pyz);
-        const double s = 1.5 * (double)omega / (double)rho;
-        acc[1] += 2.0 * nu * s * s * pipi;
+        const float pipi = pxx * pxx + pyy * pyy + pzz * pzz +
+                           2.0f * (pxy * pxy + pxz * pxz + pyz * pyz);
+        const float s = 1.5f * omega / rho;
+        acc[1] += (double)(2.0f * nu * s * s * pipi);
     }
     block_reduce_store<2>(acc, partials + 2u * blockIdx.x);
 }
@@ -289,8 +292,9 @@ cudaError_t launch_render(const FieldView& v, int half_storage, const float* eps
 cudaError_t launch_observables(const FieldView& v, int half_storage, float omega,
                                double* partials, double* out, cudaStream_t st) {
     const int nb = reduction_blocks(v.N);
-    if (half_storage) k_observables<__half><<<nb, kThreads, 0, st>>>(v, omega, partials);
-    else k_observables<float><<<nb, kThreads, 0, st>>>(v, omega, partials);
+    const float nu = float((1.0 / double(omega) - 0.5) / 3.0);
+    if (half_storage) k_observables<__half><<<nb, kThreads, 0, st>>>(v, omega, nu, partials);
+    else k_observables<float><<<nb, kThreads, 0, st>>>(v, omega, nu, partials);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return launch_fold(partials, nb, 2, out, st);
