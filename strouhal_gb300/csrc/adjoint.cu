@@ -224,10 +224,18 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
                                   cudaMemcpyDeviceToDevice, st));
         for (int64_t k = 1; k < len; ++k) {
             void* cur = state_at(a->d_seg, a->state_bytes, k);
-            STRO_CUDA(cudaMemcpyAsync(cur, state_at(a->d_seg, a->state_bytes, k - 1),
-                                      a->state_bytes, cudaMemcpyDeviceToDevice, st));
+            void* prev = state_at(a->d_seg, a->state_bytes, k - 1);
             StepArgs sa = step_args(s, a->t0 + k0 + k - 1);
-            sa.f = cur;
+            if (geo) {
+                // walled lattices run one-cell or block-list kernels, which can
+                // write the pass out of place: no copy of the previous state
+                sa.f = prev;
+                sa.f_out = cur;
+            } else {
+                STRO_CUDA(cudaMemcpyAsync(cur, prev, a->state_bytes, cudaMemcpyDeviceToDevice,
+                                          st));
+                sa.f = cur;
+            }
             STRO_CUDA(launch_sim_step(s, sa, a->t0 + k0 + k - 1, false));
         }
         int rc = timed(a, &a->recompute_seconds, STRO_OK);

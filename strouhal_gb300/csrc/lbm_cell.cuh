@@ -596,12 +596,11 @@ struct OutflowVel {
 
 // Scatter with moving-wall corrections, Kernels.metal:317-350.
 template <typename S, bool PROBE>
-__device__ __forceinline__ void moving_wall_stores(const float (&fh)[19], const StepArgs& a,
-                                                   const WallVel& wv, uint32_t n, uint32_t wb,
-                                                   uint32_t lm, int x, int y, int z,
-                                                   const NbrOffsets& nb, float& ax, float& ay,
-                                                   float& az, const OutflowVel& ov) {
-    S* __restrict__ f = static_cast<S*>(a.f);
+__device__ __forceinline__ void moving_wall_stores(S* __restrict__ f, const float (&fh)[19],
+                                                   const StepArgs& a, const WallVel& wv,
+                                                   uint32_t n, uint32_t wb, uint32_t lm, int x,
+                                                   int y, int z, const NbrOffsets& nb, float& ax,
+                                                   float& ay, float& az, const OutflowVel& ov) {
     const uint64_t P = a.plane;
     sfor<1, 19>([&](auto I) {
         constexpr int i = I;
@@ -674,8 +673,10 @@ __device__ __forceinline__ void forget_ptr(P& p) {
 
 // Even (in-cell) pass of one cell, Kernels.metal:252-260. Non-fluid cells are
 // skipped. With LOG, u2 receives |u|^2 of the state before the step.
+// OUT: honour StepArgs::f_out (out-of-place pass); on by default where the
+// lattice has walls, and for the block-list kernels of the bulk / boundary split.
 template <typename S, int GEO, int FEAT, bool LOG = false, bool CG = false,
-          int ARITH = ARITH_REFERENCE>
+          int ARITH = ARITH_REFERENCE, bool OUT = (GEO != 0)>
 __device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z,
                                           float* u2 = nullptr) {
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
@@ -697,6 +698,9 @@ __device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z
     float ntx = 0.f, nty = 0.f, ntz = 0.f;
     collide<FEAT, ARITH>(fh, a, x, eps, Fx, Fy, Fz, ntx, nty, ntz);
     forget_ptr(f);
+    if constexpr (OUT) {  // out of place
+        if (a.f_out != nullptr) f = static_cast<S*>(a.f_out);
+    }
     store_ddf<S>(f + n, fh[0]);
     sfor<1, 19>([&](auto I) { store_ddf<S>(f + uint64_t(opp(I)) * P + n, fh[I]); });
 }
@@ -705,7 +709,7 @@ __device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z
 // Kernels.metal:261-354. With PROBE the cell's momentum-exchange force is
 // returned in contrib when the cell is a boundary cell inside the probe box.
 template <typename S, int GEO, int FEAT, bool PROBE, bool CG = false,
-          int ARITH = ARITH_REFERENCE>
+          int ARITH = ARITH_REFERENCE, bool OUT = (GEO != 0)>
 __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, int x, int y,
                                          int z, double (&contrib)[3]) {
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
@@ -765,6 +769,9 @@ __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, i
         az += ntz;
     }
     forget_ptr(f);
+    if constexpr (OUT) {  // out of place
+        if (a.f_out != nullptr) f = static_cast<S*>(a.f_out);
+    }
     store_ddf<S>(f + n, fh[0]);
     if constexpr (GEO) {
         // A warp that holds a moving-wall cell runs the moving-wall scatter for
@@ -785,7 +792,7 @@ __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, i
         } else {
             OutflowVel ov;
             if (a.outflow_pressure && (g & GEO_MOVING)) ov.estimate(fh);
-            moving_wall_stores<S, PROBE>(fh, a, wv, n, wb, lm, x, y, z, nb, ax, ay, az, ov);
+            moving_wall_stores<S, PROBE>(f, fh, a, wv, n, wb, lm, x, y, z, nb, ax, ay, az, ov);
         }
     } else {
         sfor<1, 19>([&](auto I) {

@@ -122,6 +122,10 @@ struct StepArgs {
     float sponge_x0, sponge_inv_w, sponge_tau;
     int32_t force_on;         // any nonzero uniform force or a force field
     int32_t outflow_pressure; // outflow walls: 0 the reference's sign flip, 1 with the u-terms
+    void* f_out;              // one-cell kernels of walled lattices and the block-list
+                              // kernels of the split: write the pass here instead of in
+                              // place (same layout; every slot a fluid cell owns is
+                              // written, the other slots are not)
     // force probe (odd pass only)
     int32_t box_x0, box_x1, box_y0, box_y1;
     double* partials;         // 3 doubles per block

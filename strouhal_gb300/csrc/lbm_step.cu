@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(256) k_list_even(const StepArgs a, const uint3
     int x, y, z;
     list_block(list, gx, gy, x, y, z);
     if (x >= a.nx || y >= a.ny) return;
-    even_cell<S, GEO, FEAT, false, false, STRO_ARITH>(a, x, y, z);
+    even_cell<S, GEO, FEAT, false, false, STRO_ARITH, true>(a, x, y, z);
 }
 
 template <typename S, int GEO, int FEAT>
@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(256) k_list_odd(const StepArgs a, const uint32
     list_block(list, gx, gy, x, y, z);
     if (x >= a.nx || y >= a.ny) return;
     double contrib[3];
-    odd_cell<S, GEO, FEAT, false, false, STRO_ARITH>(a, WallVel(a), x, y, z, contrib);
+    odd_cell<S, GEO, FEAT, false, false, STRO_ARITH, true>(a, WallVel(a), x, y, z, contrib);
 }
 
 template <typename S, int GEO, int FEAT>

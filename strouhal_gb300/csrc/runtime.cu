@@ -113,6 +113,7 @@ StepArgs step_args(const stro_sim* s, int64_t t) {
     a.force_on = force_on(s) ? 1 : 0;
     a.outflow_pressure = s->outflow == STRO_OUTFLOW_PRESSURE ? 1 : 0;
     a.box_x0 = 0; a.box_x1 = -1; a.box_y0 = 0; a.box_y1 = -1;
+    a.f_out = nullptr;
     a.partials = s->d_partials;
     return a;
 }

@@ -157,12 +157,15 @@ def test_adjoint_cost_and_gradients():
     r = rec("sphere_adjoint")
     assert r["grad_finite"]
     assert r["adjoint_step_over_forward_step"] <= 3.0
+    # the whole backward sweep, recomputation included, within 3x the forward window
+    assert r["backward_over_forward"] <= 3.0
     d = os.path.join(REC, "dfg2_adjoint.json")
     if os.path.exists(d):
         with open(d) as fh:
             a = json.load(fh)
         worst = max(abs(c["adjoint"] - c["fd"]) / max(abs(c["fd"]), 1e-12) for c in a["fd"])
         assert worst < 5e-2, a["fd"]
+        assert a["backward_over_forward"] <= 3.0
 
 
 def test_precision_record():
