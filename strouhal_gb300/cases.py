@@ -127,11 +127,13 @@ def ghia_rms(rec, table_u, table_v):
 
 # ------------------------------------------------------------ DFG 2D-2 (C3)
 def dfg2(gpu, D=64, uin_max=0.06, nz=3, transient=None, sample_cycles=22, stride=26,
-         sponge_d=3, sponge_tau=1.0, ramp=24000, precision="fp32", max_steps=None):
+         sponge_d=3, sponge_tau=1.0, ramp=24000, precision="fp32", max_steps=None, tune=True):
     """Cylinder channel with Noble-Torczynski walls (Cases.swift:840-951,
     CaseSetups.swift:29-65): C_D and C_L sampled every `stride` steps by the
     two-step force probe, Strouhal number from the upward zero crossings of
-    C_L, peaks and cycle means over complete cycles."""
+    C_L, peaks and cycle means over complete cycles. The transient and the
+    samples run as one sampled submission (the same steps and probes as
+    run(stride - 2) + probeForce per sample, bit for bit)."""
     nx = 22 * D + 2
     ny = int(4.1 * D) + 2
     umean = uin_max * 2.0 / 3.0
@@ -149,25 +151,25 @@ def dfg2(gpu, D=64, uin_max=0.06, nz=3, transient=None, sample_cycles=22, stride
     box_y = (int(cy) - D // 2 - 3, int(cy) + D // 2 + 3)
     if transient is None:
         transient = (int(60000 * 0.075 / uin_max) + 1) & ~1
+    if tune:
+        s.autotune(steps=200)  # kernel variant, launch shape and split (state restored)
     t0 = time.perf_counter()
-    s.run(transient)
     period = D / (0.30 * umean)
     samples = int(period * sample_cycles / stride) + 64
     if max_steps is not None:
         samples = min(samples, max(1, (max_steps - transient) // stride))
     norm = umean * umean * D * nz  # force per unit depth: the z extent holds nz cells
-    cd, cl, t = [], [], []
-    for _ in range(samples):
-        s.run(stride - 2)
-        f = s.probeForce(box_x, box_y)
-        cd.append(2.0 * f[0] / norm)
-        cl.append(2.0 * f[1] / norm)
-        t.append(s.stepsDone)
+    forces, at = s.runSampled(transient, samples * stride, stride, box_x, box_y)
+    cd = [float(v) for v in 2.0 * forces[:, 0] / norm]
+    cl = [float(v) for v in 2.0 * forces[:, 1] / norm]
+    t = [int(v) for v in at]
     wall = time.perf_counter() - t0
     stats = cycle_stats(t, cd, cl, D, umean)
     out = {"D": D, "nx": nx, "ny": ny, "nz": nz, "uin_max": uin_max, "steps": s.stepsDone,
            "stride": stride, "t": t, "cd": cd, "cl": cl, "digest": s.stateDigest,
            "gpu_seconds": s.gpuSeconds, "wall_seconds": wall,
+           "glups": nx * ny * nz * s.stepsDone / max(s.gpuSeconds, 1e-30) / 1e9,
+           "variant": s.variant, "block": list(s.block), "path": s.lastPath,
            "cells": nx * ny * nz}
     out.update(stats)
     s.close()
@@ -477,12 +479,14 @@ def _dfg2_sim(gpu, D, uin_max, nz, precision, ramp, sponge_d=3, sponge_tau=1.0):
 
 
 def dfg2_adjoint(gpu, D=64, uin_max=0.06, nz=3, total=200000, window=10000, checkpoints=20,
-                 fd_cells=8, fd_h=0.02, seed=7, precision="fp32", ramp=24000):
+                 fd_cells=8, fd_h=0.02, seed=7, precision="fp32", ramp=24000, tune=False):
     """Adjoint of the time-averaged C_D over the last `window` steps of the
     cylinder run with respect to the solid-fraction field (20 checkpoints),
     checked by central differences of the same FP32 forward on `fd_cells`
     random boundary cells with 0 < eps < 1. Also times forward and backward."""
     s, eps, box, umean = _dfg2_sim(gpu, D, uin_max, nz, precision, ramp)
+    if tune:
+        s.autotune(steps=200)  # the forward's kernel and launch shape (state restored)
     s.run(total - window)
     start = s.downloadState()
     t_start = s.stepsDone
