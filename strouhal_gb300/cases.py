@@ -529,7 +529,7 @@ def dfg2_adjoint(gpu, D=64, uin_max=0.06, nz=3, total=200000, window=10000, chec
 
 
 def sphere_adjoint(gpu, nx=512, ny=256, nz=256, D=48, u=0.05, re=300.0, cs=0.1, spinup=4000,
-                   window=2000, checkpoints=45, precision="fp16s"):
+                   window=2000, checkpoints=45, precision="fp16s", tune=False):
     """Adjoint of the mean drag over `window` steps of the sphere wake with
     respect to the Guo force field, sqrt(window) checkpoints: gradient
     statistics and the forward / backward device time."""
@@ -546,6 +546,8 @@ def sphere_adjoint(gpu, nx=512, ny=256, nz=256, D=48, u=0.05, re=300.0, cs=0.1, 
     s.setForceField(np.zeros((3, nx * ny * nz), np.float32))
     s.sponge = (float(nx - 1 - D), float(D), 1.0)
     box = ((int(cx) - D // 2 - 3, int(cx) + D // 2 + 3), (int(cy) - D // 2 - 3, int(cy) + D // 2 + 3))
+    if tune:
+        s.autotune(steps=10)  # the forward's kernel and launch shape (state restored)
     s.run(spinup)
     adj = sg.Adjoint(s, window, box, checkpoints=checkpoints)
     J = adj.forward()

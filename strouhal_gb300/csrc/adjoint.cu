@@ -34,6 +34,8 @@ struct stro_adjoint {
     float* d_geps = nullptr;
     float* d_gf = nullptr;
     double* d_forces = nullptr;  // 3 doubles per odd step
+    uint32_t* d_lists = nullptr; // bulk blocks, then boundary blocks, of the reverse-step grid
+    uint32_t nbulk = 0, nedge = 0;
     int64_t nodd = 0;
     double J = 0.0;
     double fwd_seconds = 0.0, recompute_seconds = 0.0, adjoint_seconds = 0.0;
@@ -50,6 +52,7 @@ void adj_free(stro_adjoint* a) {
     cudaFree(a->d_geps);
     cudaFree(a->d_gf);
     cudaFree(a->d_forces);
+    cudaFree(a->d_lists);
     if (a->e0) cudaEventDestroy(a->e0);
     if (a->e1) cudaEventDestroy(a->e1);
 }
@@ -212,6 +215,20 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
     STRO_CUDA(cudaMemsetAsync(a->d_gf, 0, 3 * N * sizeof(float), st));
     const float w = a->nodd ? float(1.0 / double(a->nodd)) : 0.0f;
     const dim3 ablock(32, 4, 1);
+    // walled lattice: bulk blocks take the wall-free reverse step, as the forward split does
+    const bool split = geo && s->split && s->geo_host.size() == N;
+    if (split) {  // from the geometry as it is now
+        cudaFree(a->d_lists);
+        a->d_lists = nullptr;
+        std::vector<uint32_t> bulk, edge;
+        block_lists(s, ablock, bulk, edge);
+        a->nbulk = uint32_t(bulk.size());
+        a->nedge = uint32_t(edge.size());
+        bulk.insert(bulk.end(), edge.begin(), edge.end());
+        STRO_CUDA(cudaMalloc(&a->d_lists, std::max<size_t>(bulk.size(), 1) * sizeof(uint32_t)));
+        STRO_CUDA(cudaMemcpy(a->d_lists, bulk.data(), bulk.size() * sizeof(uint32_t),
+                             cudaMemcpyHostToDevice));
+    }
     void* live = s->d_f;  // the forward kernels step the buffer a StepArgs points to
     for (int32_t c = a->ncheck - 1; c >= 0; --c) {
         const int64_t k0 = int64_t(c) * a->seg;
@@ -255,7 +272,11 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
             for (int q = 0; q < 3; ++q) g.dir[q] = float(a->dir[q]);
             std::memcpy(g.box, a->box, sizeof g.box);
             g.force_terms = 1;
-            STRO_CUDA(launch_adjoint_step(g, half, int(t & 1), geo, ablock, st));
+            if (split)
+                STRO_CUDA(launch_adjoint_split(g, half, int(t & 1), ablock, a->d_lists, a->nbulk,
+                                               a->d_lists + a->nbulk, a->nedge, st));
+            else
+                STRO_CUDA(launch_adjoint_step(g, half, int(t & 1), geo, ablock, st));
             ++a->adjoint_launches;
         }
         rc = timed(a, &a->adjoint_seconds, STRO_OK);

@@ -313,13 +313,10 @@ __device__ __forceinline__ void add_grads(const AdjArgs& g, uint32_t n, float ep
     }
 }
 
+// One cell of the reverse even (in-cell) pass.
 template <typename S, int GEO>
-__global__ void __launch_bounds__(128) k_adj_even(const AdjArgs g) {
+__device__ __forceinline__ void adj_even_cell(const AdjArgs& g, int x, int y, int z) {
     const StepArgs& a = g.a;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z;
-    if (x >= a.nx || y >= a.ny) return;
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
     float eps = 0.0f;
     if constexpr (GEO) {
@@ -343,17 +340,10 @@ __global__ void __launch_bounds__(128) k_adj_even(const AdjArgs g) {
     add_grads(g, n, eps, epsb, Fbx, Fby, Fbz);
 }
 
-// At least four resident blocks: left to itself the compiler gives the odd
-// adjoint 184 registers (two blocks of 128 threads per SM, 12% of the warp
-// slots, IPC 1.0); capped at 128 (a few spilled words) the reverse step of
-// the cylinder runs in 1.78x a forward step instead of 2.20x.
+// One cell of the reverse odd (streaming) pass.
 template <typename S, int GEO>
-__global__ void __launch_bounds__(128, 4) k_adj_odd(const AdjArgs g) {
+__device__ __forceinline__ void adj_odd_cell(const AdjArgs& g, int x, int y, int z) {
     const StepArgs& a = g.a;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z;
-    if (x >= a.nx || y >= a.ny) return;
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
     uint32_t geo = 0, lm = 0;
     float eps = 0.0f;
@@ -444,7 +434,84 @@ __global__ void __launch_bounds__(128, 4) k_adj_odd(const AdjArgs g) {
     add_grads(g, n, eps, epsb, Fbx, Fby, Fbz);
 }
 
+// Block of a block list: block i of the grid processes lattice block list[i]
+// (linear index bx + gx * (by + gy * bz)) of the (blockDim.x, blockDim.y) grid.
+__device__ __forceinline__ void adj_list_block(const uint32_t* list, uint32_t gx, uint32_t gy,
+                                               int& x, int& y, int& z) {
+    const uint32_t blk = list[blockIdx.x];
+    const uint32_t t = blk / gx;
+    x = int((blk - t * gx) * blockDim.x + threadIdx.x);
+    y = int((t % gy) * blockDim.y + threadIdx.y);
+    z = int(t / gy);
+}
+
+template <typename S, int GEO>
+__global__ void __launch_bounds__(128) k_adj_even(const AdjArgs g) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= g.a.nx || y >= g.a.ny) return;
+    adj_even_cell<S, GEO>(g, x, y, blockIdx.z);
+}
+
+// At least four resident blocks: left to itself the compiler gives the odd
+// adjoint 184 registers (two blocks of 128 threads per SM, 12% of the warp
+// slots, IPC 1.0); capped at 128 (a few spilled words) the reverse step of
+// the cylinder runs in 1.78x a forward step instead of 2.20x.
+template <typename S, int GEO>
+__global__ void __launch_bounds__(128, 4) k_adj_odd(const AdjArgs g) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= g.a.nx || y >= g.a.ny) return;
+    adj_odd_cell<S, GEO>(g, x, y, blockIdx.z);
+}
+
+// Block-list forms for the bulk / boundary split of a walled lattice: the
+// bulk blocks (no wall, no wall neighbour, no solid fraction) take the
+// wall-free reverse step, the boundary blocks the wall-aware one, as in the
+// forward split. The per-cell values are the same as the grid forms'.
+template <typename S, int GEO>
+__global__ void __launch_bounds__(128) k_adj_list_even(const AdjArgs g, const uint32_t* list,
+                                                       uint32_t gx, uint32_t gy) {
+    int x, y, z;
+    adj_list_block(list, gx, gy, x, y, z);
+    if (x >= g.a.nx || y >= g.a.ny) return;
+    adj_even_cell<S, GEO>(g, x, y, z);
+}
+
+template <typename S, int GEO>
+__global__ void __launch_bounds__(128, 4) k_adj_list_odd(const AdjArgs g, const uint32_t* list,
+                                                         uint32_t gx, uint32_t gy) {
+    int x, y, z;
+    adj_list_block(list, gx, gy, x, y, z);
+    if (x >= g.a.nx || y >= g.a.ny) return;
+    adj_odd_cell<S, GEO>(g, x, y, z);
+}
+
+template <typename S, int GEO>
+void launch_adj_list(const AdjArgs& g, int parity, const uint32_t* list, uint32_t count,
+                     dim3 block, cudaStream_t st) {
+    if (count == 0) return;
+    const uint32_t gx = (uint32_t(g.a.nx) + block.x - 1) / block.x;
+    const uint32_t gy = (uint32_t(g.a.ny) + block.y - 1) / block.y;
+    if (parity == 0) k_adj_list_even<S, GEO><<<count, block, 0, st>>>(g, list, gx, gy);
+    else k_adj_list_odd<S, GEO><<<count, block, 0, st>>>(g, list, gx, gy);
+}
+
 }  // namespace
+
+cudaError_t launch_adjoint_split(const AdjArgs& g, int half_storage, int parity, dim3 block,
+                                 const uint32_t* bulk, uint32_t nbulk, const uint32_t* edge,
+                                 uint32_t nedge, cudaStream_t st) {
+    if (block.x * block.y > 128) return cudaErrorInvalidValue;
+    if (half_storage) {
+        launch_adj_list<__half, 0>(g, parity, bulk, nbulk, block, st);
+        launch_adj_list<__half, 1>(g, parity, edge, nedge, block, st);
+    } else {
+        launch_adj_list<float, 0>(g, parity, bulk, nbulk, block, st);
+        launch_adj_list<float, 1>(g, parity, edge, nedge, block, st);
+    }
+    return cudaGetLastError();
+}
 
 cudaError_t launch_adjoint_step(const AdjArgs& g, int half_storage, int parity, int geo, dim3 block,
                                 cudaStream_t st) {

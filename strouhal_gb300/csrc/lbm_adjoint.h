@@ -20,5 +20,11 @@ struct AdjArgs {
 
 cudaError_t launch_adjoint_step(const AdjArgs& g, int half_storage, int parity, int geo, dim3 block,
                                 cudaStream_t st);
+// The reverse step split like the forward one over block lists of the
+// (block.x, block.y) grid: `bulk` blocks wall-free, `edge` blocks wall-aware.
+// At most 128 threads per block.
+cudaError_t launch_adjoint_split(const AdjArgs& g, int half_storage, int parity, dim3 block,
+                                 const uint32_t* bulk, uint32_t nbulk, const uint32_t* edge,
+                                 uint32_t nedge, cudaStream_t st);
 
 }  // namespace stro

@@ -249,14 +249,13 @@ int ensure_partials(stro_sim* s, size_t doubles) {
 // Bulk / boundary block lists for the current block shape (rebuilt when the
 // shape or the geometry changes). A block is bulk when every cell it covers is
 // fluid with no wall neighbour, no moving wall nearby and no solid fraction.
-static int ensure_block_lists(stro_sim* s) {
-    if (s->lists_version == s->geo_version && s->lists_block.x == s->block.x &&
-        s->lists_block.y == s->block.y)
-        return STRO_OK;
-    const uint32_t bx = s->block.x, by = s->block.y;
+void block_lists(const stro_sim* s, dim3 shape, std::vector<uint32_t>& bulk,
+                 std::vector<uint32_t>& edge) {
+    const uint32_t bx = shape.x, by = shape.y;
     const uint32_t gx = (uint32_t(s->nx) + bx - 1) / bx, gy = (uint32_t(s->ny) + by - 1) / by;
     const uint64_t nblocks = uint64_t(gx) * gy * uint64_t(s->nz);
-    std::vector<uint32_t> bulk, edge;
+    bulk.clear();
+    edge.clear();
     bulk.reserve(nblocks);
     for (uint64_t b = 0; b < nblocks; ++b) {
         const uint32_t bxi = uint32_t(b % gx), t = uint32_t(b / gx), byi = t % gy, z = t / gy;
@@ -271,6 +270,17 @@ static int ensure_block_lists(stro_sim* s) {
         }
         (is_bulk ? bulk : edge).push_back(uint32_t(b));
     }
+}
+
+static int ensure_block_lists(stro_sim* s) {
+    if (s->lists_version == s->geo_version && s->lists_block.x == s->block.x &&
+        s->lists_block.y == s->block.y)
+        return STRO_OK;
+    const uint32_t bx = s->block.x, by = s->block.y;
+    const uint32_t gx = (uint32_t(s->nx) + bx - 1) / bx, gy = (uint32_t(s->ny) + by - 1) / by;
+    const uint64_t nblocks = uint64_t(gx) * gy * uint64_t(s->nz);
+    std::vector<uint32_t> bulk, edge;
+    block_lists(s, s->block, bulk, edge);
     cudaFree(s->d_blocks);
     s->d_blocks = nullptr;
     STRO_CUDA(cudaMalloc(&s->d_blocks, std::max<size_t>(nblocks, 1) * sizeof(uint32_t)));

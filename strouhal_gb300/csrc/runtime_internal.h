@@ -93,6 +93,11 @@ namespace rt {
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
 bool geo_on(const stro_sim* s);
+// Bulk and boundary blocks of the (shape.x, shape.y) block grid of a walled
+// lattice (host geometry copies must be current): a bulk block holds only
+// fluid cells without wall neighbours or solid fractions.
+void block_lists(const stro_sim* s, dim3 shape, std::vector<uint32_t>& bulk,
+                 std::vector<uint32_t>& edge);
 // Feature level of the step kernels: 0 lean, 1 sponge / force / NT, 2 also LES,
 // 3 the KBC collision.
 int feat_on(const stro_sim* s);
