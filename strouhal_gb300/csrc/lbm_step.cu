@@ -44,8 +44,11 @@ namespace stro {
 namespace STRO_ARITH_NS {
 
 // ---------------------------------------------------------------- kernels
+// The KBC collision (FEAT 3) is capped at 80 registers (three blocks of 256
+// per SM, a few spilled words): 31.6 GLUPS on the FP16 256^3 TGV against
+// 29.1 at the compiler's 93/114. The other levels keep the compiler's choice.
 template <typename S, int GEO, int FEAT>
-__global__ void __launch_bounds__(256) k_step_even(const StepArgs a) {
+__global__ void __launch_bounds__(256, FEAT == 3 ? 3 : 0) k_step_even(const StepArgs a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= a.nx || y >= a.ny) return;
@@ -53,7 +56,7 @@ __global__ void __launch_bounds__(256) k_step_even(const StepArgs a) {
 }
 
 template <typename S, int GEO, int FEAT, bool PROBE>
-__global__ void __launch_bounds__(256) k_step_odd(const StepArgs a) {
+__global__ void __launch_bounds__(256, FEAT == 3 && GEO == 0 ? 3 : 0) k_step_odd(const StepArgs a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     double contrib[3] = {0.0, 0.0, 0.0};
