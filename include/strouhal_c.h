@@ -242,6 +242,13 @@ int stro_batch_set_mode(stro_batch* batch, int32_t mode);
 int stro_batch_set_tile(stro_batch* batch, int32_t bx, int32_t by);
 /* Polls before a grid-barrier wait gives up with STRO_ERR_TIMEOUT. */
 int stro_batch_set_spin_limit(stro_batch* batch, int64_t polls);
+/* STRO_BATCH_ROUNDS on simulations with walls or solid fractions: when on (the
+ * default) each round runs the tiles whose cells are all plain fluid without
+ * wall neighbours on the wall-free kernels and the rest on the wall-aware
+ * ones (results bitwise the same). stro_batch_split_tiles reports the last
+ * run's bulk and boundary tile counts (0, 0 when it ran unsplit). */
+int stro_batch_set_split(stro_batch* batch, int32_t on);
+int stro_batch_split_tiles(const stro_batch* batch, int64_t* bulk, int64_t* edge);
 /* Advance sims[i] by steps[i] steps (DDFs bitwise identical to stro_sim_run).
  * If log_every != NULL and log_every[i] > 0 (even; sims[i] at an even step
  * count), sum |u|^2 is sampled before the first step and after every

@@ -155,6 +155,8 @@ def lib():
         "stro_batch_set_mode": ([_P, ctypes.c_int32], c_int),
         "stro_batch_set_tile": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
         "stro_batch_set_spin_limit": ([_P, c_i64], c_int),
+        "stro_batch_set_split": ([_P, ctypes.c_int32], c_int),
+        "stro_batch_split_tiles": ([_P, _P, _P], c_int),
         "stro_batch_run": ([_P, _P, _P, _P, ctypes.c_int32, _P], c_int),
         "stro_batch_gpu_seconds": ([_P, ctypes.POINTER(c_double)], c_int),
         "stro_batch_run_sampled": ([_P, _P, _P, _P, _P, _P, _P, _P], c_int),
@@ -660,6 +662,17 @@ class Batch:
 
     def setSpinLimit(self, polls):
         _check(lib().stro_batch_set_spin_limit(self._h, int(polls)))
+
+    def setSplit(self, on):
+        """Rounds mode on walled lattices: bulk tiles on the wall-free kernels."""
+        _check(lib().stro_batch_set_split(self._h, 1 if on else 0))
+
+    @property
+    def splitTiles(self):
+        """(bulk, boundary) tiles of the last run; (0, 0) when it ran unsplit."""
+        bu, ed = ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().stro_batch_split_tiles(self._h, ctypes.byref(bu), ctypes.byref(ed)))
+        return bu.value, ed.value
 
     def run(self, steps, logEvery=None):
         """Advance sims[i] by steps[i]; returns kinetic-energy traces (lists) or None."""

@@ -47,6 +47,10 @@ struct stro_batch {
     size_t fpart_cap = 0;
     double* d_samples = nullptr;
     size_t samples_cap = 0;
+    uint32_t* d_tiles = nullptr;  // rounds mode: bulk tile list, then boundary tile list
+    size_t tiles_cap = 0;
+    int split = 1;
+    int64_t last_bulk = 0, last_edge = 0;
     BatchCtl* d_ctl = nullptr;
     float* d_ramp = nullptr;
     size_t ramp_cap = 0;
@@ -134,6 +138,15 @@ int run_sequential(stro_batch* b, const int64_t* steps, const int32_t* log_every
     return STRO_OK;
 }
 
+// A lattice whose geometry has walls, inlets, outlets or solid fractions
+// (some cell flag or geometry word set); its batch tiles are 2-D blocks.
+bool walled(const stro_sim* s) {
+    if (s->cell_host.size() != s->N || s->geo_host.size() != s->N) return false;
+    for (size_t c = 0; c < s->N; ++c)
+        if (s->cell_host[c] != 0 || s->geo_host[c] != 0) return true;
+    return false;
+}
+
 int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
               std::vector<std::vector<double>>& traces, const SamplePlan* plans = nullptr,
               std::vector<std::vector<double>>* samples = nullptr) {
@@ -175,6 +188,11 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
         const uint32_t threads = b->block.x * b->block.y;
         I.cells = uint32_t(s->N);
         I.ntiles = (I.cells + threads - 1) / threads;
+        if (walled(s)) {
+            I.tiles_x = (uint32_t(s->nx) + b->block.x - 1) / b->block.x;
+            I.tiles_y = (uint32_t(s->ny) + b->block.y - 1) / b->block.y;
+            I.ntiles = I.tiles_x * I.tiles_y * uint32_t(s->nz);
+        }
         I.tile_begin = uint32_t(tiles);
         tiles += I.ntiles;
         if (I.log_every > 0) {
@@ -198,12 +216,40 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
         max_steps = std::max(max_steps, I.steps);
     }
     if (tiles >= (1ull << 31)) return fail(STRO_ERR_INVALID, "batch too large");
+    // Rounds mode on a walled batch: bulk tiles (every cell fluid, without
+    // wall neighbours or solid fraction) go to the wall-free kernels, the rest
+    // to the wall-aware ones. Both lists are in instance order, so the tiles of
+    // the instances still running at round r are a prefix of each.
+    const bool split = b->mode == STRO_BATCH_ROUNDS && geo && b->split;
+    std::vector<uint32_t> tile_list;
+    std::vector<uint32_t> bulk_end(n, 0), edge_end(n, 0);
+    uint32_t nbulk_total = 0;
+    if (split) {
+        std::vector<uint32_t> edges, bulk_k, edge_k;
+        tile_list.reserve(tiles);
+        for (size_t k = 0; k < n; ++k) {
+            const stro_sim* s = b->sims[order[k]];
+            if (inst[k].tiles_x != 0) {
+                block_lists(s, b->block, bulk_k, edge_k);
+                for (uint32_t t : bulk_k) tile_list.push_back(inst[k].tile_begin + t);
+                for (uint32_t t : edge_k) edges.push_back(inst[k].tile_begin + t);
+            } else {  // no walls: every tile is bulk
+                for (uint32_t t = 0; t < inst[k].ntiles; ++t)
+                    tile_list.push_back(inst[k].tile_begin + t);
+            }
+            bulk_end[k] = uint32_t(tile_list.size());
+            edge_end[k] = uint32_t(edges.size());
+        }
+        nbulk_total = uint32_t(tile_list.size());
+        tile_list.insert(tile_list.end(), edges.begin(), edges.end());
+    }
     int rc = grow(&b->d_inst, &b->inst_cap, n);
     if (rc == STRO_OK) rc = grow(&b->d_kepart, &b->kepart_cap, tiles);
     if (rc == STRO_OK) rc = grow(&b->d_ramp, &b->ramp_cap, ramp.size());
     if (rc == STRO_OK) rc = grow(&b->d_traces, &b->traces_cap, trace_total);
     if (rc == STRO_OK && probes) rc = grow(&b->d_fpart, &b->fpart_cap, 3 * tiles);
     if (rc == STRO_OK && probes) rc = grow(&b->d_samples, &b->samples_cap, sample_total);
+    if (rc == STRO_OK && split) rc = grow(&b->d_tiles, &b->tiles_cap, tile_list.size());
     if (rc == STRO_OK && !b->d_ctl) STRO_CUDA(cudaMalloc(&b->d_ctl, sizeof(BatchCtl)));
     if (rc != STRO_OK) return rc;
     for (size_t k = 0; k < n; ++k) {
@@ -216,6 +262,11 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
     if (!ramp.empty())
         STRO_CUDA(cudaMemcpyAsync(b->d_ramp, ramp.data(), ramp.size() * sizeof(float),
                                   cudaMemcpyHostToDevice, st));
+    if (split)
+        STRO_CUDA(cudaMemcpyAsync(b->d_tiles, tile_list.data(), tile_list.size() * sizeof(uint32_t),
+                                  cudaMemcpyHostToDevice, st));
+    b->last_bulk = split ? nbulk_total : 0;
+    b->last_edge = split ? int64_t(tile_list.size()) - nbulk_total : 0;
     BatchArgs args{};
     args.inst = b->d_inst;
     args.count = int32_t(n);
@@ -231,8 +282,11 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
                                 int64_t(reinterpret_cast<uintptr_t>(b->d_inst)),
                                 int64_t(reinterpret_cast<uintptr_t>(b->d_kepart)),
                                 int64_t(reinterpret_cast<uintptr_t>(b->d_ctl)), probes,
-                                int64_t(reinterpret_cast<uintptr_t>(args.fpart))};
+                                int64_t(reinterpret_cast<uintptr_t>(args.fpart)), split,
+                                int64_t(reinterpret_cast<uintptr_t>(b->d_tiles))};
     for (size_t k = 0; k < n; ++k) {
+        key.push_back(bulk_end[k]);
+        key.push_back(edge_end[k]);
         key.push_back(inst[k].steps);
         key.push_back(inst[k].log_every);
         key.push_back(inst[k].ntiles);
@@ -243,12 +297,15 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
     }
     // what round r launches in rounds mode: the active tile prefix, and whether
     // some instance logs or probes in it
-    auto round_plan = [&](int64_t r, uint32_t* active, bool* logs, bool* probing) {
-        *active = 0;
+    auto round_plan = [&](int64_t r, uint32_t* active, uint32_t* nbulk, uint32_t* nedge,
+                          bool* logs, bool* probing) {
+        *active = *nbulk = *nedge = 0;
         *logs = *probing = false;
         for (size_t k = 0; k < n; ++k) {
             if (inst[k].steps <= r) break;
             *active = inst[k].tile_begin + inst[k].ntiles;
+            *nbulk = bulk_end[k];
+            *nedge = edge_end[k];
             if (inst[k].log_every > 0 && r % inst[k].log_every == 0 && ((inst[k].t0 + r) & 1) == 0)
                 *logs = true;
             if (inst[k].probe_first >= 0 && r >= inst[k].probe_first &&
@@ -260,11 +317,15 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
     auto launch_rounds = [&]() {
         cudaError_t le = cudaSuccess;
         for (int64_t r = 0; r < max_steps && le == cudaSuccess; ++r) {
-            uint32_t active;
+            uint32_t active, nbulk, nedge;
             bool logs, probing;
-            round_plan(r, &active, &logs, &probing);
-            le = launch_batch_round(args, b->half, geo, feat, probing ? 1 : 0, r, active, b->block,
-                                    st);
+            round_plan(r, &active, &nbulk, &nedge, &logs, &probing);
+            if (split)
+                le = launch_batch_round_lists(args, b->half, feat, probing ? 1 : 0, r, b->d_tiles,
+                                              nbulk, b->d_tiles + nbulk_total, nedge, b->block, st);
+            else
+                le = launch_batch_round(args, b->half, geo, feat, probing ? 1 : 0, r, active,
+                                        b->block, st);
             if (le == cudaSuccess && (logs || probing)) le = launch_batch_fold(args, r, st);
         }
         return le;
@@ -460,6 +521,7 @@ int stro_batch_destroy(stro_batch* b) {
     cudaFree(b->d_kepart);
     cudaFree(b->d_fpart);
     cudaFree(b->d_samples);
+    cudaFree(b->d_tiles);
     cudaFree(b->d_ctl);
     cudaFree(b->d_ramp);
     cudaFree(b->d_traces);
@@ -483,6 +545,19 @@ int stro_batch_set_tile(stro_batch* b, int32_t bx, int32_t by) {
     if (bx < 1 || by < 1 || bx * by > 256 || (bx * by) % 32 != 0)
         return fail(STRO_ERR_INVALID, "tile must have a multiple of 32 threads, at most 256");
     b->block = dim3(bx, by, 1);
+    return STRO_OK;
+}
+
+int stro_batch_set_split(stro_batch* b, int32_t on) {
+    if (!b) return fail(STRO_ERR_INVALID, "null batch");
+    b->split = on ? 1 : 0;
+    return STRO_OK;
+}
+
+int stro_batch_split_tiles(const stro_batch* b, int64_t* bulk, int64_t* edge) {
+    if (!b || !bulk || !edge) return fail(STRO_ERR_INVALID, "null argument");
+    *bulk = b->last_bulk;
+    *edge = b->last_edge;
     return STRO_OK;
 }
 

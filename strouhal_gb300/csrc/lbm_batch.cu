@@ -72,13 +72,23 @@ __device__ __forceinline__ bool probes_at(const BatchInstance& I, int64_t r) {
 template <typename S, int GEO, int FEAT, bool PROBES, bool CG>
 __device__ __forceinline__ void process_tile(const BatchArgs& b, const BatchInstance& I,
                                              uint32_t tile, int64_t r) {
-    const uint32_t threads = blockDim.x * blockDim.y;
-    const uint32_t lin = (tile - I.tile_begin) * threads + threadIdx.y * blockDim.x + threadIdx.x;
-    const bool in = lin < I.cells;
-    const uint32_t nx = uint32_t(I.a.nx), t = lin / nx;
-    const int x = int(lin - t * nx);
-    const int y = int(t % uint32_t(I.a.ny));
-    const int z = int(t / uint32_t(I.a.ny));
+    const uint32_t tl = tile - I.tile_begin;
+    int x, y, z;
+    bool in;
+    if (I.tiles_x != 0) {
+        const uint32_t row = tl / I.tiles_x;
+        x = int((tl - row * I.tiles_x) * blockDim.x + threadIdx.x);
+        y = int((row % I.tiles_y) * blockDim.y + threadIdx.y);
+        z = int(row / I.tiles_y);
+        in = x < I.a.nx && y < I.a.ny;
+    } else {
+        const uint32_t lin = tl * (blockDim.x * blockDim.y) + threadIdx.y * blockDim.x + threadIdx.x;
+        in = lin < I.cells;
+        const uint32_t nx = uint32_t(I.a.nx), t = lin / nx;
+        x = int(lin - t * nx);
+        y = int(t % uint32_t(I.a.ny));
+        z = int(t / uint32_t(I.a.ny));
+    }
     if (((I.t0 + r) & 1) == 0) {
         if (logs_at(I, r)) {
             float u2 = 0.0f;
@@ -211,6 +221,19 @@ __global__ void __launch_bounds__(256) k_batch_round(const BatchArgs b, int64_t 
     process_tile<S, GEO, FEAT, PROBES, false>(b, I, tile, r);
 }
 
+// Rounds over a tile list: block i processes tile list[i]. The bulk tiles of
+// a walled batch (only fluid cells without wall neighbours or solid
+// fractions) run the wall-free kernel, the boundary tiles the wall-aware one,
+// as the single-lattice bulk / boundary split does. In a probe round a bulk
+// tile still stores its (zero) force partials, so the fold sees every tile.
+template <typename S, int GEO, int FEAT, bool PROBES>
+__global__ void __launch_bounds__(256) k_batch_round_list(const BatchArgs b, int64_t r,
+                                                          const uint32_t* list) {
+    const uint32_t tile = list[blockIdx.x];
+    const BatchInstance& I = b.inst[find_instance(b, tile)];
+    process_tile<S, GEO, FEAT, PROBES, false>(b, I, tile, r);
+}
+
 __global__ void __launch_bounds__(256) k_batch_fold(const BatchArgs b, int64_t r) {
     fold_round(b, r);
 }
@@ -242,6 +265,29 @@ void launch_round_feat(const BatchArgs& b, int feat, int64_t r, uint32_t tiles, 
     if (feat == 2) k_batch_round<S, GEO, 2, PROBES><<<tiles, block, 0, st>>>(b, r);
     else if (feat == 1) k_batch_round<S, GEO, 1, PROBES><<<tiles, block, 0, st>>>(b, r);
     else k_batch_round<S, GEO, 0, PROBES><<<tiles, block, 0, st>>>(b, r);
+}
+
+template <typename S, int GEO, bool PROBES>
+void launch_list_feat(const BatchArgs& b, int feat, int64_t r, const uint32_t* list,
+                      uint32_t count, dim3 block, cudaStream_t st) {
+    if (feat == 2) k_batch_round_list<S, GEO, 2, PROBES><<<count, block, 0, st>>>(b, r, list);
+    else if (feat == 1) k_batch_round_list<S, GEO, 1, PROBES><<<count, block, 0, st>>>(b, r, list);
+    else k_batch_round_list<S, GEO, 0, PROBES><<<count, block, 0, st>>>(b, r, list);
+}
+
+template <typename S>
+cudaError_t launch_lists_typed(const BatchArgs& b, int feat, int probes, int64_t r,
+                               const uint32_t* bulk, uint32_t nbulk, const uint32_t* edge,
+                               uint32_t nedge, dim3 block, cudaStream_t st) {
+    if (nbulk) {
+        if (probes) launch_list_feat<S, 0, true>(b, feat, r, bulk, nbulk, block, st);
+        else launch_list_feat<S, 0, false>(b, feat, r, bulk, nbulk, block, st);
+    }
+    if (nedge) {
+        if (probes) launch_list_feat<S, 1, true>(b, feat, r, edge, nedge, block, st);
+        else launch_list_feat<S, 1, false>(b, feat, r, edge, nedge, block, st);
+    }
+    return cudaGetLastError();
 }
 
 template <typename S>
@@ -282,6 +328,15 @@ cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, in
     if (tiles == 0) return cudaSuccess;
     return half_storage ? launch_round_typed<__half>(b, geo, feat, probes, r, tiles, block, st)
                         : launch_round_typed<float>(b, geo, feat, probes, r, tiles, block, st);
+}
+
+cudaError_t launch_batch_round_lists(const BatchArgs& b, int half_storage, int feat, int probes,
+                                     int64_t r, const uint32_t* bulk, uint32_t nbulk,
+                                     const uint32_t* edge, uint32_t nedge, dim3 block,
+                                     cudaStream_t st) {
+    return half_storage
+               ? launch_lists_typed<__half>(b, feat, probes, r, bulk, nbulk, edge, nedge, block, st)
+               : launch_lists_typed<float>(b, feat, probes, r, bulk, nbulk, edge, nedge, block, st);
 }
 
 cudaError_t launch_batch_fold(const BatchArgs& b, int64_t r, cudaStream_t st) {

@@ -24,8 +24,16 @@ struct BatchInstance {
     int32_t probe_count;      // probes in this run
     double* samples;          // box forces, samples[3 k + d] for probe k
     uint32_t tile_begin;      // first tile of this instance in the batch tile list
-    uint32_t ntiles;          // ceil(cells / threads per block)
+    uint32_t ntiles;          // tiles of this instance
     uint32_t cells;           // nx * ny * nz
+    // Tile layout. tiles_x == 0: tile t holds the cells t * threads ..
+    // (t + 1) * threads - 1 in x-fastest order. Otherwise (lattices with walls
+    // or solid fractions) tile t is the block (t % tiles_x, t / tiles_x %
+    // tiles_y, z = t / (tiles_x tiles_y)) of blockDim.x x blockDim.y cells, as
+    // in a single-lattice step, so that the tiles away from the walls hold
+    // plain fluid only.
+    uint32_t tiles_x;
+    uint32_t tiles_y;
 };
 
 // Grid-barrier and error state of the persistent launch (zeroed before each launch).
@@ -53,6 +61,13 @@ cudaError_t launch_batch_persistent(const BatchArgs& b, int half_storage, int ge
                                     int probes, unsigned grid, dim3 block, cudaStream_t st);
 cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, int feat, int probes,
                                int64_t r, uint32_t tiles, dim3 block, cudaStream_t st);
+// One round over two tile lists of a walled batch: `bulk` tiles on the
+// wall-free kernels, `edge` tiles on the wall-aware ones (each list the
+// active prefix of its instance-ordered tiles).
+cudaError_t launch_batch_round_lists(const BatchArgs& b, int half_storage, int feat, int probes,
+                                     int64_t r, const uint32_t* bulk, uint32_t nbulk,
+                                     const uint32_t* edge, uint32_t nedge, dim3 block,
+                                     cudaStream_t st);
 cudaError_t launch_batch_fold(const BatchArgs& b, int64_t r, cudaStream_t st);
 int batch_persistent_blocks_per_sm(int half_storage, int geo, int feat, int probes, dim3 block);
 

@@ -67,11 +67,14 @@ def test_run_sampled_matches_oracle(gpu, oracle):
     s.close()
 
 
-@pytest.mark.parametrize("mode", ["persistent", "rounds", "sequential"])
+@pytest.mark.parametrize("mode", ["persistent", "rounds", "rounds-unsplit", "sequential"])
 def test_batch_run_sampled_equals_single_runs(gpu, mode):
     """Three variants of different sizes and schedules in one batched sampled
     run: DDFs and step counts bitwise those of Simulation.runSampled, forces
-    within FP64 rounding (box sums folded per tile)."""
+    within FP64 rounding (box sums folded per tile). Rounds mode runs the bulk
+    tiles on the wall-free kernels unless the split is switched off."""
+    unsplit = mode == "rounds-unsplit"
+    mode = "rounds" if unsplit else mode
     case = cr.StreetLadder()
     plan = [(8, 1.0, 101, 300, 10), (10, 1.0, 40, 120, 26), (12, 0.5, 0, 64, 4)]
     solo, group = [], []
@@ -80,10 +83,17 @@ def test_batch_run_sampled_equals_single_runs(gpu, mode):
         solo.append((a, a.sim.runSampled(tr, sa, sd, *a.box)))
         group.append(b)
     batch = sg.Batch(gpu, [v.sim for v in group], mode=mode)
+    if unsplit:
+        batch.setSplit(False)
     out = batch.runSampled([p[2] for p in plan], [p[3] for p in plan], [p[4] for p in plan],
                            [v.box for v in group])
     assert batch.lastPath in ({"persistent": "persistent-graph", "rounds": "rounds-graph",
                                "sequential": "sequential"}[mode],)
+    bulk, edge = batch.splitTiles
+    if mode == "rounds" and not unsplit:
+        assert bulk > 0 and edge > 0, (bulk, edge)
+    else:
+        assert (bulk, edge) == (0, 0)
     for (a, (fa, ata)), b, (fb, atb) in zip(solo, group, out):
         assert np.array_equal(ata, atb)
         assert b.sim.stepsDone == a.sim.stepsDone and b.sim.stateDigest == a.sim.stateDigest
@@ -106,7 +116,7 @@ def test_batch_run_sampled_long_rounds_stream(gpu):
     assert np.all(np.isfinite(fa)) and np.all(fa[:, 0] > 0)
     batch = sg.Batch(gpu, [b.sim], mode="rounds")
     (fb, _), = batch.runSampled([32000], [1000], [40], [b.box])
-    assert batch.lastPath == "rounds-stream"
+    assert batch.lastPath == "rounds-stream" and min(batch.splitTiles) > 0
     assert b.sim.stateDigest == a.sim.stateDigest
     assert np.allclose(fb, fa, rtol=1e-12, atol=1e-16)
     batch.close()

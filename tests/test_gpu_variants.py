@@ -175,6 +175,8 @@ def test_batch_matches_independent_runs(gpu, mode, precision):
     traces = b.run(steps, logs)
     assert b.lastPath.startswith({"persistent": "persistent", "rounds": "rounds",
                                   "sequential": "sequential"}[mode])
+    if mode == "rounds":  # the walled channel's bulk tiles ran on the wall-free kernels
+        assert min(b.splitTiles) > 0, b.splitTiles
     for s, r, k, tr, rtr in zip(sims, ref, steps, traces, ref_traces):
         assert s.stepsDone == r.stepsDone == k
         assert np.array_equal(s.downloadState(), r.downloadState())
