@@ -226,8 +226,10 @@ __global__ void __launch_bounds__(256) k_batch_round(const BatchArgs b, int64_t 
 // fractions) run the wall-free kernel, the boundary tiles the wall-aware one,
 // as the single-lattice bulk / boundary split does. In a probe round a bulk
 // tile still stores its (zero) force partials, so the fold sees every tile.
+// The wall-aware form is capped at 128 registers (two 256-thread blocks per
+// SM instead of one; it spills a few words).
 template <typename S, int GEO, int FEAT, bool PROBES>
-__global__ void __launch_bounds__(256) k_batch_round_list(const BatchArgs b, int64_t r,
+__global__ void __launch_bounds__(256, GEO == 1 ? 2 : 0) k_batch_round_list(const BatchArgs b, int64_t r,
                                                           const uint32_t* list) {
     const uint32_t tile = list[blockIdx.x];
     const BatchInstance& I = b.inst[find_instance(b, tile)];
