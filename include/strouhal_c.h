@@ -222,6 +222,11 @@ int stro_sim_get_rows_tile(stro_sim* sim, int32_t* threads, int32_t* rows);
  * with the wall-aware ones (default on); 0 runs the wall-aware kernels on
  * every block. Results are identical either way. */
 int stro_sim_set_block_split(stro_sim* sim, int32_t enabled);
+/* stro_sim_run and stro_sim_run_sampled replay CUDA graphs of plain steps once
+ * the ramp is over (default on): the launches of a run of steps are captured
+ * once per configuration and replayed. 0 launches every step from the host.
+ * Results are identical either way. */
+int stro_sim_set_graphs(stro_sim* sim, int32_t enabled);
 /* Autotuner: times `steps` steps per candidate variant and launch shape on the current
  * state (saved and restored, stepsDone unchanged) and keeps the fastest. */
 int stro_sim_autotune(stro_sim* sim, int64_t steps, int32_t* bx, int32_t* by, double* glups);

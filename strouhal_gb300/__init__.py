@@ -145,6 +145,7 @@ def lib():
         "stro_sim_get_arithmetic": ([_P, ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_get_rows_tile": ([_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_set_block_split": ([_P, ctypes.c_int32], c_int),
+        "stro_sim_set_graphs": ([_P, ctypes.c_int32], c_int),
         "stro_sim_get_variant": ([_P, ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_set_block": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
         "stro_sim_get_block": ([_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)], c_int),
@@ -623,6 +624,10 @@ class Simulation:
     def setBlockSplit(self, enabled):
         """Bulk blocks of a walled lattice on the wall-free kernels (default True)."""
         _check(lib().stro_sim_set_block_split(self._h, int(bool(enabled))))
+
+    def setGraphs(self, enabled):
+        """Replay CUDA graphs of plain steps past the ramp (default True)."""
+        _check(lib().stro_sim_set_graphs(self._h, int(bool(enabled))))
 
     def autotune(self, steps=20):
         """Pick the fastest kernel variant and launch shape (state restored); returns (bx, by, GLUPS)."""

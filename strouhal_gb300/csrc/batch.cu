@@ -723,6 +723,13 @@ int stro_sim_set_block_split(stro_sim* s, int32_t enabled) {
     return STRO_OK;
 }
 
+int stro_sim_set_graphs(stro_sim* s, int32_t enabled) {
+    if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
+    s->graphs = enabled != 0;
+    if (!s->graphs) drop_graphs(s);
+    return STRO_OK;
+}
+
 int stro_sim_set_pair_block(stro_sim* s, int32_t bx, int32_t by) {
     if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
     if (bx < 32 || bx > 256 || bx % 32 != 0 || by != 1)

@@ -84,8 +84,10 @@ float ramp_factor(const stro_sim* s, int64_t t) {
     return 1.0f * float(0.5 * (1.0 - std::cos(3.141592653589793 * x)));
 }
 
-StepArgs step_args(const stro_sim* s, int64_t t) {
-    StepArgs a{};
+// Writes every field of *a (its padding is left as it was, so a zeroed object
+// stays comparable byte for byte).
+static void fill_step_args(const stro_sim* s, int64_t t, StepArgs* out) {
+    StepArgs& a = *out;
     a.f = s->d_f;
     a.plane = s->plane;
     a.nx = s->nx; a.ny = s->ny; a.nz = s->nz;
@@ -115,6 +117,12 @@ StepArgs step_args(const stro_sim* s, int64_t t) {
     a.box_x0 = 0; a.box_x1 = -1; a.box_y0 = 0; a.box_y1 = -1;
     a.f_out = nullptr;
     a.partials = s->d_partials;
+}
+
+StepArgs step_args(const stro_sim* s, int64_t t) {
+    StepArgs a;
+    std::memset(&a, 0, sizeof a);
+    fill_step_args(s, t, &a);
     return a;
 }
 
@@ -185,6 +193,7 @@ int upload_geometry(stro_sim* s) {
 }
 
 void free_sim(stro_sim* s) {
+    drop_graphs(s);
     cudaFree(s->d_f);
     cudaFree(s->d_cell);
     cudaFree(s->d_geo);
@@ -211,14 +220,23 @@ int launch_one_step(stro_sim* s, int64_t t, bool probe, const int box[4]) {
     return STRO_OK;
 }
 
+// Steps per replayed graph in stro_sim_run (runs of at least twice as many).
+constexpr int64_t kRunGraphSteps = 32;
+
 int run_steps(stro_sim* s, int64_t steps, int64_t probe_step = -1, const int* box = nullptr) {
     cudaStream_t st = s->ctx->stream;
     STRO_CUDA(cudaEventRecord(s->ev0, st));
-    for (int64_t k = 0; k < steps; ++k) {
-        const int64_t t = s->steps_done + k;
-        const int rc = launch_one_step(s, t, t == probe_step, box);
-        if (rc != STRO_OK) return rc;
+    const int64_t t0 = s->steps_done, t1 = t0 + steps;
+    const int64_t G = steps >= 2 * kRunGraphSteps ? kRunGraphSteps : 0;
+    int rc;
+    if (probe_step >= t0 && probe_step < t1) {
+        rc = launch_plain_steps(s, t0, probe_step - t0, G);
+        if (rc == STRO_OK) rc = launch_one_step(s, probe_step, true, box);
+        if (rc == STRO_OK) rc = launch_plain_steps(s, probe_step + 1, t1 - probe_step - 1, G);
+    } else {
+        rc = launch_plain_steps(s, t0, steps, G);
     }
+    if (rc != STRO_OK) return rc;
     STRO_CUDA(cudaEventRecord(s->ev1, st));
     STRO_CUDA(cudaEventSynchronize(s->ev1));
     float ms = 0.0f;
@@ -332,6 +350,116 @@ cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool prob
     s->last_path = probe ? "probe" : "cell";
     return L.step(a, half, int(t & 1), geo, feat_on(s), probe, probe ? s->probe_block : s->block,
                   s->ctx->stream);
+}
+
+// ---- CUDA graphs of plain steps ---------------------------------------------
+// Once the inflow / lid ramp is over, a step's launches depend only on its
+// parity, so a run of G plain steps (G even) is the same launch sequence each
+// time. It is captured once and replayed with one cudaGraphLaunch: on lattices
+// of a few hundred thousand cells the host's per-kernel launch cost and the gaps
+// between dependent launches are a large part of a step.
+
+void drop_graphs(stro_sim* s) {
+    for (auto& g : s->graph_cache) cudaGraphExecDestroy(g.second);
+    s->graph_cache.clear();
+}
+
+namespace {
+
+constexpr size_t kGraphCacheSize = 4;
+
+template <typename T>
+void put_bytes(std::vector<uint8_t>& k, const T& v) {
+    const uint8_t* p = reinterpret_cast<const uint8_t*>(&v);
+    k.insert(k.end(), p, p + sizeof(T));
+}
+
+// Everything the launches of a plain step at parity (t & 1) read from the
+// simulation: its arguments (ramp over, so the same for every t of that
+// parity) and the launch configuration.
+std::vector<uint8_t> graph_key(const stro_sim* s, int64_t t, int64_t G) {
+    std::vector<uint8_t> k;
+    StepArgs a;
+    std::memset(&a, 0, sizeof a);
+    fill_step_args(s, t, &a);
+    put_bytes(k, a);
+    const int64_t cfg[] = {t & 1, G, s->variant, s->split ? 1 : 0, s->block.x, s->block.y,
+                           s->pair_block.x, s->pair_block.y, s->rows_threads, s->rows_per_tile,
+                           s->arith, s->collision, s->precision, geo_on(s) ? 1 : 0, feat_on(s),
+                           bulk_feat(s), int64_t(reinterpret_cast<uintptr_t>(s->d_blocks)),
+                           s->nbulk, s->nedge, int64_t(s->lists_version),
+                           int64_t(s->geo_version), s->lists_block.x, s->lists_block.y,
+                           int64_t(reinterpret_cast<uintptr_t>(s->d_error)), s->ctx->sm_count,
+                           int64_t(reinterpret_cast<uintptr_t>(s->ctx->stream))};
+    put_bytes(k, cfg);
+    return k;
+}
+
+}  // namespace
+
+// Capture G steps starting at parity (t & 1). The block lists of the split are
+// built before the capture, so nothing inside it allocates or copies
+// synchronously. (The row-staged variant sets kernel attributes at its first
+// launch and is not captured.)
+static int graph_for(stro_sim* s, int64_t t, int64_t G, cudaGraphExec_t* out) {
+    if (geo_on(s) && s->variant == 0 && s->split && s->geo_host.size() == s->N) {
+        const int rc = ensure_block_lists(s);
+        if (rc != STRO_OK) return rc;
+    }
+    std::vector<uint8_t> key = graph_key(s, t, G);
+    for (size_t i = 0; i < s->graph_cache.size(); ++i)
+        if (s->graph_cache[i].first == key) {
+            *out = s->graph_cache[i].second;
+            return STRO_OK;
+        }
+    cudaStream_t st = s->ctx->stream;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(e, "step graph capture");
+    cudaError_t le = cudaSuccess;
+    for (int64_t j = 0; j < G && le == cudaSuccess; ++j)
+        le = launch_sim_step(s, step_args(s, t + j), t + j, false);
+    e = cudaStreamEndCapture(st, &graph);
+    if (le != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return cuda_fail(le, "step launch (graph capture)");
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "step graph capture");
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "step graph instantiate");
+    if (s->graph_cache.size() >= kGraphCacheSize) {
+        cudaGraphExecDestroy(s->graph_cache.front().second);
+        s->graph_cache.erase(s->graph_cache.begin());
+    }
+    s->graph_cache.emplace_back(std::move(key), exec);
+    *out = exec;
+    return STRO_OK;
+}
+
+int launch_plain_steps(stro_sim* s, int64_t t, int64_t count, int64_t graph_steps) {
+    const int64_t end = t + count;
+    const bool graphs = s->graphs && s->variant != 2 && graph_steps >= 2 && graph_steps % 2 == 0;
+    // ramped steps go one by one (their arguments change every step)
+    const int64_t ramp_end = s->ramp_steps > 0 ? std::max<int64_t>(t, s->ramp_steps) : t;
+    int64_t k = t;
+    for (; k < end && (k < ramp_end || !graphs); ++k) {
+        const int rc = launch_one_step(s, k, false, nullptr);
+        if (rc != STRO_OK) return rc;
+    }
+    if (graphs && end - k >= graph_steps) {
+        cudaGraphExec_t exec = nullptr;
+        const int rc = graph_for(s, k, graph_steps, &exec);
+        if (rc != STRO_OK) return rc;
+        for (; end - k >= graph_steps; k += graph_steps)
+            STRO_CUDA(cudaGraphLaunch(exec, s->ctx->stream));
+    }
+    for (; k < end; ++k) {
+        const int rc = launch_one_step(s, k, false, nullptr);
+        if (rc != STRO_OK) return rc;
+    }
+    return STRO_OK;
 }
 
 void ctx_retain(stro_ctx* c) { ++c->refs; }
@@ -703,14 +831,23 @@ int stro_sim_run_sampled(stro_sim* s, int64_t transient, int64_t sample_steps, i
     int rc = STRO_OK;
     cudaError_t e = cudaEventRecord(s->ev0, st);
     int64_t t = s->steps_done;
-    auto steps = [&](int64_t count, int64_t probe_at) {
-        for (int64_t k = 0; k < count && rc == STRO_OK; ++k, ++t)
-            rc = launch_one_step(s, t, geo && t == probe_at, box);
+    // plain steps replay CUDA graphs: one of `chunk` steps per sample when it
+    // is short, else runs of 32
+    const int64_t g_transient = transient >= 2 * kRunGraphSteps ? kRunGraphSteps : 0;
+    const int64_t g_chunk = (n >= 2 && chunk <= 256) ? chunk
+                                                     : (chunk >= 2 * kRunGraphSteps ? kRunGraphSteps : 0);
+    auto plain = [&](int64_t count, int64_t G) {
+        if (rc == STRO_OK) rc = launch_plain_steps(s, t, count, G);
+        t += count;
     };
-    if (e == cudaSuccess) steps(transient, -1);
+    auto probe_pair = [&]() {  // the force is taken on the odd step
+        for (int64_t k = 0; k < 2 && rc == STRO_OK; ++k, ++t)
+            rc = launch_one_step(s, t, geo && k == 1, box);
+    };
+    if (e == cudaSuccess) plain(transient, g_transient);
     for (int64_t k = 0; k < n && rc == STRO_OK && e == cudaSuccess; ++k) {
-        steps(chunk, -1);
-        steps(2, t + 1);  // probe pair: the force is taken on its odd step
+        plain(chunk, g_chunk);
+        probe_pair();
         if (rc == STRO_OK && geo)
             e = launch_fold(s->d_partials, nblocks, 3, d_samples + 3 * k, st);
         if (steps_at) steps_at[k] = t;

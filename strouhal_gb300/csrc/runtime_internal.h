@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "lbm_launch.h"
@@ -85,6 +86,9 @@ struct stro_sim {
     dim3 lists_block{0, 0, 0};
     uint64_t lists_version = ~0ull;
     uint64_t geo_version = 0;      // bumped whenever the device geometry changes
+    // CUDA graphs of runs of plain steps, keyed by everything their launches read
+    bool graphs = true;
+    std::vector<std::pair<std::vector<uint8_t>, cudaGraphExec_t>> graph_cache;
 };
 
 namespace stro {
@@ -109,6 +113,12 @@ FieldView field_view(const stro_sim* s);
 int ensure_geometry(stro_sim* s);
 // Launch one lattice step t on the simulation stream (variant and shape of the sim).
 cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool probe);
+// Launch the plain steps t .. t + count - 1 (no force probe). With graph_steps
+// > 0 (even), whole runs of graph_steps steps past the ramp replay one cached
+// CUDA graph; everything else is launched step by step. Same kernels, same
+// arguments, same results either way.
+int launch_plain_steps(stro_sim* s, int64_t t, int64_t count, int64_t graph_steps);
+void drop_graphs(stro_sim* s);
 void ctx_retain(stro_ctx* c);
 void ctx_release(stro_ctx* c);
 int observables(stro_sim* s, double out[2]);
