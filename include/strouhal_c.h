@@ -239,7 +239,9 @@ typedef struct stro_batch stro_batch;
 enum {
     STRO_BATCH_PERSISTENT = 0, /* one cooperative persistent kernel, bounded grid barrier, in a CUDA graph */
     STRO_BATCH_ROUNDS = 1,     /* a CUDA graph of one launch per round */
-    STRO_BATCH_SEQUENTIAL = 2  /* one instance after another, one launch per step */
+    STRO_BATCH_SEQUENTIAL = 2, /* one instance after another, one launch per step */
+    STRO_BATCH_STREAMS = 3     /* every instance on its own stream with its own kernels and
+                                  CUDA graphs, all enqueued before any is waited for */
 };
 int stro_batch_create(stro_ctx* ctx, int32_t count, stro_sim* const* sims, stro_batch** out);
 int stro_batch_destroy(stro_batch* batch);
@@ -269,12 +271,15 @@ int stro_batch_run(stro_batch* batch, const int64_t* steps, const int32_t* log_e
  * their number to samples[i]. DDFs and step counts are bitwise those of
  * stro_sim_run_sampled; the box sums are folded per tile, so forces agree with
  * it to rounding (FP64). In STRO_BATCH_SEQUENTIAL mode the simulations run one
- * after another through stro_sim_run_sampled (the reference's order). */
+ * after another through stro_sim_run_sampled (the reference's order); in
+ * STRO_BATCH_STREAMS mode each runs stro_sim_run_sampled's schedule on its own
+ * stream, all at once, and forces equal stro_sim_run_sampled's bit for bit. */
 int stro_batch_run_sampled(stro_batch* batch, const int64_t* transient, const int64_t* sample_steps,
                            const int64_t* stride, const int32_t* boxes, double* const* forces,
                            const int64_t* capacity, int64_t* samples);
 int stro_batch_gpu_seconds(stro_batch* batch, double* seconds);
-/* "persistent-graph", "rounds-graph" or "sequential": the path the last run took. */
+/* "persistent-graph", "rounds-graph", "rounds-stream", "sequential" or "streams": the path
+ * the last run took. */
 int stro_batch_last_path(stro_batch* batch, char* buf, size_t len);
 /* Times each mode and tile shape for `rounds` rounds (states restored) and keeps the fastest. */
 int stro_batch_autotune(stro_batch* batch, int64_t rounds, int32_t* mode, int32_t* bx,

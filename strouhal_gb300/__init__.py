@@ -641,10 +641,11 @@ class Batch:
     """Several simulations of one precision advanced together (stro_batch_*).
 
     mode: "persistent" (one cooperative kernel in a CUDA graph), "rounds" (a
-    graph of one launch per round) or "sequential" (one instance after another,
-    the reference's order)."""
+    graph of one launch per round), "sequential" (one instance after another,
+    the reference's order) or "streams" (every instance on its own stream with
+    its own kernels and step graphs, all enqueued at once)."""
 
-    MODES = {"persistent": 0, "rounds": 1, "sequential": 2}
+    MODES = {"persistent": 0, "rounds": 1, "sequential": 2, "streams": 3}
 
     def __init__(self, gpu, sims, mode="persistent"):
         self.sims = list(sims)

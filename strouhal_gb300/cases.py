@@ -336,7 +336,7 @@ def ladder_instances(count=32, seed=1234, edges=(32, 48, 64, 96, 128, 160),
 
 
 def ladder(gpu, count=32, seed=1234, precision="fp32",
-           modes=("persistent", "rounds", "sequential"), t_star=5.0, tune=True,
+           modes=("persistent", "rounds", "streams", "sequential"), t_star=5.0, tune=True,
            edges=(32, 48, 64, 96, 128, 160)):
     """32 periodic TGV instances of uneven size and Mach number, FP32 SRT,
     Re = 1600, 5 convective times each, kinetic-energy traces every 0.1 t*;
@@ -357,7 +357,7 @@ def ladder(gpu, count=32, seed=1234, precision="fp32",
             sims.append(s)
         b = sg.Batch(gpu, sims, mode=mode)
         tuned = None
-        if tune and mode != "sequential":
+        if tune and mode not in ("sequential", "streams"):  # those keep each lattice's shape
             chosen, bx, by, _ = b.autotune(rounds=40)  # tile shape (and mode), states restored
             b.mode = mode
             tuned = [bx, by]
@@ -569,16 +569,16 @@ def sphere_adjoint(gpu, nx=512, ny=256, nz=256, D=48, u=0.05, re=300.0, cs=0.1, 
 
 # ------------------------------------------------------------ credibility ladder
 def credibility(gpu, resolutions=(32, 48, 64), base_mach=0.075, steps_factor=1.0,
-                precision="fp32", report=None, modes=("sequential", "concurrent", "batched"),
-                autotune=True):
+                precision="fp32", report=None,
+                modes=("sequential", "concurrent", "batched", "streams"), autotune=True):
     """The DFG 2D-2 credibility run (mean C_D; three resolutions and a half-Mach
     anchor at the finest) with the four checks the reference's credibility gate
     makes (Sources/strouhal/Cases.swift:1103-1160): a finite calibrated bar in
     the validated domain, a bar that reaches the published mean C_D 3.18 (within
     0.05), a ladder of every resolution, and a refusal out of the domain
     (Re 250000). Each mode in `modes` runs the whole ladder: the final lattices
-    must be bitwise equal across modes, the QoIs equal (sequential, concurrent)
-    or equal to FP64 rounding (batched: box sums folded per tile)."""
+    must be bitwise equal across modes, the QoIs equal (sequential, concurrent,
+    streams) or equal to FP64 rounding (batched: box sums folded per tile)."""
     from . import credibility as cr
     case = cr.StreetLadder(baseMach=base_mach, precision=precision, stepsFactor=steps_factor)
     runs = {}

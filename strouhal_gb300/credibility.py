@@ -17,10 +17,13 @@ independent lattices, and `Ladder.credibility(mode=...)` runs them
                 host thread,
   "batched"     all in one batched submission (`stro_batch_run_sampled`: one
                 persistent kernel or one launch per round over every
-                variant's tiles, force probes fused into the odd pass).
+                variant's tiles, force probes fused into the odd pass),
+  "streams"     one `stro_batch_run_sampled` submission in the batch's
+                streams mode: every variant's own schedule on its own stream
+                of one context, enqueued from one host thread.
 The lattices end bitwise the same in every mode; the batched box-force sums
 are folded per tile instead of per block, so its samples agree to FP64
-rounding.
+rounding (the other modes' samples are equal).
 """
 from __future__ import annotations
 
@@ -35,7 +38,7 @@ import numpy as np
 from . import (Batch, Cell, DomainVerdict, GPU, LadderRungC, NumUQ, Simulation, StatUQ,
                _check, diskSolidFractions, lib, trtOmegas)
 
-MODES = ("sequential", "concurrent", "batched")
+MODES = ("sequential", "concurrent", "batched", "streams")
 
 NAN = float("nan")
 
@@ -382,12 +385,16 @@ class Ladder:
             finally:
                 v.sim.close()
 
-        if mode == "batched":
+        if mode in ("batched", "streams"):
             variants = [case.variant(gpu, n, ms) for n, ms in jobs]
             batch = None
             try:
-                batch = Batch(gpu, [v.sim for v in variants], mode="persistent")
-                if autotune:
+                if mode == "streams" and autotune:
+                    for v in variants:  # each variant keeps its own kernel and shape
+                        v.sim.autotune(200)
+                batch = Batch(gpu, [v.sim for v in variants],
+                              mode="persistent" if mode == "batched" else "streams")
+                if autotune and mode == "batched":
                     batch.autotune(rounds=200)
                 g0 = batch.gpuSeconds
                 s0 = [v.sim.stepsDone for v in variants]
@@ -507,7 +514,8 @@ def report_markdown(run, buildGates=()):
             "- %.1f s wall time, %.1f s on the GPU, %.3g cell updates, variants run %s" % (
                 run.wallSeconds, run.gpuSeconds, float(run.cellUpdates),
                 {"sequential": "one after another", "concurrent": "on concurrent streams",
-                 "batched": "in one batched submission"}[run.mode]),
+                 "batched": "in one batched submission",
+                 "streams": "on one stream each from one host thread"}[run.mode]),
             "", "## Not covered by the bar", "",
             "- Model-form error of the collision closure.",
             "- A grid convergence index: not defined for scale-resolving runs.",

@@ -3,15 +3,15 @@
 //
 // A batch groups existing simulations of one precision on one context. A run
 // advances instance i by steps[i] lattice steps, exactly as calling
-// stro_sim_run on each in turn would (same kernels, bitwise identical DDFs),
-// but in one launch:
+// stro_sim_run on each in turn would (bitwise identical DDFs), in one of:
 //   STRO_BATCH_PERSISTENT  one cooperative persistent kernel with a bounded
 //                          grid barrier between rounds, captured in a CUDA
 //                          graph together with the reset of its control word;
 //   STRO_BATCH_ROUNDS      a CUDA graph of one launch per round;
-//   STRO_BATCH_SEQUENTIAL  the reference's order: one instance after another,
-//                          one launch per step (the baseline the batch is
-//                          measured against).
+//   STRO_BATCH_STREAMS     each instance's own launches on a stream of its
+//                          own, enqueued in turns from this thread;
+//   STRO_BATCH_SEQUENTIAL  the reference's order: one instance after another
+//                          (the baseline the batch is measured against).
 // The instantiated graph is cached and replayed while the schedule (step
 // counts, logging, tile shape) is unchanged; the per-instance descriptors are
 // re-uploaded before every replay.
@@ -47,6 +47,7 @@ struct stro_batch {
     size_t fpart_cap = 0;
     double* d_samples = nullptr;
     size_t samples_cap = 0;
+    std::vector<cudaStream_t> streams;  // STRO_BATCH_STREAMS: one per instance
     uint32_t* d_tiles = nullptr;  // rounds mode: bulk tile list, then boundary tile list
     size_t tiles_cap = 0;
     int split = 1;
@@ -133,6 +134,137 @@ int run_sequential(stro_batch* b, const int64_t* steps, const int32_t* log_every
         } else if (left > 0) {
             const int rc = stro_sim_run(s, left);
             if (rc != STRO_OK) return rc;
+        }
+    }
+    return STRO_OK;
+}
+
+// STRO_BATCH_STREAMS: each instance on a stream of its own, every instance's
+// work enqueued from this thread before any is waited for. Each instance runs
+// exactly what stro_sim_run would (its own tuned kernels, CUDA graphs of its
+// plain steps) and the GPU overlaps the instances, which small lattices leave
+// room for. The instance streams wait for the batch event ev0 (recorded on
+// the context stream by the caller) and the context stream waits for each
+// instance's last event, so ev0 / ev1 on the context stream bracket the run.
+int ensure_streams(stro_batch* b) {
+    while (b->streams.size() < b->sims.size()) {
+        cudaStream_t x = nullptr;
+        STRO_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+        b->streams.push_back(x);
+    }
+    return STRO_OK;
+}
+
+// Graph length for a run of `count` plain steps that repeats: the whole run
+// when it is short, else runs of kRunGraphSteps.
+int64_t repeat_graph_steps(int64_t count) {
+    if (count >= 2 && count <= 256 && count % 2 == 0) return count;
+    return count >= 2 * kRunGraphSteps ? kRunGraphSteps : 0;
+}
+
+int run_streams(stro_batch* b, const int64_t* steps, const int32_t* log_every,
+                std::vector<std::vector<double>>& traces) {
+    const size_t n = b->sims.size();
+    int rc = ensure_streams(b);
+    if (rc != STRO_OK) return rc;
+    std::vector<size_t> off(n, 0), cnt(n, 0);
+    size_t total = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const int64_t le = log_every ? log_every[i] : 0;
+        if (le > 0) {
+            cnt[i] = size_t(1 + steps[i] / le);
+            off[i] = total;
+            total += cnt[i];
+        }
+    }
+    rc = grow(&b->d_traces, &b->traces_cap, total);
+    if (rc != STRO_OK) return rc;
+    // per instance: next step, steps left, trace slots written
+    struct Cursor {
+        int64_t t = 0, left = 0;
+        size_t k = 0;
+        bool done = false;
+    };
+    std::vector<Cursor> cur(n);
+    size_t queued = 0;
+    for (size_t i = 0; i < n && rc == STRO_OK; ++i) {
+        stro_sim* s = b->sims[i];
+        cudaError_t e = cudaStreamWaitEvent(b->streams[i], b->ev0, 0);
+        if (e == cudaSuccess) e = cudaEventRecord(s->ev0, b->streams[i]);
+        if (e != cudaSuccess) rc = cuda_fail(e, "instance stream");
+        cur[i].t = s->steps_done;
+        cur[i].left = steps[i];
+        queued = i + 1;
+    }
+    // One piece of each instance in turn (a logging interval, or up to 1024
+    // steps): a stream's queue of pending launches is bounded, and a host
+    // thread blocked on one full queue must not leave the others without work.
+    for (bool more = true; more && rc == STRO_OK;) {
+        more = false;
+        for (size_t i = 0; i < n && rc == STRO_OK; ++i) {
+            Cursor& c = cur[i];
+            if (c.done) continue;
+            stro_sim* s = b->sims[i];
+            cudaStream_t ss = b->streams[i];
+            const int64_t le = log_every ? log_every[i] : 0;
+            s->stream = ss;
+            auto log = [&]() {  // sum |u|^2 into trace slot k, as observables() computes it
+                cudaError_t e = launch_observables(field_view(s), s->precision == STRO_FP16S,
+                                                   s->omega, s->d_partials, s->d_out, ss);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(b->d_traces + off[i] + c.k, s->d_out, sizeof(double),
+                                        cudaMemcpyDeviceToDevice, ss);
+                ++c.k;
+                return e == cudaSuccess ? STRO_OK : cuda_fail(e, "instance trace");
+            };
+            if (le > 0 && c.k == 0) {
+                rc = log();
+            } else if (le > 0 && c.left >= le) {
+                rc = launch_plain_steps(s, c.t, le, repeat_graph_steps(le));
+                c.t += le;
+                c.left -= le;
+                if (rc == STRO_OK) rc = log();
+            } else if (c.left > 0) {
+                const int64_t piece = le > 0 ? c.left : std::min<int64_t>(c.left, 1024);
+                rc = launch_plain_steps(s, c.t, piece,
+                                        piece >= 2 * kRunGraphSteps ? kRunGraphSteps : 0);
+                c.t += piece;
+                c.left -= piece;
+            }
+            if (rc == STRO_OK && c.left == 0 && (le == 0 || c.k > 0)) {
+                cudaError_t e = cudaEventRecord(s->ev1, ss);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(b->ctx->stream, s->ev1, 0);
+                if (e != cudaSuccess) rc = cuda_fail(e, "instance stream");
+                c.done = true;
+            }
+            s->stream = nullptr;
+            more = more || !c.done;
+        }
+    }
+    // wait for every instance that was enqueued, whatever happened after it
+    for (size_t i = 0; i < queued; ++i) {
+        cudaError_t e = cudaStreamSynchronize(b->streams[i]);
+        if (e != cudaSuccess && rc == STRO_OK) rc = cuda_fail(e, "instance stream");
+    }
+    if (rc != STRO_OK) return rc;
+    for (size_t i = 0; i < n; ++i) {
+        stro_sim* s = b->sims[i];
+        float ms = 0.0f;
+        STRO_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+        s->gpu_seconds += double(ms) * 1e-3;
+        s->steps_done += steps[i];
+        if (s->variant == 2) {
+            int err = 0;
+            STRO_CUDA(cudaMemcpy(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost));
+            if (err != 0) {
+                cudaMemset(s->d_error, 0, sizeof(int));
+                return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-staged step timed out");
+            }
+        }
+        if (cnt[i]) {
+            traces[i].resize(cnt[i]);
+            STRO_CUDA(cudaMemcpy(traces[i].data(), b->d_traces + off[i], cnt[i] * sizeof(double),
+                                 cudaMemcpyDeviceToHost));
         }
     }
     return STRO_OK;
@@ -522,6 +654,7 @@ int stro_batch_destroy(stro_batch* b) {
     cudaFree(b->d_fpart);
     cudaFree(b->d_samples);
     cudaFree(b->d_tiles);
+    for (cudaStream_t x : b->streams) cudaStreamDestroy(x);
     cudaFree(b->d_ctl);
     cudaFree(b->d_ramp);
     cudaFree(b->d_traces);
@@ -534,7 +667,8 @@ int stro_batch_destroy(stro_batch* b) {
 
 int stro_batch_set_mode(stro_batch* b, int32_t mode) {
     if (!b) return fail(STRO_ERR_INVALID, "null batch");
-    if (mode != STRO_BATCH_PERSISTENT && mode != STRO_BATCH_ROUNDS && mode != STRO_BATCH_SEQUENTIAL)
+    if (mode != STRO_BATCH_PERSISTENT && mode != STRO_BATCH_ROUNDS && mode != STRO_BATCH_SEQUENTIAL &&
+        mode != STRO_BATCH_STREAMS)
         return fail(STRO_ERR_INVALID, "unknown batch mode");
     b->mode = mode;
     return STRO_OK;
@@ -594,6 +728,9 @@ int stro_batch_run(stro_batch* b, const int64_t* steps, const int32_t* log_every
     if (b->mode == STRO_BATCH_SEQUENTIAL) {
         rc = run_sequential(b, steps, log_every, tr);
         b->last_path = "sequential";
+    } else if (b->mode == STRO_BATCH_STREAMS) {
+        rc = run_streams(b, steps, log_every, tr);
+        b->last_path = "streams";
     } else {
         rc = run_fused(b, steps, log_every, tr);
     }
@@ -674,6 +811,63 @@ int stro_batch_run_sampled(stro_batch* b, const int64_t* transient, const int64_
         }
         b->gpu_seconds = g0 + g;
         b->last_path = "sequential";
+        return STRO_OK;
+    }
+    if (b->mode == STRO_BATCH_STREAMS) {  // stro_sim_run_sampled on every instance at once
+        int rc = ensure_streams(b);
+        if (rc != STRO_OK) return rc;
+        STRO_CUDA(cudaEventRecord(b->ev0, st));
+        std::vector<SampledRun> runs(n);
+        size_t queued = 0;
+        for (size_t i = 0; i < n && rc == STRO_OK; ++i) {
+            stro_sim* s = b->sims[i];
+            const cudaError_t e = cudaStreamWaitEvent(b->streams[i], b->ev0, 0);
+            if (e != cudaSuccess) {
+                rc = cuda_fail(e, "instance stream");
+                break;
+            }
+            s->stream = b->streams[i];
+            int64_t got = 0;
+            rc = sampled_begin(s, transient[i], sample_steps[i], stride[i], boxes + 4 * i,
+                               forces[i], capacity[i], &got, nullptr, &runs[i]);
+            s->stream = nullptr;
+            if (rc != STRO_OK) break;
+            queued = i + 1;
+        }
+        // Enqueue the schedules in turns, one piece of each instance at a
+        // time: a stream's queue of pending launches is bounded, and a host
+        // thread blocked on one full queue must not leave the other streams
+        // without work.
+        for (bool more = true; more && rc == STRO_OK;) {
+            more = false;
+            for (size_t i = 0; i < n && rc == STRO_OK; ++i) {
+                if (runs[i].done) continue;
+                b->sims[i]->stream = b->streams[i];
+                rc = sampled_advance(b->sims[i], &runs[i]);
+                b->sims[i]->stream = nullptr;
+                more = more || !runs[i].done;
+            }
+        }
+        for (size_t i = 0; i < n && rc == STRO_OK; ++i) {
+            const cudaError_t w = cudaStreamWaitEvent(st, b->sims[i]->ev1, 0);
+            if (w != cudaSuccess) rc = cuda_fail(w, "instance stream");
+        }
+        if (rc == STRO_OK) {
+            const cudaError_t e = cudaEventRecord(b->ev1, st);
+            if (e != cudaSuccess) rc = cuda_fail(e, "batch event");
+        }
+        for (size_t i = 0; i < queued; ++i) {  // every enqueued run is waited for and freed
+            b->sims[i]->stream = b->streams[i];
+            const int r = sampled_finish(b->sims[i], &runs[i]);
+            b->sims[i]->stream = nullptr;
+            if (rc == STRO_OK) rc = r;
+        }
+        if (rc != STRO_OK) return rc;
+        STRO_CUDA(cudaEventSynchronize(b->ev1));
+        float ms = 0.0f;
+        STRO_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+        b->gpu_seconds += double(ms) * 1e-3;
+        b->last_path = "streams";
         return STRO_OK;
     }
     std::vector<std::vector<double>> tr(n), out(n);

@@ -220,9 +220,6 @@ int launch_one_step(stro_sim* s, int64_t t, bool probe, const int box[4]) {
     return STRO_OK;
 }
 
-// Steps per replayed graph in stro_sim_run (runs of at least twice as many).
-constexpr int64_t kRunGraphSteps = 32;
-
 int run_steps(stro_sim* s, int64_t steps, int64_t probe_step = -1, const int* box = nullptr) {
     cudaStream_t st = s->ctx->stream;
     STRO_CUDA(cudaEventRecord(s->ev0, st));
@@ -329,27 +326,27 @@ cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool prob
         if (ensure_block_lists(s) != STRO_OK) return cudaErrorMemoryAllocation;
         s->last_path = "split";
         return L.split(a, half, int(t & 1), bulk_feat(s), feat_on(s), s->block, s->d_blocks,
-                       s->nbulk, s->d_blocks + s->nbulk, s->nedge, s->ctx->stream);
+                       s->nbulk, s->d_blocks + s->nbulk, s->nedge, sim_stream(s));
     }
     const PairLaunchers& PL = fused ? fused::kPair : exact::kPair;
     const bool kbc = s->collision == STRO_COLLISION_KBC;  // one-cell kernels only
     if (!kbc && s->variant == 1 && PL.supported(half, geo, probe, s->nx, s->plane, s->pair_block)) {
         s->last_path = "pair";
-        return PL.launch(a, int(t & 1), feat_on(s), s->pair_block, s->ctx->stream);
+        return PL.launch(a, int(t & 1), feat_on(s), s->pair_block, sim_stream(s));
     }
     if (!kbc && s->variant == 3 && !geo && !probe && s->block.x * s->block.y <= 128) {
         s->last_path = "capped";
-        return L.capped(a, half, int(t & 1), feat_on(s), s->block, s->ctx->stream);
+        return L.capped(a, half, int(t & 1), feat_on(s), s->block, sim_stream(s));
     }
     if (!kbc && s->variant == 2 &&
         R.supported(half, geo, probe, s->nx, s->ny, s->rows_threads, s->rows_per_tile)) {
         s->last_path = "rows";
         return R.launch(a, half, int(t & 1), feat_on(s), s->rows_threads, s->rows_per_tile,
-                        s->ctx->sm_count, s->d_error, s->ctx->stream);
+                        s->ctx->sm_count, s->d_error, sim_stream(s));
     }
     s->last_path = probe ? "probe" : "cell";
     return L.step(a, half, int(t & 1), geo, feat_on(s), probe, probe ? s->probe_block : s->block,
-                  s->ctx->stream);
+                  sim_stream(s));
 }
 
 // ---- CUDA graphs of plain steps ---------------------------------------------
@@ -390,7 +387,7 @@ std::vector<uint8_t> graph_key(const stro_sim* s, int64_t t, int64_t G) {
                            s->nbulk, s->nedge, int64_t(s->lists_version),
                            int64_t(s->geo_version), s->lists_block.x, s->lists_block.y,
                            int64_t(reinterpret_cast<uintptr_t>(s->d_error)), s->ctx->sm_count,
-                           int64_t(reinterpret_cast<uintptr_t>(s->ctx->stream))};
+                           int64_t(reinterpret_cast<uintptr_t>(sim_stream(s)))};
     put_bytes(k, cfg);
     return k;
 }
@@ -412,7 +409,7 @@ static int graph_for(stro_sim* s, int64_t t, int64_t G, cudaGraphExec_t* out) {
             *out = s->graph_cache[i].second;
             return STRO_OK;
         }
-    cudaStream_t st = s->ctx->stream;
+    cudaStream_t st = sim_stream(s);
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_fail(e, "step graph capture");
@@ -453,7 +450,7 @@ int launch_plain_steps(stro_sim* s, int64_t t, int64_t count, int64_t graph_step
         const int rc = graph_for(s, k, graph_steps, &exec);
         if (rc != STRO_OK) return rc;
         for (; end - k >= graph_steps; k += graph_steps)
-            STRO_CUDA(cudaGraphLaunch(exec, s->ctx->stream));
+            STRO_CUDA(cudaGraphLaunch(exec, sim_stream(s)));
     }
     for (; k < end; ++k) {
         const int rc = launch_one_step(s, k, false, nullptr);
@@ -475,6 +472,114 @@ int ensure_geometry(stro_sim* s) {
     if (s->d_cell) return STRO_OK;
     s->force_geometry = true;
     return upload_geometry(s);
+}
+
+int sampled_begin(stro_sim* s, int64_t transient, int64_t sample_steps, int64_t stride,
+                  const int32_t box_in[4], double* forces, int64_t capacity, int64_t* samples,
+                  int64_t* steps_at, SampledRun* run) {
+    const int32_t x0 = box_in[0], x1 = box_in[1], y0 = box_in[2], y1 = box_in[3];
+    if (!samples) return fail(STRO_ERR_INVALID, "null sample count");
+    if (!s->wants_forces) return fail(STRO_ERR_STATE, "force samples require wants_forces");
+    if (s->steps_done % 2 != 0)
+        return fail(STRO_ERR_STATE, "a sampled run must start at an even step count");
+    if (transient < 0 || sample_steps < 0 || stride < 1)
+        return fail(STRO_ERR_INVALID, "negative step counts or stride < 1");
+    if (x0 < 0 || x1 >= s->nx || y0 < 0 || y1 >= s->ny || x0 > x1 || y0 > y1)
+        return fail(STRO_ERR_INVALID, "force box outside the lattice");
+    // Ladder.measure (Ladder.swift:55-66): even transient, then chunks of
+    // max(2, stride - 2) rounded down to even steps, each followed by the
+    // two-step force probe, until sample_steps steps are taken
+    transient &= ~int64_t(1);
+    const int64_t chunk = std::max<int64_t>(2, stride - 2) & ~int64_t(1);
+    const int64_t n = (sample_steps + chunk + 1) / (chunk + 2);
+    *samples = n;
+    if (n > capacity || (n > 0 && !forces)) {
+        return fail(STRO_ERR_INVALID, "sample buffer holds " + std::to_string(capacity) +
+                                          " samples, the run takes " + std::to_string(n));
+    }
+    cudaSetDevice(s->ctx->device);
+    cudaStream_t st = sim_stream(s);
+    *run = SampledRun{};
+    if (n > 0) STRO_CUDA(cudaMalloc(&run->d_samples, size_t(n) * 3 * sizeof(double)));
+    cudaError_t e = cudaSuccess;
+    if (n > 0) e = cudaMemsetAsync(run->d_samples, 0, size_t(n) * 3 * sizeof(double), st);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev0, st);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(st);
+        cudaFree(run->d_samples);
+        run->d_samples = nullptr;
+        return cuda_fail(e, "sampled run");
+    }
+    run->forces = forces;
+    run->count = n;
+    run->steps_at = steps_at;
+    run->t = s->steps_done;
+    run->transient_left = transient;
+    run->chunk = chunk;
+    std::copy(box_in, box_in + 4, run->box);
+    // plain steps replay CUDA graphs: one of `chunk` steps per sample when it
+    // is short, else runs of 32
+    run->g_transient = transient >= 2 * kRunGraphSteps ? kRunGraphSteps : 0;
+    run->g_chunk = (n >= 2 && chunk <= 256) ? chunk
+                                            : (chunk >= 2 * kRunGraphSteps ? kRunGraphSteps : 0);
+    return STRO_OK;
+}
+
+int sampled_advance(stro_sim* s, SampledRun* run) {
+    if (run->done) return STRO_OK;
+    cudaStream_t st = sim_stream(s);
+    if (run->transient_left > 0) {  // the transient, in pieces of 1024 steps
+        const int64_t piece = std::min<int64_t>(run->transient_left, 1024);
+        const int rc = launch_plain_steps(s, run->t, piece, run->g_transient);
+        run->t += piece;
+        run->transient_left -= piece;
+        return rc;
+    }
+    if (run->k < run->count) {  // one sample: the chunk, then the probe pair
+        int rc = launch_plain_steps(s, run->t, run->chunk, run->g_chunk);
+        run->t += run->chunk;
+        const bool geo = geo_on(s);
+        for (int j = 0; j < 2 && rc == STRO_OK; ++j, ++run->t)  // the force is taken on the odd step
+            rc = launch_one_step(s, run->t, geo && j == 1, run->box);
+        if (rc != STRO_OK) return rc;
+        if (geo) {
+            const dim3 pgrid = step_grid(step_args(s, 0), s->probe_block);
+            const int nblocks = int(pgrid.x * pgrid.y * pgrid.z);
+            STRO_CUDA(launch_fold(s->d_partials, nblocks, 3, run->d_samples + 3 * run->k, st));
+        }
+        if (run->steps_at) run->steps_at[run->k] = run->t;
+        ++run->k;
+        return STRO_OK;
+    }
+    cudaError_t e = cudaEventRecord(s->ev1, st);
+    if (e == cudaSuccess && run->count > 0)
+        e = cudaMemcpyAsync(run->forces, run->d_samples, size_t(run->count) * 3 * sizeof(double),
+                            cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return cuda_fail(e, "sampled run");
+    run->done = true;
+    return STRO_OK;
+}
+
+int sampled_finish(stro_sim* s, SampledRun* run) {
+    cudaSetDevice(s->ctx->device);
+    const cudaError_t e = cudaStreamSynchronize(sim_stream(s));
+    cudaFree(run->d_samples);
+    run->d_samples = nullptr;
+    if (e != cudaSuccess) return cuda_fail(e, "sampled run");
+    if (!run->done) return STRO_OK;  // abandoned after an error: only freed
+    float ms = 0.0f;
+    STRO_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    s->gpu_seconds += double(ms) * 1e-3;
+    s->steps_done = run->t;
+    if (s->variant == 2) {
+        int err = 0;
+        STRO_CUDA(cudaMemcpy(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost));
+        if (err != 0) {
+            cudaMemset(s->d_error, 0, sizeof(int));
+            return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-staged step timed out");
+        }
+    }
+    return STRO_OK;
 }
 
 }  // namespace rt
@@ -800,79 +905,14 @@ int stro_sim_run_sampled(stro_sim* s, int64_t transient, int64_t sample_steps, i
                          int32_t x0, int32_t x1, int32_t y0, int32_t y1, double* forces,
                          int64_t capacity, int64_t* samples, int64_t* steps_at) {
     CHECK_SIM(s);
-    if (!samples) return fail(STRO_ERR_INVALID, "null sample count");
-    if (!s->wants_forces) return fail(STRO_ERR_STATE, "force samples require wants_forces");
-    if (s->steps_done % 2 != 0)
-        return fail(STRO_ERR_STATE, "a sampled run must start at an even step count");
-    if (transient < 0 || sample_steps < 0 || stride < 1)
-        return fail(STRO_ERR_INVALID, "negative step counts or stride < 1");
-    if (x0 < 0 || x1 >= s->nx || y0 < 0 || y1 >= s->ny || x0 > x1 || y0 > y1)
-        return fail(STRO_ERR_INVALID, "force box outside the lattice");
-    // Ladder.measure (Ladder.swift:55-66): even transient, then chunks of
-    // max(2, stride - 2) rounded down to even steps, each followed by the
-    // two-step force probe, until sample_steps steps are taken
-    transient &= ~int64_t(1);
-    const int64_t chunk = std::max<int64_t>(2, stride - 2) & ~int64_t(1);
-    const int64_t n = (sample_steps + chunk + 1) / (chunk + 2);
-    *samples = n;
-    if (n > capacity || (n > 0 && !forces)) {
-        return fail(STRO_ERR_INVALID, "sample buffer holds " + std::to_string(capacity) +
-                                          " samples, the run takes " + std::to_string(n));
-    }
-    cudaSetDevice(s->ctx->device);
-    cudaStream_t st = s->ctx->stream;
-    const bool geo = geo_on(s);
-    double* d_samples = nullptr;
-    if (n > 0) STRO_CUDA(cudaMalloc(&d_samples, size_t(n) * 3 * sizeof(double)));
-    if (n > 0) STRO_CUDA(cudaMemsetAsync(d_samples, 0, size_t(n) * 3 * sizeof(double), st));
-    const int box[4] = {x0, x1, y0, y1};
-    const dim3 pgrid = step_grid(step_args(s, 0), s->probe_block);
-    const int nblocks = int(pgrid.x * pgrid.y * pgrid.z);
-    int rc = STRO_OK;
-    cudaError_t e = cudaEventRecord(s->ev0, st);
-    int64_t t = s->steps_done;
-    // plain steps replay CUDA graphs: one of `chunk` steps per sample when it
-    // is short, else runs of 32
-    const int64_t g_transient = transient >= 2 * kRunGraphSteps ? kRunGraphSteps : 0;
-    const int64_t g_chunk = (n >= 2 && chunk <= 256) ? chunk
-                                                     : (chunk >= 2 * kRunGraphSteps ? kRunGraphSteps : 0);
-    auto plain = [&](int64_t count, int64_t G) {
-        if (rc == STRO_OK) rc = launch_plain_steps(s, t, count, G);
-        t += count;
-    };
-    auto probe_pair = [&]() {  // the force is taken on the odd step
-        for (int64_t k = 0; k < 2 && rc == STRO_OK; ++k, ++t)
-            rc = launch_one_step(s, t, geo && k == 1, box);
-    };
-    if (e == cudaSuccess) plain(transient, g_transient);
-    for (int64_t k = 0; k < n && rc == STRO_OK && e == cudaSuccess; ++k) {
-        plain(chunk, g_chunk);
-        probe_pair();
-        if (rc == STRO_OK && geo)
-            e = launch_fold(s->d_partials, nblocks, 3, d_samples + 3 * k, st);
-        if (steps_at) steps_at[k] = t;
-    }
-    if (rc == STRO_OK && e == cudaSuccess) e = cudaEventRecord(s->ev1, st);
-    if (rc == STRO_OK && e == cudaSuccess && n > 0)
-        e = cudaMemcpyAsync(forces, d_samples, size_t(n) * 3 * sizeof(double),
-                            cudaMemcpyDeviceToHost, st);
-    if (rc == STRO_OK && e == cudaSuccess) e = cudaStreamSynchronize(st);
-    cudaFree(d_samples);
+    const int32_t box[4] = {x0, x1, y0, y1};
+    SampledRun run;
+    int rc = sampled_begin(s, transient, sample_steps, stride, box, forces, capacity, samples,
+                           steps_at, &run);
     if (rc != STRO_OK) return rc;
-    if (e != cudaSuccess) return cuda_fail(e, "sampled run");
-    float ms = 0.0f;
-    STRO_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
-    s->gpu_seconds += double(ms) * 1e-3;
-    s->steps_done = t;
-    if (s->variant == 2) {
-        int err = 0;
-        STRO_CUDA(cudaMemcpy(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost));
-        if (err != 0) {
-            cudaMemset(s->d_error, 0, sizeof(int));
-            return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-staged step timed out");
-        }
-    }
-    return STRO_OK;
+    while (rc == STRO_OK && !run.done) rc = sampled_advance(s, &run);
+    const int rf = sampled_finish(s, &run);
+    return rc != STRO_OK ? rc : rf;
 }
 
 int stro_sim_render_slice(stro_sim* s, int32_t z, float uref, uint16_t* rgba, double* seconds) {

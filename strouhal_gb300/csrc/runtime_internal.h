@@ -88,11 +88,44 @@ struct stro_sim {
     uint64_t geo_version = 0;      // bumped whenever the device geometry changes
     // CUDA graphs of runs of plain steps, keyed by everything their launches read
     bool graphs = true;
+    // Stream of the step launches when not null: a batch in STRO_BATCH_STREAMS
+    // mode sets it while it enqueues this lattice's run, then clears it.
+    cudaStream_t stream = nullptr;
     std::vector<std::pair<std::vector<uint8_t>, cudaGraphExec_t>> graph_cache;
 };
 
 namespace stro {
 namespace rt {
+
+// Steps per replayed graph in stro_sim_run (runs of at least twice as many).
+constexpr int64_t kRunGraphSteps = 32;
+
+// Stream the step launches of `s` go to.
+inline cudaStream_t sim_stream(const stro_sim* s) { return s->stream ? s->stream : s->ctx->stream; }
+
+// A sampled run (stro_sim_run_sampled) in pieces: begin checks the arguments
+// and allocates the device sample buffer; each advance enqueues the next piece
+// of the schedule (up to 1024 transient steps, or one sample: chunk, probe
+// pair, fold) on the simulation's stream without waiting, the last one the
+// read-back of the forces; finish waits and does the bookkeeping (or, after
+// an error, only frees). A batch interleaves the advances of its instances.
+struct SampledRun {
+    double* d_samples = nullptr;
+    double* forces = nullptr;
+    int64_t* steps_at = nullptr;
+    int64_t count = 0;           // samples
+    int64_t k = 0;               // next sample
+    int64_t t = 0;               // step count after what is enqueued
+    int64_t transient_left = 0;
+    int64_t chunk = 0, g_transient = 0, g_chunk = 0;
+    int box[4] = {0, 0, 0, 0};
+    bool done = false;           // everything, read-back included, is enqueued
+};
+int sampled_begin(stro_sim* s, int64_t transient, int64_t sample_steps, int64_t stride,
+                  const int32_t box[4], double* forces, int64_t capacity, int64_t* samples,
+                  int64_t* steps_at, SampledRun* run);
+int sampled_advance(stro_sim* s, SampledRun* run);
+int sampled_finish(stro_sim* s, SampledRun* run);
 
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);

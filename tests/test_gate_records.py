@@ -116,7 +116,7 @@ def test_sphere_drag_against_the_reference_correlation(record):
 
 def test_batched_ladder_reproduces_sequential():
     r = rec("ladder")
-    for mode in ("persistent", "rounds"):
+    for mode in ("persistent", "rounds", "streams"):
         if mode in r and "identical_states" in r[mode]:
             assert r[mode]["identical_states"]
             assert r[mode]["max_trace_rel_diff"] < 1e-12
@@ -127,7 +127,7 @@ def test_batched_small_rungs_beat_sequential():
     per round against per-rung launches; identical states and traces."""
     r = rec("ladder_small")
     assert max(i["n"] for i in r["instances"]) <= 32
-    for mode in ("persistent", "rounds"):
+    for mode in ("persistent", "rounds", "streams"):
         assert r[mode]["identical_states"]
         assert r[mode]["max_trace_rel_diff"] < 1e-12
     assert max(r["persistent"]["speedup_vs_sequential"],
@@ -187,9 +187,10 @@ def test_credibility_gates_and_budget_from_the_oracle():
     r = rec("credibility")
     assert r["resolutions"] == [32, 48, 64] and r["steps_factor"] == 1.0
     # every mode ends on the same lattice; QoIs equal (batched: to FP64 rounding)
-    for mode in ("sequential", "concurrent", "batched"):
+    for mode in ("sequential", "concurrent", "batched", "streams"):
         assert r[mode + "_digest_equal"], mode
     assert r["concurrent_max_rel_diff"] == 0.0 and r["batched_max_rel_diff"] <= 1e-12
+    assert r["streams_max_rel_diff"] == 0.0
     rungs = []
     for n, value, stat in r["rungs"]:
         tail = r["series"][str(n)]

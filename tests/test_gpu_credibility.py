@@ -67,7 +67,8 @@ def test_run_sampled_matches_oracle(gpu, oracle):
     s.close()
 
 
-@pytest.mark.parametrize("mode", ["persistent", "rounds", "rounds-unsplit", "sequential"])
+@pytest.mark.parametrize("mode", ["persistent", "rounds", "rounds-unsplit", "sequential",
+                                  "streams"])
 def test_batch_run_sampled_equals_single_runs(gpu, mode):
     """Three variants of different sizes and schedules in one batched sampled
     run: DDFs and step counts bitwise those of Simulation.runSampled, forces
@@ -88,7 +89,7 @@ def test_batch_run_sampled_equals_single_runs(gpu, mode):
     out = batch.runSampled([p[2] for p in plan], [p[3] for p in plan], [p[4] for p in plan],
                            [v.box for v in group])
     assert batch.lastPath in ({"persistent": "persistent-graph", "rounds": "rounds-graph",
-                               "sequential": "sequential"}[mode],)
+                               "sequential": "sequential", "streams": "streams"}[mode],)
     bulk, edge = batch.splitTiles
     if mode == "rounds" and not unsplit:
         assert bulk > 0 and edge > 0, (bulk, edge)
@@ -98,7 +99,7 @@ def test_batch_run_sampled_equals_single_runs(gpu, mode):
         assert np.array_equal(ata, atb)
         assert b.sim.stepsDone == a.sim.stepsDone and b.sim.stateDigest == a.sim.stateDigest
         assert fa.shape == fb.shape and np.allclose(fb, fa, rtol=1e-12, atol=1e-16)
-        if mode == "sequential":
+        if mode in ("sequential", "streams"):
             assert np.array_equal(fa, fb)
     batch.close()
     for (a, _), b in zip(solo, group):
@@ -188,12 +189,14 @@ def test_short_ladder_budget_matches_oracle_and_modes_agree(gpu):
     seq = cr.Ladder.credibility(gpu, case, "mean C_D", res)
     con = cr.Ladder.credibility(gpu, case, "mean C_D", res, mode="concurrent")
     bat = cr.Ladder.credibility(gpu, case, "mean C_D", res, mode="batched")
-    for r in (seq, con, bat):
+    stm = cr.Ladder.credibility(gpu, case, "mean C_D", res, mode="streams")
+    for r in (seq, con, bat, stm):
         assert [x.cellsPerFeature for x in r.rungs] == res
         assert r.digest == seq.digest
     # concurrent streams give the same bits as one variant after another
     assert [(x.value, x.stat) for x in seq.rungs] == [(x.value, x.stat) for x in con.rungs]
-    assert seq.series == con.series
+    assert seq.series == con.series == stm.series
+    assert stm.path == "streams"
     # the batch folds box sums per tile: same QoIs to FP64 rounding
     for key, vals in seq.series.items():
         assert np.allclose(bat.series[key], vals, rtol=1e-12, atol=0), key

@@ -152,7 +152,7 @@ def _ladder(sg, gpu, precision="fp32"):
     return sims, steps, logs
 
 
-@pytest.mark.parametrize("mode", ["persistent", "rounds", "sequential"])
+@pytest.mark.parametrize("mode", ["persistent", "rounds", "sequential", "streams"])
 @pytest.mark.parametrize("precision", ["fp32", "fp16s"])
 def test_batch_matches_independent_runs(gpu, mode, precision):
     import strouhal_gb300 as sg
@@ -174,7 +174,7 @@ def test_batch_matches_independent_runs(gpu, mode, precision):
     b = sg.Batch(gpu, sims, mode=mode)
     traces = b.run(steps, logs)
     assert b.lastPath.startswith({"persistent": "persistent", "rounds": "rounds",
-                                  "sequential": "sequential"}[mode])
+                                  "sequential": "sequential", "streams": "streams"}[mode])
     if mode == "rounds":  # the walled channel's bulk tiles ran on the wall-free kernels
         assert min(b.splitTiles) > 0, b.splitTiles
     for s, r, k, tr, rtr in zip(sims, ref, steps, traces, ref_traces):
