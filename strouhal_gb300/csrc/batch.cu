@@ -253,14 +253,8 @@ int run_streams(stro_batch* b, const int64_t* steps, const int32_t* log_every,
         STRO_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
         s->gpu_seconds += double(ms) * 1e-3;
         s->steps_done += steps[i];
-        if (s->variant == 2) {
-            int err = 0;
-            STRO_CUDA(cudaMemcpy(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost));
-            if (err != 0) {
-                cudaMemset(s->d_error, 0, sizeof(int));
-                return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-staged step timed out");
-            }
-        }
+        const int re = check_rows_error(s);
+        if (re != STRO_OK) return re;
         if (cnt[i]) {
             traces[i].resize(cnt[i]);
             STRO_CUDA(cudaMemcpy(traces[i].data(), b->d_traces + off[i], cnt[i] * sizeof(double),

@@ -241,15 +241,19 @@ int run_steps(stro_sim* s, int64_t steps, int64_t probe_step = -1, const int* bo
     s->gpu_seconds += double(ms) * 1e-3;
     s->steps_done += steps;
     STRO_CUDA(cudaGetLastError());
-    if (s->variant == 2) {
-        int err = 0;
-        STRO_CUDA(cudaMemcpy(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost));
-        if (err != 0) {
-            cudaMemset(s->d_error, 0, sizeof(int));
-            return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-streaming step timed out");
-        }
-    }
-    return STRO_OK;
+    return check_rows_error(s);
+}
+
+// The row-staged variant records a bulk-copy wait that gave up in a device
+// word (the kernel returns instead of waiting on): read it after a run, reset
+// it and report the timeout.
+int check_rows_error(stro_sim* s) {
+    if (s->variant != 2) return STRO_OK;
+    int err = 0;
+    STRO_CUDA(cudaMemcpy(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost));
+    if (err == 0) return STRO_OK;
+    cudaMemset(s->d_error, 0, sizeof(int));
+    return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-staged step timed out");
 }
 
 int ensure_partials(stro_sim* s, size_t doubles) {
@@ -571,15 +575,7 @@ int sampled_finish(stro_sim* s, SampledRun* run) {
     STRO_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
     s->gpu_seconds += double(ms) * 1e-3;
     s->steps_done = run->t;
-    if (s->variant == 2) {
-        int err = 0;
-        STRO_CUDA(cudaMemcpy(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost));
-        if (err != 0) {
-            cudaMemset(s->d_error, 0, sizeof(int));
-            return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-staged step timed out");
-        }
-    }
-    return STRO_OK;
+    return check_rows_error(s);
 }
 
 }  // namespace rt

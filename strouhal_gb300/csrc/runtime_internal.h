@@ -152,6 +152,8 @@ cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool prob
 // arguments, same results either way.
 int launch_plain_steps(stro_sim* s, int64_t t, int64_t count, int64_t graph_steps);
 void drop_graphs(stro_sim* s);
+// STRO_ERR_TIMEOUT (and the flag reset) if a row-staged step gave up a wait.
+int check_rows_error(stro_sim* s);
 void ctx_retain(stro_ctx* c);
 void ctx_release(stro_ctx* c);
 int observables(stro_sim* s, double out[2]);
