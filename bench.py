@@ -30,6 +30,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -88,14 +89,18 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device):
+    def __init__(self, device, path=None):
+        """path: where the raw samples are kept (default: a temporary file)."""
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % device)
+        if path is None:
+            fd, path = tempfile.mkstemp(prefix="clocks_bench_%d_" % device, suffix=".csv")
+            os.close(fd)
+        self.path = path
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            os.makedirs(os.path.dirname(os.path.abspath(self.path)), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
@@ -288,6 +293,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--clocks-csv", default=None,
+                    help="keep the nvidia-smi samples of the timed region in this file")
     args = ap.parse_args()
     ws, rank, local, dist = dist_setup()
     if args.impl == "reference":
@@ -301,7 +308,7 @@ def main():
     import strouhal_gb300 as sg
 
     gpu = sg.GPU(local)
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(local, args.clocks_csv)
     # headline: FP16-storage SRT in the fused arithmetic (within the FP64 oracle's
     # tolerances, bit-exact against the oracle's fused arithmetic)
     head = run_variant(sg, gpu, "fp16s", None, args.steps, args.warmup, dist, clocks,
