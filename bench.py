@@ -93,6 +93,7 @@ class ClockSampler:
         """path: where the raw samples are kept (default: a temporary file)."""
         self.device = device
         self.proc = None
+        self.temporary = path is None
         if path is None:
             fd, path = tempfile.mkstemp(prefix="clocks_bench_%d_" % device, suffix=".csv")
             os.close(fd)
@@ -122,6 +123,8 @@ class ClockSampler:
             self.fh.close()
 
     def summary(self):
+        if getattr(self, "_summary", None) is not None:
+            return self._summary
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, smax, reasons = [], [], set()
@@ -138,9 +141,12 @@ class ClockSampler:
             for nm, val in zip(names, parts[5:9]):
                 if val.lower().startswith("active"):
                     reasons.add(nm)
-        return {"sm_mhz": statistics.median(sm) if sm else None,
-                "sm_max_mhz": max(smax) if smax else None,
-                "samples": len(sm), "reasons": sorted(reasons)}
+        if self.temporary:
+            os.remove(self.path)
+        self._summary = {"sm_mhz": statistics.median(sm) if sm else None,
+                         "sm_max_mhz": max(smax) if smax else None,
+                         "samples": len(sm), "reasons": sorted(reasons)}
+        return self._summary
 
 
 def dist_setup():
