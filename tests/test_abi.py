@@ -93,3 +93,23 @@ def test_sphere_solid_fractions(sg):
     P = np.stack(np.meshgrid(x + o, y + o, z + o, indexing="ij"), -1)
     inside = np.count_nonzero(((P - [11.5, 10.0, 10.7]) ** 2).sum(-1) <= 36.0)
     assert a[z, y, x] == np.float32(inside) / np.float32(512)
+
+
+def test_plain_c_client_compiles_links_and_runs(sg, tmp_path):
+    """The header is C99 (what a cgo, Swift or ctypes binding reads) and the
+    library links from C; on a machine without a GPU the client sees
+    STRO_ERR_NO_DEVICE with a message."""
+    exe = str(tmp_path / "c_client")
+    libdir = os.path.dirname(sg.LIB_PATH)
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                    "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "c_client.c"),
+                    "-L", libdir, "-lstrouhal_gb300", "-Wl,-rpath," + libdir, "-o", exe],
+                   check=True, capture_output=True, text=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    import torch
+
+    if not torch.cuda.is_available():
+        assert r.stdout.startswith("no-device ")
+    else:
+        assert r.stdout.startswith("digest ")
