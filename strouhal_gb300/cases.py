@@ -109,6 +109,149 @@ def cavity(gpu, n=128, re=100.0, steps=20000, lam=None, ulid=0.1, ramp=5000, nz=
     return out
 
 
+def _lid_cavity_sim(gpu, n, nz, re, ulid, lam, ramp, flags, lid=None, precision="fp32"):
+    nu = ulid * n / re
+    wp, wm = sg.trtOmegas(3.0 * nu + 0.5, lam)
+    return sg.Simulation(gpu, precision=precision, nx=n + 2, ny=n + 2, nz=nz, omega=wp,
+                         omegaMinus=wm, lid=lid if lid is not None else (ulid, 0.0, 0.0),
+                         rampSteps=ramp, flags=flags.reshape(-1))
+
+
+def cavity_zperiodic(gpu, n=128, nz=8, re=400.0, steps=120000, ulid=0.1, lam=0.25, ramp=5000):
+    """3-D lattice, 2-D physics (Cases.swift:642-686): the cavity periodic in z
+    must reproduce the 2-D solution and stay z-uniform. Records the vertical
+    centreline u(y)/u_lid of slice z = 0 and the largest |u_x| difference of
+    any interior cell from its z = 0 counterpart."""
+    N = n + 2
+    flags = np.zeros((nz, N, N), np.uint8)
+    flags[:, :, 0] = flags[:, :, -1] = flags[:, 0, :] = sg.Cell.solid
+    flags[:, -1, :] = sg.Cell.lid
+    s = _lid_cavity_sim(gpu, n, nz, re, ulid, lam, ramp, flags)
+    s.run(steps)
+    m = s.probeMoments().reshape(nz, N, N, 4)
+    ux = m[:, 1:n + 1, 1:n + 1, 0]
+    zdev = float(np.max(np.abs(ux[1:] - ux[:1]))) if nz > 1 else 0.0
+    c0, c1 = n // 2, n // 2 + 1
+    u = [(float(m[0, j, c0, 0]) + float(m[0, j, c1, 0])) / 2.0 / ulid for j in range(1, n + 1)]
+    out = {"n": n, "nz": nz, "re": re, "steps": steps, "lambda": lam, "u_centerline": u,
+           "max_z_dev": zdev, "finite": bool(np.all(np.isfinite(m))),
+           "digest": s.stateDigest, "gpu_seconds": s.gpuSeconds}
+    s.close()
+    return out
+
+
+def cavity_cubic(gpu, n=64, re=400.0, steps=120000, ulid=0.1, lam=0.25, ramp=5000):
+    """Cubic cavity, full 3-D flow (Cases.swift:688-728): stable, and mirror
+    symmetric about the mid-z plane. Records the RMS of u_x(z) - u_x(n+1-z) over
+    the interior in units of u_lid and the mid-plane centreline minimum."""
+    N = n + 2
+    flags = np.zeros((N, N, N), np.uint8)  # (z, y, x)
+    flags[0, :, :] = flags[-1, :, :] = sg.Cell.solid
+    flags[:, 0, :] = flags[:, -1, :] = sg.Cell.solid
+    flags[:, :, 0] = flags[:, :, -1] = sg.Cell.solid
+    flags[1:n + 1, -1, 1:n + 1] = sg.Cell.lid
+    s = _lid_cavity_sim(gpu, n, N, re, ulid, lam, ramp, flags)
+    s.run(steps)
+    m = s.probeMoments().reshape(N, N, N, 4)
+    ux = m[1:n + 1, 1:n + 1, 1:n + 1, 0].astype(np.float64)
+    asym = float(np.sqrt(np.mean((ux - ux[::-1]) ** 2)) / ulid)
+    umin = float(min(0.0, np.min(m[n // 2, 1:n + 1, n // 2, 0].astype(np.float64) / ulid)))
+    out = {"n": n, "re": re, "steps": steps, "lambda": lam, "asym_rms": asym,
+           "centerline_umin": umin, "finite": bool(np.all(np.isfinite(m))),
+           "digest": s.stateDigest, "gpu_seconds": s.gpuSeconds}
+    s.close()
+    return out
+
+
+def rotation(gpu, n=64, re=100.0, steps=60000, ulid=0.1, lam=0.25, ramp=2000):
+    """Rotation / anisotropy (Cases.swift:730-765): a cavity whose lid is the
+    +x face moving +y must give the standard cavity (lid on +y moving +x)
+    transposed. Records the RMS of the transposed-field difference in u_lid."""
+    N = n + 2
+    fa = np.zeros((1, N, N), np.uint8)
+    fa[0, :, 0] = fa[0, :, -1] = fa[0, 0, :] = sg.Cell.solid
+    fa[0, -1, :] = sg.Cell.lid
+    fb = np.zeros((1, N, N), np.uint8)
+    fb[0, 0, :] = fb[0, -1, :] = fb[0, :, 0] = sg.Cell.solid
+    fb[0, :, -1] = sg.Cell.lid
+    a = _lid_cavity_sim(gpu, n, 1, re, ulid, lam, ramp, fa)
+    b = _lid_cavity_sim(gpu, n, 1, re, ulid, lam, ramp, fb, lid=(0.0, ulid, 0.0))
+    a.run(steps)
+    b.run(steps)
+    ma = a.probeMoments().reshape(N, N, 4)[1:n + 1, 1:n + 1].astype(np.float64)  # [y, x]
+    mb = b.probeMoments().reshape(N, N, 4)[1:n + 1, 1:n + 1].astype(np.float64)
+    mbt = np.transpose(mb, (1, 0, 2))  # mbt[y, x] = b at (x, y) swapped: cell (y, x) of b
+    du = ma[..., 0] - mbt[..., 1]
+    dv = ma[..., 1] - mbt[..., 0]
+    rms = float(np.sqrt(np.sum(du * du + dv * dv) / (2 * n * n)) / ulid)
+    out = {"n": n, "re": re, "steps": steps, "lambda": lam, "transposed_rms": rms,
+           "finite": bool(np.all(np.isfinite(ma)) and np.all(np.isfinite(mb))),
+           "gpu_seconds": a.gpuSeconds + b.gpuSeconds}
+    a.close()
+    b.close()
+    return out
+
+
+def mass_drift(gpu, n=128, re=100.0, steps=50000, ulid=0.1, lam=0.25, ramp=5000):
+    """Lid mass drift (Cases.swift:787-799): the moving-lid bounce-back with
+    rho_w = 1 does not conserve mass exactly; |sum(rho - 1)| after 50,000 steps
+    of the 2-D cavity (TRT, Lambda = 1/4) must stay bounded."""
+    N = n + 2
+    flags = np.zeros((1, N, N), np.uint8)
+    flags[0, :, 0] = flags[0, :, -1] = flags[0, 0, :] = sg.Cell.solid
+    flags[0, -1, :] = sg.Cell.lid
+    s = _lid_cavity_sim(gpu, n, 1, re, ulid, lam, ramp, flags)
+    m0 = s.massSum()
+    s.run(steps)
+    drift = s.massSum() - m0
+    out = {"n": n, "re": re, "steps": steps, "lambda": lam, "mass_drift": drift,
+           "per_step_cell": abs(drift) / steps / (n * n), "digest": s.stateDigest,
+           "gpu_seconds": s.gpuSeconds}
+    s.close()
+    return out
+
+
+def dfg1(gpu, D=40, max_steps=240000, uin_max=0.075, upstream_d=2.0, curved=True):
+    """Schaefer-Turek DFG 2D-1, Re 20, steady (Cases.swift:440-536): C_D against
+    the spectral 5.57953523384, probed every 4,000 steps until it settles
+    (three successive relative changes below 1e-5 after three flow-throughs)."""
+    nx = int((20.0 + upstream_d) * D) + 2
+    ny = int(4.1 * D) + 2
+    u_mean = uin_max * 2.0 / 3.0
+    nu = u_mean * D / 20.0
+    wp, wm = sg.trtOmegas(3.0 * nu + 0.5, 3.0 / 16.0)
+    cx, cy = 0.5 + upstream_d * D, 0.5 + 2.0 * D
+    flags = np.zeros((ny, nx), np.uint8)
+    if not curved:
+        yy, xx = np.mgrid[0:ny, 0:nx]
+        flags[(xx - cx) ** 2 + (yy - cy) ** 2 <= D * D / 4.0] = sg.Cell.solid
+    flags[:, 0] = flags[:, -1] = sg.Cell.inflow
+    flags[0, :] = flags[-1, :] = sg.Cell.solid
+    s = sg.Simulation(gpu, precision="fp32", nx=nx, ny=ny, nz=1, omega=wp, omegaMinus=wm,
+                      uin=uin_max, rampSteps=4000, wantsForces=True, flags=flags.reshape(-1))
+    if curved:
+        s.setSolidFractions(sg.diskSolidFractions(nx, ny, cx, cy, D / 2.0))
+    box = ((int(cx) - D // 2 - 3, int(cx) + D // 2 + 3), (int(cy) - D // 2 - 3, int(cy) + D // 2 + 3))
+    flow_through = int(nx / u_mean)
+    cd = cl = 0.0
+    prev, settled = float("inf"), 0
+    while s.stepsDone < max_steps:
+        s.run(4000 - 2)  # the probe takes two more
+        f = s.probeForce(*box)
+        cd = float(2.0 * f[0] / (u_mean * u_mean * D))
+        cl = float(2.0 * f[1] / (u_mean * u_mean * D))
+        if s.stepsDone > 3 * flow_through:
+            settled = settled + 1 if abs(cd - prev) / abs(cd) < 1e-5 else 0
+            if settled >= 3:
+                break
+        prev = cd
+    out = {"D": D, "curved": curved, "uin_max": uin_max, "steps": s.stepsDone, "cd": cd,
+           "cl": cl, "cd_ref": 5.57953523384, "cd_err": abs(cd - 5.57953523384) / 5.57953523384,
+           "digest": s.stateDigest, "gpu_seconds": s.gpuSeconds}
+    s.close()
+    return out
+
+
 def ghia_rms(rec, table_u, table_v):
     """Centreline RMS against a table of (coordinate, value) pairs, linear
     interpolation between the two bracketing nodes (Cases.swift:220-270)."""
@@ -628,7 +771,9 @@ def credibility(gpu, resolutions=(32, 48, 64), base_mach=0.075, steps_factor=1.0
     return out
 
 
-CASES = {"poiseuille": poiseuille, "tg_order": tg_order, "cavity": cavity, "dfg2": dfg2,
+CASES = {"poiseuille": poiseuille, "tg_order": tg_order, "cavity": cavity,
+         "cavity_zperiodic": cavity_zperiodic, "cavity_cubic": cavity_cubic,
+         "rotation": rotation, "mass_drift": mass_drift, "dfg1": dfg1, "dfg2": dfg2,
          "dfg2_adjoint": dfg2_adjoint, "tgv": tgv, "sphere": sphere,
          "sphere_adjoint": sphere_adjoint, "ladder": ladder, "stl_voxelize": stl_voxelize,
          "render": render, "credibility": credibility}

@@ -267,3 +267,54 @@ def test_tgv_m5_configuration_trt_reproduces_and_kbc_passes():
     assert abs(f["peak_t"] - t_ref) <= 0.5                                 # Cases.swift:1312
     assert abs(kbc[320]["peak_eps"] - kbc[288]["peak_eps"]) / e_ref <= 0.01  # Cases.swift:1316
     assert abs(f["peak_eps"] - e_ref) / e_ref <= 0.01                      # gate 10%, 1% here
+
+
+def test_cavity_zperiodic_record():
+    """3-D lattice, 2-D physics (Cases.swift:642-686): the z-periodic cavity's
+    Re 400 centreline u against Ghia (the reference's interpolation) within an
+    RMS of 0.02, and every z slice equal to z = 0 within 1e-5."""
+    src = ref_source(CASES_SWIFT)
+    r = rec("cavity_zperiodic")
+    n, u = r["n"], r["u_centerline"]
+    rows = ref_table(src, "ghiaU")
+    ssq = 0.0
+    for row in rows:
+        pos = row[0] * n + 0.5
+        k0 = min(max(int(math.floor(pos)), 1), n - 1)
+        frac = pos - k0
+        ours = u[k0 - 1] * (1.0 - frac) + u[k0] * frac
+        ssq += (ours - row[2]) ** 2
+    rms = math.sqrt(ssq / len(rows))
+    assert rms <= 0.02, rms
+    assert r["max_z_dev"] <= 1e-5, r["max_z_dev"]
+
+
+def test_cavity_cubic_record():
+    """Cubic cavity (Cases.swift:688-728): stable and mirror symmetric about
+    the mid-z plane within 5e-4 u_lid RMS."""
+    r = rec("cavity_cubic")
+    assert r["finite"] and math.isfinite(r["centerline_umin"])
+    assert r["asym_rms"] <= 5e-4, r["asym_rms"]
+
+
+def test_rotation_record():
+    """Rotation / anisotropy (Cases.swift:730-765): the +x-face lid cavity
+    equals the standard one transposed within 5e-4 u_lid RMS."""
+    r = rec("rotation")
+    assert r["finite"]
+    assert r["transposed_rms"] <= 5e-4, r["transposed_rms"]
+
+
+def test_mass_drift_record():
+    """Lid mass drift (Cases.swift:787-799): |sum(rho - 1)| <= 1e-2 after
+    50,000 steps."""
+    r = rec("mass_drift")
+    assert r["steps"] == 50000
+    assert abs(r["mass_drift"]) <= 1e-2, r["mass_drift"]
+
+
+def test_dfg1_record():
+    """Schaefer-Turek 2D-1 (Cases.swift:440-536): C_D within 1% of the
+    spectral 5.57953523384."""
+    r = rec("dfg1")
+    assert r["cd_err"] <= 0.01, (r["cd"], r["cd_err"])
