@@ -739,7 +739,8 @@ def credibility(gpu, resolutions=(32, 48, 64), base_mach=0.075, steps_factor=1.0
         "out_of_domain_refuses": bool(far.isOutside and math.isnan(far_budget.combined)),
     }
     md = cr.report_markdown(first, [
-        "cavity, Poiseuille, Taylor-Green order, DFG 2D-2 and sphere gates: "
+        "cavity (2-D, z-periodic, cubic), rotation, lid mass drift, Poiseuille, Taylor-Green "
+        "order, DFG 2D-1 / 2D-2 and sphere gates: "
         "tests/test_gate_records.py over tests/records/",
         "every step kernel against the oracle: tests/test_gpu_parity.py"])
     if report:
