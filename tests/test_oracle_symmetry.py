@@ -57,8 +57,8 @@ def _walls(po, nx, ny, nz, lid_face):
 
 
 @pytest.mark.parametrize("geometry", ["periodic", "cavity"])
-@pytest.mark.parametrize("les", [0.0, 0.01])
-def test_step_commutes_with_z_mirror(oracle, geometry, les):
+@pytest.mark.parametrize("les,collision", [(0.0, "reference"), (0.01, "reference"), (0.0, "kbc")])
+def test_step_commutes_with_z_mirror(oracle, geometry, les, collision):
     po = oracle
     nx, ny, nz = 10, 9, 8
     flags = (np.zeros(nx * ny * nz, np.uint8) if geometry == "periodic"
@@ -68,11 +68,13 @@ def test_step_commutes_with_z_mirror(oracle, geometry, les):
     rng = np.random.default_rng(7)
     f0 = rng.standard_normal((19, nx * ny * nz)) * 0.01
     a = po.OracleSim(nx, ny, nz, flags=flags, force=force, **kw)
+    a.collision = collision
     a.f[:] = f0
     a.run(2)
     g0, gflags = _mirror_z(po, f0, flags, nx, ny, nz)
     kw["lid"] = (0.05, 0.0, -0.02)
     b = po.OracleSim(nx, ny, nz, flags=gflags, force=(force[0], force[1], -force[2]), **kw)
+    b.collision = collision
     b.f[:] = g0
     b.run(2)
     back, _ = _mirror_z(po, b.f, gflags, nx, ny, nz)
