@@ -217,6 +217,12 @@ int stro_sim_last_path(stro_sim* sim, char* buf, size_t len);
  * lattice rows per tile (1 to 8). */
 int stro_sim_set_rows_tile(stro_sim* sim, int32_t threads, int32_t rows);
 int stro_sim_get_rows_tile(stro_sim* sim, int32_t* threads, int32_t* rows);
+/* Polls per bounded wait of variant 2 (default 2^22; a bulk copy completes in
+ * microseconds). A wait that runs out makes every thread of the block return
+ * once the block's copies in flight have landed; the run then fails with
+ * STRO_ERR_TIMEOUT and the lattice state is undefined. 0 gives up at the first
+ * wait (exercises that path). No reference counterpart. */
+int stro_sim_set_spin_limit(stro_sim* sim, int64_t polls);
 /* Walled lattices run their bulk blocks (cells with no wall neighbour and no
  * solid fraction) with the wall-free kernels and only the boundary blocks
  * with the wall-aware ones (default on); 0 runs the wall-aware kernels on
@@ -295,8 +301,11 @@ int stro_batch_autotune(stro_batch* batch, int64_t rounds, int32_t* mode, int32_
  * library until exit.
  *   f            device pointer: 19 planes, plane i at f + i*plane_stride elements
  *                (FP32 or FP16 per `precision`)
- *   cell_types   optional device array of N cell codes (0 = fluid; other cells
- *                are skipped); NULL = all fluid
+ *   cell_types   optional device array of N cell bytes; only the low 3 bits are
+ *                read, as the Cell code (0 = fluid; cells of other codes are
+ *                skipped), so flag bits a caller keeps above them are ignored;
+ *                NULL = all fluid
+ *   omega        relaxation rate, finite and in (0, 2); others are rejected
  *   force        host pointer to the uniform force (half-force shift of u); NULL = 0
  *   out          device pointer to 2 doubles: sum |u|^2, sum 2 nu S:S (nu from omega)
  *   stream       cudaStream_t (NULL = default stream); the call only enqueues work

@@ -16,7 +16,7 @@
 // compiled as C++ (oracle/ref_metal_driver.cpp) by tests/test_oracle_pin.py.
 //
 // Only tests/, the smoke check and bench.py's CPU-baseline leg load this
-// library. Build: g++ -O2 -std=c++17 -ffp-contract=off -fopenmp (see Makefile).
+// library. Build: g++ -O2 -std=c++17 -ffp-contract=off -fopenmp (oracle/build_oracle.py).
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
@@ -792,6 +792,113 @@ void init_all(void* fv, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t mode, fl
 
 }  // namespace
 
+// Forward and reverse steps of the FP64 adjoint (orc_adjoint_force_ex below).
+namespace adj {
+
+struct Ctx {
+    const uint8_t* flags;
+    const uint32_t* solid_mask;
+    const uint32_t* lid_mask;
+    const float* eps;
+    const float* ffield;
+    const int* box;
+    const double* dir;
+    size_t N;
+    int threads;
+};
+
+inline void cell_ctx(const Params& p, const Ctx& c, size_t n, int& x, int& y, int& z,
+                     uint32_t& sm, uint32_t& lm) {
+    x = int(n % p.nx);
+    const int t = int(n / p.nx);
+    y = t % int(p.ny);
+    z = t / int(p.ny);
+    sm = (p.parity != 0u && c.solid_mask) ? c.solid_mask[n] : 0u;
+    lm = (p.parity != 0u && c.lid_mask) ? c.lid_mask[n] : 0u;
+}
+
+inline bool in_box(const Ctx& c, int x, int y) {
+    return x >= c.box[0] && x <= c.box[1] && y >= c.box[2] && y <= c.box[3];
+}
+
+// One forward step of A in place in arithmetic R, each stored value rounded to
+// S; contrib[n] = dir . a of the cells whose force counts (0 elsewhere).
+template <class R, class S>
+void step(const Params& p, const Ctx& c, double* A, double* contrib) {
+    const long long N = (long long)c.N;
+#pragma omp parallel for schedule(static) num_threads(c.threads > 0 ? c.threads : 1) if (c.threads > 1)
+    for (long long nn = 0; nn < N; ++nn) {
+        const size_t n = size_t(nn);
+        contrib[n] = 0.0;
+        if (c.flags && c.flags[n] != FLUID) continue;
+        int x, y, z;
+        uint32_t sm, lm;
+        cell_ctx(p, c, n, x, y, z, sm, lm);
+        CellSlots cs;
+        cell_slots(p, sm, c.N, n, x, y, z, cs);
+        R in[19], out[19], a[3], F[3];
+        for (int i = 0; i < 19; ++i) in[i] = R(A[cs.rd[i]]);
+        cell_force<R>(p, c.ffield, c.N, n, F);
+        const R e = (p.useEps && c.eps) ? R(c.eps[n]) : R(0);
+        bool fo = false;
+        cell_compute<R>(p, c.flags, sm, lm, x, y, z, in, e, F, out, a, fo);
+        for (int i = 0; i < 19; ++i) A[cs.wr[i]] = double(S(out[i]));
+        if (p.parity && fo && in_box(c, x, y))
+            contrib[n] = c.dir[0] * double(a[0]) + c.dir[1] * double(a[1]) +
+                         c.dir[2] * double(a[2]);
+    }
+}
+
+inline void step_traj(int traj, const Params& p, const Ctx& c, double* A, double* contrib) {
+    if (traj == 0) step<float, float>(p, c, A, contrib);
+    else if (traj == 1) step<float, _Float16>(p, c, A, contrib);
+    else step<double, double>(p, c, A, contrib);
+}
+
+// Reverse of one step about its input state S: lam (the adjoint of the state
+// after the step) becomes the adjoint of the state before it; the parameter
+// adjoints are accumulated.
+void reverse(const Params& p, const Ctx& c, const double* S, double* lam, double w,
+             double* grad_eps, double* grad_f) {
+    typedef Dual<23> D;
+    const long long N = (long long)c.N;
+#pragma omp parallel for schedule(static) num_threads(c.threads > 0 ? c.threads : 1) if (c.threads > 1)
+    for (long long nn = 0; nn < N; ++nn) {
+        const size_t n = size_t(nn);
+        if (c.flags && c.flags[n] != FLUID) continue;
+        int x, y, z;
+        uint32_t sm, lm;
+        cell_ctx(p, c, n, x, y, z, sm, lm);
+        CellSlots cs;
+        cell_slots(p, sm, c.N, n, x, y, z, cs);
+        D in[19], out[19], a[3], F[3];
+        for (int i = 0; i < 19; ++i) in[i] = D::var(S[cs.rd[i]], i);
+        double Fv[3];
+        cell_force<double>(p, c.ffield, c.N, n, Fv);
+        for (int k = 0; k < 3; ++k) F[k] = D::var(Fv[k], 20 + k);
+        const D e = D::var((p.useEps && c.eps) ? double(c.eps[n]) : 0.0, 19);
+        bool fo = false;
+        cell_compute<D>(p, c.flags, sm, lm, x, y, z, in, e, F, out, a, fo);
+        double mu[19];
+        for (int j = 0; j < 19; ++j) mu[j] = lam[cs.wr[j]];
+        const bool obj = p.parity && fo && in_box(c, x, y);
+        double g[23];
+        for (int k = 0; k < 23; ++k) {
+            double acc = 0.0;
+            for (int j = 0; j < 19; ++j) acc += mu[j] * out[j].d[k];
+            if (obj)
+                acc += w * (c.dir[0] * a[0].d[k] + c.dir[1] * a[1].d[k] + c.dir[2] * a[2].d[k]);
+            g[k] = acc;
+        }
+        for (int i = 0; i < 19; ++i) lam[cs.rd[i]] = g[i];
+        if (grad_eps) grad_eps[n] += g[19];
+        if (grad_f)
+            for (int k = 0; k < 3; ++k) grad_f[k * c.N + n] += g[20 + k];
+    }
+}
+
+}  // namespace adj
+
 extern "C" {
 
 // kind: 0 = <float,float>, 1 = <float,_Float16>, 2 = <double,double>;
@@ -916,104 +1023,84 @@ int orc_init_field(int kind, void* f, uint32_t nx, uint32_t ny, uint32_t nz, uin
 }
 
 // FP64 discrete adjoint of the time-averaged momentum-exchange force, by
-// forward-mode automatic differentiation of the restated step (Dual<23>).
+// forward-mode automatic differentiation of the restated step (Dual<23>)
+// for the local Jacobians and a reverse sweep over the steps.
 //   J = (1/K) sum over the K odd steps t of dir . F_box(t),
 // F_box(t) = sum of the per-cell force of the odd pass (the reference's force
 // probe, Kernels.metal:263-353) over cells with box[0] <= x <= box[1],
 // box[2] <= y <= box[3], all z. params: `steps` consecutive 80-byte Params
 // (writeForce is set here on odd steps). f0: initial state, 19*N doubles.
-// Outputs J and, when not null, dJ/d eps (N) and dJ/d F_field (3 planes of N).
-int orc_adjoint_force(const double* f0, const uint8_t* flags, const uint32_t* solid_mask,
-                      const uint32_t* lid_mask, const void* params, int steps, const float* eps,
-                      const float* ffield, const int box[4], const double dir[3], double* J_out,
-                      double* grad_eps, double* grad_f) {
-    if (steps <= 0) return 1;
+//
+// traj selects the forward trajectory the adjoint linearises about:
+//   2  FP64 arithmetic and storage (the FP64 oracle);
+//   0  FP32 arithmetic over FP32 storage, 1  FP32 arithmetic over FP16 storage:
+//      the library's forward step value for value, so the local Jacobians are
+//      taken in FP64 at exactly the stored states the GPU's reverse pass sees
+//      (f0 must then hold values of the storage type).
+// chk: checkpoint interval; the window's states are recomputed segment by
+// segment from checkpoints (0 = one segment). threads: OpenMP threads over cells
+// (the AA pattern gives every slot one reader and one writer, the same cell, in
+// both the forward and the reverse step). Outputs J and, when grad_eps /
+// grad_f are not null, dJ/d eps (N) and dJ/d F_field (3 planes of N); with
+// both null no state is stored.
+
+int orc_adjoint_force_ex(int traj, const double* f0, const uint8_t* flags,
+                         const uint32_t* solid_mask, const uint32_t* lid_mask, const void* params,
+                         int steps, const float* eps, const float* ffield, const int box[4],
+                         const double dir[3], int threads, int chk, double* J_out,
+                         double* grad_eps, double* grad_f) {
+    if (steps <= 0 || traj < 0 || traj > 2) return 1;
     std::vector<Params> P(steps);
     std::memcpy(P.data(), params, sizeof(Params) * steps);
-    const Params& p0 = P[0];
-    const size_t N = size_t(p0.nx) * p0.ny * p0.nz;
+    const size_t N = size_t(P[0].nx) * P[0].ny * P[0].nz;
     int K = 0;
     for (int t = 0; t < steps; ++t) {
         P[t].writeForce = P[t].parity;
         K += P[t].parity ? 1 : 0;
     }
     const double w = K > 0 ? 1.0 / K : 0.0;
-    std::vector<std::vector<double>> states(steps, std::vector<double>(19 * N));
-    std::vector<double> A(f0, f0 + 19 * N);
+    const adj::Ctx c{flags, solid_mask, lid_mask, eps, ffield, box, dir, N, threads};
+    const bool grads = grad_eps || grad_f;
+    if (chk <= 0 || chk > steps) chk = steps;
+    const int nseg = (steps + chk - 1) / chk;
+    std::vector<double> A(f0, f0 + 19 * N), contrib(N);
+    std::vector<std::vector<double>> ckpt(grads ? nseg : 0);
     double J = 0.0;
-    auto cell_ctx = [&](const Params& p, size_t n, int& x, int& y, int& z, uint32_t& sm,
-                        uint32_t& lm) {
-        x = int(n % p.nx);
-        const int t = int(n / p.nx);
-        y = t % int(p.ny);
-        z = t / int(p.ny);
-        sm = (p.parity != 0u && solid_mask) ? solid_mask[n] : 0u;
-        lm = (p.parity != 0u && lid_mask) ? lid_mask[n] : 0u;
-    };
-    auto in_box = [&](int x, int y) {
-        return x >= box[0] && x <= box[1] && y >= box[2] && y <= box[3];
-    };
-    for (int t = 0; t < steps; ++t) {  // forward, every input state kept
-        const Params& p = P[t];
-        states[t] = A;
-        for (size_t n = 0; n < N; ++n) {
-            if (flags && flags[n] != FLUID) continue;
-            int x, y, z;
-            uint32_t sm, lm;
-            cell_ctx(p, n, x, y, z, sm, lm);
-            CellSlots c;
-            cell_slots(p, sm, N, n, x, y, z, c);
-            double in[19], out[19], a[3], F[3];
-            for (int i = 0; i < 19; ++i) in[i] = A[c.rd[i]];
-            cell_force<double>(p, ffield, N, n, F);
-            const double e = (p.useEps && eps) ? double(eps[n]) : 0.0;
-            bool fo = false;
-            cell_compute<double>(p, flags, sm, lm, x, y, z, in, e, F, out, a, fo);
-            for (int i = 0; i < 19; ++i) A[c.wr[i]] = out[i];
-            if (p.parity && fo && in_box(x, y))
-                J += w * (dir[0] * a[0] + dir[1] * a[1] + dir[2] * a[2]);
-        }
+    for (int t = 0; t < steps; ++t) {  // forward; checkpoints at the segment starts
+        if (grads && t % chk == 0) ckpt[t / chk] = A;
+        adj::step_traj(traj, P[t], c, A.data(), contrib.data());
+        double s = 0.0;
+        for (size_t n = 0; n < N; ++n) s += contrib[n];
+        J += w * s;
     }
     *J_out = J;
+    if (!grads) return 0;
     if (grad_eps) std::fill(grad_eps, grad_eps + N, 0.0);
     if (grad_f) std::fill(grad_f, grad_f + 3 * N, 0.0);
     std::vector<double> lam(19 * N, 0.0);
-    typedef Dual<23> D;
-    for (int t = steps - 1; t >= 0; --t) {  // reverse
-        const Params& p = P[t];
-        const std::vector<double>& S = states[t];
-        for (size_t n = 0; n < N; ++n) {
-            if (flags && flags[n] != FLUID) continue;
-            int x, y, z;
-            uint32_t sm, lm;
-            cell_ctx(p, n, x, y, z, sm, lm);
-            CellSlots c;
-            cell_slots(p, sm, N, n, x, y, z, c);
-            D in[19], out[19], a[3], F[3];
-            for (int i = 0; i < 19; ++i) in[i] = D::var(S[c.rd[i]], i);
-            double Fv[3];
-            cell_force<double>(p, ffield, N, n, Fv);
-            for (int k = 0; k < 3; ++k) F[k] = D::var(Fv[k], 20 + k);
-            const D e = D::var((p.useEps && eps) ? double(eps[n]) : 0.0, 19);
-            bool fo = false;
-            cell_compute<D>(p, flags, sm, lm, x, y, z, in, e, F, out, a, fo);
-            double mu[19];
-            for (int j = 0; j < 19; ++j) mu[j] = lam[c.wr[j]];
-            const bool obj = p.parity && fo && in_box(x, y);
-            double g[23];
-            for (int k = 0; k < 23; ++k) {
-                double acc = 0.0;
-                for (int j = 0; j < 19; ++j) acc += mu[j] * out[j].d[k];
-                if (obj) acc += w * (dir[0] * a[0].d[k] + dir[1] * a[1].d[k] + dir[2] * a[2].d[k]);
-                g[k] = acc;
-            }
-            for (int i = 0; i < 19; ++i) lam[c.rd[i]] = g[i];
-            if (grad_eps) grad_eps[n] += g[19];
-            if (grad_f)
-                for (int k = 0; k < 3; ++k) grad_f[k * N + n] += g[20 + k];
+    std::vector<std::vector<double>> seg(chk);
+    for (int s = nseg - 1; s >= 0; --s) {  // reverse, one recomputed segment at a time
+        const int t0 = s * chk, t1 = std::min(steps, t0 + chk);
+        seg[0] = ckpt[s];
+        for (int t = t0 + 1; t < t1; ++t) {
+            seg[t - t0] = seg[t - t0 - 1];
+            adj::step_traj(traj, P[t - 1], c, seg[t - t0].data(), contrib.data());
         }
+        for (int t = t1 - 1; t >= t0; --t)
+            adj::reverse(P[t], c, seg[t - t0].data(), lam.data(), w, grad_eps, grad_f);
+        ckpt[s].clear();
+        ckpt[s].shrink_to_fit();
     }
     return 0;
+}
+
+// The FP64 trajectory, every state kept, one thread.
+int orc_adjoint_force(const double* f0, const uint8_t* flags, const uint32_t* solid_mask,
+                      const uint32_t* lid_mask, const void* params, int steps, const float* eps,
+                      const float* ffield, const int box[4], const double dir[3], double* J_out,
+                      double* grad_eps, double* grad_f) {
+    return orc_adjoint_force_ex(2, f0, flags, solid_mask, lid_mask, params, steps, eps, ffield,
+                                box, dir, 1, 0, J_out, grad_eps, grad_f);
 }
 
 // Noble-Torczynski solid fractions of a closed triangle mesh by parity ray

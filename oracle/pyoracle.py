@@ -61,6 +61,8 @@ def lib():
                                      ctypes.c_float]
         L.orc_adjoint_force.argtypes = [_P, _P, _P, _P, _P, ctypes.c_int, _P, _P, _P, _P, _P, _P,
                                         _P]
+        L.orc_adjoint_force_ex.argtypes = ([ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_int, _P,
+                                            _P, _P, _P, ctypes.c_int, ctypes.c_int, _P, _P, _P])
         L.orc_mass.argtypes = [ctypes.c_int, _P, ctypes.c_size_t]
         L.orc_mesh_solid_fractions.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                ctypes.c_int, ctypes.c_float, _P, _P]
@@ -278,28 +280,42 @@ class OracleSim:
         u2 = (m[:, 0] * m[:, 0] + m[:, 1] * m[:, 1]) + m[:, 2] * m[:, 2]
         return float(np.sum(u2.astype(np.float64)))
 
-    def adjointForce(self, steps, box, direction=(1.0, 0.0, 0.0), grads=True):
+    def adjointForce(self, steps, box, direction=(1.0, 0.0, 0.0), grads=True,
+                     trajectory="fp64", f0=None, threads=None, checkpoint=0):
         """FP64 adjoint of J = mean over the odd steps of direction . F_box.
 
-        Runs the window [stepsDone, stepsDone + steps) from the current state in
-        FP64 (the state itself is not advanced). Returns (J, dJ/deps, dJ/dF) with
+        Runs the window [stepsDone, stepsDone + steps) from the current state
+        (or from `f0`, 19 x N) without advancing it. `trajectory` is the forward
+        the adjoint linearises about: "fp64" (the FP64 oracle), or "fp32" /
+        "fp16" (FP32 arithmetic over FP32 / FP16 storage: the library's own
+        forward, value for value, with the local Jacobians taken in FP64 at the
+        stored states). `checkpoint`: states are recomputed from a checkpoint
+        every that many steps (0 keeps all). Returns (J, dJ/deps, dJ/dF) with
         dJ/dF of shape (3, N); the gradients are None when grads=False."""
-        f0 = np.ascontiguousarray(self.f, dtype=np.float64)
+        traj = {"fp32": 0, "fp16": 1, "fp64": 2}[trajectory]
+        src = self.f if f0 is None else f0
+        f0 = np.ascontiguousarray(src, dtype=np.float64).reshape(19, self.N)
+        if trajectory == "fp16" and not np.array_equal(f0.astype(np.float16).astype(np.float64), f0):
+            raise ValueError("an FP16-storage trajectory starts from FP16 values")
+        if trajectory == "fp32" and not np.array_equal(f0.astype(np.float32).astype(np.float64), f0):
+            raise ValueError("an FP32-storage trajectory starts from FP32 values")
         if self.outflowMode != "dormant" or self.collision != "reference":
             raise ValueError("the oracle adjoint covers the dormant outflow wall and the "
                              "reference collision only")
+        if threads is None:
+            threads = os.cpu_count() or 1
         P = b"".join(self.params(self.stepsDone + t) for t in range(int(steps)))
         box = (ctypes.c_int * 4)(int(box[0][0]), int(box[0][1]), int(box[1][0]), int(box[1][1]))
         d3 = (ctypes.c_double * 3)(*[float(v) for v in direction])
         J = ctypes.c_double()
         ge = np.zeros(self.N) if grads else None
         gf = np.zeros((3, self.N)) if grads else None
-        rc = lib().orc_adjoint_force(_ptr(f0), _ptr(self.flags), _ptr(self.solidMask),
-                                     _ptr(self.lidMask), P, int(steps), _ptr(self.eps),
-                                     _ptr(self.forceField), box, d3, ctypes.byref(J), _ptr(ge),
-                                     _ptr(gf))
+        rc = lib().orc_adjoint_force_ex(traj, _ptr(f0), _ptr(self.flags), _ptr(self.solidMask),
+                                        _ptr(self.lidMask), P, int(steps), _ptr(self.eps),
+                                        _ptr(self.forceField), box, d3, int(threads),
+                                        int(checkpoint), ctypes.byref(J), _ptr(ge), _ptr(gf))
         if rc != 0:
-            raise RuntimeError("orc_adjoint_force failed")
+            raise RuntimeError("orc_adjoint_force_ex failed")
         return J.value, ge, gf
 
     def massSum(self):

@@ -5,7 +5,7 @@
 //
 // Test infrastructure only: the oracle restatement in lbm_oracle.cpp is
 // checked against these entry points value-for-value. Built by
-// oracle/Makefile into oracle/_ref/ (never committed); the kernel source is
+// oracle/build_oracle.py into oracle/_ref/ (never committed); the kernel source is
 // read from the reference tree at build time, not copied.
 #include <metal_stdlib>
 #include <cstddef>

@@ -133,6 +133,7 @@ def lib():
         "stro_sim_check_finite": ([_P, ctypes.POINTER(c_int)], c_int),
         "stro_sim_set_variant": ([_P, ctypes.c_int32], c_int),
         "stro_sim_set_rows_tile": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
+        "stro_sim_set_spin_limit": ([_P, ctypes.c_int64], c_int),
         "stro_sim_set_arithmetic": ([_P, ctypes.c_int32], c_int),
         "stro_sim_set_outflow_mode": ([_P, ctypes.c_int32], c_int),
         "stro_sim_set_collision": ([_P, ctypes.c_int32], c_int),
@@ -620,6 +621,10 @@ class Simulation:
     @rowsTile.setter
     def rowsTile(self, v):
         _check(lib().stro_sim_set_rows_tile(self._h, int(v[0]), int(v[1])))
+
+    def setSpinLimit(self, polls):
+        """Polls per bounded wait of the row-staged variant (0: give up at once)."""
+        _check(lib().stro_sim_set_spin_limit(self._h, int(polls)))
 
     def setBlockSplit(self, enabled):
         """Bulk blocks of a walled lattice on the wall-free kernels (default True)."""

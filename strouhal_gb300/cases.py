@@ -798,8 +798,9 @@ def main(argv=None):
     t0 = time.perf_counter()
     res = CASES[a.name](gpu, **kw)
     res["case"] = a.name
-    res["command"] = "python -m strouhal_gb300.cases " + " ".join(argv if argv is not None
-                                                                 else __import__("sys").argv[1:])
+    # the case and its overrides; where the output went is not part of the workload
+    res["command"] = " ".join(["python -m strouhal_gb300.cases", a.name] +
+                              ["--set " + item for item in a.set])
     res["elapsed_seconds"] = time.perf_counter() - t0
     text = json.dumps(res)
     if a.out:

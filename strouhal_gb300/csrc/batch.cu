@@ -1004,6 +1004,12 @@ int stro_sim_get_rows_tile(stro_sim* s, int32_t* threads, int32_t* rows) {
     return STRO_OK;
 }
 
+int stro_sim_set_spin_limit(stro_sim* s, int64_t polls) {
+    if (!s || polls < 0) return fail(STRO_ERR_INVALID, "bad spin limit");
+    s->rows_polls = polls;
+    return STRO_OK;
+}
+
 int stro_sim_get_variant(stro_sim* s, int32_t* variant) {
     if (!s || !variant) return fail(STRO_ERR_INVALID, "null argument");
     *variant = s->variant;

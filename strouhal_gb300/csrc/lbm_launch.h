@@ -37,12 +37,13 @@ struct StepLaunchers {
 // Row-staged step (lbm_rows.cu): tiles of `rows` whole lattice rows move
 // through shared memory by bulk loads and bulk stores, `threads` computing
 // threads per block plus one copy warp, persistent over tiles. `error`
-// receives 1 if a bounded wait gave up.
+// receives 1 if a bounded wait gave up; `polls` bounds every wait (0: give up
+// at the first one).
 struct RowsLaunchers {
     bool (*supported)(int half_storage, int geo, bool probe, int nx, int ny, int threads,
                       int rows);
     cudaError_t (*launch)(const StepArgs& a, int half_storage, int parity, int feat, int threads,
-                          int rows, int sm_count, int* error, cudaStream_t st);
+                          int rows, int sm_count, int* error, long long polls, cudaStream_t st);
 };
 
 // FP16 periodic step with x-adjacent cell pairs per thread (lbm_pair.cu).
@@ -78,6 +79,9 @@ struct FieldView {
 };
 
 // Number of blocks the fixed-order reductions use for N cells (depends on N only).
+// Blocks of a fixed-order FP64 reduction over `count` items: one per 1,024,
+// at most kReductionMaxBlocks (which sizes every partials buffer).
+constexpr int kReductionMaxBlocks = 2048;
 int reduction_blocks(uint64_t count);
 
 cudaError_t launch_init_field(const FieldView& v, int half_storage, uint32_t mode,

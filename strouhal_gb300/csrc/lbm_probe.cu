@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(kThreads) k_fold(const double* partials, int n
 int reduction_blocks(uint64_t count) {
     uint64_t b = (count + 1023) / 1024;
     if (b < 1) b = 1;
-    if (b > 2048) b = 2048;
+    if (b > uint64_t(kReductionMaxBlocks)) b = kReductionMaxBlocks;
     return int(b);
 }
 
@@ -341,7 +341,10 @@ cudaError_t launch_nonfinite(const FieldView& v, int half_storage, double* parti
 
 namespace {
 
-constexpr int kNoAllocMaxBlocks = 2048;  // = the most blocks reduction_blocks() ever uses
+// The most blocks reduction_blocks() ever uses, so every lattice it accepts fits.
+constexpr int kNoAllocMaxBlocks = stro::kReductionMaxBlocks;
+static_assert(kNoAllocMaxBlocks * 2 * sizeof(double) <= 32 * 1024,
+              "the allocation-free scratch array is stated as 32 KB");
 static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxBlocks * 2];  // 32 KB
 
 constexpr int kNoAllocMaxDevices = 64;
@@ -381,6 +384,8 @@ extern "C" int stro_observables_noalloc(const void* f, int32_t precision, int32_
     const uint64_t N = uint64_t(nx) * uint64_t(ny) * uint64_t(nz);
     if (N >= (1ull << 31)) return fail(STRO_ERR_INVALID, "lattice too large (N must be < 2^31 cells)");
     if (plane_stride < N) return fail(STRO_ERR_INVALID, "plane stride must be at least nx*ny*nz");
+    if (!(omega > 0.0f && omega < 2.0f))  // also refuses NaN
+        return fail(STRO_ERR_INVALID, "omega must be finite and in (0, 2)");
     const int nb = stro::reduction_blocks(N);
     if (nb > kNoAllocMaxBlocks)
         return fail(STRO_ERR_INVALID, "reduction needs more partials than the scratch array holds");

@@ -220,7 +220,7 @@ constexpr int kMaxConsumers = 256;
 // NXC: compile-time row length (0 = a.nx at run time). blockDim.x = 32 + consumers.
 template <typename S, int PARITY, int FEAT, int NXC>
 __global__ void __launch_bounds__(kMaxConsumers + 32, FEAT == 2 ? 2 : 3)
-    k_rows(const StepArgs a, uint32_t R, uint32_t nstage, int* error) {
+    k_rows(const StepArgs a, uint32_t R, uint32_t nstage, int* error, long long limit) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const uint32_t nx = NXC ? uint32_t(NXC) : uint32_t(a.nx);
     const uint32_t tiles_y = uint32_t(a.ny) / R;
@@ -234,7 +234,11 @@ __global__ void __launch_bounds__(kMaxConsumers + 32, FEAT == 2 ? 2 : 3)
         return reinterpret_cast<S*>(smem_raw + 256 + size_t(s) * stage_bytes);
     };
     const uint32_t consumers = blockDim.x - 32;
-    const long long limit = 1ll << 22;  // polls per wait (a copy completes in microseconds)
+    // limit: polls per wait on a copy or on the consumers (a copy completes in
+    // microseconds); 0 gives up at the first wait. Loads still in flight after a
+    // timeout are drained with a fixed limit of their own, so no copy lands in
+    // the shared memory of a block that has returned.
+    const long long drain_limit = 1ll << 22;
     // this block's tiles: blockIdx.x + q * gridDim.x, q < my
     const uint32_t my = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
@@ -274,7 +278,7 @@ __global__ void __launch_bounds__(kMaxConsumers + 32, FEAT == 2 ? 2 : 3)
             atomicExch(error, 1);
             // loads still in flight: tiles q .. issued-1
             for (uint32_t t = q; t < issued; ++t)
-                mbar_wait_bounded(&full[t % nstage], (t / nstage) & 1u, limit);
+                mbar_wait_bounded(&full[t % nstage], (t / nstage) & 1u, drain_limit);
         }
         bulk_wait_all();
         return;
@@ -385,7 +389,8 @@ int rows_blocks_per_sm(const void* fn, int threads, size_t smem, cudaError_t* er
 }
 
 cudaError_t launch_rows_step(const StepArgs& a, int half_storage, int parity, int feat,
-                             int threads, int rows, int sm_count, int* error, cudaStream_t st) {
+                             int threads, int rows, int sm_count, int* error, long long polls,
+                             cudaStream_t st) {
     const void* fn = half_storage ? pick<__half>(parity, feat, a.nx) : pick<float>(parity, feat, a.nx);
     const size_t smem = half_storage ? rows_smem<__half>(a.nx, rows) : rows_smem<float>(a.nx, rows);
     uint32_t nstage = half_storage ? stages_for<__half>(a.nx, rows) : stages_for<float>(a.nx, rows);
@@ -402,7 +407,7 @@ cudaError_t launch_rows_step(const StepArgs& a, int half_storage, int parity, in
     cfg.blockDim = dim3(threads + 32, 1, 1);  // producer warp + consumers
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
-    void* args[] = {const_cast<StepArgs*>(&a), &R, &nstage, &error};
+    void* args[] = {const_cast<StepArgs*>(&a), &R, &nstage, &error, &polls};
     return cudaLaunchKernelExC(&cfg, fn, args);
 }
 

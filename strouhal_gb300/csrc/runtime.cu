@@ -346,7 +346,7 @@ cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool prob
         R.supported(half, geo, probe, s->nx, s->ny, s->rows_threads, s->rows_per_tile)) {
         s->last_path = "rows";
         return R.launch(a, half, int(t & 1), feat_on(s), s->rows_threads, s->rows_per_tile,
-                        s->ctx->sm_count, s->d_error, sim_stream(s));
+                        s->ctx->sm_count, s->d_error, s->rows_polls, sim_stream(s));
     }
     s->last_path = probe ? "probe" : "cell";
     return L.step(a, half, int(t & 1), geo, feat_on(s), probe, probe ? s->probe_block : s->block,
@@ -390,7 +390,8 @@ std::vector<uint8_t> graph_key(const stro_sim* s, int64_t t, int64_t G) {
                            bulk_feat(s), int64_t(reinterpret_cast<uintptr_t>(s->d_blocks)),
                            s->nbulk, s->nedge, int64_t(s->lists_version),
                            int64_t(s->geo_version), s->lists_block.x, s->lists_block.y,
-                           int64_t(reinterpret_cast<uintptr_t>(s->d_error)), s->ctx->sm_count,
+                           int64_t(reinterpret_cast<uintptr_t>(s->d_error)), s->rows_polls,
+                           s->ctx->sm_count,
                            int64_t(reinterpret_cast<uintptr_t>(sim_stream(s)))};
     put_bytes(k, cfg);
     return k;

@@ -79,6 +79,7 @@ struct stro_sim {
     int outflow = 0;              // STRO_OUTFLOW_DORMANT or STRO_OUTFLOW_PRESSURE
     int collision = 0;            // STRO_COLLISION_REFERENCE or STRO_COLLISION_KBC
     int* d_error = nullptr;       // device error word of the row-streaming variant
+    int64_t rows_polls = 1ll << 22;  // polls per bounded wait of the row-staged variant
     // bulk / boundary block lists of a walled lattice for the current block shape
     bool split = true;
     uint32_t* d_blocks = nullptr;  // bulk blocks first, then edge blocks

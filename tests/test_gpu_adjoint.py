@@ -35,10 +35,12 @@ def _setup(sg, po, gpu, precision, seed=0):
     eps = np.tile(sg.diskSolidFractions(NX, NY, 10.5, 8.5, 3.5), NZ)
     g.setSolidFractions(eps)
     o.setSolidFractions(eps)
-    ff = np.zeros((3, NX * NY * NZ), np.float32)
+    rng = np.random.default_rng(seed)
+    # a nonzero per-cell Guo force field, some cells without a field force
+    ff = (rng.standard_normal((3, NX * NY * NZ)) * 5e-6).astype(np.float32)
+    ff[:, rng.random(NX * NY * NZ) < 0.3] = 0.0
     g.setForceField(ff)
     o.setForceField(ff)
-    rng = np.random.default_rng(seed)
     dt = np.float32 if precision == "fp32" else np.float16
     f0 = (rng.standard_normal((19, NX * NY * NZ)) * 2e-3).astype(dt)
     f0[:, fl != 0] = 0
@@ -66,6 +68,14 @@ def test_adjoint_matches_fp64_oracle(gpu, oracle, steps, checkpoints):
     assert np.all(ge[~nt] == 0)
     assert _rel(gf, gfo) < 1e-3
     assert g.stepsDone == steps
+    # the forward with the field present ran the reference arithmetic
+    o2 = oracle.OracleSim(NX, NY, NZ, flags=_flags(oracle), kind=oracle.KIND_F32, **KW)
+    o2.sponge = (22.0, 8.0, 0.9)
+    o2.setSolidFractions(eps)
+    o2.setForceField(o.forceField)
+    o2.f[:] = o.f.astype(np.float32)
+    o2.run(steps)
+    assert np.array_equal(g.downloadState(), o2.f)
     st = adj.stats()
     assert st["adjoint_steps"] == steps and st["adjoint_s"] > 0
     adj.close()
@@ -97,13 +107,14 @@ def test_adjoint_agrees_with_finite_differences(gpu, oracle):
     scale_f = np.abs(gf).max()
     for n, k in [(6 * NX + 8, 0), (9 * NX + 14 + NX * NY, 1), (4 * NX + 20, 0)]:
         f = ff.copy()
-        f[k, n] += h
+        f[k, n] = np.float32(ff[k, n] + h)
         o.setForceField(f)
         Jp, _, _ = o.adjointForce(steps, BOX, grads=False)
-        f[k, n] -= 2 * h
+        f[k, n] = np.float32(ff[k, n] - h)
         o.setForceField(f)
         Jm, _, _ = o.adjointForce(steps, BOX, grads=False)
-        fd = (Jp - Jm) / (2 * h)
+        h2 = float(np.float32(ff[k, n] + h)) - float(np.float32(ff[k, n] - h))
+        fd = (Jp - Jm) / h2
         assert abs(gf[k, n] - fd) <= 1e-3 * max(abs(fd), 1e-2 * scale_f), (n, k, gf[k, n], fd)
     adj.close()
 

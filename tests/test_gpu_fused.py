@@ -18,7 +18,8 @@ PREC = {0: "fp32", 1: "fp16s"}
 @pytest.mark.parametrize("geometry", ["periodic", "channel"])
 @pytest.mark.parametrize("split", [True, False])
 @pytest.mark.parametrize("collision", ["trt", "srt"])
-def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split, collision):
+@pytest.mark.parametrize("ffield", [False, True])
+def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split, collision, ffield):
     import strouhal_gb300 as sg
 
     po = oracle
@@ -45,6 +46,11 @@ def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split, col
     if eps is not None:
         g.setSolidFractions(eps)
         o.setSolidFractions(eps)
+    if ffield:  # per-cell Guo force field, some cells without a field force
+        ff = (rng.standard_normal((3, nx * ny * nz)) * 2e-5).astype(np.float32)
+        ff[:, rng.random(nx * ny * nz) < 0.3] = 0.0
+        g.setForceField(ff)
+        o.setForceField(ff)
     g.setBlockSplit(split)
     g.block = (32, 4)
     f0 = (rng.standard_normal((19, nx * ny * nz)) * 0.01).astype(o.f.dtype)
@@ -65,7 +71,7 @@ def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split, col
 @pytest.mark.parametrize("variant,shape", [(0, (64, 2)), (2, (128, 1)), (2, (256, 2)),
                                            (3, (32, 4)), (1, None)])
 @pytest.mark.parametrize("kind", [0, 1])
-@pytest.mark.parametrize("feature", ["plain", "force_les_sponge"])
+@pytest.mark.parametrize("feature", ["plain", "force_les_sponge", "ffield"])
 @pytest.mark.parametrize("srt", [False, True])
 def test_fused_variants_match_fused_oracle(gpu, oracle, variant, shape, kind, feature, srt):
     """Periodic lattice: every variant in the fused arithmetic (variant 1, the
@@ -75,11 +81,11 @@ def test_fused_variants_match_fused_oracle(gpu, oracle, variant, shape, kind, fe
     po = oracle
     nx, ny, nz = 64, 6, 5
     kw = dict(omega=1.7, omegaMinus=1.7 if srt else 1.3)
-    if feature != "plain":
+    if feature == "force_les_sponge":
         kw.update(force=(2e-5, -3e-5, 1e-5), cSmago=0.01)
     g = sg.Simulation(gpu, precision=PREC[kind], nx=nx, ny=ny, nz=nz, arithmetic="fused", **kw)
     o = po.OracleSim(nx, ny, nz, kind=kind, arithmetic="fused", **kw)
-    if feature != "plain":
+    if feature == "force_les_sponge":
         g.sponge = o.sponge = (nx * 0.6, nx * 0.3, 0.9)
     g.variant = variant
     if variant == 2:
@@ -87,6 +93,11 @@ def test_fused_variants_match_fused_oracle(gpu, oracle, variant, shape, kind, fe
     elif shape is not None:
         g.block = shape
     rng = np.random.default_rng(nx + variant + 10 * kind)
+    if feature == "ffield":  # per-cell Guo force field, some cells without a field force
+        ff = (rng.standard_normal((3, nx * ny * nz)) * 2e-5).astype(np.float32)
+        ff[:, rng.random(nx * ny * nz) < 0.3] = 0.0
+        g.setForceField(ff)
+        o.setForceField(ff)
     f0 = (rng.standard_normal((19, nx * ny * nz)) * 0.01).astype(o.f.dtype)
     g.uploadState(f0)
     o.f[:] = f0

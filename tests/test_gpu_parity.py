@@ -78,7 +78,18 @@ FEATURES = {
     "sponge": dict(sponge=(14.0, 8.0, 0.85)),
     "eps": dict(eps=True),
     "all": dict(force=(3e-5, -1e-5, 2e-5), cSmago=0.01, sponge=(14.0, 8.0, 0.85), eps=True),
+    # per-cell Guo force field (the library's extension), some cells without a field force
+    "ffield": dict(ffield=True),
+    "ffield_all": dict(force=(3e-5, -1e-5, 2e-5), cSmago=0.01, sponge=(14.0, 8.0, 0.85),
+                       eps=True, ffield=True),
 }
+
+
+def random_force_field(rng, N, scale=2e-5, zero_frac=0.3):
+    """A nonzero per-cell force field (3, N) with a fraction of all-zero cells."""
+    ff = (rng.standard_normal((3, N)) * scale).astype(np.float32)
+    ff[:, rng.random(N) < zero_frac] = 0.0
+    return ff
 
 
 @pytest.mark.parametrize("kind", [0, 1])
@@ -106,10 +117,15 @@ def test_step_matches_oracle(gpu, oracle, kind, geometry, feature):
         eps = np.zeros(nx * ny * nz, np.float32)
         idx = rng.choice(nx * ny * nz, 120, replace=False)
         eps[idx] = rng.uniform(0.02, 0.98, idx.size).astype(np.float32)
+    ffield = opts.pop("ffield", False)
     g, o = _mk_pair(sg, po, gpu, kind, nx, ny, nz,
                     flags=None if flags is None else flags.reshape(-1), eps=eps,
                     omega=1.55, omegaMinus=1.2, lid=(0.07, 0.0, 0.01), uin=0.05, rampSteps=7,
                     wantsForces=True, **opts)
+    if ffield:
+        ff = random_force_field(rng, nx * ny * nz)
+        g.setForceField(ff)
+        o.setForceField(ff)
     f0 = (rng.standard_normal((19, nx * ny * nz)) * 0.01).astype(o.f.dtype)
     o.f[:] = f0
     g.uploadState(f0)

@@ -28,7 +28,7 @@ PATHS = {0: "cell", 1: "pair", 2: "rows", 3: "capped"}
 
 
 @pytest.mark.parametrize("variant,precision,nx,ny,nz,shape", VARIANT_CASES)
-@pytest.mark.parametrize("feature", ["plain", "force", "les", "sponge"])
+@pytest.mark.parametrize("feature", ["plain", "force", "les", "sponge", "ffield"])
 def test_variant_matches_oracle(gpu, oracle, variant, precision, nx, ny, nz, shape, feature):
     import strouhal_gb300 as sg
 
@@ -52,6 +52,12 @@ def test_variant_matches_oracle(gpu, oracle, variant, precision, nx, ny, nz, sha
     elif shape is not None:
         g.block = shape
     rng = np.random.default_rng(nx * 31 + ny + variant)
+    if feature == "ffield":  # per-cell Guo force field with zero-force cells, on top of a uniform one
+        ff = (rng.standard_normal((3, nx * ny * nz)) * 2e-5).astype(np.float32)
+        ff[:, rng.random(nx * ny * nz) < 0.3] = 0.0
+        g.force = o.force = (1e-5, 0.0, -1e-5)
+        g.setForceField(ff)
+        o.setForceField(ff)
     f0 = (rng.standard_normal((19, nx * ny * nz)) * 0.01).astype(o.f.dtype)
     g.uploadState(f0)
     o.f[:] = f0
@@ -111,8 +117,17 @@ def test_block_split_is_bitwise_neutral(gpu, precision):
     assert digests[0] == digests[1]
 
 
+def _field(n_cells, seed):
+    """A per-cell Guo force field with some zero-force cells."""
+    rng = np.random.default_rng(seed)
+    ff = (rng.standard_normal((3, n_cells)) * 2e-6).astype(np.float32)
+    ff[:, rng.random(n_cells) < 0.3] = 0.0
+    return ff
+
+
 def _ladder(sg, gpu, precision="fp32"):
-    """Uneven periodic TGV boxes plus a ramped cavity and a channel with NT cells."""
+    """Uneven periodic TGV boxes (one with a per-cell force field) plus a ramped
+    cavity and a channel with NT cells and a force field."""
     sims, steps, logs = [], [], []
     for n, u0, nsteps, le in [(32, 0.05, 40, 10), (48, 0.025, 62, 0), (16, 0.05, 12, 4),
                               (64, 0.05, 26, 2)]:
@@ -120,6 +135,8 @@ def _ladder(sg, gpu, precision="fp32"):
         tau = 3 * u0 * L / 1600 + 0.5
         s = sg.Simulation(gpu, precision=precision, nx=n, ny=n, nz=n, omega=1 / tau)
         s.initField(2, u0)
+        if n == 32:
+            s.setForceField(_field(n ** 3, 3))
         sims.append(s)
         steps.append(nsteps)
         logs.append(le)
@@ -145,6 +162,7 @@ def _ladder(sg, gpu, precision="fp32"):
                       flags=ch.reshape(-1))
     eps = sg.diskSolidFractions(50, 20, 15.5, 9.5, 4.0)
     d.setSolidFractions(np.tile(eps, 4))
+    d.setForceField(_field(50 * 20 * 4, 4))
     d.sponge = (35.0, 10.0, 0.9)
     sims.append(d)
     steps.append(33)
@@ -207,6 +225,43 @@ def test_batch_barrier_timeout_is_an_error_status(gpu):
     s.initField(2, 0.05)
     s.run(4)
     assert s.checkFinite()
+
+
+@pytest.mark.parametrize("precision", ["fp16s", "fp32"])
+def test_rows_wait_timeout_is_an_error_status(gpu, oracle, precision):
+    """Variant 2 with a zero poll limit: its first bulk-copy wait gives up, the
+    block drains its copies in flight and returns, the run fails with
+    STRO_ERR_TIMEOUT, and the context and the lattice stay usable."""
+    import strouhal_gb300 as sg
+
+    po = oracle
+    nx, ny, nz = 256, 8, 6
+    s = sg.Simulation(gpu, precision=precision, nx=nx, ny=ny, nz=nz, omega=1.7)
+    s.variant = 2
+    s.rowsTile = (256, 1)
+    s.initField(2, 0.05)
+    f0 = s.downloadState()
+    s.setSpinLimit(0)
+    with pytest.raises(sg.StrouhalError) as ei:
+        s.run(2)
+    assert ei.value.code == 6
+    assert s.lastPath == "rows"
+    # back to the default limit: the same lattice steps correctly again
+    s.setSpinLimit(1 << 22)
+    s.uploadState(f0)
+    s.stepsDone = 0
+    s.run(3)
+    o = po.OracleSim(nx, ny, nz, omega=1.7, kind=po.KIND_F16 if precision == "fp16s" else po.KIND_F32)
+    o.f[:] = f0
+    o.run(3)
+    assert np.array_equal(s.downloadState(), o.f)
+    s.close()
+    with pytest.raises(sg.StrouhalError):
+        s2 = sg.Simulation(gpu, nx=8, ny=8, nz=8, omega=1.5)
+        try:
+            s2.setSpinLimit(-1)
+        finally:
+            s2.close()
 
 
 def test_autotune_restores_state(gpu):

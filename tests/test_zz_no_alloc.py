@@ -57,9 +57,59 @@ def test_noalloc_observables_match_allocating_entry_point(precision):
         ke, diss = out.cpu().numpy()
         assert np.isclose(ke, sim.kineticEnergySum(), rtol=1e-12, atol=0), (call, ke)
         assert np.isclose(diss, sim.dissipationSum(), rtol=1e-12, atol=0), (call, diss)
-    # sizes beyond what the entry point accepts are refused, not attempted
-    rc = fn(state.data_ptr(), prec, 2048, 2048, 1024, 1 << 33, None, omega, None,
+    # the same state in planes padded past N (a caller's own aligned layout)
+    N = nx * ny * nz
+    stride = N + 96
+    padded = torch.full((19, stride), float("nan"), dtype=state.dtype, device="cuda")
+    padded[:, :N] = state
+    out.fill_(-1.0)
+    rc = fn(padded.data_ptr(), prec, nx, ny, nz, stride, cells.data_ptr(), omega, f3,
             out.data_ptr(), None)
-    assert rc == 1
+    assert rc == 0, sg.lib().stro_last_error()
+    torch.cuda.synchronize()
+    ke, diss = out.cpu().numpy()
+    assert np.isclose(ke, sim.kineticEnergySum(), rtol=1e-12, atol=0), ke
+    assert np.isclose(diss, sim.dissipationSum(), rtol=1e-12, atol=0), diss
+    # refusals: sizes beyond what the entry point accepts, a plane stride below N,
+    # a missing state or output pointer, and omega outside (0, 2) or NaN
+    bad = [
+        (state.data_ptr(), 2048, 2048, 1024, 1 << 33, omega, out.data_ptr()),
+        (state.data_ptr(), nx, ny, nz, N - 1, omega, out.data_ptr()),
+        (None, nx, ny, nz, N, omega, out.data_ptr()),
+        (state.data_ptr(), nx, ny, nz, N, omega, None),
+        (state.data_ptr(), nx, ny, nz, N, 0.0, out.data_ptr()),
+        (state.data_ptr(), nx, ny, nz, N, 2.5, out.data_ptr()),
+        (state.data_ptr(), nx, ny, nz, N, float("nan"), out.data_ptr()),
+    ]
+    for ptr, a, b, c, st, om, o in bad:
+        assert fn(ptr, prec, a, b, c, st, None, om, None, o, None) == 1, (a, b, c, st, om)
+    sim.close()
+    gpu.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16s"])
+def test_noalloc_observables_all_fluid_without_cell_types(precision):
+    """A periodic lattice: no cell-type array (NULL = every cell fluid)."""
+    torch = pytest.importorskip("torch")
+    import strouhal_gb300 as sg
+
+    fn = _entry(sg)
+    gpu = sg.GPU(0)
+    nx, ny, nz = 32, 24, 20
+    omega = 1.9
+    sim = sg.Simulation(gpu, precision=precision, nx=nx, ny=ny, nz=nz, omega=omega)
+    sim.initField(2, 0.05)
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    prec = 0 if precision == "fp32" else 1
+    for call in range(2):
+        sim.run(4)
+        state = torch.from_numpy(sim.downloadState()).cuda()
+        rc = fn(state.data_ptr(), prec, nx, ny, nz, nx * ny * nz, None, omega, None,
+                out.data_ptr(), None)
+        assert rc == 0, sg.lib().stro_last_error()
+        torch.cuda.synchronize()
+        ke, diss = out.cpu().numpy()
+        assert np.isclose(ke, sim.kineticEnergySum(), rtol=1e-12, atol=0), (call, ke)
+        assert np.isclose(diss, sim.dissipationSum(), rtol=1e-12, atol=0), (call, diss)
     sim.close()
     gpu.close()
