@@ -19,6 +19,16 @@ e2e   : the same metric over the whole job through the C ABI with host
 Inputs are larger than L2 (the 256^3 state is 637 MB / 1.27 GB), so no L2
 flush is needed between steps.
 
+variants.c4_batched : the batched credibility ladder (32 periodic TGV instances,
+        edges drawn from {32..160}, 5 convective times each, FP32 SRT): wall
+        time of the sequential per-rung launches against the streams, rounds
+        (CUDA graph of batched rounds) and persistent (one cooperative kernel)
+        modes, states bitwise compared.
+variants.c3_adjoint / c5_adjoint : device time of the discrete adjoint's
+        backward sweep (recomputation included) over its forward window on the
+        full cylinder (1410x264x3, 10,000-step window, 20 checkpoints) and
+        sphere-wake (512x256x256, 2,000-step window, 45 checkpoints) lattices.
+
 --impl reference times the CPU restatement of the reference arithmetic (the
 oracle, OpenMP over all host cores) on the same workload, one bench step = one
 even+odd pair of lattice steps over the full 256^3 lattice.
@@ -238,6 +248,49 @@ class _Null:
         return False
 
 
+def run_c4_ladder(gpu, t_star=5.0, tune_rounds=10):
+    """The C4 batched ladder in every mode (strouhal_gb300.cases.ladder)."""
+    from strouhal_gb300 import cases
+
+    r = cases.ladder(gpu, t_star=t_star, tune=True, tune_rounds=tune_rounds)
+    modes = ("sequential", "streams", "rounds", "persistent")
+    out = {"workload": "32 periodic TGV instances, edges from {32,48,64,96,128,160} (seed 1234), "
+                       "u0 0.05 / 0.025, FP32 SRT, Re 1600, %g convective times each, KE traces "
+                       "every 0.1 t*" % t_star,
+           "cell_updates": r["cell_updates"],
+           "wall_seconds": {m: r[m]["wall_seconds"] for m in modes},
+           "glups": {m: r[m]["glups"] for m in modes},
+           "speedup_vs_sequential": {m: r[m]["speedup_vs_sequential"] for m in modes[1:]},
+           "identical_states": all(r[m]["identical_states"] for m in modes[1:]),
+           "paths": {m: r[m]["path"] for m in modes}}
+    return out
+
+
+def run_adjoints(gpu):
+    """Backward / forward device time of the discrete adjoint on the C3 and C5 lattices."""
+    from strouhal_gb300 import cases
+
+    out = {}
+    c3 = cases.dfg2_adjoint(gpu, total=36000, window=10000, checkpoints=20, fd_cells=0, tune=True)
+    out["c3_adjoint"] = {
+        "workload": "cylinder D=64, 1410x264x3 FP32 TRT, mean drag over a 10,000-step window "
+                    "after a 26,000-step spin-up, 20 checkpoints, d/d eps",
+        "forward_s": c3["forward_seconds"], "recompute_s": c3["recompute_seconds"],
+        "adjoint_s": c3["adjoint_seconds"],
+        "backward_over_forward": c3["backward_over_forward"],
+        "adjoint_step_over_forward_step": c3["adjoint_step_over_forward_step"]}
+    c5 = cases.sphere_adjoint(gpu, spinup=2000, window=2000, checkpoints=45, tune=True)
+    out["c5_adjoint"] = {
+        "workload": "sphere wake 512x256x256 FP16 SRT + LES + NT, mean drag over a 2,000-step "
+                    "window after a 2,000-step spin-up, 45 checkpoints, d/d force field",
+        "forward_s": c5["forward_seconds"], "recompute_s": c5["recompute_seconds"],
+        "adjoint_s": c5["adjoint_seconds"],
+        "backward_over_forward": c5["backward_over_forward"],
+        "adjoint_step_over_forward_step": c5["adjoint_step_over_forward_step"],
+        "grad_finite": c5["grad_finite"]}
+    return out
+
+
 def cpu_baseline(precision="fp16s", lam=None, pairs=1, threads=None):
     """Oracle (CPU restatement, OpenMP) on the full 256^3 lattice, `pairs` AA pairs."""
     from oracle import pyoracle as po
@@ -299,6 +352,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="skip the batched-ladder and adjoint workloads (variants.c4_batched, "
+                         "c3_adjoint, c5_adjoint)")
     ap.add_argument("--clocks-csv", default=None,
                     help="keep the nvidia-smi samples of the timed region in this file")
     args = ap.parse_args()
@@ -322,6 +378,10 @@ def main():
     ref16 = run_variant(sg, gpu, "fp16s", None, args.steps, args.warmup, dist)
     trt = run_variant(sg, gpu, "fp32", 3.0 / 16.0, args.steps, args.warmup, dist)
     kbc = run_variant(sg, gpu, "fp16s", None, args.steps, args.warmup, dist, collision="kbc")
+    extra = {}
+    if not args.no_workloads:
+        extra["c4_batched"] = run_c4_ladder(gpu)
+        extra.update(run_adjoints(gpu))
     peak, peak_kind = measured_peak()
     traffic = profile_traffic()
 
@@ -398,6 +458,7 @@ def main():
                           "tuned": head["tuned"]},
         },
     }
+    line["variants"].update(extra)
     print(json.dumps(line))
     return 0
 

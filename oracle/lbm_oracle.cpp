@@ -23,6 +23,9 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 namespace {
 
@@ -744,6 +747,76 @@ void moments_all(const void* fv, const uint8_t* flags, const Params& p, const fl
     }
 }
 
+// Kinetic-energy and dissipation sums of a state, the library's observables
+// reduction restated: per fluid cell |u|^2 (u with the half-force shift, as
+// momentsEven) and 2 nu S:S with S = -(1.5 omega / rho) Pi_neq, Pi_neq the
+// second moment of f - feq (full equilibrium), nu = (1/omega - 1/2)/3. R is
+// the arithmetic of the per-cell values; both sums are accumulated in double,
+// per thread over a static range of cells and then in thread order.
+template <class R, class S>
+void observables_all(const void* fv, const uint8_t* flags, const Params& p, const float* ffield,
+                     double omega, int threads, double out[2]) {
+    const size_t N = size_t(p.nx) * p.ny * p.nz;
+    const S* f = static_cast<const S*>(fv);
+    const double nu = (1.0 / omega - 0.5) / 3.0;
+    const R om = R(omega);
+    const int T = threads > 0 ? threads : 1;
+    std::vector<double> part(2 * size_t(T), 0.0);
+#pragma omp parallel num_threads(T) if (T > 1)
+    {
+        int tid = 0, nt = 1;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+        nt = omp_get_num_threads();
+#endif
+        const size_t lo = N * size_t(tid) / size_t(nt), hi = N * size_t(tid + 1) / size_t(nt);
+        double ke = 0.0, ds = 0.0;
+        for (size_t n = lo; n < hi; ++n) {
+            if (flags && flags[n] != FLUID) continue;
+            R v[19];
+            for (int i = 0; i < 19; ++i) v[i] = R(f[size_t(i) * N + n]);
+            R rhom1 = v[0];
+            for (int i = 1; i < 19; ++i) rhom1 += v[i];
+            R pc[3] = {0, 0, 0};
+            for (int i = 1; i < 19; ++i) {
+                pc[0] += R(CX[i]) * v[i];
+                pc[1] += R(CY[i]) * v[i];
+                pc[2] += R(CZ[i]) * v[i];
+            }
+            R F[3];
+            cell_force<R>(p, ffield, N, n, F);
+            const R rho = R(1) + rhom1;
+            const R ux = (pc[0] + R(0.5) * F[0]) / rho, uy = (pc[1] + R(0.5) * F[1]) / rho,
+                    uz = (pc[2] + R(0.5) * F[2]) / rho;
+            const R u2 = ux * ux + uy * uy + uz * uz;
+            ke += double(u2);
+            R P[6] = {0, 0, 0, 0, 0, 0};
+            for (int i = 1; i < 19; ++i) {
+                const R cu = R(3) * (R(CX[i]) * ux + R(CY[i]) * uy + R(CZ[i]) * uz);
+                const R feq = weight<R>(i) * (rhom1 + rho * (cu + R(0.5) * cu * cu - R(1.5) * u2));
+                const R d = v[i] - feq;
+                P[0] += R(CX[i] * CX[i]) * d;
+                P[1] += R(CY[i] * CY[i]) * d;
+                P[2] += R(CZ[i] * CZ[i]) * d;
+                P[3] += R(CX[i] * CY[i]) * d;
+                P[4] += R(CX[i] * CZ[i]) * d;
+                P[5] += R(CY[i] * CZ[i]) * d;
+            }
+            const R pipi = P[0] * P[0] + P[1] * P[1] + P[2] * P[2] +
+                           R(2) * (P[3] * P[3] + P[4] * P[4] + P[5] * P[5]);
+            const R sc = R(1.5) * om / rho;
+            ds += 2.0 * nu * double(sc * sc * pipi);
+        }
+        part[2 * size_t(tid)] = ke;
+        part[2 * size_t(tid) + 1] = ds;
+    }
+    out[0] = out[1] = 0.0;
+    for (int t = 0; t < T; ++t) {
+        out[0] += part[2 * size_t(t)];
+        out[1] += part[2 * size_t(t) + 1];
+    }
+}
+
 // initField, Kernels.metal:393-453. Trigonometric values are evaluated in
 // double and rounded to R, so FP32 results are the correctly rounded sin/cos.
 template <class R> inline R tsin(R a) { return R(std::sin(double(a))); }
@@ -1008,6 +1081,20 @@ int orc_moments(int kind, const void* f, const uint8_t* flags, const void* param
         case 0: moments_all<float, float>(f, flags, p, ffield, static_cast<float*>(out)); return 0;
         case 1: moments_all<float, _Float16>(f, flags, p, ffield, static_cast<float*>(out)); return 0;
         case 2: moments_all<double, double>(f, flags, p, ffield, static_cast<double*>(out)); return 0;
+    }
+    return 1;
+}
+
+// Kinetic-energy and dissipation sums (observables_all above): out[0] = sum
+// |u|^2, out[1] = sum 2 nu S:S over fluid cells; kinds 0/1/2 as orc_moments.
+int orc_observables(int kind, const void* f, const uint8_t* flags, const void* params,
+                    const float* ffield, double omega, int threads, double* out) {
+    Params p;
+    std::memcpy(&p, params, sizeof p);
+    switch (kind) {
+        case 0: observables_all<float, float>(f, flags, p, ffield, omega, threads, out); return 0;
+        case 1: observables_all<float, _Float16>(f, flags, p, ffield, omega, threads, out); return 0;
+        case 2: observables_all<double, double>(f, flags, p, ffield, omega, threads, out); return 0;
     }
     return 1;
 }

@@ -64,6 +64,8 @@ def lib():
         L.orc_adjoint_force_ex.argtypes = ([ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_int, _P,
                                             _P, _P, _P, ctypes.c_int, ctypes.c_int, _P, _P, _P])
         L.orc_mass.argtypes = [ctypes.c_int, _P, ctypes.c_size_t]
+        L.orc_observables.argtypes = [ctypes.c_int, _P, _P, _P, _P, ctypes.c_double,
+                                      ctypes.c_int, _P]
         L.orc_mesh_solid_fractions.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                ctypes.c_int, ctypes.c_float, _P, _P]
         L.orc_colorize.argtypes = [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -279,6 +281,18 @@ class OracleSim:
             return float(np.sum(m[:, 0] * m[:, 0] + m[:, 1] * m[:, 1] + m[:, 2] * m[:, 2]))
         u2 = (m[:, 0] * m[:, 0] + m[:, 1] * m[:, 1]) + m[:, 2] * m[:, 2]
         return float(np.sum(u2.astype(np.float64)))
+
+    def observables(self):
+        """(sum |u|^2, sum 2 nu S:S) over fluid cells of the current state, in
+        the arithmetic of the oracle's kind, summed in double (the library's
+        kineticEnergySum / dissipationSum restated). Even step counts only."""
+        if self.stepsDone % 2 != 0:
+            raise RuntimeError("observables require an even step count")
+        out = np.zeros(2)
+        lib().orc_observables(self.kind, _ptr(self.f), _ptr(self.flags),
+                              self.params(self.stepsDone), _ptr(self.forceField), self.omega,
+                              int(self.threads), _ptr(out))
+        return float(out[0]), float(out[1])
 
     def adjointForce(self, steps, box, direction=(1.0, 0.0, 0.0), grads=True,
                      trajectory="fp64", f0=None, threads=None, checkpoint=0):

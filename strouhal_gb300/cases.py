@@ -480,11 +480,12 @@ def ladder_instances(count=32, seed=1234, edges=(32, 48, 64, 96, 128, 160),
 
 def ladder(gpu, count=32, seed=1234, precision="fp32",
            modes=("persistent", "rounds", "streams", "sequential"), t_star=5.0, tune=True,
-           edges=(32, 48, 64, 96, 128, 160)):
+           edges=(32, 48, 64, 96, 128, 160), tune_rounds=40):
     """32 periodic TGV instances of uneven size and Mach number, FP32 SRT,
     Re = 1600, 5 convective times each, kinetic-energy traces every 0.1 t*;
     wall time of the batched launch against instance-after-instance.
-    `edges` is the set the lattice edges are drawn from."""
+    `edges` is the set the lattice edges are drawn from; the fused modes'
+    tile shape is autotuned over `tune_rounds` rounds (states restored)."""
     inst = ladder_instances(count, seed, edges=tuple(edges), t_star=t_star)
     results = {"instances": [{"n": n, "u0": u0, "steps": k, "log_every": le}
                              for n, u0, k, le in inst],
@@ -501,7 +502,7 @@ def ladder(gpu, count=32, seed=1234, precision="fp32",
         b = sg.Batch(gpu, sims, mode=mode)
         tuned = None
         if tune and mode not in ("sequential", "streams"):  # those keep each lattice's shape
-            chosen, bx, by, _ = b.autotune(rounds=40)  # tile shape (and mode), states restored
+            chosen, bx, by, _ = b.autotune(rounds=tune_rounds)  # tile shape (and mode), states restored
             b.mode = mode
             tuned = [bx, by]
         t0 = time.perf_counter()

@@ -218,6 +218,9 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
     // walled lattice: bulk blocks take the wall-free reverse step, as the forward split does
     const bool split = geo && s->split && s->geo_host.size() == N;
     if (split) {  // from the geometry as it is now
+        // as the step's block lists: no launch still reads the old buffer, and
+        // the upload is ordered on this stream ahead of the reverse steps
+        STRO_CUDA(cudaStreamSynchronize(st));
         cudaFree(a->d_lists);
         a->d_lists = nullptr;
         std::vector<uint32_t> bulk, edge;
@@ -226,8 +229,9 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
         a->nedge = uint32_t(edge.size());
         bulk.insert(bulk.end(), edge.begin(), edge.end());
         STRO_CUDA(cudaMalloc(&a->d_lists, std::max<size_t>(bulk.size(), 1) * sizeof(uint32_t)));
-        STRO_CUDA(cudaMemcpy(a->d_lists, bulk.data(), bulk.size() * sizeof(uint32_t),
-                             cudaMemcpyHostToDevice));
+        STRO_CUDA(cudaMemcpyAsync(a->d_lists, bulk.data(), bulk.size() * sizeof(uint32_t),
+                                  cudaMemcpyHostToDevice, st));
+        STRO_CUDA(cudaStreamSynchronize(st));
     }
     void* live = s->d_f;  // the forward kernels step the buffer a StepArgs points to
     for (int32_t c = a->ncheck - 1; c >= 0; --c) {

@@ -572,8 +572,10 @@ int tune_sim_shape(stro_sim* s, int64_t steps, int variant, dim3 cand, double* s
     float ms = 0.0f;
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, s->ev0, s->ev1);
     int err = 0;
-    if (e == cudaSuccess && variant == 2)
-        e = cudaMemcpy(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && variant == 2) {
+        e = cudaMemcpyAsync(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
     s->block = saved;
     s->pair_block = saved_pair;
     s->variant = saved_variant;
@@ -582,7 +584,7 @@ int tune_sim_shape(stro_sim* s, int64_t steps, int variant, dim3 cand, double* s
     s->gpu_seconds = g0;
     if (e != cudaSuccess) return cuda_fail(e, "autotune launch");
     if (err != 0) {
-        cudaMemset(s->d_error, 0, sizeof(int));
+        cudaMemsetAsync(s->d_error, 0, sizeof(int), st);
         return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-staged step timed out");
     }
     *seconds = double(ms) * 1e-3;

@@ -474,7 +474,7 @@ __global__ void __launch_bounds__(128) k_adj_list_even(const AdjArgs g, const ui
                                                        uint32_t gx, uint32_t gy) {
     int x, y, z;
     adj_list_block(list, gx, gy, x, y, z);
-    if (x >= g.a.nx || y >= g.a.ny) return;
+    if (x >= g.a.nx || y >= g.a.ny || z >= g.a.nz) return;
     adj_even_cell<S, GEO>(g, x, y, z);
 }
 
@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(128, 4) k_adj_list_odd(const AdjArgs g, const 
                                                          uint32_t gx, uint32_t gy) {
     int x, y, z;
     adj_list_block(list, gx, gy, x, y, z);
-    if (x >= g.a.nx || y >= g.a.ny) return;
+    if (x >= g.a.nx || y >= g.a.ny || z >= g.a.nz) return;
     adj_odd_cell<S, GEO>(g, x, y, z);
 }
 

@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(256) k_list_even(const StepArgs a, const uint3
                                                    uint32_t gx, uint32_t gy) {
     int x, y, z;
     list_block(list, gx, gy, x, y, z);
-    if (x >= a.nx || y >= a.ny) return;
+    if (x >= a.nx || y >= a.ny || z >= a.nz) return;
     even_cell<S, GEO, FEAT, false, false, STRO_ARITH, true>(a, x, y, z);
 }
 
@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(256) k_list_odd(const StepArgs a, const uint32
                                                   uint32_t gx, uint32_t gy) {
     int x, y, z;
     list_block(list, gx, gy, x, y, z);
-    if (x >= a.nx || y >= a.ny) return;
+    if (x >= a.nx || y >= a.ny || z >= a.nz) return;
     double contrib[3];
     odd_cell<S, GEO, FEAT, false, false, STRO_ARITH, true>(a, WallVel(a), x, y, z, contrib);
 }

@@ -250,9 +250,11 @@ int run_steps(stro_sim* s, int64_t steps, int64_t probe_step = -1, const int* bo
 int check_rows_error(stro_sim* s) {
     if (s->variant != 2) return STRO_OK;
     int err = 0;
-    STRO_CUDA(cudaMemcpy(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost));
+    cudaStream_t st = sim_stream(s);
+    STRO_CUDA(cudaMemcpyAsync(&err, s->d_error, sizeof err, cudaMemcpyDeviceToHost, st));
+    STRO_CUDA(cudaStreamSynchronize(st));
     if (err == 0) return STRO_OK;
-    cudaMemset(s->d_error, 0, sizeof(int));
+    cudaMemsetAsync(s->d_error, 0, sizeof(int), st);  // ordered before the next launch
     return fail(STRO_ERR_TIMEOUT, "a bulk-copy wait of the row-staged step timed out");
 }
 
@@ -300,12 +302,22 @@ static int ensure_block_lists(stro_sim* s) {
     const uint64_t nblocks = uint64_t(gx) * gy * uint64_t(s->nz);
     std::vector<uint32_t> bulk, edge;
     block_lists(s, s->block, bulk, edge);
+    // Launches of this lattice still in flight read the old lists: let them
+    // finish before the buffer is released. The new lists go up on the
+    // lattice's own stream, so every launch after this call is ordered behind
+    // the copy. (A plain cudaMemcpy runs on the legacy default stream, which
+    // this non-blocking stream does not wait for, and from pageable memory it
+    // may return before its DMA has landed: a launch could then read a fresh,
+    // uninitialised allocation.)
+    cudaStream_t st = sim_stream(s);
+    STRO_CUDA(cudaStreamSynchronize(st));
     cudaFree(s->d_blocks);
     s->d_blocks = nullptr;
     STRO_CUDA(cudaMalloc(&s->d_blocks, std::max<size_t>(nblocks, 1) * sizeof(uint32_t)));
     bulk.insert(bulk.end(), edge.begin(), edge.end());
-    STRO_CUDA(cudaMemcpy(s->d_blocks, bulk.data(), nblocks * sizeof(uint32_t),
-                         cudaMemcpyHostToDevice));
+    STRO_CUDA(cudaMemcpyAsync(s->d_blocks, bulk.data(), nblocks * sizeof(uint32_t),
+                              cudaMemcpyHostToDevice, st));
+    STRO_CUDA(cudaStreamSynchronize(st));  // `bulk` is released on return
     s->nbulk = uint32_t(nblocks - edge.size());
     s->nedge = uint32_t(edge.size());
     s->lists_block = s->block;

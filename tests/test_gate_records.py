@@ -170,9 +170,15 @@ def test_adjoint_cost_and_gradients():
 
 def test_precision_record():
     r = rec("precision_tgv48")
-    by = {run["precision"]: run["rows"] for run in r["runs"]}
-    assert max(x["ke_rel"] for x in by["fp32"]) < 1e-5
-    assert max(x["ke_rel"] for x in by["fp16s"]) < 5e-3
+    by = {run["precision"]: run for run in r["runs"]}
+
+    def ke(run):
+        if "err" in run:
+            return run["err"]["kinetic_energy"]
+        return max(x["ke_rel"] for x in run["rows"])
+
+    assert ke(by["fp32"]) < 1e-5
+    assert ke(by["fp16s"]) < 5e-3
 
 
 def test_credibility_gates_and_budget_from_the_oracle():

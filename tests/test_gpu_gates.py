@@ -55,42 +55,39 @@ def test_unsteady_run_replays_bitwise(gpu):
     assert a["cd"] == b["cd"] and a["cl"] == b["cl"]
 
 
+# Per-observable error bars against the FP64 oracle (tests/precision_observables.py):
+# FP32 storage / FP16 storage. DDFs: the stated tolerances after N <= 50 steps.
+OBS_BARS = {
+    "fp32": {"kinetic_energy": 1e-5, "dissipation_sum": 1e-4, "eps_dEdt": 1e-4,
+             "drag_coefficient": 1e-5, "lift_coefficient_over_max_cd": 1e-5},
+    "fp16s": {"kinetic_energy": 5e-3, "dissipation_sum": 5e-2, "eps_dEdt": 5e-2,
+              "drag_coefficient": 5e-3, "lift_coefficient_over_max_cd": 5e-3},
+}
+DDF_BARS = {"fp32": 1e-5, "fp16s": 2e-3}
+
+
 def test_precision_per_observable(gpu, oracle):
     """FP16-storage SRT and FP32-storage TRT against the FP64 oracle on a 48^3
-    Taylor-Green box over one convective time: relative error of the kinetic
-    energy and of the DDFs at every 20 steps."""
+    Taylor-Green box over one convective time (kinetic energy, the dissipation
+    reduction, eps = -dE/dt*, the DDFs), and both storages on a D = 10 cylinder
+    channel (drag and lift coefficients of the force probe)."""
+    import precision_observables as pobs
     import strouhal_gb300 as sg
 
-    po = oracle
     n, u0 = 48, 0.05
-    L = n / (2.0 * math.pi)
-    tau = 3.0 * u0 * L / 1600.0 + 0.5
-    steps = int(round(L / u0))
+    steps = int(round(n / (2.0 * math.pi) / u0))
     steps -= steps % 20
-    table = {"n": n, "u0": u0, "tau": tau, "steps": steps, "runs": []}
-    for precision, lam in (("fp16s", None), ("fp32", 3.0 / 16.0)):
-        wp, wm = sg.trtOmegas(tau, lam)
-        g = sg.Simulation(gpu, precision=precision, nx=n, ny=n, nz=n, omega=wp, omegaMinus=wm)
-        o = po.OracleSim(n, n, n, omega=wp, omegaMinus=wm, kind=po.KIND_F64, threads=16)
-        o.initField(2, u0)
-        g.uploadState(o.f.astype(np.float16 if precision == "fp16s" else np.float32))
-        rows = []
-        while True:
-            mo = o.probeMoments()
-            ke_o = float(np.sum(mo[:, 0] ** 2 + mo[:, 1] ** 2 + mo[:, 2] ** 2))
-            ke_g = g.kineticEnergySum()
-            ddf = float(np.linalg.norm(g.downloadState().astype(np.float64) - o.f) /
-                        np.linalg.norm(o.f))
-            rows.append({"step": g.stepsDone, "ke_rel": abs(ke_g - ke_o) / ke_o, "ddf_rel": ddf})
-            if g.stepsDone >= steps:
-                break
-            g.run(20)
-            o.run(20)
-        table["runs"].append({"precision": precision, "rows": rows})
-        g.close()
-        worst_ke = max(r["ke_rel"] for r in rows)
-        if precision == "fp32":
-            assert worst_ke < 1e-5 and rows[2]["ddf_rel"] < 1e-5, rows
-        else:
-            assert worst_ke < 5e-3 and rows[2]["ddf_rel"] < 2e-3, rows
-    _record("precision_tgv48", table)
+    t = pobs.tgv(sg, oracle, gpu, n, steps, 20)
+    for run in t["runs"]:
+        bars = OBS_BARS[run["precision"]]
+        for k in ("kinetic_energy", "dissipation_sum", "eps_dEdt"):
+            assert run["err"][k] < bars[k], (run["precision"], k, run["err"])
+        early = [r for r in run["rows"] if 0 < r["step"] <= 40]
+        assert max(r["ddf_rel"] for r in early) < DDF_BARS[run["precision"]], run["rows"]
+    c = pobs.cylinder(sg, oracle, gpu, 10, 2000, 100)
+    for run in c["runs"]:
+        bars = OBS_BARS[run["precision"]]
+        for k in ("drag_coefficient", "lift_coefficient_over_max_cd"):
+            assert run["err"][k] < bars[k], (run["precision"], k, run["err"])
+    _record("precision_tgv48", t)
+    _record("precision_cylinder_d10", c)
