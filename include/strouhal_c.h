@@ -166,7 +166,10 @@ int stro_sim_get_block(stro_sim* sim, int32_t* bx, int32_t* by);
  * shared memory by bulk loads ahead of the compute and bulk stores after it
  * (periodic lattices, nx*element size a multiple of 16, ny a multiple of the
  * rows per tile); 3 = one cell per thread with registers capped at 64 for
- * more warps in flight (periodic lattices, blocks of at most 128 threads).
+ * more warps in flight (periodic lattices, blocks of at most 128 threads);
+ * 4 / 5 = FP16 storage, 4 / 8 x-adjacent cells per thread with 8- / 16-byte
+ * loads (periodic lattices, nx a multiple of 128 / 256; launch shape from
+ * stro_sim_set_block: bx a multiple of 32 dividing nx/4 or nx/8, by dividing ny).
  * A lattice a variant does not apply to runs variant 0.
  * Results are identical for every variant. */
 int stro_sim_set_variant(stro_sim* sim, int32_t variant);
@@ -208,7 +211,8 @@ int stro_sim_get_outflow_mode(stro_sim* sim, int32_t* mode);
 int stro_sim_set_pair_block(stro_sim* sim, int32_t bx, int32_t by);
 int stro_sim_get_pair_block(stro_sim* sim, int32_t* bx, int32_t* by);
 /* Kernel path of the latest step launch: "cell" (one cell per thread),
- * "split" (bulk / boundary block lists), "pair", "rows", "capped" or "probe";
+ * "split" (bulk / boundary block lists), "pair", "wide4", "wide8", "rows",
+ * "capped" or "probe";
  * "" before the first step. A lattice a variant does not apply to reports the
  * path that ran instead. */
 int stro_sim_last_path(stro_sim* sim, char* buf, size_t len);
@@ -225,8 +229,11 @@ int stro_sim_get_rows_tile(stro_sim* sim, int32_t* threads, int32_t* rows);
 int stro_sim_set_spin_limit(stro_sim* sim, int64_t polls);
 /* Walled lattices run their bulk blocks (cells with no wall neighbour and no
  * solid fraction) with the wall-free kernels and only the boundary blocks
- * with the wall-aware ones (default on); 0 runs the wall-aware kernels on
- * every block. Results are identical either way. */
+ * with the wall-aware ones (1, the default); 2 does the same with the
+ * boundary blocks' odd pass in column-major cell order (a warp covers whole
+ * columns of its block, so a column of cells next to an inflow wall runs the
+ * moving-wall code in warps of its own); 0 runs the wall-aware kernels on
+ * every block. Results are identical in every mode. */
 int stro_sim_set_block_split(stro_sim* sim, int32_t enabled);
 /* stro_sim_run and stro_sim_run_sampled replay CUDA graphs of plain steps once
  * the ramp is over (default on): the launches of a run of steps are captured

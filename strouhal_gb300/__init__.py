@@ -627,8 +627,10 @@ class Simulation:
         _check(lib().stro_sim_set_spin_limit(self._h, int(polls)))
 
     def setBlockSplit(self, enabled):
-        """Bulk blocks of a walled lattice on the wall-free kernels (default True)."""
-        _check(lib().stro_sim_set_block_split(self._h, int(bool(enabled))))
+        """Bulk blocks of a walled lattice on the wall-free kernels (default True);
+        "columns" also orders the boundary blocks' odd pass column by column."""
+        mode = 2 if enabled == "columns" else int(bool(enabled))
+        _check(lib().stro_sim_set_block_split(self._h, mode))
 
     def setGraphs(self, enabled):
         """Replay CUDA graphs of plain steps past the ramp (default True)."""

@@ -623,11 +623,14 @@ def _dfg2_sim(gpu, D, uin_max, nz, precision, ramp, sponge_d=3, sponge_tau=1.0):
 
 
 def dfg2_adjoint(gpu, D=64, uin_max=0.06, nz=3, total=200000, window=10000, checkpoints=20,
-                 fd_cells=8, fd_h=0.02, seed=7, precision="fp32", ramp=24000, tune=False):
+                 fd_cells=8, fd_h=0.02, seed=7, precision="fp32", ramp=24000, tune=False,
+                 fd_steps=(1.0, 0.5)):
     """Adjoint of the time-averaged C_D over the last `window` steps of the
     cylinder run with respect to the solid-fraction field (20 checkpoints),
-    checked by central differences of the same FP32 forward on `fd_cells`
-    random boundary cells with 0 < eps < 1. Also times forward and backward."""
+    compared with central differences of the same FP32 forward on `fd_cells`
+    random boundary cells with 0 < eps < 1, at step sizes fd_h * fd_steps (the
+    spread between those shows what FP32 differences can resolve). Also times
+    forward and backward."""
     s, eps, box, umean = _dfg2_sim(gpu, D, uin_max, nz, precision, ramp)
     if tune:
         s.autotune(steps=200)  # the forward's kernel and launch shape (state restored)
@@ -648,19 +651,23 @@ def dfg2_adjoint(gpu, D=64, uin_max=0.06, nz=3, total=200000, window=10000, chec
     cells = rng.choice(cand, size=min(fd_cells, cand.size), replace=False)
     fd = []
     for n in cells:
-        vals = []
-        for sgn in (1.0, -1.0):
-            e = eps.copy()
-            e[n] = np.float32(e[n] + sgn * fd_h)
-            s.setSolidFractions(e)
-            s.uploadState(start)
-            s.stepsDone = t_start
-            a2 = sg.Adjoint(s, window, box, checkpoints=1)
-            vals.append(a2.forward())
-            a2.close()
-        h_eff = float(np.float32(eps[n] + fd_h)) - float(np.float32(eps[n] - fd_h))
+        ests = []
+        for scale in fd_steps:
+            h = fd_h * scale
+            vals = []
+            for sgn in (1.0, -1.0):
+                e = eps.copy()
+                e[n] = np.float32(e[n] + sgn * h)
+                s.setSolidFractions(e)
+                s.uploadState(start)
+                s.stepsDone = t_start
+                a2 = sg.Adjoint(s, window, box, checkpoints=1)
+                vals.append(a2.forward())
+                a2.close()
+            h_eff = float(np.float32(eps[n] + h)) - float(np.float32(eps[n] - h))
+            ests.append((vals[0] - vals[1]) / h_eff * norm)
         fd.append({"cell": int(n), "eps": float(eps[n]), "adjoint": float(ge[n]) * norm,
-                   "fd": (vals[0] - vals[1]) / h_eff * norm})
+                   "fd": ests[0], "fd_steps": list(fd_steps), "fd_all": ests})
     s.setSolidFractions(eps)
     fwd_step = st["forward_s"] / window
     out = {"D": D, "window": window, "checkpoints": checkpoints, "mean_cd": J * norm,

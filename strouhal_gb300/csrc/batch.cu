@@ -50,6 +50,8 @@ struct stro_batch {
     std::vector<cudaStream_t> streams;  // STRO_BATCH_STREAMS: one per instance
     uint32_t* d_tiles = nullptr;  // rounds mode: bulk tile list, then boundary tile list
     size_t tiles_cap = 0;
+    uint16_t* d_tile_inst = nullptr;  // instance of every tile
+    size_t tile_inst_cap = 0;
     int split = 1;
     int64_t last_bulk = 0, last_edge = 0;
     BatchCtl* d_ctl = nullptr;
@@ -313,6 +315,8 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
         }
         const uint32_t threads = b->block.x * b->block.y;
         I.cells = uint32_t(s->N);
+        division_magic(uint32_t(s->nx), &I.div_nx_m, &I.div_nx_s);
+        division_magic(uint32_t(s->ny), &I.div_ny_m, &I.div_ny_s);
         I.ntiles = (I.cells + threads - 1) / threads;
         if (walled(s)) {
             I.tiles_x = (uint32_t(s->nx) + b->block.x - 1) / b->block.x;
@@ -342,6 +346,10 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
         max_steps = std::max(max_steps, I.steps);
     }
     if (tiles >= (1ull << 31)) return fail(STRO_ERR_INVALID, "batch too large");
+    std::vector<uint16_t> tile_inst(tiles);
+    for (size_t k = 0; k < n; ++k)
+        std::fill(tile_inst.begin() + inst[k].tile_begin,
+                  tile_inst.begin() + inst[k].tile_begin + inst[k].ntiles, uint16_t(k));
     // Rounds mode on a walled batch: bulk tiles (every cell fluid, without
     // wall neighbours or solid fraction) go to the wall-free kernels, the rest
     // to the wall-aware ones. Both lists are in instance order, so the tiles of
@@ -376,6 +384,7 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
     if (rc == STRO_OK && probes) rc = grow(&b->d_fpart, &b->fpart_cap, 3 * tiles);
     if (rc == STRO_OK && probes) rc = grow(&b->d_samples, &b->samples_cap, sample_total);
     if (rc == STRO_OK && split) rc = grow(&b->d_tiles, &b->tiles_cap, tile_list.size());
+    if (rc == STRO_OK) rc = grow(&b->d_tile_inst, &b->tile_inst_cap, tiles);
     if (rc == STRO_OK && !b->d_ctl) STRO_CUDA(cudaMalloc(&b->d_ctl, sizeof(BatchCtl)));
     if (rc != STRO_OK) return rc;
     for (size_t k = 0; k < n; ++k) {
@@ -391,10 +400,13 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
     if (split)
         STRO_CUDA(cudaMemcpyAsync(b->d_tiles, tile_list.data(), tile_list.size() * sizeof(uint32_t),
                                   cudaMemcpyHostToDevice, st));
+    STRO_CUDA(cudaMemcpyAsync(b->d_tile_inst, tile_inst.data(), tiles * sizeof(uint16_t),
+                              cudaMemcpyHostToDevice, st));
     b->last_bulk = split ? nbulk_total : 0;
     b->last_edge = split ? int64_t(tile_list.size()) - nbulk_total : 0;
     BatchArgs args{};
     args.inst = b->d_inst;
+    args.tile_inst = b->d_tile_inst;
     args.count = int32_t(n);
     args.max_steps = max_steps;
     args.kepart = b->d_kepart;
@@ -409,7 +421,8 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
                                 int64_t(reinterpret_cast<uintptr_t>(b->d_kepart)),
                                 int64_t(reinterpret_cast<uintptr_t>(b->d_ctl)), probes,
                                 int64_t(reinterpret_cast<uintptr_t>(args.fpart)), split,
-                                int64_t(reinterpret_cast<uintptr_t>(b->d_tiles))};
+                                int64_t(reinterpret_cast<uintptr_t>(b->d_tiles)),
+                                int64_t(reinterpret_cast<uintptr_t>(b->d_tile_inst))};
     for (size_t k = 0; k < n; ++k) {
         key.push_back(bulk_end[k]);
         key.push_back(edge_end[k]);
@@ -605,6 +618,7 @@ extern "C" {
 
 int stro_batch_create(stro_ctx* ctx, int32_t count, stro_sim* const* sims, stro_batch** out) {
     if (!ctx || !sims || !out || count < 1) return fail(STRO_ERR_INVALID, "bad batch arguments");
+    if (count > 65535) return fail(STRO_ERR_INVALID, "a batch holds at most 65535 lattices");
     *out = nullptr;
     for (int32_t i = 0; i < count; ++i) {
         if (!sims[i]) return fail(STRO_ERR_INVALID, "null simulation in batch");
@@ -650,6 +664,7 @@ int stro_batch_destroy(stro_batch* b) {
     cudaFree(b->d_fpart);
     cudaFree(b->d_samples);
     cudaFree(b->d_tiles);
+    cudaFree(b->d_tile_inst);
     for (cudaStream_t x : b->streams) cudaStreamDestroy(x);
     cudaFree(b->d_ctl);
     cudaFree(b->d_ramp);
@@ -902,14 +917,16 @@ int stro_sim_set_block(stro_sim* s, int32_t bx, int32_t by) {
 
 int stro_sim_set_variant(stro_sim* s, int32_t variant) {
     if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
-    if (variant < 0 || variant > 3) return fail(STRO_ERR_INVALID, "variant must be 0..3");
+    if (variant < 0 || variant > 5) return fail(STRO_ERR_INVALID, "variant must be 0..5");
     s->variant = variant;
     return STRO_OK;
 }
 
 int stro_sim_set_block_split(stro_sim* s, int32_t enabled) {
     if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
+    if (enabled < 0 || enabled > 2) return fail(STRO_ERR_INVALID, "split must be 0, 1 or 2");
     s->split = enabled != 0;
+    s->edge_colmajor = enabled == 2;
     return STRO_OK;
 }
 
@@ -1042,11 +1059,14 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
     const int half = s->precision == STRO_FP16S ? 1 : 0;
     const bool saved_split = s->split;
     bool best_split = saved_split;
+    bool best_col = s->edge_colmajor;
     const int geo = geo_on(s) ? 1 : 0;
-    for (int split : {1, 0}) {
-        if (!split && !geo) break;  // the split only exists for walled lattices
+    // split 2: the split with the boundary blocks' odd pass in column-major order
+    for (int split : {1, 2, 0}) {
+        if (split != 1 && !geo) break;  // the split only exists for walled lattices
         s->split = split != 0;
-        for (int variant : {0, 1, 2, 3}) {
+        s->edge_colmajor = split == 2;
+        for (int variant : {0, 1, 2, 3, 4, 5}) {
             const dim3* shapes = variant == 2 ? kRowShapes : kShapes;
             const size_t nshapes = variant == 2 ? sizeof(kRowShapes) / sizeof(dim3)
                                                 : sizeof(kShapes) / sizeof(dim3);
@@ -1058,10 +1078,14 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
                 if (variant == 3 && (geo || c.x * c.y > 128)) continue;
                 if (variant == 1 && !exact::kPair.supported(half, geo, false, s->nx, s->plane, c))
                     continue;
+                if ((variant == 4 || variant == 5) &&
+                    !exact::kPair.wide_supported(half, geo, false, s->nx, s->ny, s->plane, c,
+                                                 variant == 4 ? 4 : 8))
+                    continue;
                 if (variant == 2 && !exact::kRows.supported(half, geo, false, s->nx, s->ny,
                                                             int(c.x), int(c.y)))
                     continue;
-                if (variant != 0 && split == 0) continue;  // the split only changes variant 0
+                if (variant != 0 && split != 1) continue;  // the split only changes variant 0
                 if (variant != 0 && s->collision != STRO_COLLISION_REFERENCE) continue;
                 double sec = 0.0;
                 rc = tune_sim_shape(s, steps, variant, c, &sec);
@@ -1070,11 +1094,13 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
                     best_shape = c;
                     best_variant = variant;
                     best_split = s->split;
+                    best_col = s->edge_colmajor;
                 }
             }
         }
     }
     s->split = best_split;
+    s->edge_colmajor = best_col;
     e = cudaMemcpyAsync(s->d_f, saved, bytes, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     cudaFree(saved);

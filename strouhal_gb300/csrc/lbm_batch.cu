@@ -8,7 +8,7 @@
 // and each round processes the active prefix. A tile is a run of consecutive
 // cells in the instance's linear index (x fastest), so one block size fits
 // every instance without idle threads, whatever its edge length; the only
-// partial tile is an instance's last one.
+// partial tile is an instance's last one. A table gives each tile's instance.
 //
 // Two launch forms, both captured in a CUDA graph by the host:
 //   k_batch_persistent  one cooperative launch; blocks loop over rounds and
@@ -19,8 +19,12 @@
 //   k_batch_round       one launch per round over the active tiles (the graph
 //                       holds the rounds in order; kernel boundaries are the
 //                       barriers).
-// DDFs are read through L2 only inside the persistent kernel: a slot written by
-// another SM in the previous round must not be served from this SM's L1.
+// The persistent kernel reads DDFs with ordinary (L1-cached) loads: a slot
+// another SM wrote in the previous round is read only after the grid barrier,
+// whose release / acquire pattern (gpu-scope fences around the arrival and
+// generation atomics, then a block barrier) makes that write visible to every
+// thread of the block, the same ordering a cooperative grid sync gives. Within
+// a round no slot is read by one thread and written by another.
 //
 // Optional per-instance kinetic-energy traces are fused into the even pass:
 // on a logging round each tile reduces sum |u|^2 of its cells (FP64, fixed
@@ -39,15 +43,12 @@ namespace stro {
 
 namespace {
 
-// Instance owning `tile`: binary search over the ascending tile_begin.
-__device__ __forceinline__ int find_instance(const BatchArgs& b, uint32_t tile) {
-    int lo = 0, hi = b.count - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (b.inst[mid].tile_begin <= tile) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
+// Descriptor of the instance owning `tile`, copied into registers: one table
+// load finds the instance, and the step kernels then read its fields from
+// the local copy (a reference into global memory would have to be reloaded
+// after every DDF store, which the compiler cannot prove does not alias it).
+__device__ __forceinline__ BatchInstance tile_instance(const BatchArgs& b, uint32_t tile) {
+    return b.inst[b.tile_inst[tile]];
 }
 
 __device__ __forceinline__ uint32_t active_tiles(const BatchArgs& b, int64_t r) {
@@ -84,10 +85,12 @@ __device__ __forceinline__ void process_tile(const BatchArgs& b, const BatchInst
     } else {
         const uint32_t lin = tl * (blockDim.x * blockDim.y) + threadIdx.y * blockDim.x + threadIdx.x;
         in = lin < I.cells;
-        const uint32_t nx = uint32_t(I.a.nx), t = lin / nx;
-        x = int(lin - t * nx);
-        y = int(t % uint32_t(I.a.ny));
-        z = int(t / uint32_t(I.a.ny));
+        // multiply-shift division by nx and ny (exact for indices below 2^31)
+        const uint32_t t = uint32_t((uint64_t(lin) * I.div_nx_m) >> (32 + I.div_nx_s));
+        const uint32_t zz = uint32_t((uint64_t(t) * I.div_ny_m) >> (32 + I.div_ny_s));
+        x = int(lin - t * uint32_t(I.a.nx));
+        y = int(t - zz * uint32_t(I.a.ny));
+        z = int(zz);
     }
     if (((I.t0 + r) & 1) == 0) {
         if (logs_at(I, r)) {
@@ -206,8 +209,8 @@ __global__ void __launch_bounds__(256) k_batch_persistent(const BatchArgs b) {
         if (blockIdx.x == 0 && r > 0) fold_round(b, r - 1);
         const uint32_t tiles = active_tiles(b, r);
         for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-            const BatchInstance& I = b.inst[find_instance(b, tile)];
-            process_tile<S, GEO, FEAT, PROBES, true>(b, I, tile, r);
+            const BatchInstance I = tile_instance(b, tile);
+            process_tile<S, GEO, FEAT, PROBES, false>(b, I, tile, r);
         }
         if (!grid_barrier(b.ctl, gen, b.spin_limit, r)) return;
     }
@@ -217,7 +220,7 @@ __global__ void __launch_bounds__(256) k_batch_persistent(const BatchArgs b) {
 template <typename S, int GEO, int FEAT, bool PROBES>
 __global__ void __launch_bounds__(256) k_batch_round(const BatchArgs b, int64_t r) {
     const uint32_t tile = blockIdx.x;
-    const BatchInstance& I = b.inst[find_instance(b, tile)];
+    const BatchInstance I = tile_instance(b, tile);
     process_tile<S, GEO, FEAT, PROBES, false>(b, I, tile, r);
 }
 
@@ -232,7 +235,7 @@ template <typename S, int GEO, int FEAT, bool PROBES>
 __global__ void __launch_bounds__(256, GEO == 1 ? 2 : 0) k_batch_round_list(const BatchArgs b, int64_t r,
                                                           const uint32_t* list) {
     const uint32_t tile = list[blockIdx.x];
-    const BatchInstance& I = b.inst[find_instance(b, tile)];
+    const BatchInstance I = tile_instance(b, tile);
     process_tile<S, GEO, FEAT, PROBES, false>(b, I, tile, r);
 }
 

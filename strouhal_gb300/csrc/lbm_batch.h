@@ -34,7 +34,20 @@ struct BatchInstance {
     // plain fluid only.
     uint32_t tiles_x;
     uint32_t tiles_y;
+    // Exact division of a linear cell index (< 2^31) by nx and by ny:
+    // n / d = (n * m) >> (32 + s) with s = ceil(log2 d), m = ceil(2^(32+s) / d).
+    uint64_t div_nx_m, div_ny_m;
+    uint32_t div_nx_s, div_ny_s;
 };
+
+// Multiplier and shift of the exact division above (host side).
+inline void division_magic(uint32_t d, uint64_t* m, uint32_t* s) {
+    uint32_t sh = 0;
+    while ((uint64_t(1) << sh) < d) ++sh;
+    const unsigned __int128 num = (unsigned __int128)1 << (32 + sh);
+    *m = uint64_t((num + d - 1) / d);
+    *s = sh;
+}
 
 // Grid-barrier and error state of the persistent launch (zeroed before each launch).
 struct BatchCtl {
@@ -47,6 +60,7 @@ struct BatchCtl {
 
 struct BatchArgs {
     const BatchInstance* inst;  // sorted by `steps`, longest first
+    const uint16_t* tile_inst;  // instance (index into inst) of every tile
     int32_t count;
     int64_t max_steps;
     double* kepart;             // one kinetic-energy partial per tile

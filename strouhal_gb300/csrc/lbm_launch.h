@@ -28,10 +28,13 @@ struct StepLaunchers {
     // (every cell fluid, no wall neighbour, no solid fraction) run the
     // wall-free kernels at feature level feat_bulk, `edge` blocks the
     // wall-aware kernels at feat_edge. Each cell touches only its own slots,
-    // so the two launches are independent.
+    // so the two launches are independent. edge_colmajor: the edge blocks of
+    // the odd pass take their cells column by column (a warp covers whole
+    // columns of the block) instead of row by row.
     cudaError_t (*split)(const StepArgs& a, int half_storage, int parity, int feat_bulk,
                          int feat_edge, dim3 block, const uint32_t* bulk, uint32_t nbulk,
-                         const uint32_t* edge, uint32_t nedge, cudaStream_t st);
+                         const uint32_t* edge, uint32_t nedge, int edge_colmajor,
+                         cudaStream_t st);
 };
 
 // Row-staged step (lbm_rows.cu): tiles of `rows` whole lattice rows move
@@ -51,6 +54,13 @@ struct RowsLaunchers {
 struct PairLaunchers {
     bool (*supported)(int half_storage, int geo, bool probe, int nx, uint64_t plane, dim3 block);
     cudaError_t (*launch)(const StepArgs& a, int parity, int feat, dim3 block, cudaStream_t st);
+    // Wide form: `cells` = 4 or 8 cells per thread (8- or 16-byte words),
+    // block = bx threads along x (a multiple of 32 dividing nx / cells) by
+    // `by` rows (dividing ny).
+    bool (*wide_supported)(int half_storage, int geo, bool probe, int nx, int ny, uint64_t plane,
+                           dim3 block, int cells);
+    cudaError_t (*wide_launch)(const StepArgs& a, int parity, int feat, dim3 block, int cells,
+                               cudaStream_t st);
 };
 
 namespace exact {
@@ -78,9 +88,9 @@ struct FieldView {
     float fx, fy, fz;       // uniform force
 };
 
-// Number of blocks the fixed-order reductions use for N cells (depends on N only).
-// Blocks of a fixed-order FP64 reduction over `count` items: one per 1,024,
-// at most kReductionMaxBlocks (which sizes every partials buffer).
+// Blocks of a fixed-order FP64 reduction over `count` items (depends on the
+// count only): one per 1,024, at most kReductionMaxBlocks (which sizes every
+// partials buffer).
 constexpr int kReductionMaxBlocks = 2048;
 int reduction_blocks(uint64_t count);
 

@@ -25,6 +25,9 @@
 // exchange and no warp-edge special case. Every slot is still written exactly
 // once.
 //
+// The wide kernels (V = 4 or 8 cells per thread, below) reuse this pair code
+// with 8- or 16-byte loads.
+//
 // The per-cell arithmetic is the shared collide(), so results are identical to
 // the one-cell kernels of the same arithmetic. Compiled twice like
 // lbm_step.cu: STRO_ARITH=0 (stro::exact) and 1 (stro::fused); each copy
@@ -137,13 +140,16 @@ __global__ void __launch_bounds__(256, FEAT == 2 ? 2 : 4) k_pair_even(const Step
     });
 }
 
-// Row indices (z * ny + y) of the block's row and its neighbour rows. One
-// row per block, so every value here is block-uniform.
+// Row indices (z * ny + y) of a row and its neighbour rows. The pair kernel
+// has one row per block, so there every value is block-uniform; the wide
+// kernels below have one row per warp.
 struct PairRows {
     uint32_t ym, y0, yp, zm, z0, zp, ny;
-    __device__ __forceinline__ PairRows(const StepArgs& a) {
+    __device__ __forceinline__ PairRows(const StepArgs& a)
+        : PairRows(a, blockIdx.y, blockIdx.z) {}
+    __device__ __forceinline__ PairRows(const StepArgs& a, uint32_t y, uint32_t z) {
         ny = uint32_t(a.ny);
-        const uint32_t y = blockIdx.y, z = blockIdx.z, nz = uint32_t(a.nz);
+        const uint32_t nz = uint32_t(a.nz);
         y0 = y;
         ym = (y == 0) ? ny - 1 : y - 1;
         yp = (y == ny - 1) ? 0 : y + 1;
@@ -163,10 +169,9 @@ struct PairRows {
 // of the gather stays in registers across the collisions) plus a
 // block-uniform plane-and-row offset.
 __device__ __forceinline__ void scatter_pair(const StepArgs& a, const __half2 (&ao)[10],
-                                             const float (&fh)[19], int x) {
+                                             const float (&fh)[19], int x, const PairRows& rows) {
     forget_int(x);
     const uint32_t nx = uint32_t(a.nx), hnx = nx / 2;
-    const PairRows rows(a);
     const uint32_t P = uint32_t(a.plane), P2 = P / 2;
     __half2* __restrict__ f2x = static_cast<__half2*>(a.f) + x / 2;
     __half* __restrict__ f1 = static_cast<__half*>(a.f);
@@ -230,7 +235,106 @@ __global__ void __launch_bounds__(256, FEAT == 2 ? 2 : 4) k_pair_odd(const StepA
     __half2 ao[10];
     float fh[19];
     collide_pair<FEAT>(v, ao, fh, a, x, n);
-    scatter_pair(a, ao, fh, x);
+    scatter_pair(a, ao, fh, x, rows);
+}
+
+// ------------------------------------------------------------ wide variant
+// V cells per thread (V = 4: one 8-byte word per direction; V = 8: one
+// 16-byte word), so a warp loads 256 or 512 contiguous bytes of a plane per
+// request and each thread keeps 19 * 2V bytes in flight. The cells are then
+// collided two at a time with the pair kernel's code (collide_pair) and
+// stored as it does (one 4-byte word per direction, or two 2-byte stores for
+// x-shifted directions of the odd pass) as soon as each pair is done, which
+// frees its input registers. Odd-pass gather: a direction with c_x = +1 needs
+// cells x-1 .. x+V-2, i.e. the thread's own word shifted by one half, filled
+// from the 4-byte word (x-2, x-1) to its left; c_x = -1 takes the word
+// (x+V, x+V+1) to its right. The shift is a funnel shift per 4-byte lane;
+// the neighbour words are the adjacent threads' own data, served by L1.
+// Blocks are bx threads along x (a multiple of 32 dividing nx / V) by `by`
+// rows, so every warp covers 32 V cells of one row.
+template <int V> struct WideWord { uint32_t w[V / 2]; };
+
+template <int V>
+__device__ __forceinline__ WideWord<V> load_wide(const __half* p) {
+    WideWord<V> r;
+    if constexpr (V == 4) {
+        const uint2 t = *reinterpret_cast<const uint2*>(p);
+        r.w[0] = t.x; r.w[1] = t.y;
+    } else {
+        const uint4 t = *reinterpret_cast<const uint4*>(p);
+        r.w[0] = t.x; r.w[1] = t.y; r.w[2] = t.z; r.w[3] = t.w;
+    }
+    return r;
+}
+
+__device__ __forceinline__ __half2 as_half2(uint32_t w) {
+    return *reinterpret_cast<const __half2*>(&w);
+}
+
+template <int FEAT, int V>
+__global__ void __launch_bounds__(256, V == 8 ? 2 : 3) k_wide_even(const StepArgs a) {
+    const int x = V * int(blockIdx.x * blockDim.x + threadIdx.x);
+    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
+    const uint32_t n = (z * uint32_t(a.ny) + y) * uint32_t(a.nx) + uint32_t(x);
+    const uint32_t P = uint32_t(a.plane);
+    const __half* __restrict__ fn = static_cast<const __half*>(a.f) + n;
+    WideWord<V> W[19];
+    sfor<0, 19>([&](auto I) { W[I] = load_wide<V>(fn + uint32_t(I) * P); });
+    sfor<0, V / 2>([&](auto J) {
+        constexpr int j = J;
+        __half2 v[19];
+        sfor<0, 19>([&](auto I) { v[I] = as_half2(W[I].w[j]); });
+        __half2 ao[10];
+        float fh[19];
+        collide_pair<FEAT>(v, ao, fh, a, x + 2 * j, n + 2 * j);
+        __half2* __restrict__ q = reinterpret_cast<__half2*>(static_cast<__half*>(a.f) + n) + j;
+        forget(q);
+        // direction i of both cells goes to slot opp(i)
+        sfor<0, 19>([&](auto I) {
+            q[uint32_t(opp(I)) * (P / 2)] = __halves2half2(out_lo<I>(ao), __float2half_rn(fh[I]));
+        });
+    });
+}
+
+template <int FEAT, int V>
+__global__ void __launch_bounds__(256, V == 8 ? 2 : 3) k_wide_odd(const StepArgs a) {
+    const int x = V * int(blockIdx.x * blockDim.x + threadIdx.x);
+    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
+    const uint32_t nx = uint32_t(a.nx);
+    const PairRows rows(a, y, z);
+    const uint32_t P = uint32_t(a.plane);
+    const __half* __restrict__ f = static_cast<const __half*>(a.f);
+    const int xl = wrap_x(x - 2, int(nx));  // word (x-2, x-1)
+    const int xr = wrap_x(x + V, int(nx));  // word (x+V, x+V+1)
+    WideWord<V> W[19];
+    W[0] = load_wide<V>(f + rows.row<0, 0>() * nx + uint32_t(x));
+    sfor<1, 19>([&](auto I) {
+        constexpr int i = I;
+        // slot opp(i) of the source row (y, z shifted by -c_i)
+        const __half* __restrict__ src = f + uint32_t(opp(i)) * P + rows.row<-dcy(i), -dcz(i)>() * nx;
+        const WideWord<V> w = load_wide<V>(src + uint32_t(x));
+        if constexpr (dcx(i) == 0) {
+            W[i] = w;
+        } else if constexpr (dcx(i) > 0) {  // sources x-1 .. x+V-2
+            const uint32_t l = *reinterpret_cast<const uint32_t*>(src + xl);
+            W[i].w[0] = __funnelshift_r(l, w.w[0], 16);
+            sfor<1, V / 2>([&](auto K) { W[i].w[K] = __funnelshift_r(w.w[K - 1], w.w[K], 16); });
+        } else {  // sources x+1 .. x+V
+            const uint32_t r = *reinterpret_cast<const uint32_t*>(src + xr);
+            sfor<0, V / 2 - 1>([&](auto K) { W[i].w[K] = __funnelshift_r(w.w[K], w.w[K + 1], 16); });
+            W[i].w[V / 2 - 1] = __funnelshift_r(w.w[V / 2 - 1], r, 16);
+        }
+    });
+    const uint32_t n = rows.row<0, 0>() * nx + uint32_t(x);
+    sfor<0, V / 2>([&](auto J) {
+        constexpr int j = J;
+        __half2 v[19];
+        sfor<0, 19>([&](auto I) { v[I] = as_half2(W[I].w[j]); });
+        __half2 ao[10];
+        float fh[19];
+        collide_pair<FEAT>(v, ao, fh, a, x + 2 * j, n + 2 * j);
+        scatter_pair(a, ao, fh, x + 2 * j, rows);
+    });
 }
 
 }  // namespace
@@ -256,7 +360,38 @@ cudaError_t launch_pair_step(const StepArgs& a, int parity, int feat, dim3 block
     return cudaGetLastError();
 }
 
-const PairLaunchers kPair = {&pair_step_supported, &launch_pair_step};
+bool wide_step_supported(int half_storage, int geo, bool probe, int nx, int ny, uint64_t plane,
+                         dim3 block, int cells) {
+    return half_storage && !geo && !probe && (cells == 4 || cells == 8) &&
+           nx % (32 * cells) == 0 && plane % 8 == 0 && block.x % 32 == 0 &&
+           (nx / cells) % int(block.x) == 0 && block.y >= 1 && ny % int(block.y) == 0 &&
+           block.x * block.y <= 256 && 19 * plane < (uint64_t(1) << 32);
+}
+
+template <int V>
+static void launch_wide_cells(const StepArgs& a, int parity, int feat, dim3 block,
+                              cudaStream_t st) {
+    const dim3 grid(unsigned(a.nx / V) / block.x, unsigned(a.ny) / block.y, unsigned(a.nz));
+    if (parity == 0) {
+        if (feat == 2) k_wide_even<2, V><<<grid, block, 0, st>>>(a);
+        else if (feat == 1) k_wide_even<1, V><<<grid, block, 0, st>>>(a);
+        else k_wide_even<0, V><<<grid, block, 0, st>>>(a);
+    } else {
+        if (feat == 2) k_wide_odd<2, V><<<grid, block, 0, st>>>(a);
+        else if (feat == 1) k_wide_odd<1, V><<<grid, block, 0, st>>>(a);
+        else k_wide_odd<0, V><<<grid, block, 0, st>>>(a);
+    }
+}
+
+cudaError_t launch_wide_step(const StepArgs& a, int parity, int feat, dim3 block, int cells,
+                             cudaStream_t st) {
+    if (cells == 8) launch_wide_cells<8>(a, parity, feat, block, st);
+    else launch_wide_cells<4>(a, parity, feat, block, st);
+    return cudaGetLastError();
+}
+
+const PairLaunchers kPair = {&pair_step_supported, &launch_pair_step, &wide_step_supported,
+                             &launch_wide_step};
 
 }  // namespace STRO_ARITH_NS
 }  // namespace stro

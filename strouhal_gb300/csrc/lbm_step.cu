@@ -136,11 +136,29 @@ __global__ void __launch_bounds__(256) k_list_even(const StepArgs a, const uint3
     even_cell<S, GEO, FEAT, false, false, STRO_ARITH, true>(a, x, y, z);
 }
 
-template <typename S, int GEO, int FEAT>
+// Column-major cell order inside a block: thread t takes column t / by, row
+// t % by, so a warp covers 32 / by whole columns of the tile instead of 32 / bx
+// whole rows. On the boundary blocks of the odd pass this keeps a column of
+// wall-adjacent cells (the cells next to an inflow wall at x = 0 or nx - 1)
+// in warps of their own: the plain cells beside them no longer sit in warps
+// that also run the moving-wall branches. The rows of a tile are re-read by
+// its other warps, so the narrower warp accesses are served from L1.
+__device__ __forceinline__ void list_block_colmajor(const uint32_t* list, uint32_t gx,
+                                                    uint32_t gy, int& x, int& y, int& z) {
+    const uint32_t blk = list[blockIdx.x];
+    const uint32_t t = blk / gx;
+    const uint32_t tid = threadIdx.x + blockDim.x * threadIdx.y;
+    x = int((blk - t * gx) * blockDim.x + tid / blockDim.y);
+    y = int((t % gy) * blockDim.y + tid % blockDim.y);
+    z = int(t / gy);
+}
+
+template <typename S, int GEO, int FEAT, bool COLMAJOR = false>
 __global__ void __launch_bounds__(256) k_list_odd(const StepArgs a, const uint32_t* list,
                                                   uint32_t gx, uint32_t gy) {
     int x, y, z;
-    list_block(list, gx, gy, x, y, z);
+    if constexpr (COLMAJOR) list_block_colmajor(list, gx, gy, x, y, z);
+    else list_block(list, gx, gy, x, y, z);
     if (x >= a.nx || y >= a.ny || z >= a.nz) return;
     double contrib[3];
     odd_cell<S, GEO, FEAT, false, false, STRO_ARITH, true>(a, WallVel(a), x, y, z, contrib);
@@ -148,31 +166,34 @@ __global__ void __launch_bounds__(256) k_list_odd(const StepArgs a, const uint32
 
 template <typename S, int GEO, int FEAT>
 static void launch_list(const StepArgs& a, int parity, const uint32_t* list, uint32_t count,
-                        dim3 block, cudaStream_t st) {
+                        dim3 block, bool colmajor, cudaStream_t st) {
     if (count == 0) return;
     const uint32_t gx = (a.nx + block.x - 1) / block.x, gy = (a.ny + block.y - 1) / block.y;
     if (parity == 0) k_list_even<S, GEO, FEAT><<<count, block, 0, st>>>(a, list, gx, gy);
+    else if (GEO == 1 && colmajor) k_list_odd<S, GEO, FEAT, true><<<count, block, 0, st>>>(a, list, gx, gy);
     else k_list_odd<S, GEO, FEAT><<<count, block, 0, st>>>(a, list, gx, gy);
 }
 
 template <typename S, int GEO>
 static void launch_list_level(const StepArgs& a, int parity, int feat, const uint32_t* list,
-                              uint32_t count, dim3 block, cudaStream_t st) {
-    if (feat == 3) launch_list<S, GEO, 3>(a, parity, list, count, block, st);
-    else if (feat == 2) launch_list<S, GEO, 2>(a, parity, list, count, block, st);
-    else if (feat == 1) launch_list<S, GEO, 1>(a, parity, list, count, block, st);
-    else launch_list<S, GEO, 0>(a, parity, list, count, block, st);
+                              uint32_t count, dim3 block, bool colmajor, cudaStream_t st) {
+    if (feat == 3) launch_list<S, GEO, 3>(a, parity, list, count, block, colmajor, st);
+    else if (feat == 2) launch_list<S, GEO, 2>(a, parity, list, count, block, colmajor, st);
+    else if (feat == 1) launch_list<S, GEO, 1>(a, parity, list, count, block, colmajor, st);
+    else launch_list<S, GEO, 0>(a, parity, list, count, block, colmajor, st);
 }
 
 cudaError_t launch_step_split(const StepArgs& a, int half_storage, int parity, int feat_bulk,
                               int feat_edge, dim3 block, const uint32_t* bulk, uint32_t nbulk,
-                              const uint32_t* edge, uint32_t nedge, cudaStream_t st) {
+                              const uint32_t* edge, uint32_t nedge, int edge_colmajor,
+                              cudaStream_t st) {
+    const bool col = edge_colmajor != 0;
     if (half_storage) {
-        launch_list_level<__half, 0>(a, parity, feat_bulk, bulk, nbulk, block, st);
-        launch_list_level<__half, 1>(a, parity, feat_edge, edge, nedge, block, st);
+        launch_list_level<__half, 0>(a, parity, feat_bulk, bulk, nbulk, block, false, st);
+        launch_list_level<__half, 1>(a, parity, feat_edge, edge, nedge, block, col, st);
     } else {
-        launch_list_level<float, 0>(a, parity, feat_bulk, bulk, nbulk, block, st);
-        launch_list_level<float, 1>(a, parity, feat_edge, edge, nedge, block, st);
+        launch_list_level<float, 0>(a, parity, feat_bulk, bulk, nbulk, block, false, st);
+        launch_list_level<float, 1>(a, parity, feat_edge, edge, nedge, block, col, st);
     }
     return cudaGetLastError();
 }

@@ -342,13 +342,21 @@ cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool prob
         if (ensure_block_lists(s) != STRO_OK) return cudaErrorMemoryAllocation;
         s->last_path = "split";
         return L.split(a, half, int(t & 1), bulk_feat(s), feat_on(s), s->block, s->d_blocks,
-                       s->nbulk, s->d_blocks + s->nbulk, s->nedge, sim_stream(s));
+                       s->nbulk, s->d_blocks + s->nbulk, s->nedge, s->edge_colmajor ? 1 : 0,
+                       sim_stream(s));
     }
     const PairLaunchers& PL = fused ? fused::kPair : exact::kPair;
     const bool kbc = s->collision == STRO_COLLISION_KBC;  // one-cell kernels only
     if (!kbc && s->variant == 1 && PL.supported(half, geo, probe, s->nx, s->plane, s->pair_block)) {
         s->last_path = "pair";
         return PL.launch(a, int(t & 1), feat_on(s), s->pair_block, sim_stream(s));
+    }
+    if (!kbc && (s->variant == 4 || s->variant == 5)) {
+        const int cells = s->variant == 4 ? 4 : 8;
+        if (PL.wide_supported(half, geo, probe, s->nx, s->ny, s->plane, s->block, cells)) {
+            s->last_path = cells == 4 ? "wide4" : "wide8";
+            return PL.wide_launch(a, int(t & 1), feat_on(s), s->block, cells, sim_stream(s));
+        }
     }
     if (!kbc && s->variant == 3 && !geo && !probe && s->block.x * s->block.y <= 128) {
         s->last_path = "capped";
@@ -396,7 +404,8 @@ std::vector<uint8_t> graph_key(const stro_sim* s, int64_t t, int64_t G) {
     std::memset(&a, 0, sizeof a);
     fill_step_args(s, t, &a);
     put_bytes(k, a);
-    const int64_t cfg[] = {t & 1, G, s->variant, s->split ? 1 : 0, s->block.x, s->block.y,
+    const int64_t cfg[] = {t & 1, G, s->variant, s->split ? 1 : 0, s->edge_colmajor ? 1 : 0,
+                           s->block.x, s->block.y,
                            s->pair_block.x, s->pair_block.y, s->rows_threads, s->rows_per_tile,
                            s->arith, s->collision, s->precision, geo_on(s) ? 1 : 0, feat_on(s),
                            bulk_feat(s), int64_t(reinterpret_cast<uintptr_t>(s->d_blocks)),

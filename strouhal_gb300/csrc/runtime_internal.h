@@ -82,6 +82,7 @@ struct stro_sim {
     int64_t rows_polls = 1ll << 22;  // polls per bounded wait of the row-staged variant
     // bulk / boundary block lists of a walled lattice for the current block shape
     bool split = true;
+    bool edge_colmajor = false;    // boundary blocks of the odd pass in column-major cell order
     uint32_t* d_blocks = nullptr;  // bulk blocks first, then edge blocks
     uint32_t nbulk = 0, nedge = 0;
     dim3 lists_block{0, 0, 0};

@@ -29,8 +29,9 @@ def main(argv=None):
                     help="the DFG 2D-2 street at D cells per diameter instead of the TGV box")
     ap.add_argument("--sphere", action="store_true",
                     help="the 512x256x256 sphere wake (FP16 storage, LES, NT sphere, sponge)")
-    ap.add_argument("--split", type=int, default=-1, choices=[-1, 0, 1],
-                    help="bulk / boundary split of walled lattices (-1 = library default)")
+    ap.add_argument("--split", type=int, default=-1, choices=[-1, 0, 1, 2],
+                    help="bulk / boundary split of walled lattices (-1 = library default, "
+                         "2 = split with column-major boundary blocks in the odd pass)")
     ap.add_argument("--collision", default="reference", choices=["reference", "kbc"],
                     help="collision operator (stro_sim_set_collision)")
     ap.add_argument("--steps", type=int, default=20)
@@ -59,7 +60,7 @@ def main(argv=None):
     if a.collision != "reference":
         s.collision = a.collision
     if a.split >= 0:
-        s.setBlockSplit(bool(a.split))
+        s.setBlockSplit("columns" if a.split == 2 else bool(a.split))
     if a.variant < 0:
         s.autotune(steps=10)
     else:
@@ -75,10 +76,11 @@ def main(argv=None):
     s.run(a.steps)
     dt = s.gpuSeconds - t0
     bx, by = {1: s.pairBlock, 2: s.rowsTile}.get(s.variant, s.block)
-    print("%s %s %s %s variant %d (%s) block %dx%d: %.4f ms/step, %.2f GLUPS"
+    print("%s %s %s %s variant %d (%s) block %dx%d split %s: %.4f ms/step, %.2f GLUPS"
           % (what, a.precision, "KBC" if a.collision == "kbc" else
              ("TRT" if a.trt or a.street else "SRT"), a.arith, s.variant,
-             s.lastPath, bx, by, 1e3 * dt / a.steps, s.cells * a.steps / dt / 1e9))
+             s.lastPath, bx, by, a.split if a.split >= 0 else "default",
+             1e3 * dt / a.steps, s.cells * a.steps / dt / 1e9))
     s.close()
     gpu.close()
 

@@ -154,18 +154,42 @@ def test_voxelizer_record_equals_oracle():
 
 
 def test_adjoint_cost_and_gradients():
+    """Cost of the full-size adjoint windows: the whole backward sweep,
+    recomputation included, within 3x the forward window (C3 cylinder, C5
+    sphere wake). The gradients' 1e-3 check is test_adjoint_crop_records: an
+    FP32 forward cannot resolve 1e-3 by finite differences (its own central
+    differences at two step sizes disagree by more than that; the record keeps
+    them as an indication only)."""
     r = rec("sphere_adjoint")
     assert r["grad_finite"]
     assert r["adjoint_step_over_forward_step"] <= 3.0
-    # the whole backward sweep, recomputation included, within 3x the forward window
     assert r["backward_over_forward"] <= 3.0
-    d = os.path.join(REC, "dfg2_adjoint.json")
-    if os.path.exists(d):
-        with open(d) as fh:
-            a = json.load(fh)
-        worst = max(abs(c["adjoint"] - c["fd"]) / max(abs(c["fd"]), 1e-12) for c in a["fd"])
-        assert worst < 5e-2, a["fd"]
-        assert a["backward_over_forward"] <= 3.0
+    a = rec("dfg2_adjoint")
+    assert a["backward_over_forward"] <= 3.0
+
+
+def test_adjoint_crop_records():
+    """Long windows (2,000 steps, sqrt(N) checkpoints) on crops of the C3
+    cylinder and C5 sphere-wake lattices (tests/adjoint_crops.py): the GPU
+    adjoint against the FP64 host adjoint of its own trajectory, and the GPU
+    and FP64 adjoints against FP64 central differences, all within 1e-3
+    (the FP16-storage solid-fraction gradient against differences of the FP64
+    trajectory: the FP16 bar, 2e-2)."""
+    for name in ("adjoint_crop_cylinder", "adjoint_crop_sphere"):
+        r = rec(name)
+        assert r["runs"]
+        for run in r["runs"]:
+            assert run["window"] >= 2000 and run["finite"], (name, run["precision"])
+            assert run["J_rel_err"] < 1e-9
+            assert run["grad_eps_rel_err"] < 1e-3, (name, run["precision"])
+            assert run["grad_eps_zero_off_nt"]
+            if name == "adjoint_crop_sphere":
+                assert run["grad_force_rel_err"] < 1e-3, (name, run["precision"])
+            for d in run["fd"]:
+                assert d["fp64_adjoint_rel_err"] < 1e-3, (name, d)
+                fp16_eps = run["precision"] == "fp16s" and d["param"] == "eps"
+                assert d["gpu_adjoint_rel_err"] < (2e-2 if fp16_eps else 1e-3), (name, d)
+        assert sum(len(run["fd"]) for run in r["runs"]) >= 8
 
 
 def test_precision_record():

@@ -16,7 +16,7 @@ PREC = {0: "fp32", 1: "fp16s"}
 
 @pytest.mark.parametrize("kind", [0, 1])
 @pytest.mark.parametrize("geometry", ["periodic", "channel"])
-@pytest.mark.parametrize("split", [True, False])
+@pytest.mark.parametrize("split", [True, False, "columns"])
 @pytest.mark.parametrize("collision", ["trt", "srt"])
 @pytest.mark.parametrize("ffield", [False, True])
 def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split, collision, ffield):
@@ -24,7 +24,7 @@ def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split, col
 
     po = oracle
     nx, ny, nz = 37, 21, 9
-    rng = np.random.default_rng(17 + kind + 2 * (geometry == "channel") + 4 * split)
+    rng = np.random.default_rng(17 + kind + 2 * (geometry == "channel") + 4 * bool(split))
     flags = None
     eps = None
     kw = dict(omega=1.55, omegaMinus=1.2 if collision == "trt" else 1.55, uin=0.05, rampSteps=7,
@@ -69,17 +69,17 @@ def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split, col
 
 
 @pytest.mark.parametrize("variant,shape", [(0, (64, 2)), (2, (128, 1)), (2, (256, 2)),
-                                           (3, (32, 4)), (1, None)])
+                                           (3, (32, 4)), (1, None), (4, (32, 2)), (5, (32, 1))])
 @pytest.mark.parametrize("kind", [0, 1])
 @pytest.mark.parametrize("feature", ["plain", "force_les_sponge", "ffield"])
 @pytest.mark.parametrize("srt", [False, True])
 def test_fused_variants_match_fused_oracle(gpu, oracle, variant, shape, kind, feature, srt):
-    """Periodic lattice: every variant in the fused arithmetic (variant 1, the
-    FP16 pair kernel, has no fused build and runs variant 0)."""
+    """Periodic lattice: every variant in the fused arithmetic (variants 1, 4
+    and 5 exist for FP16 storage; with FP32 storage they run variant 0)."""
     import strouhal_gb300 as sg
 
     po = oracle
-    nx, ny, nz = 64, 6, 5
+    nx, ny, nz = (256 if variant in (4, 5) else 64), 6, 5
     kw = dict(omega=1.7, omegaMinus=1.7 if srt else 1.3)
     if feature == "force_les_sponge":
         kw.update(force=(2e-5, -3e-5, 1e-5), cSmago=0.01)
@@ -105,7 +105,8 @@ def test_fused_variants_match_fused_oracle(gpu, oracle, variant, shape, kind, fe
         g.run(chunk)
         o.run(chunk)
         assert np.array_equal(g.downloadState(), o.f), chunk
-    expect = {0: "cell", 1: "pair" if kind == 1 else "cell", 2: "rows", 3: "capped"}[variant]
+    expect = {0: "cell", 1: "pair" if kind == 1 else "cell", 2: "rows", 3: "capped",
+              4: "wide4" if kind == 1 else "cell", 5: "wide8" if kind == 1 else "cell"}[variant]
     assert g.lastPath == expect, g.lastPath
     g.close()
 

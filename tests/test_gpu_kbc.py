@@ -29,7 +29,7 @@ def flags_walls(po, nx, ny, nz):
 @pytest.mark.parametrize("kind", [0, 1])
 @pytest.mark.parametrize("arith", ["reference", "fused"])
 @pytest.mark.parametrize("geometry", ["periodic", "walls"])
-@pytest.mark.parametrize("split", [True, False])
+@pytest.mark.parametrize("split", [True, False, "columns"])
 def test_kbc_matches_oracle(gpu, oracle, kind, arith, geometry, split):
     po = oracle
     nx, ny, nz = 35, 16, 5

@@ -24,7 +24,7 @@ def channel_flags(po, nx, ny, nz):
 @pytest.mark.parametrize("kind", [0, 1])
 @pytest.mark.parametrize("mode", ["dormant", "pressure"])
 @pytest.mark.parametrize("arith", ["reference", "fused"])
-@pytest.mark.parametrize("split", [True, False])
+@pytest.mark.parametrize("split", [True, False, "columns"])
 def test_outflow_matches_oracle(gpu, oracle, kind, mode, arith, split):
     po = oracle
     nx, ny, nz = 33, 14, 4

@@ -21,10 +21,14 @@ VARIANT_CASES = [
     (2, "fp32", 36, 7, 5, (64, 1)), (2, "fp32", 128, 6, 3, (96, 2)), (2, "fp32", 4, 6, 5, (32, 6)),
     (2, "fp32", 256, 4, 2, (256, 2)),
     (3, "fp16s", 37, 7, 5, (32, 4)), (3, "fp32", 64, 6, 4, (32, 4)),
+    # wide FP16 kernels: 4 / 8 cells per thread, one warp per row segment
+    (4, "fp16s", 128, 6, 4, (32, 2)), (4, "fp16s", 256, 3, 3, (64, 1)),
+    (4, "fp16s", 512, 2, 2, (32, 1)), (5, "fp16s", 256, 4, 3, (32, 4)),
+    (5, "fp16s", 512, 3, 2, (64, 1)), (5, "fp16s", 256, 2, 2, (32, 2)),
 ]
 
 
-PATHS = {0: "cell", 1: "pair", 2: "rows", 3: "capped"}
+PATHS = {0: "cell", 1: "pair", 2: "rows", 3: "capped", 4: "wide4", 5: "wide8"}
 
 
 @pytest.mark.parametrize("variant,precision,nx,ny,nz,shape", VARIANT_CASES)
@@ -74,7 +78,8 @@ def test_variants_agree_bitwise(gpu, precision):
     import strouhal_gb300 as sg
 
     digests = []
-    for variant, shape in ([(0, None), (1, None), (2, (256, 1)), (2, (256, 2)), (3, (64, 2))]
+    for variant, shape in ([(0, None), (1, None), (2, (256, 1)), (2, (256, 2)), (3, (64, 2)),
+                            (4, (32, 4)), (5, (32, 2)), (5, (64, 1))]
                            if precision == "fp16s" else
                            [(0, None), (2, (128, 1)), (2, (256, 4)), (3, (64, 2))]):
         s = sg.Simulation(gpu, precision=precision, nx=128, ny=40, nz=24, omega=1.95)
@@ -103,7 +108,7 @@ def test_block_split_is_bitwise_neutral(gpu, precision):
     flags[:, 0, :] = sg.Cell.solid
     eps = sg.sphereSolidFractions(nx, ny, nz, 30.5, 20.0, 12.0, 6.0, 4)
     digests = []
-    for split in (True, False):
+    for split in (True, False, "columns"):
         s = sg.Simulation(gpu, precision=precision, nx=nx, ny=ny, nz=nz, omega=1.8, uin=0.05,
                           rampSteps=10, cSmago=0.01, flags=flags.reshape(-1))
         s.inflowUniform = True
@@ -114,7 +119,7 @@ def test_block_split_is_bitwise_neutral(gpu, precision):
         s.run(13)
         digests.append(s.stateDigest)
         s.close()
-    assert digests[0] == digests[1]
+    assert digests[0] == digests[1] == digests[2]
 
 
 def _field(n_cells, seed):
