@@ -31,7 +31,7 @@ struct stro_adjoint {
     void* d_check = nullptr;   // ncheck states
     void* d_seg = nullptr;     // seg states
     float* d_lam = nullptr;
-    float* d_geps = nullptr;
+    double* d_geps = nullptr;  // dJ/d eps, summed in FP64
     float* d_gf = nullptr;
     double* d_forces = nullptr;  // 3 doubles per odd step
     uint32_t* d_lists = nullptr; // bulk blocks, then boundary blocks, of the reverse-step grid
@@ -103,7 +103,7 @@ int stro_adj_create(stro_sim* s, const double dir[3], const int32_t box[4], int6
     const uint64_t N = s->N;
     cudaError_t e = cudaMalloc(&a->d_check, a->state_bytes * size_t(a->ncheck));
     if (e == cudaSuccess) e = cudaMalloc(&a->d_lam, 19 * s->plane * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&a->d_geps, N * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&a->d_geps, N * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&a->d_gf, 3 * N * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&a->d_forces, size_t(steps / 2 + 2) * 3 * sizeof(double));
     if (e == cudaSuccess) e = cudaEventCreate(&a->e0);
@@ -211,7 +211,7 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
         STRO_CUDA(cudaMalloc(&a->d_seg, a->state_bytes * size_t(a->seg)));
     const int geo = geo_on(s) ? 1 : 0;
     STRO_CUDA(cudaMemsetAsync(a->d_lam, 0, 19 * s->plane * sizeof(float), st));
-    STRO_CUDA(cudaMemsetAsync(a->d_geps, 0, N * sizeof(float), st));
+    STRO_CUDA(cudaMemsetAsync(a->d_geps, 0, N * sizeof(double), st));
     STRO_CUDA(cudaMemsetAsync(a->d_gf, 0, 3 * N * sizeof(float), st));
     const float w = a->nodd ? float(1.0 / double(a->nodd)) : 0.0f;
     const dim3 ablock(32, 4, 1);
@@ -287,10 +287,18 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
         if (rc != STRO_OK) return rc;
     }
     (void)live;
-    if (grad_eps)
-        STRO_CUDA(cudaMemcpy(grad_eps, a->d_geps, N * sizeof(float), cudaMemcpyDeviceToHost));
-    if (grad_force)
-        STRO_CUDA(cudaMemcpy(grad_force, a->d_gf, 3 * N * sizeof(float), cudaMemcpyDeviceToHost));
+    if (grad_eps) {
+        std::vector<double> ge(N);
+        STRO_CUDA(cudaMemcpyAsync(ge.data(), a->d_geps, N * sizeof(double), cudaMemcpyDeviceToHost,
+                                  st));
+        STRO_CUDA(cudaStreamSynchronize(st));
+        for (uint64_t k = 0; k < N; ++k) grad_eps[k] = float(ge[k]);
+    }
+    if (grad_force) {
+        STRO_CUDA(cudaMemcpyAsync(grad_force, a->d_gf, 3 * N * sizeof(float),
+                                  cudaMemcpyDeviceToHost, st));
+        STRO_CUDA(cudaStreamSynchronize(st));
+    }
     return STRO_OK;
 }
 

@@ -302,9 +302,14 @@ __device__ __forceinline__ void cell_force_any(const StepArgs& a, uint32_t n, fl
     }
 }
 
+// The solid-fraction gradient is summed in FP64: a cell's per-step terms can
+// be far larger than their sum over a long window (inside a fully solid body
+// the adjoint is bounced without damping and grows with the window), and an
+// FP32 running sum would lose the result's leading digits. Only cells with a
+// solid fraction touch the array, so the FP64 adds cost nothing measurable.
 __device__ __forceinline__ void add_grads(const AdjArgs& g, uint32_t n, float eps, float epsb,
                                           float Fbx, float Fby, float Fbz) {
-    if (g.grad_eps != nullptr && eps != 0.0f) g.grad_eps[n] += epsb;
+    if (g.grad_eps != nullptr && eps != 0.0f) g.grad_eps[n] += double(epsb);
     if (g.grad_f != nullptr) {
         const uint32_t N = g.a.ffield_plane;
         g.grad_f[n] += Fbx;

@@ -10,7 +10,7 @@ namespace stro {
 struct AdjArgs {
     StepArgs a;         // forward arguments of the step; a.f = the stored input state of the step
     float* lam;         // adjoint of the state, 19 planes, plane stride a.plane (FP32)
-    float* grad_eps;    // dJ/d eps (N), or null
+    double* grad_eps;   // dJ/d eps (N), or null: summed in FP64 (see add_grads)
     float* grad_f;      // dJ/d F_field (3 planes of a.ffield_plane), or null
     float obj_w;        // weight of this step's force in J (odd steps), 0 = none
     float dir[3];       // force direction of the objective

@@ -132,7 +132,7 @@ def cylinder_crop(sg, po, gpu, precision, spinup=30000):
 
 # ------------------------------------------------------------------ the checks
 def run_checks(sg, o, g, f0, box, eps, ff, window, precision, fd_eps=8, fd_force=8, seed=5,
-               threads=None, h_eps=2.0 ** -12, h_force=2.0 ** -16):
+               threads=None, h_eps=2.0 ** -12, h_force=2.0 ** -16, fd_solid=2):
     """The three comparisons; returns a dict of errors and timings."""
     out = {"window": window, "precision": precision, "cells": int(g.cells)}
     ck = max(1, int(math.ceil(math.sqrt(window))))
@@ -155,6 +155,9 @@ def run_checks(sg, o, g, f0, box, eps, ff, window, precision, fd_eps=8, fd_force
     out["J_same_trajectory"] = Jt
     out["J_rel_err"] = abs(J - Jt) / max(abs(Jt), 1e-300)
     out["grad_eps_rel_err"] = rel(ge[nt], get[nt])
+    surf, full = nt & (eps < 1), eps == 1
+    out["grad_eps_rel_err_surface"] = rel(ge[surf], get[surf])
+    out["grad_eps_rel_err_solid"] = rel(ge[full], get[full]) if full.any() else None
     out["grad_eps_zero_off_nt"] = bool(np.all(ge[~nt] == 0))
     out["grad_force_rel_err"] = rel(gf, gft)
     t = time.perf_counter()
@@ -184,6 +187,23 @@ def run_checks(sg, o, g, f0, box, eps, ff, window, precision, fd_eps=8, fd_force
             d = (vals[0] - vals[1]) / h
             fd.append({"param": "eps", "cell": int(n), "fd": d, "fp64_adjoint": float(ge64[n]),
                        "gpu_adjoint": float(ge[n])})
+    # Fully solid cells (eps = 1): eps > 1 is outside the model (the blend
+    # factor B exceeds 1 and the cell amplifies its non-equilibrium), so the
+    # difference there is one-sided, second order: (3 J(1) - 4 J(1-h) + J(1-2h)) / 2h.
+    full_cand = np.flatnonzero(eps == 1)
+    if fd_solid and full_cand.size:
+        mag = np.abs(ge64[full_cand])
+        for n in full_cand[np.argsort(-mag)][:fd_solid]:
+            vals = []
+            for k in (1, 2):
+                e = eps.copy()
+                e[n] = np.float32(1.0 - k * h_eps)
+                o.setSolidFractions(e)
+                vals.append(o.adjointForce(window, box, grads=False, f0=f0, threads=threads)[0])
+            o.setSolidFractions(eps)
+            d = (3.0 * J64 - 4.0 * vals[0] + vals[1]) / (2.0 * h_eps)
+            fd.append({"param": "eps_solid", "cell": int(n), "fd": d,
+                       "fp64_adjoint": float(ge64[n]), "gpu_adjoint": float(ge[n])})
     if fd_force and ff is not None:
         mag = np.sqrt((gf64 ** 2).sum(0))
         f_cand = np.flatnonzero(mag >= 0.1 * mag.max())

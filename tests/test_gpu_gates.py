@@ -61,7 +61,7 @@ OBS_BARS = {
     "fp32": {"kinetic_energy": 1e-5, "dissipation_sum": 1e-4, "eps_dEdt": 1e-4,
              "drag_coefficient": 1e-5, "lift_coefficient_over_max_cd": 1e-5},
     "fp16s": {"kinetic_energy": 5e-3, "dissipation_sum": 5e-2, "eps_dEdt": 5e-2,
-              "drag_coefficient": 5e-3, "lift_coefficient_over_max_cd": 5e-3},
+              "drag_coefficient": 1e-2, "lift_coefficient_over_max_cd": 1e-2},
 }
 DDF_BARS = {"fp32": 1e-5, "fp16s": 2e-3}
 
