@@ -106,6 +106,8 @@ constexpr uint32_t GEO_NONFLUID = 1u << 31;
 struct StepArgs {
     void* f;                  // DDF planes (Store*), plane stride `plane` elements
     uint64_t plane;           // plane stride in elements (>= N, padded)
+    uint32_t poff[19];        // i * plane: element offset of plane i (0 when 19 planes do
+                              // not fit 2^32 elements; read only by kernels that require it)
     int32_t nx, ny, nz;
     const uint8_t* cell;      // N cell bytes (walls or eps present)
     const uint32_t* geo;      // N geometry words

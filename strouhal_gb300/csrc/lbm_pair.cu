@@ -124,19 +124,21 @@ __global__ void __launch_bounds__(256, FEAT == 2 ? 2 : 4) k_pair_even(const Step
     const int y = int(blockIdx.y);  // one row per block: y and z are block-uniform
     const int z = int(blockIdx.z);
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
-    // per-thread base pointer plus block-uniform plane offsets (32-bit: 19
-    // planes < 2^32 elements)
-    __half2* __restrict__ f2n = static_cast<__half2*>(a.f) + n / 2;
-    const uint32_t P2 = uint32_t(a.plane / 2);
+    // per-thread base pointer plus the plane offsets of the launch arguments
+    // (constants: one wide multiply-add per address, nothing computed per block)
+    const __half* __restrict__ fn = static_cast<const __half*>(a.f) + n;
     __half2 v[19];
-    sfor<0, 19>([&](auto I) { v[I] = f2n[uint32_t(I) * P2]; });
+    sfor<0, 19>([&](auto I) { v[I] = *reinterpret_cast<const __half2*>(fn + a.poff[I]); });
     __half2 ao[10];
     float fh[19];
     collide_pair<FEAT>(v, ao, fh, a, x, n);
-    forget(f2n);
+    uint32_t m = n;
+    forget_u32(m);
+    __half* __restrict__ fq = static_cast<__half*>(a.f) + m;
     // direction i of both cells goes to slot opp(i)
     sfor<0, 19>([&](auto I) {
-        f2n[uint32_t(opp(I)) * P2] = __halves2half2(out_lo<I>(ao), __float2half_rn(fh[I]));
+        *reinterpret_cast<__half2*>(fq + a.poff[opp(I)]) =
+            __halves2half2(out_lo<I>(ao), __float2half_rn(fh[I]));
     });
 }
 
@@ -171,28 +173,28 @@ struct PairRows {
 __device__ __forceinline__ void scatter_pair(const StepArgs& a, const __half2 (&ao)[10],
                                              const float (&fh)[19], int x, const PairRows& rows) {
     forget_int(x);
-    const uint32_t nx = uint32_t(a.nx), hnx = nx / 2;
-    const uint32_t P = uint32_t(a.plane), P2 = P / 2;
-    __half2* __restrict__ f2x = static_cast<__half2*>(a.f) + x / 2;
+    const uint32_t nx = uint32_t(a.nx);
     __half* __restrict__ f1 = static_cast<__half*>(a.f);
+    __half* __restrict__ f1x = f1 + x;                       // both cells, c_x = 0
     // x-shifted destinations of the two cells (periodic in x): x-1 and x+2 wrap
     __half* __restrict__ f1m = f1 + wrap_x(x - 1, int(nx));  // cell x,   c_x = -1
     __half* __restrict__ f1a = f1 + (x + 1);                 // cell x,   c_x = +1
     __half* __restrict__ f1b = f1 + x;                       // cell x+1, c_x = -1
     __half* __restrict__ f1p = f1 + wrap_x(x + 2, int(nx));  // cell x+1, c_x = +1
-    f2x[rows.row<0, 0>() * hnx] = __halves2half2(out_lo<0>(ao), __float2half_rn(fh[0]));
+    *reinterpret_cast<__half2*>(f1x + rows.row<0, 0>() * nx) =
+        __halves2half2(out_lo<0>(ao), __float2half_rn(fh[0]));
     sfor<1, 19>([&](auto I) {
         constexpr int i = I;
         // destination row of direction i (y, z shifted by +c_i)
         const uint32_t R = rows.row<dcy(i), dcz(i)>();
         const __half ah = out_lo<i>(ao);           // cell x, direction i
         const __half bh = __float2half_rn(fh[i]);  // cell x+1, direction i
+        const uint32_t w1 = a.poff[i] + R * nx;  // element offset of the row start
         if constexpr (dcx(i) == 0) {
-            f2x[uint32_t(i) * P2 + R * hnx] = __halves2half2(ah, bh);
+            *reinterpret_cast<__half2*>(f1x + w1) = __halves2half2(ah, bh);
         } else {
             // two 2-byte stores: the warp's stores of one direction fill a
             // contiguous 64-element span between them, no lane exchange
-            const uint32_t w1 = uint32_t(i) * P + R * nx;  // element offset of the row start
             if constexpr (dcx(i) > 0) {
                 f1a[w1] = ah;
                 f1p[w1] = bh;
@@ -207,28 +209,27 @@ __device__ __forceinline__ void scatter_pair(const StepArgs& a, const __half2 (&
 template <int FEAT>
 __global__ void __launch_bounds__(256, FEAT == 2 ? 2 : 4) k_pair_odd(const StepArgs a) {
     const int x = 2 * int(blockIdx.x * blockDim.x + threadIdx.x);
-    const uint32_t nx = uint32_t(a.nx), hnx = nx / 2;
+    const uint32_t nx = uint32_t(a.nx);
     const PairRows rows(a);
-    const uint32_t P2 = uint32_t(a.plane) / 2;
-    const __half2* __restrict__ f2 = static_cast<const __half2*>(a.f);
-    const __half2* __restrict__ f2x = f2 + x / 2;
-    const __half2* __restrict__ f2l = f2 + wrap_x(x - 2, int(nx)) / 2;  // word (x-2, x-1)
-    const __half2* __restrict__ f2r = f2 + wrap_x(x + 2, int(nx)) / 2;  // word (x+2, x+3)
+    const __half* __restrict__ f = static_cast<const __half*>(a.f);
+    const __half* __restrict__ fx = f + x;
+    const __half* __restrict__ fl = f + wrap_x(x - 2, int(nx));  // word (x-2, x-1)
+    const __half* __restrict__ fr = f + wrap_x(x + 2, int(nx));  // word (x+2, x+3)
+    auto word = [](const __half* p) { return *reinterpret_cast<const __half2*>(p); };
     __half2 v[19];
-    v[0] = f2x[rows.row<0, 0>() * hnx];
+    v[0] = word(fx + rows.row<0, 0>() * nx);
     sfor<1, 19>([&](auto I) {
         constexpr int i = I;
         constexpr int o = opp(i);
-        // source row of direction i (y, z shifted by -c_i), same x
-        const uint32_t R = rows.row<-dcy(i), -dcz(i)>();
-        const uint32_t w2 = uint32_t(o) * P2 + R * hnx;
-        const __half2 w = f2x[w2];
+        // slot opp(i) of the source row (y, z shifted by -c_i), same x
+        const uint32_t w1 = a.poff[o] + rows.row<-dcy(i), -dcz(i)>() * nx;
+        const __half2 w = word(fx + w1);
         if constexpr (dcx(i) == 0) {
             v[i] = w;
         } else if constexpr (dcx(i) > 0) {  // sources x-1, x
-            v[i] = __halves2half2(__high2half(f2l[w2]), __low2half(w));
+            v[i] = __halves2half2(__high2half(word(fl + w1)), __low2half(w));
         } else {  // sources x+1, x+2
-            v[i] = __halves2half2(__high2half(w), __low2half(f2r[w2]));
+            v[i] = __halves2half2(__high2half(w), __low2half(word(fr + w1)));
         }
     });
     const uint32_t n = rows.row<0, 0>() * nx + uint32_t(x);
@@ -276,10 +277,9 @@ __global__ void __launch_bounds__(256, V == 8 ? 2 : 3) k_wide_even(const StepArg
     const int x = V * int(blockIdx.x * blockDim.x + threadIdx.x);
     const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
     const uint32_t n = (z * uint32_t(a.ny) + y) * uint32_t(a.nx) + uint32_t(x);
-    const uint32_t P = uint32_t(a.plane);
     const __half* __restrict__ fn = static_cast<const __half*>(a.f) + n;
     WideWord<V> W[19];
-    sfor<0, 19>([&](auto I) { W[I] = load_wide<V>(fn + uint32_t(I) * P); });
+    sfor<0, 19>([&](auto I) { W[I] = load_wide<V>(fn + a.poff[I]); });
     sfor<0, V / 2>([&](auto J) {
         constexpr int j = J;
         __half2 v[19];
@@ -287,11 +287,13 @@ __global__ void __launch_bounds__(256, V == 8 ? 2 : 3) k_wide_even(const StepArg
         __half2 ao[10];
         float fh[19];
         collide_pair<FEAT>(v, ao, fh, a, x + 2 * j, n + 2 * j);
-        __half2* __restrict__ q = reinterpret_cast<__half2*>(static_cast<__half*>(a.f) + n) + j;
-        forget(q);
+        uint32_t m = n + 2 * j;
+        forget_u32(m);
+        __half* __restrict__ q = static_cast<__half*>(a.f) + m;
         // direction i of both cells goes to slot opp(i)
         sfor<0, 19>([&](auto I) {
-            q[uint32_t(opp(I)) * (P / 2)] = __halves2half2(out_lo<I>(ao), __float2half_rn(fh[I]));
+            *reinterpret_cast<__half2*>(q + a.poff[opp(I)]) =
+                __halves2half2(out_lo<I>(ao), __float2half_rn(fh[I]));
         });
     });
 }
@@ -302,7 +304,6 @@ __global__ void __launch_bounds__(256, V == 8 ? 2 : 3) k_wide_odd(const StepArgs
     const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
     const uint32_t nx = uint32_t(a.nx);
     const PairRows rows(a, y, z);
-    const uint32_t P = uint32_t(a.plane);
     const __half* __restrict__ f = static_cast<const __half*>(a.f);
     const int xl = wrap_x(x - 2, int(nx));  // word (x-2, x-1)
     const int xr = wrap_x(x + V, int(nx));  // word (x+V, x+V+1)
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(256, V == 8 ? 2 : 3) k_wide_odd(const StepArgs
     sfor<1, 19>([&](auto I) {
         constexpr int i = I;
         // slot opp(i) of the source row (y, z shifted by -c_i)
-        const __half* __restrict__ src = f + uint32_t(opp(i)) * P + rows.row<-dcy(i), -dcz(i)>() * nx;
+        const __half* __restrict__ src = f + (a.poff[opp(i)] + rows.row<-dcy(i), -dcz(i)>() * nx);
         const WideWord<V> w = load_wide<V>(src + uint32_t(x));
         if constexpr (dcx(i) == 0) {
             W[i] = w;

@@ -90,6 +90,8 @@ static void fill_step_args(const stro_sim* s, int64_t t, StepArgs* out) {
     StepArgs& a = *out;
     a.f = s->d_f;
     a.plane = s->plane;
+    const bool fits = 19 * s->plane < (uint64_t(1) << 32);
+    for (int i = 0; i < 19; ++i) a.poff[i] = fits ? uint32_t(uint64_t(i) * s->plane) : 0u;
     a.nx = s->nx; a.ny = s->ny; a.nz = s->nz;
     a.cell = s->d_cell;
     a.geo = s->d_geo;
