@@ -437,14 +437,11 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
     // what round r launches in rounds mode: the active tile prefix, and whether
     // some instance logs or probes in it
     auto round_plan = [&](int64_t r, uint32_t* active, uint32_t* nbulk, uint32_t* nedge,
-                          bool* logs, bool* probing, int* parity) {
+                          bool* logs, bool* probing) {
         *active = *nbulk = *nedge = 0;
         *logs = *probing = false;
-        *parity = -2;
         for (size_t k = 0; k < n; ++k) {
             if (inst[k].steps <= r) break;
-            const int p = int((inst[k].t0 + r) & 1);
-            *parity = (*parity == -2 || *parity == p) ? p : -1;
             *active = inst[k].tile_begin + inst[k].ntiles;
             *nbulk = bulk_end[k];
             *nedge = edge_end[k];
@@ -461,14 +458,13 @@ int run_fused(stro_batch* b, const int64_t* steps, const int32_t* log_every,
         for (int64_t r = 0; r < max_steps && le == cudaSuccess; ++r) {
             uint32_t active, nbulk, nedge;
             bool logs, probing;
-            int parity;
-            round_plan(r, &active, &nbulk, &nedge, &logs, &probing, &parity);
+            round_plan(r, &active, &nbulk, &nedge, &logs, &probing);
             if (split)
                 le = launch_batch_round_lists(args, b->half, feat, probing ? 1 : 0, r, b->d_tiles,
                                               nbulk, b->d_tiles + nbulk_total, nedge, b->block, st);
             else
-                le = launch_batch_round(args, b->half, geo, feat, probing ? 1 : 0,
-                                        parity < 0 ? -1 : parity, r, active, b->block, st);
+                le = launch_batch_round(args, b->half, geo, feat, probing ? 1 : 0, r, active,
+                                        b->block, st);
             if (le == cudaSuccess && (logs || probing)) le = launch_batch_fold(args, r, st);
         }
         return le;

@@ -70,10 +70,7 @@ __device__ __forceinline__ bool probes_at(const BatchInstance& I, int64_t r) {
     return d % I.probe_period == 0 && d / I.probe_period < I.probe_count;
 }
 
-// PAR: the parity of this round when the launch knows it for every instance
-// (0 even, 1 odd; the other pass is then not compiled in, and the kernel keeps
-// the register budget of its own pass), -1 when instances differ.
-template <typename S, int GEO, int FEAT, bool PROBES, bool CG, int PAR = -1>
+template <typename S, int GEO, int FEAT, bool PROBES, bool CG>
 __device__ __forceinline__ void process_tile(const BatchArgs& b, const BatchInstance& I,
                                              uint32_t tile, int64_t r) {
     const uint32_t tl = tile - I.tile_begin;
@@ -95,8 +92,7 @@ __device__ __forceinline__ void process_tile(const BatchArgs& b, const BatchInst
         y = int(t - zz * uint32_t(I.a.ny));
         z = int(zz);
     }
-    const bool even = PAR >= 0 ? PAR == 0 : ((I.t0 + r) & 1) == 0;
-    if (PAR != 1 && even) {
+    if (((I.t0 + r) & 1) == 0) {
         if (logs_at(I, r)) {
             float u2 = 0.0f;
             if (in) even_cell<S, GEO, FEAT, true, CG>(I.a, x, y, z, &u2);
@@ -105,7 +101,7 @@ __device__ __forceinline__ void process_tile(const BatchArgs& b, const BatchInst
         } else if (in) {
             even_cell<S, GEO, FEAT, false, CG>(I.a, x, y, z);
         }
-    } else if (PAR != 0) {
+    } else {
         if constexpr (PROBES) {
             if (probes_at(I, r)) {
                 double c[3] = {0.0, 0.0, 0.0};
@@ -221,12 +217,11 @@ __global__ void __launch_bounds__(256) k_batch_persistent(const BatchArgs b) {
     if (blockIdx.x == 0 && b.max_steps > 0) fold_round(b, b.max_steps - 1);
 }
 
-template <typename S, int GEO, int FEAT, bool PROBES, int PAR>
-__global__ void __launch_bounds__(256, GEO == 0 && FEAT == 0 ? 4 : 0)
-    k_batch_round(const BatchArgs b, int64_t r) {
+template <typename S, int GEO, int FEAT, bool PROBES>
+__global__ void __launch_bounds__(256) k_batch_round(const BatchArgs b, int64_t r) {
     const uint32_t tile = blockIdx.x;
     const BatchInstance I = tile_instance(b, tile);
-    process_tile<S, GEO, FEAT, PROBES, false, PAR>(b, I, tile, r);
+    process_tile<S, GEO, FEAT, PROBES, false>(b, I, tile, r);
 }
 
 // Rounds over a tile list: block i processes tile list[i]. The bulk tiles of
@@ -269,20 +264,12 @@ const void* pick_persistent(int geo, int feat, int probes) {
                      : (feat == 1 ? persistent_fn<S, 0, 1, false>() : persistent_fn<S, 0, 0, false>());
 }
 
-template <typename S, int GEO, bool PROBES, int PAR>
-void launch_round_par(const BatchArgs& b, int feat, int64_t r, uint32_t tiles, dim3 block,
-                      cudaStream_t st) {
-    if (feat == 2) k_batch_round<S, GEO, 2, PROBES, PAR><<<tiles, block, 0, st>>>(b, r);
-    else if (feat == 1) k_batch_round<S, GEO, 1, PROBES, PAR><<<tiles, block, 0, st>>>(b, r);
-    else k_batch_round<S, GEO, 0, PROBES, PAR><<<tiles, block, 0, st>>>(b, r);
-}
-
 template <typename S, int GEO, bool PROBES>
-void launch_round_feat(const BatchArgs& b, int feat, int parity, int64_t r, uint32_t tiles,
-                       dim3 block, cudaStream_t st) {
-    if (parity == 0) launch_round_par<S, GEO, PROBES, 0>(b, feat, r, tiles, block, st);
-    else if (parity == 1) launch_round_par<S, GEO, PROBES, 1>(b, feat, r, tiles, block, st);
-    else launch_round_par<S, GEO, PROBES, -1>(b, feat, r, tiles, block, st);
+void launch_round_feat(const BatchArgs& b, int feat, int64_t r, uint32_t tiles, dim3 block,
+                       cudaStream_t st) {
+    if (feat == 2) k_batch_round<S, GEO, 2, PROBES><<<tiles, block, 0, st>>>(b, r);
+    else if (feat == 1) k_batch_round<S, GEO, 1, PROBES><<<tiles, block, 0, st>>>(b, r);
+    else k_batch_round<S, GEO, 0, PROBES><<<tiles, block, 0, st>>>(b, r);
 }
 
 template <typename S, int GEO, bool PROBES>
@@ -309,11 +296,11 @@ cudaError_t launch_lists_typed(const BatchArgs& b, int feat, int probes, int64_t
 }
 
 template <typename S>
-cudaError_t launch_round_typed(const BatchArgs& b, int geo, int feat, int probes, int parity,
-                               int64_t r, uint32_t tiles, dim3 block, cudaStream_t st) {
-    if (geo && probes) launch_round_feat<S, 1, true>(b, feat, -1, r, tiles, block, st);
-    else if (geo) launch_round_feat<S, 1, false>(b, feat, parity, r, tiles, block, st);
-    else launch_round_feat<S, 0, false>(b, feat, parity, r, tiles, block, st);
+cudaError_t launch_round_typed(const BatchArgs& b, int geo, int feat, int probes, int64_t r,
+                               uint32_t tiles, dim3 block, cudaStream_t st) {
+    if (geo && probes) launch_round_feat<S, 1, true>(b, feat, r, tiles, block, st);
+    else if (geo) launch_round_feat<S, 1, false>(b, feat, r, tiles, block, st);
+    else launch_round_feat<S, 0, false>(b, feat, r, tiles, block, st);
     return cudaGetLastError();
 }
 
@@ -342,12 +329,10 @@ cudaError_t launch_batch_persistent(const BatchArgs& b, int half_storage, int ge
 }
 
 cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, int feat, int probes,
-                               int parity, int64_t r, uint32_t tiles, dim3 block,
-                               cudaStream_t st) {
+                               int64_t r, uint32_t tiles, dim3 block, cudaStream_t st) {
     if (tiles == 0) return cudaSuccess;
-    return half_storage
-               ? launch_round_typed<__half>(b, geo, feat, probes, parity, r, tiles, block, st)
-               : launch_round_typed<float>(b, geo, feat, probes, parity, r, tiles, block, st);
+    return half_storage ? launch_round_typed<__half>(b, geo, feat, probes, r, tiles, block, st)
+                        : launch_round_typed<float>(b, geo, feat, probes, r, tiles, block, st);
 }
 
 cudaError_t launch_batch_round_lists(const BatchArgs& b, int half_storage, int feat, int probes,

@@ -73,11 +73,8 @@ struct BatchArgs {
 // only; the probe-capable kernels are used then).
 cudaError_t launch_batch_persistent(const BatchArgs& b, int half_storage, int geo, int feat,
                                     int probes, unsigned grid, dim3 block, cudaStream_t st);
-// parity: 0 / 1 when every active instance takes the even / odd pass in round
-// r (the launch then runs a kernel of that pass alone), -1 otherwise.
 cudaError_t launch_batch_round(const BatchArgs& b, int half_storage, int geo, int feat, int probes,
-                               int parity, int64_t r, uint32_t tiles, dim3 block,
-                               cudaStream_t st);
+                               int64_t r, uint32_t tiles, dim3 block, cudaStream_t st);
 // One round over two tile lists of a walled batch: `bulk` tiles on the
 // wall-free kernels, `edge` tiles on the wall-aware ones (each list the
 // active prefix of its instance-ordered tiles).

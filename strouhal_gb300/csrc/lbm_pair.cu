@@ -124,21 +124,21 @@ __global__ void __launch_bounds__(256, FEAT == 2 ? 2 : 4) k_pair_even(const Step
     const int y = int(blockIdx.y);  // one row per block: y and z are block-uniform
     const int z = int(blockIdx.z);
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
-    // per-thread base pointer plus the plane offsets of the launch arguments
-    // (constants: one wide multiply-add per address, nothing computed per block)
-    const __half* __restrict__ fn = static_cast<const __half*>(a.f) + n;
+    // per-thread base pointer plus block-uniform plane offsets (32-bit: 19
+    // planes < 2^32 elements). Taking the offsets from the launch constants
+    // (StepArgs::poff, as the odd pass does) cut this pass's instructions by 15%
+    // but made it 3.6% slower: the constant loads sit ahead of the DDF loads.
+    __half2* __restrict__ f2n = static_cast<__half2*>(a.f) + n / 2;
+    const uint32_t P2 = uint32_t(a.plane / 2);
     __half2 v[19];
-    sfor<0, 19>([&](auto I) { v[I] = *reinterpret_cast<const __half2*>(fn + a.poff[I]); });
+    sfor<0, 19>([&](auto I) { v[I] = f2n[uint32_t(I) * P2]; });
     __half2 ao[10];
     float fh[19];
     collide_pair<FEAT>(v, ao, fh, a, x, n);
-    uint32_t m = n;
-    forget_u32(m);
-    __half* __restrict__ fq = static_cast<__half*>(a.f) + m;
+    forget(f2n);
     // direction i of both cells goes to slot opp(i)
     sfor<0, 19>([&](auto I) {
-        *reinterpret_cast<__half2*>(fq + a.poff[opp(I)]) =
-            __halves2half2(out_lo<I>(ao), __float2half_rn(fh[I]));
+        f2n[uint32_t(opp(I)) * P2] = __halves2half2(out_lo<I>(ao), __float2half_rn(fh[I]));
     });
 }
 

@@ -132,7 +132,8 @@ def cylinder_crop(sg, po, gpu, precision, spinup=30000):
 
 # ------------------------------------------------------------------ the checks
 def run_checks(sg, o, g, f0, box, eps, ff, window, precision, fd_eps=8, fd_force=8, seed=5,
-               threads=None, h_eps=2.0 ** -12, h_force=2.0 ** -16, fd_solid=2):
+               threads=None, h_eps=2.0 ** -12, h_force=2.0 ** -16, fd_solid=2,
+               h_solid=2.0 ** -22):
     """The three comparisons; returns a dict of errors and timings."""
     out = {"window": window, "precision": precision, "cells": int(g.cells)}
     ck = max(1, int(math.ceil(math.sqrt(window))))
@@ -190,6 +191,10 @@ def run_checks(sg, o, g, f0, box, eps, ff, window, precision, fd_eps=8, fd_force
     # Fully solid cells (eps = 1): eps > 1 is outside the model (the blend
     # factor B exceeds 1 and the cell amplifies its non-equilibrium), so the
     # difference there is one-sided, second order: (3 J(1) - 4 J(1-h) + J(1-2h)) / 2h.
+    # Its step is far smaller: below eps = 1 the cell's frozen non-equilibrium
+    # relaxes at a rate of about B'(1) h omega per step (B'(1) = (1 + tw) / tw,
+    # 14 at tau = 0.577), so J is linear in h only while the window times that
+    # rate is small; h = 2^-22 keeps it below 1e-2 for 2,000 steps.
     full_cand = np.flatnonzero(eps == 1)
     if fd_solid and full_cand.size:
         mag = np.abs(ge64[full_cand])
@@ -197,11 +202,11 @@ def run_checks(sg, o, g, f0, box, eps, ff, window, precision, fd_eps=8, fd_force
             vals = []
             for k in (1, 2):
                 e = eps.copy()
-                e[n] = np.float32(1.0 - k * h_eps)
+                e[n] = np.float32(1.0 - k * h_solid)
                 o.setSolidFractions(e)
                 vals.append(o.adjointForce(window, box, grads=False, f0=f0, threads=threads)[0])
             o.setSolidFractions(eps)
-            d = (3.0 * J64 - 4.0 * vals[0] + vals[1]) / (2.0 * h_eps)
+            d = (3.0 * J64 - 4.0 * vals[0] + vals[1]) / (2.0 * h_solid)
             fd.append({"param": "eps_solid", "cell": int(n), "fd": d,
                        "fp64_adjoint": float(ge64[n]), "gpu_adjoint": float(ge[n])})
     if fd_force and ff is not None:
