@@ -55,6 +55,7 @@ STEPS_PER_BENCH_STEP = 100
 ALG_BYTES = {"fp32": 152, "fp16s": 76}  # 19 reads + 19 writes per cell per step
 # Kernels of each launch path (Simulation.lastPath), named as in the launch list.
 KERNEL_NAMES = {"cell": "k_step_even/k_step_odd", "pair": "k_pair_even/k_pair_odd",
+                "wide4": "k_wide_even<4>/k_wide_odd<4>", "wide8": "k_wide_even<8>/k_wide_odd<8>",
                 "rows": "k_rows<even>/k_rows<odd>",
                 "capped": "k_step_even_capped/k_step_odd_capped"}
 

@@ -203,7 +203,7 @@ __device__ bool grid_barrier(BatchCtl* ctl, unsigned& gen, long long spin_limit,
 }
 
 template <typename S, int GEO, int FEAT, bool PROBES>
-__global__ void __launch_bounds__(256, GEO == 0 && FEAT == 0 ? 4 : 0) k_batch_persistent(const BatchArgs b) {
+__global__ void __launch_bounds__(256) k_batch_persistent(const BatchArgs b) {
     unsigned gen = 0;
     for (int64_t r = 0; r < b.max_steps; ++r) {
         if (blockIdx.x == 0 && r > 0) fold_round(b, r - 1);
