@@ -216,6 +216,10 @@ int stro_sim_get_pair_block(stro_sim* sim, int32_t* bx, int32_t* by);
  * "" before the first step. A lattice a variant does not apply to reports the
  * path that ran instead. */
 int stro_sim_last_path(stro_sim* sim, char* buf, size_t len);
+/* Block counts of the lists the "split" path last ran: bulk (wall-free
+ * kernels), x-face and boundary (wall-aware kernels) blocks; all 0 before the
+ * split first ran. No reference counterpart. */
+int stro_sim_split_blocks(const stro_sim* sim, int64_t* bulk, int64_t* face, int64_t* edge);
 /* Launch shape of variant 2: `threads` computing threads per block (a
  * multiple of 32, at most 256; one more warp issues the copies) and `rows`
  * lattice rows per tile (1 to 8). */
@@ -228,12 +232,14 @@ int stro_sim_get_rows_tile(stro_sim* sim, int32_t* threads, int32_t* rows);
  * wait (exercises that path). No reference counterpart. */
 int stro_sim_set_spin_limit(stro_sim* sim, int64_t polls);
 /* Walled lattices run their bulk blocks (cells with no wall neighbour and no
- * solid fraction) with the wall-free kernels and only the boundary blocks
- * with the wall-aware ones (1, the default); 2 does the same with the
- * boundary blocks' odd pass in column-major cell order (a warp covers whole
- * columns of its block, so a column of cells next to an inflow wall runs the
- * moving-wall code in warps of its own); 0 runs the wall-aware kernels on
- * every block. Results are identical in every mode. */
+ * solid fraction) with the wall-free kernels, the blocks whose only walls are
+ * velocity-inflow columns at x = 0 and x = nx - 1 with x-face kernels (the
+ * wall links follow from x; no geometry is read), and only the other
+ * boundary blocks with the wall-aware ones (1, the default); 2 does the same
+ * with the boundary blocks' odd pass in column-major cell order (a warp
+ * covers whole columns of its block); 3 is 1 without the x-face blocks (they
+ * run the wall-aware kernels); 0 runs the wall-aware kernels on every block.
+ * Results are identical in every mode. */
 int stro_sim_set_block_split(stro_sim* sim, int32_t enabled);
 /* stro_sim_run and stro_sim_run_sampled replay CUDA graphs of plain steps once
  * the ramp is over (default on): the launches of a run of steps are captured

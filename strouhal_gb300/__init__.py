@@ -143,6 +143,7 @@ def lib():
         "stro_sim_set_pair_block": ([_P, ctypes.c_int32, ctypes.c_int32], c_int),
         "stro_sim_get_pair_block": ([_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_last_path": ([_P, ctypes.c_char_p, ctypes.c_size_t], c_int),
+        "stro_sim_split_blocks": ([_P, _P, _P, _P], c_int),
         "stro_sim_get_arithmetic": ([_P, ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_get_rows_tile": ([_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)], c_int),
         "stro_sim_set_block_split": ([_P, ctypes.c_int32], c_int),
@@ -612,6 +613,14 @@ class Simulation:
         return buf.value.decode()
 
     @property
+    def splitBlocks(self):
+        """(bulk, x-face, boundary) block counts of the split's last lists."""
+        bu, fa, ed = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().stro_sim_split_blocks(self._h, ctypes.byref(bu), ctypes.byref(fa),
+                                           ctypes.byref(ed)))
+        return bu.value, fa.value, ed.value
+
+    @property
     def rowsTile(self):
         """(threads per block, lattice rows per tile) of the row-staged variant 2."""
         t, r = ctypes.c_int32(), ctypes.c_int32()
@@ -627,9 +636,14 @@ class Simulation:
         _check(lib().stro_sim_set_spin_limit(self._h, int(polls)))
 
     def setBlockSplit(self, enabled):
-        """Bulk blocks of a walled lattice on the wall-free kernels (default True);
-        "columns" also orders the boundary blocks' odd pass column by column."""
-        mode = 2 if enabled == "columns" else int(bool(enabled))
+        """Bulk blocks of a walled lattice on the wall-free kernels and blocks at
+        velocity-inflow x faces on the x-face kernels (default True); "columns"
+        also orders the boundary blocks' odd pass column by column; "noface"
+        runs the x-face blocks on the wall-aware kernels."""
+        mode = {"columns": 2, "noface": 3}.get(enabled) if isinstance(enabled, str) \
+            else int(bool(enabled))
+        if mode is None:
+            raise ValueError("block split: True, False, 'columns' or 'noface'")
         _check(lib().stro_sim_set_block_split(self._h, mode))
 
     def setGraphs(self, enabled):

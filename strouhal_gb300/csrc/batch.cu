@@ -924,9 +924,10 @@ int stro_sim_set_variant(stro_sim* s, int32_t variant) {
 
 int stro_sim_set_block_split(stro_sim* s, int32_t enabled) {
     if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
-    if (enabled < 0 || enabled > 2) return fail(STRO_ERR_INVALID, "split must be 0, 1 or 2");
+    if (enabled < 0 || enabled > 3) return fail(STRO_ERR_INVALID, "split must be 0, 1, 2 or 3");
     s->split = enabled != 0;
     s->edge_colmajor = enabled == 2;
+    s->face_lists = enabled != 3;
     return STRO_OK;
 }
 
@@ -955,6 +956,14 @@ int stro_sim_get_pair_block(stro_sim* s, int32_t* bx, int32_t* by) {
 int stro_sim_last_path(stro_sim* s, char* buf, size_t len) {
     if (!s || !buf || !len) return fail(STRO_ERR_INVALID, "null argument");
     std::snprintf(buf, len, "%s", s->last_path);
+    return STRO_OK;
+}
+
+int stro_sim_split_blocks(const stro_sim* s, int64_t* bulk, int64_t* face, int64_t* edge) {
+    if (!s || !bulk || !face || !edge) return fail(STRO_ERR_INVALID, "null argument");
+    *bulk = s->nbulk;
+    *face = s->nface;
+    *edge = s->nedge;
     return STRO_OK;
 }
 
@@ -1060,12 +1069,15 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
     const bool saved_split = s->split;
     bool best_split = saved_split;
     bool best_col = s->edge_colmajor;
+    bool best_face = s->face_lists;
     const int geo = geo_on(s) ? 1 : 0;
-    // split 2: the split with the boundary blocks' odd pass in column-major order
-    for (int split : {1, 2, 0}) {
+    // split 2: the split with the boundary blocks' odd pass in column-major
+    // order; 3: the split without x-face blocks
+    for (int split : {1, 2, 3, 0}) {
         if (split != 1 && !geo) break;  // the split only exists for walled lattices
         s->split = split != 0;
         s->edge_colmajor = split == 2;
+        s->face_lists = split != 3;
         for (int variant : {0, 1, 2, 3, 4, 5}) {
             const dim3* shapes = variant == 2 ? kRowShapes : kShapes;
             const size_t nshapes = variant == 2 ? sizeof(kRowShapes) / sizeof(dim3)
@@ -1095,12 +1107,14 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
                     best_variant = variant;
                     best_split = s->split;
                     best_col = s->edge_colmajor;
+                    best_face = s->face_lists;
                 }
             }
         }
     }
     s->split = best_split;
     s->edge_colmajor = best_col;
+    s->face_lists = best_face;
     e = cudaMemcpyAsync(s->d_f, saved, bytes, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     cudaFree(saved);

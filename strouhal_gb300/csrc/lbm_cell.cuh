@@ -675,13 +675,19 @@ __device__ __forceinline__ void forget_ptr(P& p) {
 // skipped. With LOG, u2 receives |u|^2 of the state before the step.
 // OUT: honour StepArgs::f_out (out-of-place pass); on by default where the
 // lattice has walls, and for the block-list kernels of the bulk / boundary split.
+// GEO 2 (blocks of the x-face list, see odd_cell_xface): the non-fluid cells
+// are the columns x = 0 and x = nx - 1 and no cell is partially saturated, so
+// no cell byte is read.
 template <typename S, int GEO, int FEAT, bool LOG = false, bool CG = false,
           int ARITH = ARITH_REFERENCE, bool OUT = (GEO != 0)>
 __device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z,
                                           float* u2 = nullptr) {
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
     float eps = 0.0f;
-    if constexpr (GEO) {
+    if constexpr (GEO == 2) {
+        if (x == 0 || x == a.nx - 1) return;
+    }
+    if constexpr (GEO == 1) {
         const uint8_t c = a.cell[n];
         if (c & CELL_TYPE_MASK) return;
         if constexpr (FEAT) {
@@ -809,6 +815,78 @@ __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, i
             contrib[2] = (double)az;
         }
     }
+}
+
+// Odd pass of one cell of an x-face block: a block whose only walls are
+// velocity-inflow columns at x = 0 and x = nx - 1, every link of a cell at
+// x = 1 (x = nx - 2) toward x = 0 (x = nx - 1) a moving-wall link and no other
+// link a wall link, and no cell partially saturated (the host checks this cell
+// by cell before it lists the block). The wall links then follow from x alone:
+// no geometry word, moving-link mask or wall cell byte is read. The values are
+// the ones odd_cell computes for these cells (the same gather, moving-wall
+// corrections of Kernels.metal:292-314 and 317-350, collision and scatter);
+// inflow walls take no outflow terms.
+template <typename S, int FEAT, int ARITH = ARITH_REFERENCE>
+__device__ __forceinline__ void odd_cell_xface(const StepArgs& a, const WallVel& wv, int x, int y,
+                                               int z) {
+    if (x == 0 || x == a.nx - 1) return;
+    const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
+    const bool wl = x == 1, wr = x == a.nx - 2;  // next to the x = 0 / x = nx - 1 wall
+    S* __restrict__ f = static_cast<S*>(a.f);
+    const uint64_t P = a.plane;
+    const NbrOffsets nb(x, y, z, a.nx, a.ny, a.nz);
+    float fh[19];
+    fh[0] = load_slot<S, false>(f + n);
+    sfor<1, 19>([&](auto I) {
+        constexpr int i = I;
+        constexpr int o = opp(i);
+        const uint32_t src = uint32_t(int(n) + nb.template off<-dcx(i), -dcy(i), -dcz(i)>());
+        if constexpr (dcx(i) == 0) {
+            fh[i] = load_slot<S, false>(f + uint64_t(o) * P + src);
+        } else {
+            // n - c_i lies in a wall column: the link reflects within the cell
+            const bool bb = dcx(i) > 0 ? wl : wr;
+            fh[i] = load_slot<S, false>(f + (bb ? uint64_t(i) * P + n : uint64_t(o) * P + src));
+        }
+    });
+    if (wl || wr) {
+        sfor<1, 19>([&](auto I) {
+            constexpr int i = I;
+            if constexpr (dcx(i) != 0) {
+                if (dcx(i) > 0 ? wl : wr) {
+                    float uwx, uwy, uwz;
+                    wall_velocity(CELL_INFLOW, wrapi(y - dcy(i), a.ny), a, wv, uwx, uwy, uwz);
+                    const float corr = 6.0f * wgt(i) * cdot<i>(uwx, uwy, uwz);
+                    fh[i] += corr;
+                }
+            }
+        });
+    }
+    float Fx = 0.f, Fy = 0.f, Fz = 0.f;
+    cell_force<FEAT>(a, n, Fx, Fy, Fz);
+    float ntx = 0.f, nty = 0.f, ntz = 0.f;
+    collide<FEAT, ARITH>(fh, a, x, 0.0f, Fx, Fy, Fz, ntx, nty, ntz);
+    forget_ptr(f);
+    if (a.f_out != nullptr) f = static_cast<S*>(a.f_out);
+    store_ddf<S>(f + n, fh[0]);
+    sfor<1, 19>([&](auto I) {
+        constexpr int i = I;
+        const uint32_t dst = uint32_t(int(n) + nb.template off<dcx(i), dcy(i), dcz(i)>());
+        if constexpr (dcx(i) == 0) {
+            store_ddf<S>(f + uint64_t(i) * P + dst, fh[i]);
+        } else {
+            // n + c_i lies in a wall column: store into the cell's own opposite slot
+            const bool bb = dcx(i) < 0 ? wl : wr;
+            float out = fh[i];
+            if (bb) {
+                float uwx, uwy, uwz;
+                wall_velocity(CELL_INFLOW, wrapi(y + dcy(i), a.ny), a, wv, uwx, uwy, uwz);
+                const float corr = 6.0f * wgt(i) * cdot<i>(uwx, uwy, uwz);
+                out = fh[i] - corr;
+            }
+            store_ddf<S>(f + (bb ? uint64_t(opp(i)) * P + n : uint64_t(i) * P + dst), out);
+        }
+    });
 }
 
 }  // namespace stro

@@ -24,17 +24,19 @@ struct StepLaunchers {
     // Register-capped one-cell kernels for periodic lattices (block <= 128 threads).
     cudaError_t (*capped)(const StepArgs& a, int half_storage, int parity, int feat, dim3 block,
                           cudaStream_t st);
-    // One pass split over two block lists of the (bx,by) grid: `bulk` blocks
+    // One pass split over three block lists of the (bx,by) grid: `bulk` blocks
     // (every cell fluid, no wall neighbour, no solid fraction) run the
-    // wall-free kernels at feature level feat_bulk, `edge` blocks the
-    // wall-aware kernels at feat_edge. Each cell touches only its own slots,
-    // so the two launches are independent. edge_colmajor: the edge blocks of
-    // the odd pass take their cells column by column (a warp covers whole
-    // columns of the block) instead of row by row.
+    // wall-free kernels at feature level feat_bulk, `face` blocks (walls only
+    // in velocity-inflow columns at x = 0 / x = nx - 1, no solid fraction;
+    // GEO 2) the x-face kernels at feat_bulk, `edge` blocks the wall-aware
+    // kernels at feat_edge. Each cell touches only its own slots, so the
+    // launches are independent. edge_colmajor: the edge blocks of the odd
+    // pass take their cells column by column (a warp covers whole columns of
+    // the block) instead of row by row.
     cudaError_t (*split)(const StepArgs& a, int half_storage, int parity, int feat_bulk,
                          int feat_edge, dim3 block, const uint32_t* bulk, uint32_t nbulk,
-                         const uint32_t* edge, uint32_t nedge, int edge_colmajor,
-                         cudaStream_t st);
+                         const uint32_t* face, uint32_t nface, const uint32_t* edge,
+                         uint32_t nedge, int edge_colmajor, cudaStream_t st);
 };
 
 // Row-staged step (lbm_rows.cu): tiles of `rows` whole lattice rows move

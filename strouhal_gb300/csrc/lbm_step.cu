@@ -16,7 +16,9 @@
 //
 // Specialisations (all value-preserving):
 //   GEO  = 0 periodic all-fluid box: no cell bytes, masks or wall logic;
-//          1 walls and/or partially saturated cells.
+//          1 walls and/or partially saturated cells;
+//          2 (block lists only) blocks whose only walls are velocity-inflow
+//            columns at x = 0 and x = nx - 1: wall links from x alone.
 //   FEAT = 0 lean collide: no sponge, LES, body force or NT cells;
 //          1 sponge, body force, NT cells, each behind a uniform or per-cell branch;
 //          2 also the Smagorinsky LES block;
@@ -160,8 +162,12 @@ __global__ void __launch_bounds__(256) k_list_odd(const StepArgs a, const uint32
     if constexpr (COLMAJOR) list_block_colmajor(list, gx, gy, x, y, z);
     else list_block(list, gx, gy, x, y, z);
     if (x >= a.nx || y >= a.ny || z >= a.nz) return;
-    double contrib[3];
-    odd_cell<S, GEO, FEAT, false, false, STRO_ARITH, true>(a, WallVel(a), x, y, z, contrib);
+    if constexpr (GEO == 2) {
+        odd_cell_xface<S, FEAT, STRO_ARITH>(a, WallVel(a), x, y, z);
+    } else {
+        double contrib[3];
+        odd_cell<S, GEO, FEAT, false, false, STRO_ARITH, true>(a, WallVel(a), x, y, z, contrib);
+    }
 }
 
 template <typename S, int GEO, int FEAT>
@@ -185,14 +191,16 @@ static void launch_list_level(const StepArgs& a, int parity, int feat, const uin
 
 cudaError_t launch_step_split(const StepArgs& a, int half_storage, int parity, int feat_bulk,
                               int feat_edge, dim3 block, const uint32_t* bulk, uint32_t nbulk,
-                              const uint32_t* edge, uint32_t nedge, int edge_colmajor,
-                              cudaStream_t st) {
+                              const uint32_t* face, uint32_t nface, const uint32_t* edge,
+                              uint32_t nedge, int edge_colmajor, cudaStream_t st) {
     const bool col = edge_colmajor != 0;
     if (half_storage) {
         launch_list_level<__half, 0>(a, parity, feat_bulk, bulk, nbulk, block, false, st);
+        launch_list_level<__half, 2>(a, parity, feat_bulk, face, nface, block, false, st);
         launch_list_level<__half, 1>(a, parity, feat_edge, edge, nedge, block, col, st);
     } else {
         launch_list_level<float, 0>(a, parity, feat_bulk, bulk, nbulk, block, false, st);
+        launch_list_level<float, 2>(a, parity, feat_bulk, face, nface, block, false, st);
         launch_list_level<float, 1>(a, parity, feat_edge, edge, nedge, block, col, st);
     }
     return cudaGetLastError();

@@ -272,38 +272,70 @@ int ensure_partials(stro_sim* s, size_t doubles) {
 // Bulk / boundary block lists for the current block shape (rebuilt when the
 // shape or the geometry changes). A block is bulk when every cell it covers is
 // fluid with no wall neighbour, no moving wall nearby and no solid fraction.
+// Whether cell (x, y, z) is one the x-face kernels (odd_cell_xface) compute
+// as the wall-aware ones do: a velocity-inflow cell of column 0 or nx - 1, or a
+// fluid cell without solid fraction whose wall links are exactly its links
+// into those columns, all of them into inflow cells.
+static bool xface_cell(const stro_sim* s, int x, int y, int z) {
+    const int nx = s->nx, ny = s->ny, nz = s->nz;
+    const uint64_t idx = (uint64_t(z) * ny + y) * nx + x;
+    if (x == 0 || x == nx - 1) return s->flags[idx] == STRO_INFLOW;
+    if (s->flags[idx] != STRO_FLUID || s->cell_host[idx] != 0) return false;
+    uint32_t expect = 0;
+    for (int i = 1; i < 19; ++i)
+        if ((x == 1 && CX[i] < 0) || (x == nx - 2 && CX[i] > 0)) expect |= 1u << (i - 1);
+    if (s->smask[idx] != expect || s->lmask[idx] != expect) return false;
+    for (int i = 1; i < 19; ++i) {
+        if (!((expect >> (i - 1)) & 1u)) continue;
+        const int xn = x + CX[i], yn = (y + CY[i] + ny) % ny, zn = (z + CZ[i] + nz) % nz;
+        if (s->flags[(uint64_t(zn) * ny + yn) * nx + xn] != STRO_INFLOW) return false;
+    }
+    return true;
+}
+
 void block_lists(const stro_sim* s, dim3 shape, std::vector<uint32_t>& bulk,
-                 std::vector<uint32_t>& edge) {
+                 std::vector<uint32_t>& edge, std::vector<uint32_t>* face) {
     const uint32_t bx = shape.x, by = shape.y;
     const uint32_t gx = (uint32_t(s->nx) + bx - 1) / bx, gy = (uint32_t(s->ny) + by - 1) / by;
     const uint64_t nblocks = uint64_t(gx) * gy * uint64_t(s->nz);
     bulk.clear();
     edge.clear();
+    if (face) face->clear();
     bulk.reserve(nblocks);
     for (uint64_t b = 0; b < nblocks; ++b) {
         const uint32_t bxi = uint32_t(b % gx), t = uint32_t(b / gx), byi = t % gy, z = t / gy;
+        const uint32_t y1 = std::min<uint32_t>((byi + 1) * by, s->ny);
+        const uint32_t x1 = std::min<uint32_t>((bxi + 1) * bx, s->nx);
         bool is_bulk = true;
-        for (uint32_t yy = byi * by; yy < std::min<uint32_t>((byi + 1) * by, s->ny) && is_bulk; ++yy) {
+        for (uint32_t yy = byi * by; yy < y1 && is_bulk; ++yy) {
             const uint64_t row = (uint64_t(z) * s->ny + yy) * s->nx;
-            for (uint32_t xx = bxi * bx; xx < std::min<uint32_t>((bxi + 1) * bx, s->nx); ++xx)
+            for (uint32_t xx = bxi * bx; xx < x1; ++xx)
                 if (s->cell_host[row + xx] != 0 || s->geo_host[row + xx] != 0) {
                     is_bulk = false;
                     break;
                 }
         }
-        (is_bulk ? bulk : edge).push_back(uint32_t(b));
+        if (is_bulk) {
+            bulk.push_back(uint32_t(b));
+            continue;
+        }
+        bool is_face = face != nullptr;
+        for (uint32_t yy = byi * by; yy < y1 && is_face; ++yy)
+            for (uint32_t xx = bxi * bx; xx < x1 && is_face; ++xx)
+                is_face = xface_cell(s, int(xx), int(yy), int(z));
+        (is_face ? *face : edge).push_back(uint32_t(b));
     }
 }
 
 static int ensure_block_lists(stro_sim* s) {
     if (s->lists_version == s->geo_version && s->lists_block.x == s->block.x &&
-        s->lists_block.y == s->block.y)
+        s->lists_block.y == s->block.y && s->lists_face == s->face_lists)
         return STRO_OK;
     const uint32_t bx = s->block.x, by = s->block.y;
     const uint32_t gx = (uint32_t(s->nx) + bx - 1) / bx, gy = (uint32_t(s->ny) + by - 1) / by;
     const uint64_t nblocks = uint64_t(gx) * gy * uint64_t(s->nz);
-    std::vector<uint32_t> bulk, edge;
-    block_lists(s, s->block, bulk, edge);
+    std::vector<uint32_t> bulk, edge, face;
+    block_lists(s, s->block, bulk, edge, s->face_lists ? &face : nullptr);
     // Launches of this lattice still in flight read the old lists: let them
     // finish before the buffer is released. The new lists go up on the
     // lattice's own stream, so every launch after this call is ordered behind
@@ -316,14 +348,17 @@ static int ensure_block_lists(stro_sim* s) {
     cudaFree(s->d_blocks);
     s->d_blocks = nullptr;
     STRO_CUDA(cudaMalloc(&s->d_blocks, std::max<size_t>(nblocks, 1) * sizeof(uint32_t)));
+    s->nbulk = uint32_t(bulk.size());
+    s->nface = uint32_t(face.size());
+    s->nedge = uint32_t(edge.size());
+    bulk.insert(bulk.end(), face.begin(), face.end());
     bulk.insert(bulk.end(), edge.begin(), edge.end());
     STRO_CUDA(cudaMemcpyAsync(s->d_blocks, bulk.data(), nblocks * sizeof(uint32_t),
                               cudaMemcpyHostToDevice, st));
     STRO_CUDA(cudaStreamSynchronize(st));  // `bulk` is released on return
-    s->nbulk = uint32_t(nblocks - edge.size());
-    s->nedge = uint32_t(edge.size());
     s->lists_block = s->block;
     s->lists_version = s->geo_version;
+    s->lists_face = s->face_lists;
     return STRO_OK;
 }
 
@@ -344,7 +379,8 @@ cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool prob
         if (ensure_block_lists(s) != STRO_OK) return cudaErrorMemoryAllocation;
         s->last_path = "split";
         return L.split(a, half, int(t & 1), bulk_feat(s), feat_on(s), s->block, s->d_blocks,
-                       s->nbulk, s->d_blocks + s->nbulk, s->nedge, s->edge_colmajor ? 1 : 0,
+                       s->nbulk, s->d_blocks + s->nbulk, s->nface,
+                       s->d_blocks + s->nbulk + s->nface, s->nedge, s->edge_colmajor ? 1 : 0,
                        sim_stream(s));
     }
     const PairLaunchers& PL = fused ? fused::kPair : exact::kPair;
@@ -411,7 +447,8 @@ std::vector<uint8_t> graph_key(const stro_sim* s, int64_t t, int64_t G) {
                            s->pair_block.x, s->pair_block.y, s->rows_threads, s->rows_per_tile,
                            s->arith, s->collision, s->precision, geo_on(s) ? 1 : 0, feat_on(s),
                            bulk_feat(s), int64_t(reinterpret_cast<uintptr_t>(s->d_blocks)),
-                           s->nbulk, s->nedge, int64_t(s->lists_version),
+                           s->nbulk, s->nface, s->nedge, int64_t(s->lists_version),
+                           s->face_lists ? 1 : 0, s->lists_face ? 1 : 0,
                            int64_t(s->geo_version), s->lists_block.x, s->lists_block.y,
                            int64_t(reinterpret_cast<uintptr_t>(s->d_error)), s->rows_polls,
                            s->ctx->sm_count,

@@ -83,8 +83,10 @@ struct stro_sim {
     // bulk / boundary block lists of a walled lattice for the current block shape
     bool split = true;
     bool edge_colmajor = false;    // boundary blocks of the odd pass in column-major cell order
-    uint32_t* d_blocks = nullptr;  // bulk blocks first, then edge blocks
-    uint32_t nbulk = 0, nedge = 0;
+    bool face_lists = true;        // x-face blocks on their own kernels (else boundary blocks)
+    uint32_t* d_blocks = nullptr;  // bulk blocks first, then x-face, then edge blocks
+    uint32_t nbulk = 0, nface = 0, nedge = 0;
+    bool lists_face = false;       // face_lists when the lists were built
     dim3 lists_block{0, 0, 0};
     uint64_t lists_version = ~0ull;
     uint64_t geo_version = 0;      // bumped whenever the device geometry changes
@@ -134,9 +136,13 @@ int cuda_fail(cudaError_t e, const char* what);
 bool geo_on(const stro_sim* s);
 // Bulk and boundary blocks of the (shape.x, shape.y) block grid of a walled
 // lattice (host geometry copies must be current): a bulk block holds only
-// fluid cells without wall neighbours or solid fractions.
+// fluid cells without wall neighbours or solid fractions. With `face`, the
+// boundary blocks that the x-face kernels can take (every wall a
+// velocity-inflow cell of the columns x = 0 and x = nx - 1, every link into
+// those columns a moving-wall link, no other wall link, no solid fraction) go
+// there instead of into `edge`.
 void block_lists(const stro_sim* s, dim3 shape, std::vector<uint32_t>& bulk,
-                 std::vector<uint32_t>& edge);
+                 std::vector<uint32_t>& edge, std::vector<uint32_t>* face = nullptr);
 // Feature level of the step kernels: 0 lean, 1 sponge / force / NT, 2 also LES,
 // 3 the KBC collision.
 int feat_on(const stro_sim* s);

@@ -15,8 +15,8 @@ PREC = {0: "fp32", 1: "fp16s"}
 
 
 @pytest.mark.parametrize("kind", [0, 1])
-@pytest.mark.parametrize("geometry", ["periodic", "channel"])
-@pytest.mark.parametrize("split", [True, False, "columns"])
+@pytest.mark.parametrize("geometry", ["periodic", "channel", "xfaces"])
+@pytest.mark.parametrize("split", [True, False, "columns", "noface"])
 @pytest.mark.parametrize("collision", ["trt", "srt"])
 @pytest.mark.parametrize("ffield", [False, True])
 def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split, collision, ffield):
@@ -38,6 +38,16 @@ def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split, col
         eps = np.zeros(nx * ny * nz, np.float32)
         idx = rng.choice(nx * ny * nz, 120, replace=False)
         eps[idx] = rng.uniform(0.02, 0.98, idx.size).astype(np.float32)
+    elif geometry == "xfaces":  # inflow columns over every row: x-face blocks
+        fl = np.zeros((nz, ny, nx), np.uint8)
+        fl[:, :, 0] = fl[:, :, -1] = po.INFLOW
+        fl[:, 8:11, 12:15] = po.SOLID
+        flags = fl.reshape(-1)
+        eps = np.zeros(nx * ny * nz, np.float32)
+        cand = np.flatnonzero((np.arange(nx * ny * nz) % nx >= 18) &
+                              (np.arange(nx * ny * nz) % nx <= 28))
+        idx = rng.choice(cand, 120, replace=False)
+        eps[idx] = rng.uniform(0.02, 0.98, idx.size).astype(np.float32)
     g = sg.Simulation(gpu, precision=PREC[kind], nx=nx, ny=ny, nz=nz, flags=flags,
                       arithmetic="fused", **kw)
     o = po.OracleSim(nx, ny, nz, flags=flags, kind=kind, arithmetic="fused", **kw)
@@ -52,7 +62,9 @@ def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split, col
         g.setForceField(ff)
         o.setForceField(ff)
     g.setBlockSplit(split)
-    g.block = (32, 4)
+    # 16-wide blocks on xfaces: the NT cells (x = 18..28) fill the middle
+    # column of blocks only, both x faces get blocks of their own
+    g.block = (16, 4) if geometry == "xfaces" else (32, 4)
     f0 = (rng.standard_normal((19, nx * ny * nz)) * 0.01).astype(o.f.dtype)
     o.f[:] = f0
     g.uploadState(f0)
@@ -60,7 +72,11 @@ def test_fused_step_matches_fused_oracle(gpu, oracle, kind, geometry, split, col
         g.run(chunk)
         o.run(chunk)
         assert np.array_equal(g.downloadState(), o.f), (chunk, g.stepsDone)
-    if geometry == "channel":
+    if geometry == "xfaces" and split in (True, "columns"):
+        assert g.splitBlocks[1] > 0  # the x-face kernels ran
+    if split == "noface":
+        assert g.splitBlocks[1] == 0
+    if geometry != "periodic":
         box = ((3, 30), (1, 18))
         fg, fo = g.probeForce(*box), o.probeForce(*box)
         assert np.allclose(fg, fo, rtol=1e-12, atol=1e-12), (fg, fo)

@@ -93,9 +93,12 @@ def random_force_field(rng, N, scale=2e-5, zero_frac=0.3):
 
 
 @pytest.mark.parametrize("kind", [0, 1])
-@pytest.mark.parametrize("geometry", ["periodic", "cavity", "channel"])
+@pytest.mark.parametrize("geometry", ["periodic", "cavity", "channel", "xfaces", "xfaces_uniform"])
 @pytest.mark.parametrize("feature", list(FEATURES))
 def test_step_matches_oracle(gpu, oracle, kind, geometry, feature):
+    """xfaces: inflow columns at both x ends over every row (periodic y and z),
+    so the blocks along them run the x-face kernels of the block split; a solid
+    box and the NT cells keep some blocks on the wall-aware kernels."""
     import strouhal_gb300 as sg
 
     po = oracle
@@ -111,17 +114,26 @@ def test_step_matches_oracle(gpu, oracle, kind, geometry, feature):
         flags[:, 0, :] = flags[:, -1, :] = po.SOLID
         flags[:, 1:-1, 0] = flags[:, 1:-1, -1] = po.INFLOW
         flags[:, 8:11, 12:15] = po.SOLID
+    elif geometry.startswith("xfaces"):
+        flags = np.zeros((nz, ny, nx), np.uint8)
+        flags[:, :, 0] = flags[:, :, -1] = po.INFLOW
+        flags[:, 8:11, 12:15] = po.SOLID
     opts = dict(FEATURES[feature])
     eps = None
     if opts.pop("eps", False):
         eps = np.zeros(nx * ny * nz, np.float32)
-        idx = rng.choice(nx * ny * nz, 120, replace=False)
+        if geometry.startswith("xfaces"):  # NT cells in x = 10..25 only
+            cand = np.flatnonzero((np.arange(nx * ny * nz) % nx >= 10) &
+                                  (np.arange(nx * ny * nz) % nx <= 25))
+            idx = rng.choice(cand, 120, replace=False)
+        else:
+            idx = rng.choice(nx * ny * nz, 120, replace=False)
         eps[idx] = rng.uniform(0.02, 0.98, idx.size).astype(np.float32)
     ffield = opts.pop("ffield", False)
     g, o = _mk_pair(sg, po, gpu, kind, nx, ny, nz,
                     flags=None if flags is None else flags.reshape(-1), eps=eps,
                     omega=1.55, omegaMinus=1.2, lid=(0.07, 0.0, 0.01), uin=0.05, rampSteps=7,
-                    wantsForces=True, **opts)
+                    wantsForces=True, uniform=geometry == "xfaces_uniform", **opts)
     if ffield:
         ff = random_force_field(rng, nx * ny * nz)
         g.setForceField(ff)
@@ -133,6 +145,8 @@ def test_step_matches_oracle(gpu, oracle, kind, geometry, feature):
         g.run(chunk)
         o.run(chunk)
         assert np.array_equal(g.downloadState(), o.f), (chunk, g.stepsDone)
+    if geometry.startswith("xfaces"):
+        assert g.splitBlocks[1] > 0  # the x-face kernels ran
     assert np.array_equal(g.probeMoments(), o.probeMoments())
     box = ((3, 30), (1, 18))
     fg, fo = g.probeForce(*box), o.probeForce(*box)
