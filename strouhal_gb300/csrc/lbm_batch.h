@@ -40,14 +40,6 @@ struct BatchInstance {
     uint32_t div_nx_s, div_ny_s;
 };
 
-// Multiplier and shift of the exact division above (host side).
-inline void division_magic(uint32_t d, uint64_t* m, uint32_t* s) {
-    uint32_t sh = 0;
-    while ((uint64_t(1) << sh) < d) ++sh;
-    const unsigned __int128 num = (unsigned __int128)1 << (32 + sh);
-    *m = uint64_t((num + d - 1) / d);
-    *s = sh;
-}
 
 // Grid-barrier and error state of the persistent launch (zeroed before each launch).
 struct BatchCtl {

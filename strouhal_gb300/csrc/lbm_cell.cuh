@@ -408,7 +408,9 @@ __device__ __forceinline__ void collide(float (&fh)[19], const StepArgs& a, int 
                 });
             };
             float Q, tauEff;
-            const float tau0 = 1.0f / wp;
+            // 1 / wp; outside the sponge wp is omega and its reciprocal comes
+            // with the launch (the same FP32 division, done once on the host)
+            const float tau0 = wp == a.omega ? a.tau0 : 1.0f / wp;
             if constexpr (ARITH == ARITH_REFERENCE) {
                 second_moments([&](auto I) {
                     constexpr int i = I;
@@ -678,8 +680,12 @@ __device__ __forceinline__ void forget_ptr(P& p) {
 // GEO 2 (blocks of the x-face list, see odd_cell_xface): the non-fluid cells
 // are the columns x = 0 and x = nx - 1 and no cell is partially saturated, so
 // no cell byte is read.
+// PO: address the planes through the launch's 32-bit plane offsets
+// (StepArgs::poff, valid when 19 planes fit 2^32 elements) from a per-thread
+// base pointer: one wide multiply-add per address instead of a 64-bit add of
+// plane * i. Used by the wall-free and x-face block-list kernels.
 template <typename S, int GEO, int FEAT, bool LOG = false, bool CG = false,
-          int ARITH = ARITH_REFERENCE, bool OUT = (GEO != 0)>
+          int ARITH = ARITH_REFERENCE, bool OUT = (GEO != 0), bool PO = false>
 __device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z,
                                           float* u2 = nullptr) {
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
@@ -697,7 +703,12 @@ __device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z
     S* __restrict__ f = static_cast<S*>(a.f);
     const uint64_t P = a.plane;
     float fh[19];
-    sfor<0, 19>([&](auto I) { fh[I] = load_slot<S, CG>(f + uint64_t(I) * P + n); });
+    if constexpr (PO) {
+        const S* fb = f + n;
+        sfor<0, 19>([&](auto I) { fh[I] = load_slot<S, CG>(fb + a.poff[I]); });
+    } else {
+        sfor<0, 19>([&](auto I) { fh[I] = load_slot<S, CG>(f + uint64_t(I) * P + n); });
+    }
     float Fx = 0.f, Fy = 0.f, Fz = 0.f;
     cell_force<FEAT>(a, n, Fx, Fy, Fz);
     if constexpr (LOG) *u2 = cell_u2(fh, Fx, Fy, Fz);
@@ -707,15 +718,21 @@ __device__ __forceinline__ void even_cell(const StepArgs& a, int x, int y, int z
     if constexpr (OUT) {  // out of place
         if (a.f_out != nullptr) f = static_cast<S*>(a.f_out);
     }
-    store_ddf<S>(f + n, fh[0]);
-    sfor<1, 19>([&](auto I) { store_ddf<S>(f + uint64_t(opp(I)) * P + n, fh[I]); });
+    if constexpr (PO) {
+        S* fb = f + n;
+        store_ddf<S>(fb, fh[0]);
+        sfor<1, 19>([&](auto I) { store_ddf<S>(fb + a.poff[opp(I)], fh[I]); });
+    } else {
+        store_ddf<S>(f + n, fh[0]);
+        sfor<1, 19>([&](auto I) { store_ddf<S>(f + uint64_t(opp(I)) * P + n, fh[I]); });
+    }
 }
 
 // Odd (streaming) pass of one cell with halfway / moving-wall bounce-back,
 // Kernels.metal:261-354. With PROBE the cell's momentum-exchange force is
 // returned in contrib when the cell is a boundary cell inside the probe box.
 template <typename S, int GEO, int FEAT, bool PROBE, bool CG = false,
-          int ARITH = ARITH_REFERENCE, bool OUT = (GEO != 0)>
+          int ARITH = ARITH_REFERENCE, bool OUT = (GEO != 0), bool PO = false>
 __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, int x, int y,
                                          int z, double (&contrib)[3]) {
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
@@ -747,7 +764,8 @@ __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, i
                 if (bb) acc_sub<i>(ax, ay, az, fh[i]);
             }
         } else {
-            fh[i] = load_slot<S, CG>(f + uint64_t(o) * P + src);
+            if constexpr (PO) fh[i] = load_slot<S, CG>(f + (a.poff[o] + src));
+            else fh[i] = load_slot<S, CG>(f + uint64_t(o) * P + src);
         }
     });
     uint32_t lm = 0;
@@ -804,7 +822,8 @@ __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, i
         sfor<1, 19>([&](auto I) {
             constexpr int i = I;
             const uint32_t dst = uint32_t(int(n) + nb.template off<dcx(i), dcy(i), dcz(i)>());
-            store_ddf<S>(f + uint64_t(i) * P + dst, fh[i]);
+            if constexpr (PO) store_ddf<S>(f + (a.poff[i] + dst), fh[i]);
+            else store_ddf<S>(f + uint64_t(i) * P + dst, fh[i]);
         });
     }
     if constexpr (PROBE) {
@@ -826,7 +845,7 @@ __device__ __forceinline__ void odd_cell(const StepArgs& a, const WallVel& wv, i
 // the ones odd_cell computes for these cells (the same gather, moving-wall
 // corrections of Kernels.metal:292-314 and 317-350, collision and scatter);
 // inflow walls take no outflow terms.
-template <typename S, int FEAT, int ARITH = ARITH_REFERENCE>
+template <typename S, int FEAT, int ARITH = ARITH_REFERENCE, bool PO = false>
 __device__ __forceinline__ void odd_cell_xface(const StepArgs& a, const WallVel& wv, int x, int y,
                                                int z) {
     if (x == 0 || x == a.nx - 1) return;
@@ -842,11 +861,15 @@ __device__ __forceinline__ void odd_cell_xface(const StepArgs& a, const WallVel&
         constexpr int o = opp(i);
         const uint32_t src = uint32_t(int(n) + nb.template off<-dcx(i), -dcy(i), -dcz(i)>());
         if constexpr (dcx(i) == 0) {
-            fh[i] = load_slot<S, false>(f + uint64_t(o) * P + src);
+            if constexpr (PO) fh[i] = load_slot<S, false>(f + (a.poff[o] + src));
+            else fh[i] = load_slot<S, false>(f + uint64_t(o) * P + src);
         } else {
             // n - c_i lies in a wall column: the link reflects within the cell
             const bool bb = dcx(i) > 0 ? wl : wr;
-            fh[i] = load_slot<S, false>(f + (bb ? uint64_t(i) * P + n : uint64_t(o) * P + src));
+            if constexpr (PO)
+                fh[i] = load_slot<S, false>(f + (bb ? a.poff[i] + n : a.poff[o] + src));
+            else
+                fh[i] = load_slot<S, false>(f + (bb ? uint64_t(i) * P + n : uint64_t(o) * P + src));
         }
     });
     if (wl || wr) {
@@ -873,7 +896,8 @@ __device__ __forceinline__ void odd_cell_xface(const StepArgs& a, const WallVel&
         constexpr int i = I;
         const uint32_t dst = uint32_t(int(n) + nb.template off<dcx(i), dcy(i), dcz(i)>());
         if constexpr (dcx(i) == 0) {
-            store_ddf<S>(f + uint64_t(i) * P + dst, fh[i]);
+            if constexpr (PO) store_ddf<S>(f + (a.poff[i] + dst), fh[i]);
+            else store_ddf<S>(f + uint64_t(i) * P + dst, fh[i]);
         } else {
             // n + c_i lies in a wall column: store into the cell's own opposite slot
             const bool bb = dcx(i) < 0 ? wl : wr;
@@ -884,7 +908,10 @@ __device__ __forceinline__ void odd_cell_xface(const StepArgs& a, const WallVel&
                 const float corr = 6.0f * wgt(i) * cdot<i>(uwx, uwy, uwz);
                 out = fh[i] - corr;
             }
-            store_ddf<S>(f + (bb ? uint64_t(opp(i)) * P + n : uint64_t(i) * P + dst), out);
+            if constexpr (PO)
+                store_ddf<S>(f + (bb ? a.poff[opp(i)] + n : a.poff[i] + dst), out);
+            else
+                store_ddf<S>(f + (bb ? uint64_t(opp(i)) * P + n : uint64_t(i) * P + dst), out);
         }
     });
 }

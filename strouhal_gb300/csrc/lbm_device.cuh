@@ -89,6 +89,18 @@ template <> __device__ __forceinline__ void store_ddf<__half>(__half* p, float v
     *p = __float2half_rn(v);
 }
 
+// Multiplier and shift of an exact unsigned division by d (host side):
+// n / d = (n * m) >> (32 + s) with s = ceil(log2 d), m = ceil(2^(32+s) / d),
+// for n < 2^32 (the error m d - 2^(32+s) is below d <= 2^s); the 64-bit
+// product n * m (m < 2^33) does not overflow for n < 2^31.
+inline void division_magic(uint32_t d, uint64_t* m, uint32_t* s) {
+    uint32_t sh = 0;
+    while ((uint64_t(1) << sh) < d) ++sh;
+    const unsigned __int128 num = (unsigned __int128)1 << (32 + sh);
+    *m = uint64_t((num + d - 1) / d);
+    *s = sh;
+}
+
 // Cell byte (even pass): low 3 bits = cell type; bit 3 = partially saturated (eps != 0).
 constexpr uint8_t CELL_TYPE_MASK = 0x7u;
 constexpr uint8_t CELL_EPS_BIT = 0x8u;
@@ -116,6 +128,7 @@ struct StepArgs {
     const float* ffield;      // optional force field: 3 planes of N floats
     uint32_t ffield_plane;    // plane stride of ffield (= N)
     float omega, omega_minus; // omega+ and omega-
+    float tau0;               // 1 / omega (FP32 division), for cells the sponge leaves alone
     float uin;                // ramped inflow peak / uniform velocity
     float c_smago;            // Smagorinsky Cs^2
     float fx, fy, fz;         // uniform Guo force

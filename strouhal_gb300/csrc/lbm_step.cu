@@ -119,23 +119,48 @@ cudaError_t launch_step_capped(const StepArgs& a, int half_storage, int parity, 
 // Block-list launches: block i of the grid processes lattice block list[i]
 // (linear index bx + gx * (by + gy * bz)). Used to run the bulk of a walled
 // lattice with the wall-free kernels and only its boundary blocks with the
-// wall-aware ones.
-__device__ __forceinline__ void list_block(const uint32_t* list, uint32_t gx, uint32_t gy,
-                                           int& x, int& y, int& z) {
-    const uint32_t blk = list[blockIdx.x];
-    const uint32_t t = blk / gx;
-    x = int((blk - t * gx) * blockDim.x + threadIdx.x);
-    y = int((t % gy) * blockDim.y + threadIdx.y);
-    z = int(t / gy);
+// wall-aware ones. The index is split by multiply-shift divisions (a block
+// index is below 2^27: at most 2^32 cells, at least 32 per block), a few
+// instructions per thread instead of two integer divisions.
+struct ListGrid {
+    uint64_t mx, my;  // division_magic of gx and gy
+    uint32_t gx, gy, sx, sy;
+};
+
+static ListGrid list_grid(const StepArgs& a, dim3 block) {
+    ListGrid g;
+    g.gx = (uint32_t(a.nx) + block.x - 1) / block.x;
+    g.gy = (uint32_t(a.ny) + block.y - 1) / block.y;
+    division_magic(g.gx, &g.mx, &g.sx);
+    division_magic(g.gy, &g.my, &g.sy);
+    return g;
 }
 
-template <typename S, int GEO, int FEAT>
+__device__ __forceinline__ void list_coords(const uint32_t* list, const ListGrid& g,
+                                            uint32_t& bxi, uint32_t& byi, uint32_t& z) {
+    const uint32_t blk = list[blockIdx.x];
+    const uint32_t t = uint32_t((uint64_t(blk) * g.mx) >> (32 + g.sx));  // blk / gx
+    z = uint32_t((uint64_t(t) * g.my) >> (32 + g.sy));                    // t / gy
+    bxi = blk - t * g.gx;
+    byi = t - z * g.gy;
+}
+
+__device__ __forceinline__ void list_block(const uint32_t* list, const ListGrid& g, int& x,
+                                           int& y, int& z) {
+    uint32_t bxi, byi, bz;
+    list_coords(list, g, bxi, byi, bz);
+    x = int(bxi * blockDim.x + threadIdx.x);
+    y = int(byi * blockDim.y + threadIdx.y);
+    z = int(bz);
+}
+
+template <typename S, int GEO, int FEAT, bool PO>
 __global__ void __launch_bounds__(256) k_list_even(const StepArgs a, const uint32_t* list,
-                                                   uint32_t gx, uint32_t gy) {
+                                                   const ListGrid g) {
     int x, y, z;
-    list_block(list, gx, gy, x, y, z);
+    list_block(list, g, x, y, z);
     if (x >= a.nx || y >= a.ny || z >= a.nz) return;
-    even_cell<S, GEO, FEAT, false, false, STRO_ARITH, true>(a, x, y, z);
+    even_cell<S, GEO, FEAT, false, false, STRO_ARITH, true, PO>(a, x, y, z);
 }
 
 // Column-major cell order inside a block: thread t takes column t / by, row
@@ -145,39 +170,51 @@ __global__ void __launch_bounds__(256) k_list_even(const StepArgs a, const uint3
 // in warps of their own: the plain cells beside them no longer sit in warps
 // that also run the moving-wall branches. The rows of a tile are re-read by
 // its other warps, so the narrower warp accesses are served from L1.
-__device__ __forceinline__ void list_block_colmajor(const uint32_t* list, uint32_t gx,
-                                                    uint32_t gy, int& x, int& y, int& z) {
-    const uint32_t blk = list[blockIdx.x];
-    const uint32_t t = blk / gx;
+__device__ __forceinline__ void list_block_colmajor(const uint32_t* list, const ListGrid& g,
+                                                    int& x, int& y, int& z) {
+    uint32_t bxi, byi, bz;
+    list_coords(list, g, bxi, byi, bz);
     const uint32_t tid = threadIdx.x + blockDim.x * threadIdx.y;
-    x = int((blk - t * gx) * blockDim.x + tid / blockDim.y);
-    y = int((t % gy) * blockDim.y + tid % blockDim.y);
-    z = int(t / gy);
+    x = int(bxi * blockDim.x + tid / blockDim.y);
+    y = int(byi * blockDim.y + tid % blockDim.y);
+    z = int(bz);
 }
 
-template <typename S, int GEO, int FEAT, bool COLMAJOR = false>
+template <typename S, int GEO, int FEAT, bool PO, bool COLMAJOR = false>
 __global__ void __launch_bounds__(256) k_list_odd(const StepArgs a, const uint32_t* list,
-                                                  uint32_t gx, uint32_t gy) {
+                                                  const ListGrid g) {
     int x, y, z;
-    if constexpr (COLMAJOR) list_block_colmajor(list, gx, gy, x, y, z);
-    else list_block(list, gx, gy, x, y, z);
+    if constexpr (COLMAJOR) list_block_colmajor(list, g, x, y, z);
+    else list_block(list, g, x, y, z);
     if (x >= a.nx || y >= a.ny || z >= a.nz) return;
     if constexpr (GEO == 2) {
-        odd_cell_xface<S, FEAT, STRO_ARITH>(a, WallVel(a), x, y, z);
+        odd_cell_xface<S, FEAT, STRO_ARITH, PO>(a, WallVel(a), x, y, z);
     } else {
         double contrib[3];
-        odd_cell<S, GEO, FEAT, false, false, STRO_ARITH, true>(a, WallVel(a), x, y, z, contrib);
+        odd_cell<S, GEO, FEAT, false, false, STRO_ARITH, true, PO>(a, WallVel(a), x, y, z,
+                                                                   contrib);
     }
 }
 
+// The wall-free and x-face lists address the planes through the 32-bit plane
+// offsets when the lattice's 19 planes fit 2^32 elements (StepArgs::poff
+// filled), the wall-aware list always through 64-bit plane products.
 template <typename S, int GEO, int FEAT>
 static void launch_list(const StepArgs& a, int parity, const uint32_t* list, uint32_t count,
                         dim3 block, bool colmajor, cudaStream_t st) {
     if (count == 0) return;
-    const uint32_t gx = (a.nx + block.x - 1) / block.x, gy = (a.ny + block.y - 1) / block.y;
-    if (parity == 0) k_list_even<S, GEO, FEAT><<<count, block, 0, st>>>(a, list, gx, gy);
-    else if (GEO == 1 && colmajor) k_list_odd<S, GEO, FEAT, true><<<count, block, 0, st>>>(a, list, gx, gy);
-    else k_list_odd<S, GEO, FEAT><<<count, block, 0, st>>>(a, list, gx, gy);
+    const ListGrid g = list_grid(a, block);
+    const bool po = GEO != 1 && a.poff[1] != 0;
+    if (parity == 0) {
+        if (po) k_list_even<S, GEO, FEAT, GEO != 1><<<count, block, 0, st>>>(a, list, g);
+        else k_list_even<S, GEO, FEAT, false><<<count, block, 0, st>>>(a, list, g);
+    } else if (GEO == 1 && colmajor) {
+        k_list_odd<S, GEO, FEAT, false, true><<<count, block, 0, st>>>(a, list, g);
+    } else if (po) {
+        k_list_odd<S, GEO, FEAT, GEO != 1><<<count, block, 0, st>>>(a, list, g);
+    } else {
+        k_list_odd<S, GEO, FEAT, false><<<count, block, 0, st>>>(a, list, g);
+    }
 }
 
 template <typename S, int GEO>

@@ -101,6 +101,7 @@ static void fill_step_args(const stro_sim* s, int64_t t, StepArgs* out) {
     a.ffield_plane = uint32_t(s->N);
     a.omega = s->omega;
     a.omega_minus = s->omega_minus;
+    a.tau0 = 1.0f / s->omega;  // IEEE single division, as the kernels would do it
     const float r = ramp_factor(s, t);
     a.uin = s->uin * r;
     a.c_smago = s->c_smago;
