@@ -24,6 +24,10 @@ variants.c4_batched : the batched credibility ladder (32 periodic TGV instances,
         time of the sequential per-rung launches against the streams, rounds
         (CUDA graph of batched rounds) and persistent (one cooperative kernel)
         modes, states bitwise compared.
+variants.c5_sphere : the sphere-wake lattice (512x256x256, FP16 storage, LES,
+        NT sphere, outlet sponge, uniform-inflow walls at both x ends) in the
+        fused and the reference arithmetic, autotuned: GLUPS and the fraction
+        of the HBM roofline at 76 B per cell.
 variants.c3_adjoint / c5_adjoint : device time of the discrete adjoint's
         backward sweep (recomputation included) over its forward window on the
         full cylinder (1410x264x3, 10,000-step window, 20 checkpoints) and
@@ -267,6 +271,31 @@ def run_c4_ladder(gpu, t_star=5.0, tune_rounds=10):
     return out
 
 
+def run_sphere(gpu, peak, steps=200):
+    """Step throughput of the C5 sphere-wake lattice, each arithmetic autotuned."""
+    from strouhal_gb300 import cases
+
+    out = {"workload": "sphere wake 512x256x256, FP16 storage, SRT + Smagorinsky LES (Cs 0.1), "
+                       "NT sphere D = 48, outlet sponge, uniform-inflow walls at x = 0 and 511; "
+                       "%d steps after 20 warm-up steps" % steps}
+    for arith in ("fused", "reference"):
+        s = cases.sphere_sim(gpu, arithmetic=arith)
+        bx, by, _ = s.autotune(steps=10)
+        s.run(20)
+        t0 = s.gpuSeconds
+        s.run(steps)
+        dev = s.gpuSeconds - t0
+        glups = s.cells * steps / dev / 1e9
+        out[arith] = {"value": glups, "unit": "GLUPS", "ms_per_step": 1e3 * dev / steps,
+                      "roofline": {"achieved": ALG_BYTES["fp16s"] * glups, "peak": peak,
+                                   "frac": ALG_BYTES["fp16s"] * glups / peak, "unit": "GB/s",
+                                   "alg_bytes_per_cell": ALG_BYTES["fp16s"]},
+                      "tuned": {"variant": s.variant, "shape": [bx, by], "path": s.lastPath},
+                      "finite": s.checkFinite()}
+        s.close()
+    return out
+
+
 def run_adjoints(gpu):
     """Backward / forward device time of the discrete adjoint on the C3 and C5 lattices."""
     from strouhal_gb300 import cases
@@ -354,8 +383,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-workloads", action="store_true",
-                    help="skip the batched-ladder and adjoint workloads (variants.c4_batched, "
-                         "c3_adjoint, c5_adjoint)")
+                    help="skip the sphere-wake, batched-ladder and adjoint workloads "
+                         "(variants.c5_sphere, c4_batched, c3_adjoint, c5_adjoint)")
     ap.add_argument("--clocks-csv", default=None,
                     help="keep the nvidia-smi samples of the timed region in this file")
     args = ap.parse_args()
@@ -380,10 +409,11 @@ def main():
     trt = run_variant(sg, gpu, "fp32", 3.0 / 16.0, args.steps, args.warmup, dist)
     kbc = run_variant(sg, gpu, "fp16s", None, args.steps, args.warmup, dist, collision="kbc")
     extra = {}
+    peak, peak_kind = measured_peak()
     if not args.no_workloads:
+        extra["c5_sphere"] = run_sphere(gpu, peak)
         extra["c4_batched"] = run_c4_ladder(gpu)
         extra.update(run_adjoints(gpu))
-    peak, peak_kind = measured_peak()
     traffic = profile_traffic()
 
     def summarise(r, precision):

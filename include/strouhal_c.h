@@ -238,8 +238,13 @@ int stro_sim_set_spin_limit(stro_sim* sim, int64_t polls);
  * boundary blocks with the wall-aware ones (1, the default); 2 does the same
  * with the boundary blocks' odd pass in column-major cell order (a warp
  * covers whole columns of its block); 3 is 1 without the x-face blocks (they
- * run the wall-aware kernels); 0 runs the wall-aware kernels on every block.
- * Results are identical in every mode. */
+ * run the wall-aware kernels); 4 is 1 with the bulk and x-face blocks in one
+ * launch from one list in block order (a DRAM line shared by an x-face block
+ * and the bulk block beside it is fetched once); 5 is 4 with the bulk blocks
+ * of an FP16-storage lattice taken two x-adjacent cells per thread in 4-byte
+ * words (feature levels without KBC, nx and the block width even; otherwise
+ * as 4); 0 runs the wall-aware kernels on every block. Results are identical
+ * in every mode. */
 int stro_sim_set_block_split(stro_sim* sim, int32_t enabled);
 /* stro_sim_run and stro_sim_run_sampled replay CUDA graphs of plain steps once
  * the ramp is over (default on): the launches of a run of steps are captured

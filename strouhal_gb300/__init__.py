@@ -639,11 +639,13 @@ class Simulation:
         """Bulk blocks of a walled lattice on the wall-free kernels and blocks at
         velocity-inflow x faces on the x-face kernels (default True); "columns"
         also orders the boundary blocks' odd pass column by column; "noface"
-        runs the x-face blocks on the wall-aware kernels."""
-        mode = {"columns": 2, "noface": 3}.get(enabled) if isinstance(enabled, str) \
-            else int(bool(enabled))
+        runs the x-face blocks on the wall-aware kernels; "merged" runs the bulk
+        and x-face blocks in one launch; "pair" does that with the bulk blocks
+        of an FP16-storage lattice two cells per thread."""
+        modes = {"columns": 2, "noface": 3, "merged": 4, "pair": 5}
+        mode = modes.get(enabled) if isinstance(enabled, str) else int(bool(enabled))
         if mode is None:
-            raise ValueError("block split: True, False, 'columns' or 'noface'")
+            raise ValueError("block split: True, False, 'columns', 'noface', 'merged' or 'pair'")
         _check(lib().stro_sim_set_block_split(self._h, mode))
 
     def setGraphs(self, enabled):

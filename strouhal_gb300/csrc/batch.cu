@@ -924,10 +924,12 @@ int stro_sim_set_variant(stro_sim* s, int32_t variant) {
 
 int stro_sim_set_block_split(stro_sim* s, int32_t enabled) {
     if (!s) return fail(STRO_ERR_INVALID, "null simulation handle");
-    if (enabled < 0 || enabled > 3) return fail(STRO_ERR_INVALID, "split must be 0, 1, 2 or 3");
+    if (enabled < 0 || enabled > 5) return fail(STRO_ERR_INVALID, "split must be 0 to 5");
     s->split = enabled != 0;
     s->edge_colmajor = enabled == 2;
     s->face_lists = enabled != 3;
+    s->merged_faces = enabled == 4;
+    s->pair_bulk = enabled == 5;
     return STRO_OK;
 }
 
@@ -1070,14 +1072,20 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
     bool best_split = saved_split;
     bool best_col = s->edge_colmajor;
     bool best_face = s->face_lists;
+    bool best_merged = s->merged_faces;
+    bool best_pair = s->pair_bulk;
     const int geo = geo_on(s) ? 1 : 0;
     // split 2: the split with the boundary blocks' odd pass in column-major
-    // order; 3: the split without x-face blocks
-    for (int split : {1, 2, 3, 0}) {
+    // order; 3: the split without x-face blocks; 4: bulk and x-face blocks in
+    // one launch; 5: as 4 with FP16 bulk blocks two cells per thread
+    for (int split : {1, 4, 5, 2, 3, 0}) {
         if (split != 1 && !geo) break;  // the split only exists for walled lattices
+        if (split == 5 && (!half || s->collision != STRO_COLLISION_REFERENCE)) continue;
         s->split = split != 0;
         s->edge_colmajor = split == 2;
         s->face_lists = split != 3;
+        s->merged_faces = split == 4;
+        s->pair_bulk = split == 5;
         for (int variant : {0, 1, 2, 3, 4, 5}) {
             const dim3* shapes = variant == 2 ? kRowShapes : kShapes;
             const size_t nshapes = variant == 2 ? sizeof(kRowShapes) / sizeof(dim3)
@@ -1108,6 +1116,8 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
                     best_split = s->split;
                     best_col = s->edge_colmajor;
                     best_face = s->face_lists;
+                    best_merged = s->merged_faces;
+                    best_pair = s->pair_bulk;
                 }
             }
         }
@@ -1115,6 +1125,8 @@ int stro_sim_autotune(stro_sim* s, int64_t steps, int32_t* bx, int32_t* by, doub
     s->split = best_split;
     s->edge_colmajor = best_col;
     s->face_lists = best_face;
+    s->merged_faces = best_merged;
+    s->pair_bulk = best_pair;
     e = cudaMemcpyAsync(s->d_f, saved, bytes, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     cudaFree(saved);

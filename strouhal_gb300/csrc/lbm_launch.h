@@ -13,6 +13,45 @@ inline dim3 step_grid(const StepArgs& a, dim3 block) {
     return dim3((a.nx + block.x - 1) / block.x, (a.ny + block.y - 1) / block.y, a.nz);
 }
 
+// Block lists of the bulk / boundary split: list entry k names the lattice
+// block (bx cells by by rows) with linear index bxi + gx * (byi + gy * z).
+// The index is split by multiply-shift divisions (a block index is below
+// 2^27: at most 2^32 cells, at least 32 per block), a few instructions per
+// thread instead of two integer divisions.
+struct ListGrid {
+    uint64_t mx, my;  // division_magic of gx and gy
+    uint32_t gx, gy, sx, sy;
+};
+
+// Grid of the lattice blocks of shape `block` (in cells).
+inline ListGrid list_grid(const StepArgs& a, dim3 block) {
+    ListGrid g;
+    g.gx = (uint32_t(a.nx) + block.x - 1) / block.x;
+    g.gy = (uint32_t(a.ny) + block.y - 1) / block.y;
+    division_magic(g.gx, &g.mx, &g.sx);
+    division_magic(g.gy, &g.my, &g.sy);
+    return g;
+}
+
+// Block coordinates of the linear block index blk.
+__device__ __forceinline__ void block_coords(uint32_t blk, const ListGrid& g, uint32_t& bxi,
+                                             uint32_t& byi, uint32_t& z) {
+    const uint32_t t = uint32_t((uint64_t(blk) * g.mx) >> (32 + g.sx));  // blk / gx
+    z = uint32_t((uint64_t(t) * g.my) >> (32 + g.sy));                    // t / gy
+    bxi = blk - t * g.gx;
+    byi = t - z * g.gy;
+}
+
+// Block coordinates of the list entry of this CUDA block.
+__device__ __forceinline__ void list_coords(const uint32_t* list, const ListGrid& g,
+                                            uint32_t& bxi, uint32_t& byi, uint32_t& z) {
+    block_coords(list[blockIdx.x], g, bxi, byi, z);
+}
+
+// Flag bit of a list entry of the pair kernels' merged bulk list: the block
+// is an x-face block (block indices stay below 2^27).
+constexpr uint32_t kListFaceBit = 0x80000000u;
+
 // Launchers of the step kernels (lbm_step.cu), one table per arithmetic:
 // exact::kStep (the reference's expressions as written) and fused::kStep
 // (the fused-multiply-add collision).
@@ -32,11 +71,13 @@ struct StepLaunchers {
     // kernels at feat_edge. Each cell touches only its own slots, so the
     // launches are independent. edge_colmajor: the edge blocks of the odd
     // pass take their cells column by column (a warp covers whole columns of
-    // the block) instead of row by row.
+    // the block) instead of row by row. merged: `bulk` holds the bulk and the
+    // x-face blocks in block order (x-face entries flagged kListFaceBit), run
+    // in one launch; face / nface are unused.
     cudaError_t (*split)(const StepArgs& a, int half_storage, int parity, int feat_bulk,
                          int feat_edge, dim3 block, const uint32_t* bulk, uint32_t nbulk,
                          const uint32_t* face, uint32_t nface, const uint32_t* edge,
-                         uint32_t nedge, int edge_colmajor, cudaStream_t st);
+                         uint32_t nedge, int edge_colmajor, int merged, cudaStream_t st);
 };
 
 // Row-staged step (lbm_rows.cu): tiles of `rows` whole lattice rows move
@@ -63,6 +104,14 @@ struct PairLaunchers {
                            dim3 block, int cells);
     cudaError_t (*wide_launch)(const StepArgs& a, int parity, int feat, dim3 block, int cells,
                                cudaStream_t st);
+    // Bulk and x-face blocks of the split in one launch, FP16 storage,
+    // block.x / 2 by block.y threads per lattice block of shape `block` (in
+    // cells): bulk blocks two x-adjacent cells per thread in 4-byte words,
+    // blocks whose entry carries kListFaceBit the x-face code, two cells per
+    // thread one after the other. Honours StepArgs::f_out.
+    bool (*list_supported)(int half_storage, int feat, int nx, uint64_t plane, dim3 block);
+    cudaError_t (*list_launch)(const StepArgs& a, int parity, int feat, dim3 block,
+                               const uint32_t* list, uint32_t count, cudaStream_t st);
 };
 
 namespace exact {

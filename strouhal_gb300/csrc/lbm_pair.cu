@@ -170,11 +170,12 @@ struct PairRows {
 // (the x part, formed again from x after an opaque asm statement so nothing
 // of the gather stays in registers across the collisions) plus a
 // block-uniform plane-and-row offset.
-__device__ __forceinline__ void scatter_pair(const StepArgs& a, const __half2 (&ao)[10],
+// `out` is the state written (StepArgs::f, or f_out for an out-of-place pass).
+__device__ __forceinline__ void scatter_pair(const StepArgs& a, void* out, const __half2 (&ao)[10],
                                              const float (&fh)[19], int x, const PairRows& rows) {
     forget_int(x);
     const uint32_t nx = uint32_t(a.nx);
-    __half* __restrict__ f1 = static_cast<__half*>(a.f);
+    __half* __restrict__ f1 = static_cast<__half*>(out);
     __half* __restrict__ f1x = f1 + x;                       // both cells, c_x = 0
     // x-shifted destinations of the two cells (periodic in x): x-1 and x+2 wrap
     __half* __restrict__ f1m = f1 + wrap_x(x - 1, int(nx));  // cell x,   c_x = -1
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(256, FEAT == 2 ? 2 : 4) k_pair_odd(const StepA
     __half2 ao[10];
     float fh[19];
     collide_pair<FEAT>(v, ao, fh, a, x, n);
-    scatter_pair(a, ao, fh, x, rows);
+    scatter_pair(a, a.f, ao, fh, x, rows);
 }
 
 // ------------------------------------------------------------ wide variant
@@ -334,8 +335,130 @@ __global__ void __launch_bounds__(256, V == 8 ? 2 : 3) k_wide_odd(const StepArgs
         __half2 ao[10];
         float fh[19];
         collide_pair<FEAT>(v, ao, fh, a, x + 2 * j, n + 2 * j);
-        scatter_pair(a, ao, fh, x + 2 * j, rows);
+        scatter_pair(a, a.f, ao, fh, x + 2 * j, rows);
     });
+}
+
+
+// ------------------------------------------------------ block-list variant
+// The bulk blocks of a walled lattice's bulk / boundary split (every cell
+// fluid, no wall neighbour, no solid fraction) in FP16 storage, two
+// x-adjacent cells per thread: list entry blockIdx.x names a lattice block of
+// bx cells by by rows, covered by bx / 2 by by threads. A bulk cell streams as
+// a cell of a periodic lattice does (every neighbour is fluid; y, z and x
+// wrap), so gather, collision and scatter are the pair kernel's, with the
+// neighbour rows taken per thread (a warp spans 64 / bx rows of the block).
+// The x-shifted gather reads the aligned word beside the thread's own, which
+// may belong to a neighbouring lattice block of another list: only its half
+// inside this block's reach is used, and that slot is written by this thread
+// alone, as in the pair kernel. Writes go to StepArgs::f_out when it is set
+// (the adjoint's out-of-place recomputation). Requirements (checked by the
+// host): nx and bx even, even plane stride, 19 planes below 2^32 elements.
+//
+// The same launch takes the x-face blocks (entries flagged kListFaceBit;
+// blocks whose only walls are velocity-inflow columns at x = 0 / nx - 1): each
+// thread computes two cells of the block one after the other with the
+// one-cell x-face code (the block's cells in row-major order, thread t taking
+// cells t and t + threads, so each round is a contiguous, coalesced half of
+// the block). Run in one launch with the bulk blocks, a 128-byte line shared
+// by an x-face block and the bulk block beside it is fetched from DRAM once;
+// as separate launches each fetched the whole line for its half.
+template <int FEAT, bool ODD>
+__device__ __forceinline__ void face_block(const StepArgs& a, uint32_t bxi, uint32_t byi,
+                                           uint32_t z) {
+    const uint32_t bx = 2u * blockDim.x, nt = blockDim.x * blockDim.y;
+    const uint32_t tid = threadIdx.x + blockDim.x * threadIdx.y;
+#pragma unroll 1
+    for (uint32_t c = tid; c < 2u * nt; c += nt) {
+        const uint32_t cy = c / bx, cx = c - cy * bx;
+        const int x = int(bxi * bx + cx), y = int(byi * blockDim.y + cy);
+        if (x >= a.nx || y >= a.ny) continue;
+        if constexpr (ODD)
+            odd_cell_xface<__half, FEAT, STRO_ARITH, true>(a, WallVel(a), x, y, int(z));
+        else
+            even_cell<__half, 2, FEAT, false, false, STRO_ARITH, true, true>(a, x, y, int(z));
+    }
+}
+
+// Cell pair (x, x + 1) of this thread in bulk block (bxi, byi, z).
+__device__ __forceinline__ void pair_list_cell(uint32_t bxi, uint32_t byi, int& x, uint32_t& y) {
+    x = int(2u * (bxi * blockDim.x + threadIdx.x));
+    y = byi * blockDim.y + threadIdx.y;
+}
+
+template <int FEAT>
+__global__ void __launch_bounds__(256, FEAT == 2 ? 3 : 4)
+    k_pair_list_even(const StepArgs a, const uint32_t* list, const ListGrid g) {
+    const uint32_t e = list[blockIdx.x];
+    uint32_t bxi, byi, z;
+    block_coords(e & ~kListFaceBit, g, bxi, byi, z);
+    if (e & kListFaceBit) {
+        face_block<FEAT, false>(a, bxi, byi, z);
+        return;
+    }
+    int x;
+    uint32_t y;
+    pair_list_cell(bxi, byi, x, y);
+    if (x >= a.nx || y >= uint32_t(a.ny) || z >= uint32_t(a.nz)) return;
+    const uint32_t n = (z * uint32_t(a.ny) + y) * uint32_t(a.nx) + uint32_t(x);
+    const __half* __restrict__ fn = static_cast<const __half*>(a.f) + n;
+    __half2 v[19];
+    sfor<0, 19>([&](auto I) { v[I] = *reinterpret_cast<const __half2*>(fn + a.poff[I]); });
+    __half2 ao[10];
+    float fh[19];
+    collide_pair<FEAT>(v, ao, fh, a, x, n);
+    uint32_t m = n;
+    forget_u32(m);
+    __half* __restrict__ q = static_cast<__half*>(a.f_out != nullptr ? a.f_out : a.f) + m;
+    // direction i of both cells goes to slot opp(i)
+    sfor<0, 19>([&](auto I) {
+        *reinterpret_cast<__half2*>(q + a.poff[opp(I)]) =
+            __halves2half2(out_lo<I>(ao), __float2half_rn(fh[I]));
+    });
+}
+
+template <int FEAT>
+__global__ void __launch_bounds__(256, FEAT == 2 ? 3 : 4)
+    k_pair_list_odd(const StepArgs a, const uint32_t* list, const ListGrid g) {
+    const uint32_t e = list[blockIdx.x];
+    uint32_t bxi, byi, z;
+    block_coords(e & ~kListFaceBit, g, bxi, byi, z);
+    if (e & kListFaceBit) {
+        face_block<FEAT, true>(a, bxi, byi, z);
+        return;
+    }
+    int x;
+    uint32_t y;
+    pair_list_cell(bxi, byi, x, y);
+    if (x >= a.nx || y >= uint32_t(a.ny) || z >= uint32_t(a.nz)) return;
+    const uint32_t nx = uint32_t(a.nx);
+    const PairRows rows(a, y, z);
+    const __half* __restrict__ f = static_cast<const __half*>(a.f);
+    const __half* __restrict__ fx = f + x;
+    const __half* __restrict__ fl = f + wrap_x(x - 2, int(nx));  // word (x-2, x-1)
+    const __half* __restrict__ fr = f + wrap_x(x + 2, int(nx));  // word (x+2, x+3)
+    auto word = [](const __half* p) { return *reinterpret_cast<const __half2*>(p); };
+    __half2 v[19];
+    v[0] = word(fx + rows.row<0, 0>() * nx);
+    sfor<1, 19>([&](auto I) {
+        constexpr int i = I;
+        constexpr int o = opp(i);
+        // slot opp(i) of the source row (y, z shifted by -c_i), same x
+        const uint32_t w1 = a.poff[o] + rows.row<-dcy(i), -dcz(i)>() * nx;
+        const __half2 w = word(fx + w1);
+        if constexpr (dcx(i) == 0) {
+            v[i] = w;
+        } else if constexpr (dcx(i) > 0) {  // sources x-1, x
+            v[i] = __halves2half2(__high2half(word(fl + w1)), __low2half(w));
+        } else {  // sources x+1, x+2
+            v[i] = __halves2half2(__high2half(w), __low2half(word(fr + w1)));
+        }
+    });
+    const uint32_t n = rows.row<0, 0>() * nx + uint32_t(x);
+    __half2 ao[10];
+    float fh[19];
+    collide_pair<FEAT>(v, ao, fh, a, x, n);
+    scatter_pair(a, a.f_out != nullptr ? a.f_out : a.f, ao, fh, x, rows);
 }
 
 }  // namespace
@@ -391,8 +514,31 @@ cudaError_t launch_wide_step(const StepArgs& a, int parity, int feat, dim3 block
     return cudaGetLastError();
 }
 
+bool pair_list_supported(int half_storage, int feat, int nx, uint64_t plane, dim3 block) {
+    return half_storage && feat >= 0 && feat <= 2 && nx % 2 == 0 && block.x % 2 == 0 &&
+           (block.x / 2) * block.y <= 256 && plane % 2 == 0 &&
+           19 * plane < (uint64_t(1) << 32);  // element indices fit 32 bits
+}
+
+cudaError_t launch_pair_list(const StepArgs& a, int parity, int feat, dim3 block,
+                             const uint32_t* list, uint32_t count, cudaStream_t st) {
+    if (count == 0) return cudaSuccess;
+    const ListGrid g = list_grid(a, block);
+    const dim3 threads(block.x / 2, block.y);
+    if (parity == 0) {
+        if (feat == 2) k_pair_list_even<2><<<count, threads, 0, st>>>(a, list, g);
+        else if (feat == 1) k_pair_list_even<1><<<count, threads, 0, st>>>(a, list, g);
+        else k_pair_list_even<0><<<count, threads, 0, st>>>(a, list, g);
+    } else {
+        if (feat == 2) k_pair_list_odd<2><<<count, threads, 0, st>>>(a, list, g);
+        else if (feat == 1) k_pair_list_odd<1><<<count, threads, 0, st>>>(a, list, g);
+        else k_pair_list_odd<0><<<count, threads, 0, st>>>(a, list, g);
+    }
+    return cudaGetLastError();
+}
+
 const PairLaunchers kPair = {&pair_step_supported, &launch_pair_step, &wide_step_supported,
-                             &launch_wide_step};
+                             &launch_wide_step, &pair_list_supported, &launch_pair_list};
 
 }  // namespace STRO_ARITH_NS
 }  // namespace stro

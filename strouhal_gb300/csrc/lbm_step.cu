@@ -18,7 +18,8 @@
 //   GEO  = 0 periodic all-fluid box: no cell bytes, masks or wall logic;
 //          1 walls and/or partially saturated cells;
 //          2 (block lists only) blocks whose only walls are velocity-inflow
-//            columns at x = 0 and x = nx - 1: wall links from x alone.
+//            columns at x = 0 and x = nx - 1: wall links from x alone;
+//          3 (block lists only) a merged list of GEO 0 and GEO 2 blocks.
 //   FEAT = 0 lean collide: no sponge, LES, body force or NT cells;
 //          1 sponge, body force, NT cells, each behind a uniform or per-cell branch;
 //          2 also the Smagorinsky LES block;
@@ -117,34 +118,8 @@ cudaError_t launch_step_capped(const StepArgs& a, int half_storage, int parity, 
 }
 
 // Block-list launches: block i of the grid processes lattice block list[i]
-// (linear index bx + gx * (by + gy * bz)). Used to run the bulk of a walled
-// lattice with the wall-free kernels and only its boundary blocks with the
-// wall-aware ones. The index is split by multiply-shift divisions (a block
-// index is below 2^27: at most 2^32 cells, at least 32 per block), a few
-// instructions per thread instead of two integer divisions.
-struct ListGrid {
-    uint64_t mx, my;  // division_magic of gx and gy
-    uint32_t gx, gy, sx, sy;
-};
-
-static ListGrid list_grid(const StepArgs& a, dim3 block) {
-    ListGrid g;
-    g.gx = (uint32_t(a.nx) + block.x - 1) / block.x;
-    g.gy = (uint32_t(a.ny) + block.y - 1) / block.y;
-    division_magic(g.gx, &g.mx, &g.sx);
-    division_magic(g.gy, &g.my, &g.sy);
-    return g;
-}
-
-__device__ __forceinline__ void list_coords(const uint32_t* list, const ListGrid& g,
-                                            uint32_t& bxi, uint32_t& byi, uint32_t& z) {
-    const uint32_t blk = list[blockIdx.x];
-    const uint32_t t = uint32_t((uint64_t(blk) * g.mx) >> (32 + g.sx));  // blk / gx
-    z = uint32_t((uint64_t(t) * g.my) >> (32 + g.sy));                    // t / gy
-    bxi = blk - t * g.gx;
-    byi = t - z * g.gy;
-}
-
+// (ListGrid, lbm_launch.h). Used to run the bulk of a walled lattice with the
+// wall-free kernels and only its boundary blocks with the wall-aware ones.
 __device__ __forceinline__ void list_block(const uint32_t* list, const ListGrid& g, int& x,
                                            int& y, int& z) {
     uint32_t bxi, byi, bz;
@@ -154,10 +129,33 @@ __device__ __forceinline__ void list_block(const uint32_t* list, const ListGrid&
     z = int(bz);
 }
 
+// GEO 3: a merged list of bulk and x-face blocks in block order (x-face
+// entries flagged kListFaceBit); each block runs the GEO 0 or GEO 2 code, a
+// block-uniform branch. A 128-byte line shared by an x-face block and the
+// bulk block beside it is then fetched from DRAM once: from separate
+// launches each fetched the whole line for its half.
+__device__ __forceinline__ bool list_block_merged(const uint32_t* list, const ListGrid& g, int& x,
+                                                  int& y, int& z) {
+    const uint32_t e = list[blockIdx.x];
+    uint32_t bxi, byi, bz;
+    block_coords(e & ~kListFaceBit, g, bxi, byi, bz);
+    x = int(bxi * blockDim.x + threadIdx.x);
+    y = int(byi * blockDim.y + threadIdx.y);
+    z = int(bz);
+    return (e & kListFaceBit) != 0u;
+}
+
 template <typename S, int GEO, int FEAT, bool PO>
 __global__ void __launch_bounds__(256) k_list_even(const StepArgs a, const uint32_t* list,
                                                    const ListGrid g) {
     int x, y, z;
+    if constexpr (GEO == 3) {
+        const bool face = list_block_merged(list, g, x, y, z);
+        if (x >= a.nx || y >= a.ny || z >= a.nz) return;
+        if (face) even_cell<S, 2, FEAT, false, false, STRO_ARITH, true, PO>(a, x, y, z);
+        else even_cell<S, 0, FEAT, false, false, STRO_ARITH, true, PO>(a, x, y, z);
+        return;
+    }
     list_block(list, g, x, y, z);
     if (x >= a.nx || y >= a.ny || z >= a.nz) return;
     even_cell<S, GEO, FEAT, false, false, STRO_ARITH, true, PO>(a, x, y, z);
@@ -184,6 +182,18 @@ template <typename S, int GEO, int FEAT, bool PO, bool COLMAJOR = false>
 __global__ void __launch_bounds__(256) k_list_odd(const StepArgs a, const uint32_t* list,
                                                   const ListGrid g) {
     int x, y, z;
+    if constexpr (GEO == 3) {
+        const bool face = list_block_merged(list, g, x, y, z);
+        if (x >= a.nx || y >= a.ny || z >= a.nz) return;
+        if (face) {
+            odd_cell_xface<S, FEAT, STRO_ARITH, PO>(a, WallVel(a), x, y, z);
+        } else {
+            double contrib[3];
+            odd_cell<S, 0, FEAT, false, false, STRO_ARITH, true, PO>(a, WallVel(a), x, y, z,
+                                                                     contrib);
+        }
+        return;
+    }
     if constexpr (COLMAJOR) list_block_colmajor(list, g, x, y, z);
     else list_block(list, g, x, y, z);
     if (x >= a.nx || y >= a.ny || z >= a.nz) return;
@@ -206,12 +216,12 @@ static void launch_list(const StepArgs& a, int parity, const uint32_t* list, uin
     const ListGrid g = list_grid(a, block);
     const bool po = GEO != 1 && a.poff[1] != 0;
     if (parity == 0) {
-        if (po) k_list_even<S, GEO, FEAT, GEO != 1><<<count, block, 0, st>>>(a, list, g);
+        if (po) k_list_even<S, GEO, FEAT, true><<<count, block, 0, st>>>(a, list, g);
         else k_list_even<S, GEO, FEAT, false><<<count, block, 0, st>>>(a, list, g);
     } else if (GEO == 1 && colmajor) {
         k_list_odd<S, GEO, FEAT, false, true><<<count, block, 0, st>>>(a, list, g);
     } else if (po) {
-        k_list_odd<S, GEO, FEAT, GEO != 1><<<count, block, 0, st>>>(a, list, g);
+        k_list_odd<S, GEO, FEAT, true><<<count, block, 0, st>>>(a, list, g);
     } else {
         k_list_odd<S, GEO, FEAT, false><<<count, block, 0, st>>>(a, list, g);
     }
@@ -229,15 +239,23 @@ static void launch_list_level(const StepArgs& a, int parity, int feat, const uin
 cudaError_t launch_step_split(const StepArgs& a, int half_storage, int parity, int feat_bulk,
                               int feat_edge, dim3 block, const uint32_t* bulk, uint32_t nbulk,
                               const uint32_t* face, uint32_t nface, const uint32_t* edge,
-                              uint32_t nedge, int edge_colmajor, cudaStream_t st) {
+                              uint32_t nedge, int edge_colmajor, int merged, cudaStream_t st) {
     const bool col = edge_colmajor != 0;
     if (half_storage) {
-        launch_list_level<__half, 0>(a, parity, feat_bulk, bulk, nbulk, block, false, st);
-        launch_list_level<__half, 2>(a, parity, feat_bulk, face, nface, block, false, st);
+        if (merged) {
+            launch_list_level<__half, 3>(a, parity, feat_bulk, bulk, nbulk, block, false, st);
+        } else {
+            launch_list_level<__half, 0>(a, parity, feat_bulk, bulk, nbulk, block, false, st);
+            launch_list_level<__half, 2>(a, parity, feat_bulk, face, nface, block, false, st);
+        }
         launch_list_level<__half, 1>(a, parity, feat_edge, edge, nedge, block, col, st);
     } else {
-        launch_list_level<float, 0>(a, parity, feat_bulk, bulk, nbulk, block, false, st);
-        launch_list_level<float, 2>(a, parity, feat_bulk, face, nface, block, false, st);
+        if (merged) {
+            launch_list_level<float, 3>(a, parity, feat_bulk, bulk, nbulk, block, false, st);
+        } else {
+            launch_list_level<float, 0>(a, parity, feat_bulk, bulk, nbulk, block, false, st);
+            launch_list_level<float, 2>(a, parity, feat_bulk, face, nface, block, false, st);
+        }
         launch_list_level<float, 1>(a, parity, feat_edge, edge, nedge, block, col, st);
     }
     return cudaGetLastError();

@@ -328,9 +328,34 @@ void block_lists(const stro_sim* s, dim3 shape, std::vector<uint32_t>& bulk,
     }
 }
 
+// Feature level of wall-free cells (no solid fraction among them).
+static int bulk_feat(const stro_sim* s) {
+    if (s->collision == STRO_COLLISION_KBC) return 3;
+    if (s->c_smago > 0.0f) return 2;
+    return (sponge_active(s) || force_on(s)) ? 1 : 0;
+}
+
+// Split modes 4 and 5: bulk and x-face blocks run in one launch, from one
+// merged list; mode 5 takes FP16 bulk blocks two cells per thread where the
+// pair kernels apply.
+static bool merged_split(const stro_sim* s) {
+    return (s->merged_faces || s->pair_bulk) && s->face_lists;
+}
+static bool pair_split(const stro_sim* s) {
+    return s->pair_bulk && merged_split(s) &&
+           exact::kPair.list_supported(s->precision == STRO_FP16S ? 1 : 0, bulk_feat(s), s->nx,
+                                       s->plane, s->block);
+}
+
+// d_blocks holds the bulk, x-face and edge lists one after another; in split
+// modes 4 and 5 the bulk and x-face blocks form one list in block order (x-face
+// entries flagged kListFaceBit), so a bulk block and the x-face block beside it
+// run at about the same time and share the DRAM lines they both touch.
 static int ensure_block_lists(stro_sim* s) {
+    const bool merged = merged_split(s);
     if (s->lists_version == s->geo_version && s->lists_block.x == s->block.x &&
-        s->lists_block.y == s->block.y && s->lists_face == s->face_lists)
+        s->lists_block.y == s->block.y && s->lists_face == s->face_lists &&
+        s->lists_merged == merged)
         return STRO_OK;
     const uint32_t bx = s->block.x, by = s->block.y;
     const uint32_t gx = (uint32_t(s->nx) + bx - 1) / bx, gy = (uint32_t(s->ny) + by - 1) / by;
@@ -352,22 +377,27 @@ static int ensure_block_lists(stro_sim* s) {
     s->nbulk = uint32_t(bulk.size());
     s->nface = uint32_t(face.size());
     s->nedge = uint32_t(edge.size());
-    bulk.insert(bulk.end(), face.begin(), face.end());
-    bulk.insert(bulk.end(), edge.begin(), edge.end());
-    STRO_CUDA(cudaMemcpyAsync(s->d_blocks, bulk.data(), nblocks * sizeof(uint32_t),
+    std::vector<uint32_t> all;
+    all.reserve(nblocks);
+    if (merged) {
+        size_t i = 0, j = 0;  // both lists ascend in block index
+        while (i < bulk.size() || j < face.size()) {
+            if (j == face.size() || (i < bulk.size() && bulk[i] < face[j])) all.push_back(bulk[i++]);
+            else all.push_back(face[j++] | kListFaceBit);
+        }
+    } else {
+        all = bulk;
+        all.insert(all.end(), face.begin(), face.end());
+    }
+    all.insert(all.end(), edge.begin(), edge.end());
+    STRO_CUDA(cudaMemcpyAsync(s->d_blocks, all.data(), nblocks * sizeof(uint32_t),
                               cudaMemcpyHostToDevice, st));
-    STRO_CUDA(cudaStreamSynchronize(st));  // `bulk` is released on return
+    STRO_CUDA(cudaStreamSynchronize(st));  // `all` is released on return
     s->lists_block = s->block;
     s->lists_version = s->geo_version;
     s->lists_face = s->face_lists;
+    s->lists_merged = merged;
     return STRO_OK;
-}
-
-// Feature level of wall-free cells (no solid fraction among them).
-static int bulk_feat(const stro_sim* s) {
-    if (s->collision == STRO_COLLISION_KBC) return 3;
-    if (s->c_smago > 0.0f) return 2;
-    return (sponge_active(s) || force_on(s)) ? 1 : 0;
 }
 
 cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool probe) {
@@ -378,11 +408,19 @@ cudaError_t launch_sim_step(stro_sim* s, const StepArgs& a, int64_t t, bool prob
     const RowsLaunchers& R = fused ? fused::kRows : exact::kRows;
     if (geo && !probe && s->variant == 0 && s->split && s->geo_host.size() == s->N) {
         if (ensure_block_lists(s) != STRO_OK) return cudaErrorMemoryAllocation;
-        s->last_path = "split";
+        const bool merged = s->lists_merged, pair = merged && pair_split(s);
+        s->last_path = pair ? "split-pair" : (merged ? "split-merged" : "split");
+        if (pair) {
+            const PairLaunchers& PL = fused ? fused::kPair : exact::kPair;
+            const cudaError_t e = PL.list_launch(a, int(t & 1), bulk_feat(s), s->block,
+                                                 s->d_blocks, s->nbulk + s->nface, sim_stream(s));
+            if (e != cudaSuccess) return e;
+        }
         return L.split(a, half, int(t & 1), bulk_feat(s), feat_on(s), s->block, s->d_blocks,
-                       s->nbulk, s->d_blocks + s->nbulk, s->nface,
+                       pair ? 0u : (merged ? s->nbulk + s->nface : s->nbulk),
+                       s->d_blocks + s->nbulk, merged ? 0u : s->nface,
                        s->d_blocks + s->nbulk + s->nface, s->nedge, s->edge_colmajor ? 1 : 0,
-                       sim_stream(s));
+                       merged ? 1 : 0, sim_stream(s));
     }
     const PairLaunchers& PL = fused ? fused::kPair : exact::kPair;
     const bool kbc = s->collision == STRO_COLLISION_KBC;  // one-cell kernels only
@@ -449,7 +487,8 @@ std::vector<uint8_t> graph_key(const stro_sim* s, int64_t t, int64_t G) {
                            s->arith, s->collision, s->precision, geo_on(s) ? 1 : 0, feat_on(s),
                            bulk_feat(s), int64_t(reinterpret_cast<uintptr_t>(s->d_blocks)),
                            s->nbulk, s->nface, s->nedge, int64_t(s->lists_version),
-                           s->face_lists ? 1 : 0, s->lists_face ? 1 : 0,
+                           s->face_lists ? 1 : 0, s->lists_face ? 1 : 0, s->pair_bulk ? 1 : 0,
+                           s->merged_faces ? 1 : 0, s->lists_merged ? 1 : 0,
                            int64_t(s->geo_version), s->lists_block.x, s->lists_block.y,
                            int64_t(reinterpret_cast<uintptr_t>(s->d_error)), s->rows_polls,
                            s->ctx->sm_count,

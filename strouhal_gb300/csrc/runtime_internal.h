@@ -84,9 +84,12 @@ struct stro_sim {
     bool split = true;
     bool edge_colmajor = false;    // boundary blocks of the odd pass in column-major cell order
     bool face_lists = true;        // x-face blocks on their own kernels (else boundary blocks)
+    bool merged_faces = false;     // bulk and x-face blocks in one launch (split mode 4)
+    bool pair_bulk = false;        // and FP16 bulk blocks two cells per thread (split mode 5)
     uint32_t* d_blocks = nullptr;  // bulk blocks first, then x-face, then edge blocks
     uint32_t nbulk = 0, nface = 0, nedge = 0;
     bool lists_face = false;       // face_lists when the lists were built
+    bool lists_merged = false;     // bulk and x-face blocks in one list (split modes 4 and 5)
     dim3 lists_block{0, 0, 0};
     uint64_t lists_version = ~0ull;
     uint64_t geo_version = 0;      // bumped whenever the device geometry changes

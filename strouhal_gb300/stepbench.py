@@ -29,10 +29,11 @@ def main(argv=None):
                     help="the DFG 2D-2 street at D cells per diameter instead of the TGV box")
     ap.add_argument("--sphere", action="store_true",
                     help="the 512x256x256 sphere wake (FP16 storage, LES, NT sphere, sponge)")
-    ap.add_argument("--split", type=int, default=-1, choices=[-1, 0, 1, 2, 3],
+    ap.add_argument("--split", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 4, 5],
                     help="bulk / boundary split of walled lattices (-1 = library default, "
                          "2 = split with column-major boundary blocks in the odd pass, "
-                         "3 = split without the x-face blocks)")
+                         "3 = split without the x-face blocks, 4 = bulk and x-face blocks "
+                         "in one launch, 5 = as 4 with FP16 bulk blocks two cells per thread)")
     ap.add_argument("--collision", default="reference", choices=["reference", "kbc"],
                     help="collision operator (stro_sim_set_collision)")
     ap.add_argument("--steps", type=int, default=20)
@@ -61,7 +62,8 @@ def main(argv=None):
     if a.collision != "reference":
         s.collision = a.collision
     if a.split >= 0:
-        s.setBlockSplit({2: "columns", 3: "noface"}.get(a.split, bool(a.split)))
+        s.setBlockSplit({2: "columns", 3: "noface", 4: "merged", 5: "pair"}.get(
+            a.split, bool(a.split)))
     if a.variant < 0:
         s.autotune(steps=10)
     else:

@@ -148,3 +148,28 @@ def test_adjoint_fp16_storage(gpu, oracle):
     assert _rel(ge[nt], geo[nt]) < 2e-2
     assert _rel(gf, gfo) < 2e-2
     adj.close()
+
+
+def test_adjoint_merged_split_is_bitwise_neutral(gpu, oracle):
+    """FP16 storage: the forward window and the segment recomputation (out of
+    place) with the bulk and x-face blocks in one launch, one or two cells per
+    thread, give the objective and gradients of the default split bit for bit."""
+    import strouhal_gb300 as sg
+
+    out = []
+    for split in (True, "merged", "pair"):
+        g, o, eps, _ = _setup(sg, oracle, gpu, "fp16s", seed=11)
+        g.block = (8, 4)  # 8-wide blocks leave bulk blocks between the disk and the walls
+        g.setBlockSplit(split)
+        adj = sg.Adjoint(g, 10, BOX, checkpoints=3)
+        J = adj.forward()
+        ge, gf = adj.backward()
+        if split != True:  # noqa: E712
+            assert g.lastPath == "split-" + split, g.lastPath
+            assert g.splitBlocks[0] > 0 and g.splitBlocks[1] > 0
+        out.append((J, ge, gf))
+        adj.close()
+        g.close()
+    for J, ge, gf in out[1:]:
+        assert J == out[0][0]
+        assert np.array_equal(ge, out[0][1]) and np.array_equal(gf, out[0][2])

@@ -155,6 +155,73 @@ def test_step_matches_oracle(gpu, oracle, kind, geometry, feature):
     g.close()
 
 
+@pytest.mark.parametrize("split,kind", [("pair", 1), ("merged", 1), ("merged", 0)])
+@pytest.mark.parametrize("arith", ["reference", "fused"])
+@pytest.mark.parametrize("geometry", ["channel", "xfaces", "ywalls"])
+@pytest.mark.parametrize("feature", ["plain", "les", "ffield_all"])
+@pytest.mark.parametrize("block", [(16, 4), (64, 1), (8, 8), (32, 3)])
+def test_merged_split_matches_oracle(gpu, oracle, split, kind, arith, geometry, feature, block):
+    """Block splits "merged" and "pair": the bulk and x-face blocks of a walled
+    lattice run in one launch from one list, beside the wall-aware blocks;
+    "pair" takes the bulk blocks of FP16 storage two x-adjacent cells per
+    thread (4-byte words) and the x-face blocks two cells per thread one after
+    the other. ywalls: walls at y = 0 and y = ny - 1 only, so bulk blocks reach
+    x = 0 and x = nx - 1 and the pair gather wraps in x. Odd ny and nz leave
+    partial blocks."""
+    import strouhal_gb300 as sg
+
+    po = oracle
+    nx, ny, nz = 134, 21, 7
+    rng = np.random.default_rng(hash((split, kind, arith, geometry, feature, block)) & 0xFFFFFF)
+    flags = np.zeros((nz, ny, nx), np.uint8)
+    if geometry == "channel":
+        flags[:, 0, :] = flags[:, -1, :] = po.SOLID
+        flags[:, 1:-1, 0] = flags[:, 1:-1, -1] = po.INFLOW
+        flags[:, 8:11, 70:74] = po.SOLID
+    elif geometry == "xfaces":
+        flags[:, :, 0] = flags[:, :, -1] = po.INFLOW
+        flags[:, 8:11, 70:74] = po.SOLID
+    else:
+        flags[:, 0, :] = po.SOLID
+        flags[:, -1, :] = po.LID
+    opts = dict(FEATURES[feature])
+    eps = None
+    if opts.pop("eps", False):  # NT cells in x = 40..60 only
+        eps = np.zeros(nx * ny * nz, np.float32)
+        cand = np.flatnonzero((np.arange(nx * ny * nz) % nx >= 40) &
+                              (np.arange(nx * ny * nz) % nx <= 60))
+        idx = rng.choice(cand, 150, replace=False)
+        eps[idx] = rng.uniform(0.02, 0.98, idx.size).astype(np.float32)
+    ffield = opts.pop("ffield", False)
+    g, o = _mk_pair(sg, po, gpu, kind, nx, ny, nz, flags=flags.reshape(-1), eps=eps,
+                    omega=1.55, omegaMinus=1.2, lid=(0.07, 0.0, 0.01), uin=0.05, rampSteps=7,
+                    wantsForces=True, arithmetic=arith, **opts)
+    if ffield:
+        ff = random_force_field(rng, nx * ny * nz)
+        g.setForceField(ff)
+        o.setForceField(ff)
+    g.setBlockSplit(split)
+    g.block = block
+    f0 = (rng.standard_normal((19, nx * ny * nz)) * 0.01).astype(o.f.dtype)
+    o.f[:] = f0
+    g.uploadState(f0)
+    for chunk in (1, 4, 3):
+        g.run(chunk)
+        o.run(chunk)
+        assert g.lastPath == "split-" + split, g.lastPath
+        assert np.array_equal(g.downloadState(), o.f), (chunk, g.stepsDone)
+    assert g.splitBlocks[0] > 0  # the merged launch ran bulk blocks
+    if geometry == "xfaces":
+        assert g.splitBlocks[1] > 0  # and x-face blocks
+    box = ((3, 100), (1, 18))
+    fg, fo = g.probeForce(*box), o.probeForce(*box)
+    assert np.allclose(fg, fo, rtol=1e-12, atol=1e-12), (fg, fo)
+    g.run(2)
+    o.run(2)
+    assert np.array_equal(g.downloadState(), o.f)
+    g.close()
+
+
 @pytest.mark.parametrize("kind,tol", [(0, 1e-5), (1, 2e-3)])
 def test_fp64_oracle_tolerance(gpu, oracle, kind, tol):
     """DDFs after N = 50 steps vs the FP64 oracle: normwise relative error <= tol.

@@ -108,7 +108,7 @@ def test_block_split_is_bitwise_neutral(gpu, precision):
     flags[:, 0, :] = sg.Cell.solid
     eps = sg.sphereSolidFractions(nx, ny, nz, 30.5, 20.0, 12.0, 6.0, 4)
     digests = []
-    for split in (True, False, "columns", "noface"):
+    for split in (True, False, "columns", "noface", "merged", "pair"):
         s = sg.Simulation(gpu, precision=precision, nx=nx, ny=ny, nz=nz, omega=1.8, uin=0.05,
                           rampSteps=10, cSmago=0.01, flags=flags.reshape(-1))
         s.inflowUniform = True
