@@ -32,6 +32,8 @@ variants.c3_adjoint / c5_adjoint : device time of the discrete adjoint's
         backward sweep (recomputation included) over its forward window on the
         full cylinder (1410x264x3, 10,000-step window, 20 checkpoints) and
         sphere-wake (512x256x256, 2,000-step window, 45 checkpoints) lattices.
+variants.c2_dissipation_adjoint : the same for the time-averaged dissipation
+        objective on the 256^3 Taylor-Green lattice (FP16 storage).
 
 --impl reference times the CPU restatement of the reference arithmetic (the
 oracle, OpenMP over all host cores) on the same workload, one bench step = one
@@ -296,6 +298,33 @@ def run_sphere(gpu, peak, steps=200):
     return out
 
 
+def run_dissipation_adjoint(sg, gpu, window=200, every=20, checkpoints=14):
+    """Discrete adjoint of the time-averaged dissipation on the C2 lattice."""
+    L, nu, tau = tgv_params()
+    wp, wm = sg.trtOmegas(tau, None)
+    s = sg.Simulation(gpu, precision="fp16s", nx=N_EDGE, ny=N_EDGE, nz=N_EDGE, omega=wp,
+                      omegaMinus=wm)
+    s.initField(2, U0)
+    s.autotune(steps=10)
+    s.run(200)
+    adj = sg.Adjoint(s, window, checkpoints=checkpoints, dissipationEvery=every)
+    J = adj.forward()
+    _, gf = adj.backward()
+    st = adj.stats()
+    adj.close()
+    s.close()
+    fwd = st["forward_s"]
+    return {"workload": "TGV Re=1600 periodic 256^3, FP16-storage SRT (reference arithmetic), "
+                        "mean dissipation sum over the states after every %d of %d steps, "
+                        "after a 200-step spin-up, %d checkpoints, d/d force field"
+                        % (every, window, checkpoints),
+            "J": J, "grad_force_norm": float(np.linalg.norm(gf)),
+            "grad_finite": bool(np.all(np.isfinite(gf))),
+            "forward_s": fwd, "recompute_s": st["recompute_s"], "adjoint_s": st["adjoint_s"],
+            "backward_over_forward": (st["recompute_s"] + st["adjoint_s"]) / fwd,
+            "adjoint_step_over_forward_step": st["adjoint_s"] / fwd}
+
+
 def run_adjoints(gpu):
     """Backward / forward device time of the discrete adjoint on the C3 and C5 lattices."""
     from strouhal_gb300 import cases
@@ -384,7 +413,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-workloads", action="store_true",
                     help="skip the sphere-wake, batched-ladder and adjoint workloads "
-                         "(variants.c5_sphere, c4_batched, c3_adjoint, c5_adjoint)")
+                         "(variants.c5_sphere, c4_batched, c3_adjoint, c5_adjoint, "
+                         "c2_dissipation_adjoint)")
     ap.add_argument("--clocks-csv", default=None,
                     help="keep the nvidia-smi samples of the timed region in this file")
     args = ap.parse_args()
@@ -414,6 +444,7 @@ def main():
         extra["c5_sphere"] = run_sphere(gpu, peak)
         extra["c4_batched"] = run_c4_ladder(gpu)
         extra.update(run_adjoints(gpu))
+        extra["c2_dissipation_adjoint"] = run_dissipation_adjoint(sg, gpu)
     traffic = profile_traffic()
 
     def summarise(r, precision):

@@ -353,6 +353,16 @@ int stro_adj_create(stro_sim* sim, const double dir[3], const int32_t box[4], in
 int stro_adj_destroy(stro_adjoint* adj);
 int stro_adj_forward(stro_adjoint* adj, double* J);
 int stro_adj_backward(stro_adjoint* adj, float* grad_eps, float* grad_force);
+/* Switches the objective to the time-averaged dissipation:
+ *   J = mean over m = 1 .. steps / every of D(t0 + m every),
+ * D = the dissipation sum of stro_sim_dissipation (2 nu S:S over the fluid
+ * cells; the viscous dissipation the reference's Taylor-Green case reads,
+ * Cases.swift:1254-1270) of the state after m * every steps. `every` is even
+ * and at most the window; the window must start at an even step count
+ * (STRO_ERR_STATE otherwise). dir and box are then unused; the gradients keep
+ * their meaning (dJ/d F_field includes D's own dependence on the force through
+ * u = (p + F/2) / rho). */
+int stro_adj_set_dissipation(stro_adjoint* adj, int64_t every);
 /* Device seconds of the last forward, of the recomputation and of the adjoint
  * steps, and the number of adjoint steps run. */
 int stro_adj_stats(stro_adjoint* adj, double* forward_s, double* recompute_s, double* adjoint_s,

@@ -753,6 +753,43 @@ void moments_all(const void* fv, const uint8_t* flags, const Params& p, const fl
 // second moment of f - feq (full equilibrium), nu = (1/omega - 1/2)/3. R is
 // the arithmetic of the per-cell values; both sums are accumulated in double,
 // per thread over a static range of cells and then in thread order.
+// |u|^2 (u2) and sc^2 Pi:Pi of one fluid cell from its 19 DDFs v (natural
+// slots, even step count) and its Guo force F: Pi is the non-equilibrium
+// second moment and sc = 1.5 omega / rho, so the cell's dissipation 2 nu S:S
+// is 2 nu times the result. Shared by the observables and, in dual numbers,
+// by the adjoint of the time-averaged dissipation.
+template <class R>
+inline R cell_strain2(const R (&v)[19], const R (&F)[3], R om, R& u2) {
+    R rhom1 = v[0];
+    for (int i = 1; i < 19; ++i) rhom1 += v[i];
+    R pc[3] = {R(0), R(0), R(0)};
+    for (int i = 1; i < 19; ++i) {
+        pc[0] += R(CX[i]) * v[i];
+        pc[1] += R(CY[i]) * v[i];
+        pc[2] += R(CZ[i]) * v[i];
+    }
+    const R rho = R(1) + rhom1;
+    const R ux = (pc[0] + R(0.5) * F[0]) / rho, uy = (pc[1] + R(0.5) * F[1]) / rho,
+            uz = (pc[2] + R(0.5) * F[2]) / rho;
+    u2 = ux * ux + uy * uy + uz * uz;
+    R P[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};
+    for (int i = 1; i < 19; ++i) {
+        const R cu = R(3) * (R(CX[i]) * ux + R(CY[i]) * uy + R(CZ[i]) * uz);
+        const R feq = weight<R>(i) * (rhom1 + rho * (cu + R(0.5) * cu * cu - R(1.5) * u2));
+        const R d = v[i] - feq;
+        P[0] += R(CX[i] * CX[i]) * d;
+        P[1] += R(CY[i] * CY[i]) * d;
+        P[2] += R(CZ[i] * CZ[i]) * d;
+        P[3] += R(CX[i] * CY[i]) * d;
+        P[4] += R(CX[i] * CZ[i]) * d;
+        P[5] += R(CY[i] * CZ[i]) * d;
+    }
+    const R pipi = P[0] * P[0] + P[1] * P[1] + P[2] * P[2] +
+                   R(2) * (P[3] * P[3] + P[4] * P[4] + P[5] * P[5]);
+    const R sc = R(1.5) * om / rho;
+    return sc * sc * pipi;
+}
+
 template <class R, class S>
 void observables_all(const void* fv, const uint8_t* flags, const Params& p, const float* ffield,
                      double omega, int threads, double out[2]) {
@@ -775,37 +812,12 @@ void observables_all(const void* fv, const uint8_t* flags, const Params& p, cons
             if (flags && flags[n] != FLUID) continue;
             R v[19];
             for (int i = 0; i < 19; ++i) v[i] = R(f[size_t(i) * N + n]);
-            R rhom1 = v[0];
-            for (int i = 1; i < 19; ++i) rhom1 += v[i];
-            R pc[3] = {0, 0, 0};
-            for (int i = 1; i < 19; ++i) {
-                pc[0] += R(CX[i]) * v[i];
-                pc[1] += R(CY[i]) * v[i];
-                pc[2] += R(CZ[i]) * v[i];
-            }
             R F[3];
             cell_force<R>(p, ffield, N, n, F);
-            const R rho = R(1) + rhom1;
-            const R ux = (pc[0] + R(0.5) * F[0]) / rho, uy = (pc[1] + R(0.5) * F[1]) / rho,
-                    uz = (pc[2] + R(0.5) * F[2]) / rho;
-            const R u2 = ux * ux + uy * uy + uz * uz;
+            R u2;
+            const R t = cell_strain2<R>(v, F, om, u2);
             ke += double(u2);
-            R P[6] = {0, 0, 0, 0, 0, 0};
-            for (int i = 1; i < 19; ++i) {
-                const R cu = R(3) * (R(CX[i]) * ux + R(CY[i]) * uy + R(CZ[i]) * uz);
-                const R feq = weight<R>(i) * (rhom1 + rho * (cu + R(0.5) * cu * cu - R(1.5) * u2));
-                const R d = v[i] - feq;
-                P[0] += R(CX[i] * CX[i]) * d;
-                P[1] += R(CY[i] * CY[i]) * d;
-                P[2] += R(CZ[i] * CZ[i]) * d;
-                P[3] += R(CX[i] * CY[i]) * d;
-                P[4] += R(CX[i] * CZ[i]) * d;
-                P[5] += R(CY[i] * CZ[i]) * d;
-            }
-            const R pipi = P[0] * P[0] + P[1] * P[1] + P[2] * P[2] +
-                           R(2) * (P[3] * P[3] + P[4] * P[4] + P[5] * P[5]);
-            const R sc = R(1.5) * om / rho;
-            ds += 2.0 * nu * double(sc * sc * pipi);
+            ds += 2.0 * nu * double(t);
         }
         part[2 * size_t(tid)] = ke;
         part[2 * size_t(tid) + 1] = ds;
@@ -967,6 +979,46 @@ void reverse(const Params& p, const Ctx& c, const double* S, double* lam, double
         if (grad_eps) grad_eps[n] += g[19];
         if (grad_f)
             for (int k = 0; k < 3; ++k) grad_f[k * c.N + n] += g[20 + k];
+    }
+}
+
+// Sum of 2 nu S:S over the fluid cells of the state A (an even step count),
+// in FP64: the dissipation observable of the adjoint's dissipation objective.
+double dissipation(const Params& p, const Ctx& c, const double* A, double omega) {
+    const double nu = (1.0 / omega - 0.5) / 3.0;
+    double out = 0.0;
+    for (size_t n = 0; n < c.N; ++n) {
+        if (c.flags && c.flags[n] != FLUID) continue;
+        double v[19], F[3], u2;
+        for (int i = 0; i < 19; ++i) v[i] = A[size_t(i) * c.N + n];
+        cell_force<double>(p, c.ffield, c.N, n, F);
+        out += 2.0 * nu * cell_strain2<double>(v, F, omega, u2);
+    }
+    return out;
+}
+
+// lam += w dD/dA and grad_f += w dD/dF_field for the dissipation D of the
+// state A (natural slots at an even step count), each cell's gradient from
+// dual numbers over its 19 DDFs and its force.
+void inject_dissipation(const Params& p, const Ctx& c, const double* A, double omega, double w,
+                        double* lam, double* grad_f) {
+    typedef Dual<22> D;
+    const double nu = (1.0 / omega - 0.5) / 3.0;
+    const long long N = (long long)c.N;
+#pragma omp parallel for schedule(static) num_threads(c.threads > 0 ? c.threads : 1) if (c.threads > 1)
+    for (long long nn = 0; nn < N; ++nn) {
+        const size_t n = size_t(nn);
+        if (c.flags && c.flags[n] != FLUID) continue;
+        D v[19], F[3], u2;
+        for (int i = 0; i < 19; ++i) v[i] = D::var(A[size_t(i) * c.N + n], i);
+        double Fv[3];
+        cell_force<double>(p, c.ffield, c.N, n, Fv);
+        for (int k = 0; k < 3; ++k) F[k] = D::var(Fv[k], 19 + k);
+        const D t = cell_strain2<D>(v, F, D(omega), u2);
+        const double g = w * 2.0 * nu;
+        for (int i = 0; i < 19; ++i) lam[size_t(i) * c.N + n] += g * t.d[i];
+        if (grad_f)
+            for (int k = 0; k < 3; ++k) grad_f[size_t(k) * c.N + n] += g * t.d[19 + k];
     }
 }
 
@@ -1175,6 +1227,72 @@ int orc_adjoint_force_ex(int traj, const double* f0, const uint8_t* flags,
         }
         for (int t = t1 - 1; t >= t0; --t)
             adj::reverse(P[t], c, seg[t - t0].data(), lam.data(), w, grad_eps, grad_f);
+        ckpt[s].clear();
+        ckpt[s].shrink_to_fit();
+    }
+    return 0;
+}
+
+// FP64 discrete adjoint of the time-averaged dissipation
+//   J = (1/K) sum over m = 1..K of D(t0 + m every),  K = steps / every,
+// D = sum over fluid cells of 2 nu S:S of the state after m every steps of the
+// window (orc_observables' out[1], evaluated in FP64 from the stored values;
+// every even, the window starting at an even step count, so the sampled
+// states have natural slots). traj, params, chk, threads and the outputs as
+// orc_adjoint_force_ex; omega is the lattice's (nu = (1/omega - 1/2) / 3).
+// D depends on the force field directly (u = (p + F/2) / rho) and through the
+// dynamics; on eps only through the dynamics.
+int orc_adjoint_dissipation_ex(int traj, const double* f0, const uint8_t* flags,
+                               const uint32_t* solid_mask, const uint32_t* lid_mask,
+                               const void* params, int steps, int every, double omega,
+                               const float* eps, const float* ffield, int threads, int chk,
+                               double* J_out, double* grad_eps, double* grad_f) {
+    if (steps <= 0 || traj < 0 || traj > 2 || every <= 0 || every % 2 != 0) return 1;
+    const int K = steps / every;
+    if (K < 1) return 1;
+    std::vector<Params> P(steps);
+    std::memcpy(P.data(), params, sizeof(Params) * steps);
+    if (P[0].parity != 0u) return 1;  // the window starts at an even step count
+    for (int t = 0; t < steps; ++t) P[t].writeForce = 0u;
+    const size_t N = size_t(P[0].nx) * P[0].ny * P[0].nz;
+    const double w = 1.0 / K;
+    const int nobox[4] = {0, -1, 0, -1};
+    const double nodir[3] = {0.0, 0.0, 0.0};
+    const adj::Ctx c{flags, solid_mask, lid_mask, eps, ffield, nobox, nodir, N, threads};
+    const bool grads = grad_eps || grad_f;
+    if (chk <= 0 || chk > steps) chk = steps;
+    const int nseg = (steps + chk - 1) / chk;
+    std::vector<double> A(f0, f0 + 19 * N), contrib(N);
+    std::vector<std::vector<double>> ckpt(grads ? nseg : 0);
+    double J = 0.0;
+    for (int t = 0; t < steps; ++t) {  // forward; checkpoints at the segment starts
+        if (grads && t % chk == 0) ckpt[t / chk] = A;
+        adj::step_traj(traj, P[t], c, A.data(), contrib.data());
+        if ((t + 1) % every == 0 && (t + 1) / every <= K)
+            J += w * adj::dissipation(P[0], c, A.data(), omega);
+    }
+    *J_out = J;
+    if (!grads) return 0;
+    if (grad_eps) std::fill(grad_eps, grad_eps + N, 0.0);
+    if (grad_f) std::fill(grad_f, grad_f + 3 * N, 0.0);
+    std::vector<double> lam(19 * N, 0.0);
+    if (steps % every == 0)  // the final state is the last sample
+        adj::inject_dissipation(P[0], c, A.data(), omega, w, lam.data(), grad_f);
+    std::vector<std::vector<double>> seg(chk);
+    for (int s = nseg - 1; s >= 0; --s) {  // reverse, one recomputed segment at a time
+        const int t0 = s * chk, t1 = std::min(steps, t0 + chk);
+        seg[0] = ckpt[s];
+        for (int t = t0 + 1; t < t1; ++t) {
+            seg[t - t0] = seg[t - t0 - 1];
+            adj::step_traj(traj, P[t - 1], c, seg[t - t0].data(), contrib.data());
+        }
+        for (int t = t1 - 1; t >= t0; --t) {
+            adj::reverse(P[t], c, seg[t - t0].data(), lam.data(), 0.0, grad_eps, grad_f);
+            // lam is now the adjoint of the state after t steps: a sample there?
+            if (t > 0 && t % every == 0 && t / every <= K)
+                adj::inject_dissipation(P[0], c, seg[t - t0].data(), omega, w, lam.data(),
+                                        grad_f);
+        }
         ckpt[s].clear();
         ckpt[s].shrink_to_fit();
     }

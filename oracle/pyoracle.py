@@ -63,6 +63,9 @@ def lib():
                                         _P]
         L.orc_adjoint_force_ex.argtypes = ([ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_int, _P,
                                             _P, _P, _P, ctypes.c_int, ctypes.c_int, _P, _P, _P])
+        L.orc_adjoint_dissipation_ex.argtypes = ([ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_int,
+                                                  ctypes.c_int, ctypes.c_double, _P, _P,
+                                                  ctypes.c_int, ctypes.c_int, _P, _P, _P])
         L.orc_mass.argtypes = [ctypes.c_int, _P, ctypes.c_size_t]
         L.orc_observables.argtypes = [ctypes.c_int, _P, _P, _P, _P, ctypes.c_double,
                                       ctypes.c_int, _P]
@@ -330,6 +333,36 @@ class OracleSim:
                                         int(checkpoint), ctypes.byref(J), _ptr(ge), _ptr(gf))
         if rc != 0:
             raise RuntimeError("orc_adjoint_force_ex failed")
+        return J.value, ge, gf
+
+    def adjointDissipation(self, steps, every, grads=True, trajectory="fp64", f0=None,
+                           threads=None, checkpoint=0):
+        """FP64 adjoint of J = mean over m = 1 .. steps // every of the
+        dissipation sum (2 nu S:S over fluid cells, as observables()) of the
+        state after m * every steps of the window; `every` even and the window
+        starting at an even step count. Arguments and returns as adjointForce."""
+        traj = {"fp32": 0, "fp16": 1, "fp64": 2}[trajectory]
+        if self.stepsDone % 2 != 0 or every % 2 != 0 or steps < every:
+            raise ValueError("dissipation samples need even step counts and steps >= every")
+        src = self.f if f0 is None else f0
+        f0 = np.ascontiguousarray(src, dtype=np.float64).reshape(19, self.N)
+        if self.outflowMode != "dormant" or self.collision != "reference":
+            raise ValueError("the oracle adjoint covers the dormant outflow wall and the "
+                             "reference collision only")
+        if threads is None:
+            threads = os.cpu_count() or 1
+        P = b"".join(self.params(self.stepsDone + t) for t in range(int(steps)))
+        J = ctypes.c_double()
+        ge = np.zeros(self.N) if grads else None
+        gf = np.zeros((3, self.N)) if grads else None
+        rc = lib().orc_adjoint_dissipation_ex(traj, _ptr(f0), _ptr(self.flags),
+                                              _ptr(self.solidMask), _ptr(self.lidMask), P,
+                                              int(steps), int(every), float(self.omega),
+                                              _ptr(self.eps), _ptr(self.forceField),
+                                              int(threads), int(checkpoint), ctypes.byref(J),
+                                              _ptr(ge), _ptr(gf))
+        if rc != 0:
+            raise RuntimeError("orc_adjoint_dissipation_ex failed")
         return J.value, ge, gf
 
     def massSum(self):

@@ -170,6 +170,7 @@ def lib():
         "stro_adj_destroy": ([_P], c_int),
         "stro_adj_forward": ([_P, ctypes.POINTER(c_double)], c_int),
         "stro_adj_backward": ([_P, _P, _P], c_int),
+        "stro_adj_set_dissipation": ([_P, ctypes.c_int64], c_int),
         "stro_adj_stats": ([_P, ctypes.POINTER(c_double), ctypes.POINTER(c_double),
                             ctypes.POINTER(c_double), ctypes.POINTER(c_i64)], c_int),
         "stro_sha256_hex": ([_P, ctypes.c_size_t, ctypes.c_char_p], c_int),
@@ -777,20 +778,29 @@ class Batch:
 
 
 class Adjoint:
-    """Discrete adjoint of the time-averaged force over a window (stro_adj_*).
+    """Discrete adjoint of a time-averaged objective over a window (stro_adj_*).
 
-    J = mean over the odd steps of direction . F_box, F_box the force the
-    probe box sums. forward() advances the simulation through the window and
-    returns J; backward() returns (dJ/d eps, dJ/d F_field) as float32 arrays of
-    shapes (N,) and (3, N)."""
+    Default objective: J = mean over the odd steps of direction . F_box, F_box
+    the force the probe box sums. With dissipationEvery = m (even): J = mean
+    of the dissipation sum (dissipationSum) of the states after m, 2m, ...
+    steps of the window (box and direction unused). forward() advances the
+    simulation through the window and returns J; backward() returns
+    (dJ/d eps, dJ/d F_field) as float32 arrays of shapes (N,) and (3, N)."""
 
-    def __init__(self, sim, steps, box, direction=(1.0, 0.0, 0.0), checkpoints=8):
+    def __init__(self, sim, steps, box=((0, 0), (0, 0)), direction=(1.0, 0.0, 0.0),
+                 checkpoints=8, dissipationEvery=None):
         self.sim = sim
         d3 = (ctypes.c_double * 3)(*[float(v) for v in direction])
         b4 = (ctypes.c_int32 * 4)(int(box[0][0]), int(box[0][1]), int(box[1][0]), int(box[1][1]))
         self._h = _P()
         _check(lib().stro_adj_create(sim._h, d3, b4, int(steps), int(checkpoints),
                                      ctypes.byref(self._h)))
+        if dissipationEvery is not None:
+            try:
+                _check(lib().stro_adj_set_dissipation(self._h, int(dissipationEvery)))
+            except Exception:
+                self.close()
+                raise
 
     def forward(self):
         J = ctypes.c_double()

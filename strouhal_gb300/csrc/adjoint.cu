@@ -37,6 +37,12 @@ struct stro_adjoint {
     uint32_t* d_lists = nullptr; // bulk blocks, then boundary blocks, of the reverse-step grid
     uint32_t nbulk = 0, nedge = 0;
     int64_t nodd = 0;
+    // objective: 0 = mean force over the odd steps; 1 = mean dissipation sum
+    // over the states after every, 2 every, ... steps of the window
+    int objective = 0;
+    int64_t every = 0;
+    double* d_diss = nullptr;   // (kinetic energy, dissipation) per sample
+    void* d_final = nullptr;    // the window's last state, when it is a sample
     double J = 0.0;
     double fwd_seconds = 0.0, recompute_seconds = 0.0, adjoint_seconds = 0.0;
     int64_t adjoint_launches = 0;
@@ -53,6 +59,8 @@ void adj_free(stro_adjoint* a) {
     cudaFree(a->d_gf);
     cudaFree(a->d_forces);
     cudaFree(a->d_lists);
+    cudaFree(a->d_diss);
+    cudaFree(a->d_final);
     if (a->e0) cudaEventDestroy(a->e0);
     if (a->e1) cudaEventDestroy(a->e1);
 }
@@ -67,6 +75,64 @@ int timed(stro_adjoint* a, double* acc, int rc_in) {
     float ms = 0.f;
     STRO_CUDA(cudaEventElapsedTime(&ms, a->e0, a->e1));
     *acc += double(ms) * 1e-3;
+    return STRO_OK;
+}
+
+// Forward window of the dissipation objective: plain steps (no force probe),
+// the observables reduction after every `every` steps into d_diss, and a copy
+// of the last state when it is a sample (the reverse sweep injects there
+// first). J = mean of the sampled dissipation sums.
+int forward_dissipation(stro_adjoint* a) {
+    stro_sim* s = a->sim;
+    cudaStream_t st = s->ctx->stream;
+    if (s->steps_done % 2 != 0)
+        return fail(STRO_ERR_STATE, "the dissipation objective needs an even step count at the start");
+    a->t0 = s->steps_done;
+    a->nodd = 0;
+    const int64_t K = a->steps / a->every;
+    if (!a->d_diss) STRO_CUDA(cudaMalloc(&a->d_diss, size_t(2 * K) * sizeof(double)));
+    if (a->steps % a->every == 0 && !a->d_final)
+        STRO_CUDA(cudaMalloc(&a->d_final, a->state_bytes));
+    const int half = s->precision == STRO_FP16S ? 1 : 0;
+    STRO_CUDA(cudaEventRecord(a->e0, st));
+    for (int64_t k = 0; k < a->steps; ++k) {
+        const int64_t t = a->t0 + k;
+        if (k % a->seg == 0)
+            STRO_CUDA(cudaMemcpyAsync(state_at(a->d_check, a->state_bytes, k / a->seg), s->d_f,
+                                      a->state_bytes, cudaMemcpyDeviceToDevice, st));
+        STRO_CUDA(launch_sim_step(s, step_args(s, t), t, false));
+        if ((k + 1) % a->every == 0 && (k + 1) / a->every <= K)
+            STRO_CUDA(launch_observables(field_view(s), half, s->omega, s->d_partials,
+                                         a->d_diss + 2 * ((k + 1) / a->every - 1), st));
+    }
+    if (a->d_final)
+        STRO_CUDA(cudaMemcpyAsync(a->d_final, s->d_f, a->state_bytes, cudaMemcpyDeviceToDevice,
+                                  st));
+    int rc = timed(a, &a->fwd_seconds, STRO_OK);
+    if (rc != STRO_OK) return rc;
+    std::vector<double> d(size_t(2 * K));
+    STRO_CUDA(cudaMemcpy(d.data(), a->d_diss, d.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    double sum = 0.0;
+    for (int64_t m = 0; m < K; ++m) sum += d[size_t(2 * m + 1)];
+    a->J = sum / double(K);
+    s->steps_done += a->steps;
+    a->forward_done = true;
+    return STRO_OK;
+}
+
+// lam += w dD/df at the sampled state `state` (see launch_adjoint_dissipation).
+int inject_dissipation(stro_adjoint* a, const void* state, int64_t t) {
+    stro_sim* s = a->sim;
+    AdjArgs g{};
+    g.a = step_args(s, t);
+    g.a.f = const_cast<void*>(state);
+    g.a.ffield_plane = uint32_t(s->N);
+    g.lam = a->d_lam;
+    g.grad_f = a->d_gf;
+    const float nu = float((1.0 / double(s->omega) - 0.5) / 3.0);
+    const float w = float(1.0 / double(a->steps / a->every));
+    STRO_CUDA(launch_adjoint_dissipation(g, s->precision == STRO_FP16S ? 1 : 0, nu, w,
+                                         s->ctx->stream));
     return STRO_OK;
 }
 
@@ -126,6 +192,20 @@ int stro_adj_destroy(stro_adjoint* a) {
     return STRO_OK;
 }
 
+int stro_adj_set_dissipation(stro_adjoint* a, int64_t every) {
+    if (!a) return fail(STRO_ERR_INVALID, "null adjoint handle");
+    if (every < 2 || every % 2 != 0 || every > a->steps)
+        return fail(STRO_ERR_INVALID, "the sample interval must be even and within the window");
+    a->objective = 1;
+    a->every = every;
+    a->forward_done = false;
+    cudaFree(a->d_diss);
+    cudaFree(a->d_final);
+    a->d_diss = nullptr;
+    a->d_final = nullptr;
+    return STRO_OK;
+}
+
 int stro_adj_forward(stro_adjoint* a, double* J) {
     if (!a || !J) return fail(STRO_ERR_INVALID, "null argument");
     stro_sim* s = a->sim;
@@ -137,6 +217,11 @@ int stro_adj_forward(stro_adjoint* a, double* J) {
         return fail(STRO_ERR_INVALID, "the adjoint differentiates the reference collision only");
     cudaSetDevice(s->ctx->device);
     cudaStream_t st = s->ctx->stream;
+    if (a->objective == 1) {
+        const int rc = forward_dissipation(a);
+        if (rc == STRO_OK) *J = a->J;
+        return rc;
+    }
     a->t0 = s->steps_done;
     a->nodd = 0;
     const bool geo = geo_on(s);
@@ -213,7 +298,12 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
     STRO_CUDA(cudaMemsetAsync(a->d_lam, 0, 19 * s->plane * sizeof(float), st));
     STRO_CUDA(cudaMemsetAsync(a->d_geps, 0, N * sizeof(double), st));
     STRO_CUDA(cudaMemsetAsync(a->d_gf, 0, 3 * N * sizeof(float), st));
-    const float w = a->nodd ? float(1.0 / double(a->nodd)) : 0.0f;
+    const bool diss = a->objective == 1;
+    const float w = (!diss && a->nodd) ? float(1.0 / double(a->nodd)) : 0.0f;
+    if (diss && a->d_final) {  // the last state is a sample: its gradient starts the sweep
+        const int rc = inject_dissipation(a, a->d_final, a->t0 + a->steps);
+        if (rc != STRO_OK) return rc;
+    }
     const dim3 ablock(32, 4, 1);
     // walled lattice: bulk blocks take the wall-free reverse step, as the forward split does
     const bool split = geo && s->split && s->geo_host.size() == N;
@@ -282,6 +372,11 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
             else
                 STRO_CUDA(launch_adjoint_step(g, half, int(t & 1), geo, ablock, st));
             ++a->adjoint_launches;
+            // lam is now the adjoint of the state after t - t0 steps of the window
+            if (diss && t > a->t0 && (t - a->t0) % a->every == 0) {
+                const int irc = inject_dissipation(a, g.a.f, t);
+                if (irc != STRO_OK) return irc;
+            }
         }
         rc = timed(a, &a->adjoint_seconds, STRO_OK);
         if (rc != STRO_OK) return rc;

@@ -516,7 +516,84 @@ void launch_adj_list(const AdjArgs& g, int parity, const uint32_t* list, uint32_
     else k_adj_list_odd<S, GEO><<<count, block, 0, st>>>(g, list, gx, gy);
 }
 
+// Gradient of the dissipation objective at one sampled state. Per fluid cell,
+// with u = (p + F/2) / rho, Pi the non-equilibrium second moment and
+// s = 1.5 omega / rho, the cell's term 2 nu s^2 Pi:Pi has
+//   d/df_j = 4 nu s^2 [ (c_j - u).Pi.(c_j - u) - tr(Pi) / 3 - Pi:Pi / rho ],
+//   d/dF   = -4 nu s^2 Pi u,
+// because Pi_ab = sum_i c_ia c_ib f_i - (rho - 1) / 3 delta_ab - rho u_a u_b
+// (the D3Q19 equilibrium's second moment), so dPi_ab/df_j = (c_ja - u_a)
+// (c_jb - u_b) - delta_ab / 3, and s^2 falls with rho as -2 s^2 / rho. Pi
+// itself is summed direction by direction as the observable does.
+template <typename S>
+__global__ void __launch_bounds__(128) k_adj_dissipation(const AdjArgs g, float nu, float w) {
+    const StepArgs& a = g.a;
+    const uint64_t N = uint64_t(a.nx) * uint64_t(a.ny) * uint64_t(a.nz);
+    const S* __restrict__ f = static_cast<const S*>(a.f);
+    const uint64_t P = a.plane;
+    for (uint64_t n = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; n < N;
+         n += uint64_t(gridDim.x) * blockDim.x) {
+        if (a.cell != nullptr && (a.cell[n] & CELL_TYPE_MASK) != CELL_FLUID) continue;
+        float fh[19];
+        sfor<0, 19>([&](auto I) { fh[I] = load_ddf<S>(f + uint64_t(I) * P + n); });
+        float rhom1 = fh[0];
+        sfor<1, 19>([&](auto I) { rhom1 += fh[I]; });
+        float px = 0.f, py = 0.f, pz = 0.f;
+        sfor<1, 19>([&](auto I) { add_c<I>(px, py, pz, fh[I]); });
+        float Fx, Fy, Fz;
+        cell_force_any<S>(a, uint32_t(n), Fx, Fy, Fz);
+        const float rho = 1.0f + rhom1;
+        const float ux = (px + 0.5f * Fx) / rho, uy = (py + 0.5f * Fy) / rho,
+                    uz = (pz + 0.5f * Fz) / rho;
+        const float u2 = ux * ux + uy * uy + uz * uz;
+        float pxx = 0.f, pyy = 0.f, pzz = 0.f, pxy = 0.f, pxz = 0.f, pyz = 0.f;
+        sfor<1, 19>([&](auto I) {
+            constexpr int i = I;
+            const float cu = 3.0f * cdot<i>(ux, uy, uz);
+            const float feq = wgt(i) * (rhom1 + rho * (cu + 0.5f * cu * cu - 1.5f * u2));
+            const float d = fh[i] - feq;
+            if constexpr (dcx(i) != 0) pxx += d;
+            if constexpr (dcy(i) != 0) pyy += d;
+            if constexpr (dcz(i) != 0) pzz += d;
+            if constexpr (dcx(i) * dcy(i) > 0) pxy += d;
+            if constexpr (dcx(i) * dcy(i) < 0) pxy -= d;
+            if constexpr (dcx(i) * dcz(i) > 0) pxz += d;
+            if constexpr (dcx(i) * dcz(i) < 0) pxz -= d;
+            if constexpr (dcy(i) * dcz(i) > 0) pyz += d;
+            if constexpr (dcy(i) * dcz(i) < 0) pyz -= d;
+        });
+        const float pipi = pxx * pxx + pyy * pyy + pzz * pzz +
+                           2.0f * (pxy * pxy + pxz * pxz + pyz * pyz);
+        const float sc = 1.5f * a.omega / rho;
+        const float k4 = w * 4.0f * nu * sc * sc;
+        const float base = -(pxx + pyy + pzz) * (1.0f / 3.0f) - pipi / rho;
+        sfor<0, 19>([&](auto I) {
+            constexpr int i = I;
+            const float ex = float(dcx(i)) - ux, ey = float(dcy(i)) - uy, ez = float(dcz(i)) - uz;
+            const float q = ex * ex * pxx + ey * ey * pyy + ez * ez * pzz +
+                            2.0f * (ex * ey * pxy + ex * ez * pxz + ey * ez * pyz);
+            g.lam[uint64_t(i) * P + n] += k4 * (q + base);
+        });
+        if (g.grad_f != nullptr) {
+            const uint64_t FP = g.a.ffield_plane;
+            g.grad_f[n] -= k4 * (pxx * ux + pxy * uy + pxz * uz);
+            g.grad_f[FP + n] -= k4 * (pxy * ux + pyy * uy + pyz * uz);
+            g.grad_f[2 * FP + n] -= k4 * (pxz * ux + pyz * uy + pzz * uz);
+        }
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_adjoint_dissipation(const AdjArgs& g, int half_storage, float nu, float w,
+                                       cudaStream_t st) {
+    const uint64_t N = uint64_t(g.a.nx) * uint64_t(g.a.ny) * uint64_t(g.a.nz);
+    const uint64_t want = (N + 127) / 128;
+    const unsigned blocks = unsigned(want < 152u * 64u ? want : 152u * 64u);
+    if (half_storage) k_adj_dissipation<__half><<<blocks, 128, 0, st>>>(g, nu, w);
+    else k_adj_dissipation<float><<<blocks, 128, 0, st>>>(g, nu, w);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_adjoint_split(const AdjArgs& g, int half_storage, int parity, dim3 block,
                                  const uint32_t* bulk, uint32_t nbulk, const uint32_t* edge,

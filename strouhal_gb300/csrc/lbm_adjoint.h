@@ -27,4 +27,11 @@ cudaError_t launch_adjoint_split(const AdjArgs& g, int half_storage, int parity,
                                  const uint32_t* bulk, uint32_t nbulk, const uint32_t* edge,
                                  uint32_t nedge, cudaStream_t st);
 
+// Dissipation objective: lam += w dD/df and grad_f += w dD/dF_field for the
+// dissipation sum D (2 nu S:S over fluid cells, as launch_observables) of the
+// state g.a.f at an even step count (natural slots). g.lam, g.grad_f and the
+// force and cell fields of g.a are used; nu = (1/omega - 1/2) / 3.
+cudaError_t launch_adjoint_dissipation(const AdjArgs& g, int half_storage, float nu, float w,
+                                       cudaStream_t st);
+
 }  // namespace stro
