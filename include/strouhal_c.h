@@ -130,6 +130,10 @@ int stro_sim_kinetic_energy(stro_sim* sim, double* sum_u2);
  * 2 nu S:S, with S = -(3 omega / (2 rho)) Pi_neq (lattice units, FP64 sum).
  * Even steps only. */
 int stro_sim_dissipation(stro_sim* sim, double* sum_eps);
+/* Extension: both sums from one reduction over the state (the values
+ * stro_sim_kinetic_energy and stro_sim_dissipation return): out[0] = sum
+ * |u|^2, out[1] = sum 2 nu S:S. Even steps only. */
+int stro_sim_observables(stro_sim* sim, double out[2]);
 /* Simulation.stateDigest (Sim.swift:441-444): SHA-256 of the raw state bytes,
  * 64 lowercase hex chars + NUL. */
 int stro_sim_digest(stro_sim* sim, char hex[65]);

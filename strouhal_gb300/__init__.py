@@ -128,6 +128,7 @@ def lib():
                                   ctypes.c_int32, _P], c_int),
         "stro_sim_kinetic_energy": ([_P, ctypes.POINTER(c_double)], c_int),
         "stro_sim_dissipation": ([_P, ctypes.POINTER(c_double)], c_int),
+        "stro_sim_observables": ([_P, _P], c_int),
         "stro_sim_digest": ([_P, ctypes.c_char_p], c_int),
         "stro_sim_mass": ([_P, ctypes.POINTER(c_double)], c_int),
         "stro_sim_check_finite": ([_P, ctypes.POINTER(c_int)], c_int),
@@ -505,6 +506,12 @@ class Simulation:
         v = ctypes.c_double()
         _check(lib().stro_sim_dissipation(self._h, ctypes.byref(v)))
         return v.value
+
+    def observables(self):
+        """(kineticEnergySum(), dissipationSum()) from one reduction."""
+        out = (ctypes.c_double * 2)()
+        _check(lib().stro_sim_observables(self._h, out))
+        return out[0], out[1]
 
     @property
     def stateDigest(self):

@@ -323,7 +323,8 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
                                   cudaMemcpyHostToDevice, st));
         STRO_CUDA(cudaStreamSynchronize(st));
     }
-    void* live = s->d_f;  // the forward kernels step the buffer a StepArgs points to
+    // the forward kernels step the buffer a StepArgs points to: the recomputation
+    // below steps the segment buffers, never the simulation's own state
     for (int32_t c = a->ncheck - 1; c >= 0; --c) {
         const int64_t k0 = int64_t(c) * a->seg;
         const int64_t len = std::min<int64_t>(a->seg, a->steps - k0);
@@ -381,7 +382,6 @@ int stro_adj_backward(stro_adjoint* a, float* grad_eps, float* grad_force) {
         rc = timed(a, &a->adjoint_seconds, STRO_OK);
         if (rc != STRO_OK) return rc;
     }
-    (void)live;
     if (grad_eps) {
         std::vector<double> ge(N);
         STRO_CUDA(cudaMemcpyAsync(ge.data(), a->d_geps, N * sizeof(double), cudaMemcpyDeviceToHost,

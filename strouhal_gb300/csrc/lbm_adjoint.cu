@@ -47,6 +47,10 @@ __device__ __forceinline__ void add_c(float& ox, float& oy, float& oz, float v) 
 //   ab      : in  dJ/d(post-collision population i); out dJ/d(fh_i)
 //   ntb     : dJ/d(Noble-Torczynski force of the cell)
 //   force_terms: differentiate the Guo source terms (needed for dJ/dF even at F = 0)
+// LES / NT: whether the lattice can have a Smagorinsky model / Noble-Torczynski
+// cells at all; a pass without them compiles their blocks out (fewer
+// registers), with the same values for the cells it runs.
+template <bool LES, bool NT>
 __device__ __forceinline__ void collide_adj(const float (&fh)[19], const StepArgs& a, int x,
                                             float eps, float Fx, float Fy, float Fz,
                                             float (&ab)[19], float ntbx, float ntby, float ntbz,
@@ -91,7 +95,7 @@ __device__ __forceinline__ void collide_adj(const float (&fh)[19], const StepArg
     const float qx = px + 0.5f * Fx, qy = py + 0.5f * Fy, qz = pz + 0.5f * Fz;
     const float ux = qx * inv, uy = qy * inv, uz = qz * inv;
     const float u2 = ux * ux + uy * uy + uz * uz;
-    const bool les = a.c_smago > 0.0f;
+    const bool les = LES && a.c_smago > 0.0f;
     const bool srt = a.omega_minus == a.omega;
     float Q = 0.f, S = 0.f, te = 0.f, lam = 0.f;
     float pxx = 0.f, pyy = 0.f, pzz = 0.f, pxy = 0.f, pxz = 0.f, pyz = 0.f;
@@ -130,7 +134,7 @@ __device__ __forceinline__ void collide_adj(const float (&fh)[19], const StepArg
     const float W0 = wgt(0);
     const float feq0 = W0 * (rhom1 - 1.5f * rho * u2);
     const float s0 = force_terms ? W0 * ap * (-3.0f * uF) : 0.0f;
-    const bool nt = eps != 0.0f;
+    const bool nt = NT && eps != 0.0f;
     const float tw = 1.0f / wp - 0.5f;
     const float Dn = (1.0f - eps) + tw;
     const float B = nt ? eps * tw / Dn : 0.0f;
@@ -333,7 +337,7 @@ __device__ __forceinline__ void add_grads(const AdjArgs& g, uint32_t n, float ep
 }
 
 // One cell of the reverse even (in-cell) pass.
-template <typename S, int GEO>
+template <typename S, int GEO, bool LES>
 __device__ __forceinline__ void adj_even_cell(const AdjArgs& g, int x, int y, int z) {
     const StepArgs& a = g.a;
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
@@ -353,14 +357,15 @@ __device__ __forceinline__ void adj_even_cell(const AdjArgs& g, int x, int y, in
     float Fx, Fy, Fz;
     cell_force_any<S>(a, n, Fx, Fy, Fz);
     float epsb, Fbx, Fby, Fbz;
-    collide_adj(fh, a, x, eps, Fx, Fy, Fz, ab, 0.f, 0.f, 0.f, g.force_terms != 0, epsb, Fbx, Fby,
+    collide_adj<LES, GEO != 0>(fh, a, x, eps, Fx, Fy, Fz, ab, 0.f, 0.f, 0.f, g.force_terms != 0,
+                               epsb, Fbx, Fby,
                 Fbz);
     sfor<0, 19>([&](auto I) { g.lam[uint64_t(I) * P + n] = ab[I]; });
     add_grads(g, n, eps, epsb, Fbx, Fby, Fbz);
 }
 
 // One cell of the reverse odd (streaming) pass.
-template <typename S, int GEO>
+template <typename S, int GEO, bool LES>
 __device__ __forceinline__ void adj_odd_cell(const AdjArgs& g, int x, int y, int z) {
     const StepArgs& a = g.a;
     const uint32_t n = (uint32_t(z) * uint32_t(a.ny) + uint32_t(y)) * uint32_t(a.nx) + uint32_t(x);
@@ -433,7 +438,8 @@ __device__ __forceinline__ void adj_odd_cell(const AdjArgs& g, int x, int y, int
         }
     });
     float epsb, Fbx, Fby, Fbz;
-    collide_adj(fh, a, x, eps, Fx, Fy, Fz, ab, sx, sy_, sz, g.force_terms != 0, epsb, Fbx, Fby,
+    collide_adj<LES, GEO != 0>(fh, a, x, eps, Fx, Fy, Fz, ab, sx, sy_, sz, g.force_terms != 0,
+                               epsb, Fbx, Fby,
                 Fbz);
     // back to the slots that were read; load-side force -c_i * (raw load)
     g.lam[n] = ab[0];
@@ -464,56 +470,70 @@ __device__ __forceinline__ void adj_list_block(const uint32_t* list, uint32_t gx
     z = int(t / gy);
 }
 
-template <typename S, int GEO>
+template <typename S, int GEO, bool LES>
 __global__ void __launch_bounds__(128) k_adj_even(const AdjArgs g) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= g.a.nx || y >= g.a.ny) return;
-    adj_even_cell<S, GEO>(g, x, y, blockIdx.z);
+    adj_even_cell<S, GEO, LES>(g, x, y, blockIdx.z);
 }
 
 // At least four resident blocks: left to itself the compiler gives the odd
 // adjoint 184 registers (two blocks of 128 threads per SM, 12% of the warp
 // slots, IPC 1.0); capped at 128 (a few spilled words) the reverse step of
-// the cylinder runs in 1.78x a forward step instead of 2.20x.
-template <typename S, int GEO>
-__global__ void __launch_bounds__(128, 4) k_adj_odd(const AdjArgs g) {
+// the cylinder runs in 1.78x a forward step instead of 2.20x. Without walls
+// and LES the reverse step fits 96 registers (five blocks per SM; FP16 storage
+// spills a few words).
+template <int GEO, bool LES>
+constexpr int adj_odd_min_blocks() {
+    return (GEO == 0 && !LES) ? 5 : 4;
+}
+
+template <typename S, int GEO, bool LES>
+__global__ void __launch_bounds__(128, adj_odd_min_blocks<GEO, LES>()) k_adj_odd(const AdjArgs g) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= g.a.nx || y >= g.a.ny) return;
-    adj_odd_cell<S, GEO>(g, x, y, blockIdx.z);
+    adj_odd_cell<S, GEO, LES>(g, x, y, blockIdx.z);
 }
 
 // Block-list forms for the bulk / boundary split of a walled lattice: the
 // bulk blocks (no wall, no wall neighbour, no solid fraction) take the
 // wall-free reverse step, the boundary blocks the wall-aware one, as in the
 // forward split. The per-cell values are the same as the grid forms'.
-template <typename S, int GEO>
+template <typename S, int GEO, bool LES>
 __global__ void __launch_bounds__(128) k_adj_list_even(const AdjArgs g, const uint32_t* list,
                                                        uint32_t gx, uint32_t gy) {
     int x, y, z;
     adj_list_block(list, gx, gy, x, y, z);
     if (x >= g.a.nx || y >= g.a.ny || z >= g.a.nz) return;
-    adj_even_cell<S, GEO>(g, x, y, z);
+    adj_even_cell<S, GEO, LES>(g, x, y, z);
 }
 
-template <typename S, int GEO>
-__global__ void __launch_bounds__(128, 4) k_adj_list_odd(const AdjArgs g, const uint32_t* list,
+template <typename S, int GEO, bool LES>
+__global__ void __launch_bounds__(128, adj_odd_min_blocks<GEO, LES>()) k_adj_list_odd(const AdjArgs g, const uint32_t* list,
                                                          uint32_t gx, uint32_t gy) {
     int x, y, z;
     adj_list_block(list, gx, gy, x, y, z);
     if (x >= g.a.nx || y >= g.a.ny || z >= g.a.nz) return;
-    adj_odd_cell<S, GEO>(g, x, y, z);
+    adj_odd_cell<S, GEO, LES>(g, x, y, z);
+}
+
+template <typename S, int GEO, bool LES>
+void launch_adj_list_les(const AdjArgs& g, int parity, const uint32_t* list, uint32_t count,
+                         dim3 block, cudaStream_t st) {
+    const uint32_t gx = (uint32_t(g.a.nx) + block.x - 1) / block.x;
+    const uint32_t gy = (uint32_t(g.a.ny) + block.y - 1) / block.y;
+    if (parity == 0) k_adj_list_even<S, GEO, LES><<<count, block, 0, st>>>(g, list, gx, gy);
+    else k_adj_list_odd<S, GEO, LES><<<count, block, 0, st>>>(g, list, gx, gy);
 }
 
 template <typename S, int GEO>
 void launch_adj_list(const AdjArgs& g, int parity, const uint32_t* list, uint32_t count,
                      dim3 block, cudaStream_t st) {
     if (count == 0) return;
-    const uint32_t gx = (uint32_t(g.a.nx) + block.x - 1) / block.x;
-    const uint32_t gy = (uint32_t(g.a.ny) + block.y - 1) / block.y;
-    if (parity == 0) k_adj_list_even<S, GEO><<<count, block, 0, st>>>(g, list, gx, gy);
-    else k_adj_list_odd<S, GEO><<<count, block, 0, st>>>(g, list, gx, gy);
+    if (g.a.c_smago > 0.0f) launch_adj_list_les<S, GEO, true>(g, parity, list, count, block, st);
+    else launch_adj_list_les<S, GEO, false>(g, parity, list, count, block, st);
 }
 
 // Gradient of the dissipation objective at one sampled state. Per fluid cell,
@@ -609,25 +629,28 @@ cudaError_t launch_adjoint_split(const AdjArgs& g, int half_storage, int parity,
     return cudaGetLastError();
 }
 
+template <typename S, bool LES>
+static void launch_adj_grid(const AdjArgs& g, int parity, int geo, dim3 grid, dim3 block,
+                            cudaStream_t st) {
+    if (parity == 0) {
+        if (geo) k_adj_even<S, 1, LES><<<grid, block, 0, st>>>(g);
+        else k_adj_even<S, 0, LES><<<grid, block, 0, st>>>(g);
+    } else {
+        if (geo) k_adj_odd<S, 1, LES><<<grid, block, 0, st>>>(g);
+        else k_adj_odd<S, 0, LES><<<grid, block, 0, st>>>(g);
+    }
+}
+
 cudaError_t launch_adjoint_step(const AdjArgs& g, int half_storage, int parity, int geo, dim3 block,
                                 cudaStream_t st) {
     const dim3 grid((g.a.nx + block.x - 1) / block.x, (g.a.ny + block.y - 1) / block.y, g.a.nz);
-    if (parity == 0) {
-        if (half_storage) {
-            if (geo) k_adj_even<__half, 1><<<grid, block, 0, st>>>(g);
-            else k_adj_even<__half, 0><<<grid, block, 0, st>>>(g);
-        } else {
-            if (geo) k_adj_even<float, 1><<<grid, block, 0, st>>>(g);
-            else k_adj_even<float, 0><<<grid, block, 0, st>>>(g);
-        }
+    const bool les = g.a.c_smago > 0.0f;
+    if (half_storage) {
+        if (les) launch_adj_grid<__half, true>(g, parity, geo, grid, block, st);
+        else launch_adj_grid<__half, false>(g, parity, geo, grid, block, st);
     } else {
-        if (half_storage) {
-            if (geo) k_adj_odd<__half, 1><<<grid, block, 0, st>>>(g);
-            else k_adj_odd<__half, 0><<<grid, block, 0, st>>>(g);
-        } else {
-            if (geo) k_adj_odd<float, 1><<<grid, block, 0, st>>>(g);
-            else k_adj_odd<float, 0><<<grid, block, 0, st>>>(g);
-        }
+        if (les) launch_adj_grid<float, true>(g, parity, geo, grid, block, st);
+        else launch_adj_grid<float, false>(g, parity, geo, grid, block, st);
     }
     return cudaGetLastError();
 }

@@ -932,15 +932,40 @@ int stro_sim_state_bytes(stro_sim* s, size_t* bytes) {
     return STRO_OK;
 }
 
+// The canonical state (19 planes of N values) to or from the padded device
+// planes: one copy when the planes are not padded, else one copy per plane.
+// Plain copies, not one pitched 2-D copy: device-to-host, the pitched copy of
+// the 637 MB 256^3 FP16 state into pinned memory took 38.7 ms on a GB300
+// (16 GB/s), where the host-to-device one took 3.1 ms.
+static int copy_state(stro_sim* s, void* host, bool to_device) {
+    const size_t row = s->N * s->esize, pitch = s->plane * s->esize;
+    cudaStream_t st = s->ctx->stream;
+    const cudaMemcpyKind kind = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+    char* h = static_cast<char*>(host);
+    char* d = static_cast<char*>(s->d_f);
+    if (pitch == row) {
+        STRO_CUDA(cudaMemcpyAsync(to_device ? static_cast<void*>(d) : static_cast<void*>(h),
+                                  to_device ? static_cast<void*>(h) : static_cast<void*>(d),
+                                  19 * row, kind, st));
+    } else {
+        for (int i = 0; i < 19; ++i) {
+            char* hp = h + size_t(i) * row;
+            char* dp = d + size_t(i) * pitch;
+            STRO_CUDA(cudaMemcpyAsync(to_device ? static_cast<void*>(dp) : static_cast<void*>(hp),
+                                      to_device ? static_cast<void*>(hp) : static_cast<void*>(dp),
+                                      row, kind, st));
+        }
+    }
+    STRO_CUDA(cudaStreamSynchronize(st));
+    return STRO_OK;
+}
+
 int stro_sim_upload_state(stro_sim* s, const void* host, size_t bytes) {
     CHECK_SIM(s);
     if (!host || bytes != 19 * s->N * s->esize)
         return fail(STRO_ERR_INVALID, "state size must be 19*N*element_size bytes");
     cudaSetDevice(s->ctx->device);
-    STRO_CUDA(cudaMemcpy2DAsync(s->d_f, s->plane * s->esize, host, s->N * s->esize,
-                                s->N * s->esize, 19, cudaMemcpyHostToDevice, s->ctx->stream));
-    STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
-    return STRO_OK;
+    return copy_state(s, const_cast<void*>(host), true);
 }
 
 int stro_sim_download_state(stro_sim* s, void* host, size_t bytes) {
@@ -948,10 +973,7 @@ int stro_sim_download_state(stro_sim* s, void* host, size_t bytes) {
     if (!host || bytes != 19 * s->N * s->esize)
         return fail(STRO_ERR_INVALID, "state size must be 19*N*element_size bytes");
     cudaSetDevice(s->ctx->device);
-    STRO_CUDA(cudaMemcpy2DAsync(host, s->N * s->esize, s->d_f, s->plane * s->esize,
-                                s->N * s->esize, 19, cudaMemcpyDeviceToHost, s->ctx->stream));
-    STRO_CUDA(cudaStreamSynchronize(s->ctx->stream));
-    return STRO_OK;
+    return copy_state(s, host, false);
 }
 
 int stro_sim_run(stro_sim* s, int64_t steps) {
@@ -1079,6 +1101,12 @@ int stro_sim_kinetic_energy(stro_sim* s, double* sum_u2) {
     const int rc = observables(s, o);
     if (rc == STRO_OK) *sum_u2 = o[0];
     return rc;
+}
+
+int stro_sim_observables(stro_sim* s, double out[2]) {
+    CHECK_SIM(s);
+    if (!out) return fail(STRO_ERR_INVALID, "null output");
+    return observables(s, out);
 }
 
 int stro_sim_dissipation(stro_sim* s, double* sum_eps) {

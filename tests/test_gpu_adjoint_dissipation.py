@@ -98,3 +98,55 @@ def test_dissipation_adjoint_preconditions(gpu, oracle):
         adj.forward()
     adj.close()
     g.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16s"])
+def test_dissipation_adjoint_long_window_on_a_taylor_green_box(gpu, oracle, precision):
+    """Periodic 32^3 Taylor-Green box (Re 1600 scaling, u0 0.05) with a
+    nonzero per-cell force field: a 400-step window sampled every 40 steps
+    with 20 checkpoints. dJ/dF against the FP64 adjoint of the GPU's own
+    trajectory within 1e-3 normwise, and against FP64 central differences of
+    the FP64 forward within 1e-3 (FP32 storage) or the FP16 bar 2e-2: the
+    gradient about a 400-step FP16-storage trajectory is itself up to 7.5e-3
+    away from the gradient about the FP64 one (FP64 adjoints of both)."""
+    import strouhal_gb300 as sg
+
+    po = oracle
+    n, steps, every = 32, 400, 40
+    L = n / (2 * np.pi)
+    tau = 3 * 0.05 * L / 1600 + 0.5
+    g = sg.Simulation(gpu, precision=precision, nx=n, ny=n, nz=n, omega=1 / tau)
+    o = po.OracleSim(n, n, n, kind=po.KIND_F64, omega=1 / tau)
+    rng = np.random.default_rng(8)
+    ff = (rng.standard_normal((3, n ** 3)) * 2e-6).astype(np.float32)
+    ff[:, rng.random(n ** 3) < 0.3] = 0.0
+    g.setForceField(ff)
+    o.setForceField(ff)
+    g.initField(2, 0.05)
+    f0 = g.downloadState().astype(np.float64)
+    adj = sg.Adjoint(g, steps, checkpoints=20, dissipationEvery=every)
+    J = adj.forward()
+    _, gf = adj.backward()
+    adj.close()
+    g.close()
+    traj = "fp32" if precision == "fp32" else "fp16"
+    Jo, _, gfo = o.adjointDissipation(steps, every, trajectory=traj, f0=f0, checkpoint=20)
+    assert abs(J - Jo) <= 1e-4 * abs(Jo), (J, Jo)
+    assert np.all(np.isfinite(gf))
+    assert base._rel(gf, gfo) < 1e-3, base._rel(gf, gfo)
+    fmax = float(np.max(np.abs(gf)))
+    for idx in rng.choice(n ** 3, 2, replace=False):
+        # a small step: over 400 nearly inviscid steps a one-cell force of 2^-14
+        # already moves J out of its linear range (2.9e-3 off at 2^-14, 7e-7 at 2^-20)
+        h = 2.0 ** -20
+        fp, fm = ff.copy(), ff.copy()
+        fp[0, idx] += h
+        fm[0, idx] -= h
+        vals = []
+        for v in (fp, fm):
+            o.setForceField(v)
+            vals.append(o.adjointDissipation(steps, every, grads=False, f0=f0)[0])
+        o.setForceField(ff)
+        fd = (vals[0] - vals[1]) / (float(fp[0, idx]) - float(fm[0, idx]))
+        bar = 1e-3 if precision == "fp32" else 2e-2
+        assert abs(fd - gf[0, idx]) <= bar * max(abs(fd), 1e-2 * fmax), (idx, fd, gf[0, idx])

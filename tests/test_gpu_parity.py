@@ -349,6 +349,8 @@ def test_mass_energy_dissipation_vs_oracle(gpu, oracle):
     o.run(10)
     assert np.isclose(g.massSum(), o.massSum(), rtol=1e-12, atol=1e-9)
     assert np.isclose(g.kineticEnergySum(), o.kineticEnergySum(), rtol=1e-12, atol=0)
+    # both sums from one reduction, as the separate calls return them
+    assert g.observables() == (g.kineticEnergySum(), g.dissipationSum())
     # dissipation: 2 nu S:S from Pi_neq, recomputed in float64 from the same state
     f = o.f.astype(np.float64)
     m = o.probeMoments().astype(np.float64)
