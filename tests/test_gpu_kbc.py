@@ -29,7 +29,7 @@ def flags_walls(po, nx, ny, nz):
 @pytest.mark.parametrize("kind", [0, 1])
 @pytest.mark.parametrize("arith", ["reference", "fused"])
 @pytest.mark.parametrize("geometry", ["periodic", "walls"])
-@pytest.mark.parametrize("split", [True, False, "columns"])
+@pytest.mark.parametrize("split", [True, False, "columns", "merged", "pair"])
 def test_kbc_matches_oracle(gpu, oracle, kind, arith, geometry, split):
     po = oracle
     nx, ny, nz = 35, 16, 5
@@ -60,7 +60,8 @@ def test_kbc_matches_oracle(gpu, oracle, kind, arith, geometry, split):
         g.run(chunk)
         o.run(chunk)
         assert np.array_equal(g.downloadState(), o.f), (chunk, g.stepsDone)
-        assert g.lastPath in ("cell", "split")
+        # KBC has no pair form: "pair" runs the merged one-cell lists
+        assert g.lastPath in ("cell", "split", "split-merged")
     if geometry == "walls":
         box = ((2, 30), (1, 14))
         fg, fo = g.probeForce(*box), o.probeForce(*box)
