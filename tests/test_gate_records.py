@@ -365,3 +365,17 @@ def test_dfg1_record():
     spectral 5.57953523384."""
     r = rec("dfg1")
     assert r["cd_err"] <= 0.01, (r["cd"], r["cd_err"])
+
+
+def test_cpu_baseline_port_against_the_reference_source():
+    """The CPU baseline times the oracle port; the reference's own kernel
+    source (compiled as C++) cannot run on the GPU machine. On the build host
+    both run one thread on the same 96^3 Taylor-Green state
+    (tests/cpu_reference_timing.py): they end on the same state bit for bit
+    and the port's speed is within a factor of two of the reference code's, so
+    the port's figure stands for the reference's CPU speed."""
+    r = rec("cpu_reference_vs_port")
+    assert {run["precision"] for run in r["runs"]} == {"fp16s", "fp32"}
+    for run in r["runs"]:
+        assert run["identical_states"], run["precision"]
+        assert 0.5 <= run["port_over_reference_1_thread"] <= 2.0, run
