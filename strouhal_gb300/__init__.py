@@ -794,9 +794,13 @@ class Adjoint:
     simulation through the window and returns J; backward() returns
     (dJ/d eps, dJ/d F_field) as float32 arrays of shapes (N,) and (3, N)."""
 
-    def __init__(self, sim, steps, box=((0, 0), (0, 0)), direction=(1.0, 0.0, 0.0),
-                 checkpoints=8, dissipationEvery=None):
+    def __init__(self, sim, steps, box=None, direction=(1.0, 0.0, 0.0), checkpoints=8,
+                 dissipationEvery=None):
         self.sim = sim
+        if box is None:
+            if dissipationEvery is None:
+                raise ValueError("the force objective needs a probe box")
+            box = ((0, 0), (0, 0))  # unused by the dissipation objective
         d3 = (ctypes.c_double * 3)(*[float(v) for v in direction])
         b4 = (ctypes.c_int32 * 4)(int(box[0][0]), int(box[0][1]), int(box[1][0]), int(box[1][1]))
         self._h = _P()

@@ -199,6 +199,7 @@ int stro_adj_set_dissipation(stro_adjoint* a, int64_t every) {
     a->objective = 1;
     a->every = every;
     a->forward_done = false;
+    cudaSetDevice(a->sim->ctx->device);
     cudaFree(a->d_diss);
     cudaFree(a->d_final);
     a->d_diss = nullptr;
