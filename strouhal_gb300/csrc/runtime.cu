@@ -934,9 +934,6 @@ int stro_sim_state_bytes(stro_sim* s, size_t* bytes) {
 
 // The canonical state (19 planes of N values) to or from the padded device
 // planes: one copy when the planes are not padded, else one copy per plane.
-// Plain copies, not one pitched 2-D copy: device-to-host, the pitched copy of
-// the 637 MB 256^3 FP16 state into pinned memory took 38.7 ms on a GB300
-// (16 GB/s), where the host-to-device one took 3.1 ms.
 static int copy_state(stro_sim* s, void* host, bool to_device) {
     const size_t row = s->N * s->esize, pitch = s->plane * s->esize;
     cudaStream_t st = s->ctx->stream;
